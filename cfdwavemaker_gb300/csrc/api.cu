@@ -1,0 +1,679 @@
+// The exported C ABI (include/cfdwavemaker_gb300.h).
+//
+// Global model: like the reference's singletons (CFDwavemaker.cpp:129-163)
+// the library keeps one loaded wave model per process: the parsed input, the
+// device-resident irregular sea tables, the s-grid ring or the regular-wave
+// solution.  Every query goes through one device pipeline; the scalar
+// wave_* functions are batches of one point.
+//
+// Dispatch, clamping and ramps follow CFDwavemaker.cpp:1543-2009: z is
+// clamped to the seabed for the velocity/pressure queries, every output is
+// multiplied by Ramp::ramp(t, x, y), the non-hydrostatic pressure of the
+// irregular sea is ramp * (dp - rho g eta).
+#include "cfdwm.h"
+#include "../../include/cfdwavemaker_gb300.h"
+
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+namespace cfdwm {
+
+#define CKR(x)                                                 \
+    do {                                                       \
+        cudaError_t e_ = (x);                                  \
+        if (e_ != cudaSuccess) {                               \
+            set_error(std::string("CUDA: ") + cudaGetErrorString(e_)); \
+            return E_CUDA;                                     \
+        }                                                      \
+    } while (0)
+
+namespace {
+
+struct Model {
+    bool init = false;
+    Config cfg;
+    DevSea sea;
+    DevGrid grid;
+    DevRegular reg;
+    Workspace grid_ws;
+};
+Model g_model;
+std::mutex g_model_mtx;
+
+// Per-thread execution context: stream, workspace and staging buffers.
+struct ThreadCtx {
+    cudaStream_t own = nullptr;
+    cudaStream_t user = nullptr;
+    bool user_set = false;
+    Workspace ws;
+    double *d_in = nullptr;   // staging of x, y, z, t  [4][cap]
+    double *d_out = nullptr;  // pipeline outputs       [6][cap]
+    double *h_pin = nullptr;  // pinned host staging    [10][cap]
+    long cap = 0;
+    double kin[4] = {0, 0, 0, 0};
+    std::string err;
+    ~ThreadCtx() {
+        if (d_in) cudaFree(d_in);
+        if (d_out) cudaFree(d_out);
+        if (h_pin) cudaFreeHost(h_pin);
+        workspace_free(ws);
+        if (own) cudaStreamDestroy(own);
+    }
+};
+thread_local ThreadCtx t_ctx;
+
+void set_error(const std::string &s) { t_ctx.err = s; }
+
+cudaStream_t stream_of() {
+    if (t_ctx.user_set) return t_ctx.user;
+    if (!t_ctx.own) cudaStreamCreateWithFlags(&t_ctx.own, cudaStreamNonBlocking);
+    return t_ctx.own;
+}
+
+int ensure_cap(long n) {
+    if (t_ctx.cap >= n) return OK;
+    long cap = std::max<long>(n, 1024);
+    if (t_ctx.d_in) cudaFree(t_ctx.d_in);
+    if (t_ctx.d_out) cudaFree(t_ctx.d_out);
+    if (t_ctx.h_pin) cudaFreeHost(t_ctx.h_pin);
+    t_ctx.d_in = t_ctx.d_out = t_ctx.h_pin = nullptr;
+    t_ctx.cap = 0;
+    CKR(cudaMalloc(&t_ctx.d_in, sizeof(double) * 4 * cap));
+    CKR(cudaMalloc(&t_ctx.d_out, sizeof(double) * 6 * cap));
+    CKR(cudaMallocHost(&t_ctx.h_pin, sizeof(double) * 10 * cap));
+    t_ctx.cap = cap;
+    return OK;
+}
+
+bool is_device(const void *p) {
+    if (!p) return true;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+// ---------------------------------------------------------------------------
+// small kernels of the API layer
+// ---------------------------------------------------------------------------
+__global__ void k_clamp_z(long n, const double *z, double depth, double *zc) {
+    long p = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (p < n) zc[p] = fmax(-depth, z[p]);
+}
+
+// Ramp::ramp (Utils.cpp:42-68) times the selected rows of f[nf][n].
+struct RampDev {
+    int init, flags;
+    double lim[12];
+};
+__device__ double d_ramp(const RampDev &r, double t, double x, double y) {
+    if (!r.init) return 1.0;
+    double v[6] = {t, t, x, x, y, y};
+    double m = 1.0;
+    for (int q = 0; q < 6; q++) {
+        double rq = 1.0;
+        if (r.flags & (1 << q)) {
+            double a = (v[q] - r.lim[2 * q]) / (r.lim[2 * q + 1] - r.lim[2 * q]);
+            rq = (q & 1) ? fmax(fmin(1. - a, 1.), 0.) : fmax(fmin(a, 1.), 0.);
+        }
+        m = (q == 0) ? rq : fmin(m, rq);
+    }
+    return m;
+}
+
+// Irregular wave types 1/5 and regular 21 finish here: out rows
+// 0 SurfElev, 1 VeloX, 2 VeloY, 3 VeloZ, 4 DynPres, 5 nhPres.
+__global__ void k_finish(long n, int wavetype, RampDev r, double rho, double g, const double *x,
+                         const double *y, const double *t, const double *f, const double *fe,
+                         double *out) {
+    long p = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    double rr = d_ramp(r, t[p], x[p], y[p]);
+    if (wavetype == WT_IRREGULAR) {
+        // f = [5][n] eta, u, v, w, dp of Irregular::*
+        out[0 * n + p] = rr * f[0 * n + p];
+        out[1 * n + p] = rr * f[1 * n + p];
+        out[2 * n + p] = rr * f[2 * n + p];
+        out[3 * n + p] = rr * f[3 * n + p];
+        out[4 * n + p] = rr * f[4 * n + p];
+        out[5 * n + p] = rr * (f[4 * n + p] - rho * g * f[0 * n + p]);
+    } else if (wavetype == WT_IRR_SGRID) {
+        // f = [4][n] query at the clamped z, fe = [4][n] query at z = 0
+        out[0 * n + p] = fe[0 * n + p] * rr;
+        out[1 * n + p] = f[1 * n + p] * rr;
+        out[2 * n + p] = f[2 * n + p] * rr;
+        out[3 * n + p] = f[3 * n + p] * rr;
+        out[4 * n + p] = 0.0;
+        out[5 * n + p] = 0.0;
+    } else {
+        // f = [5][n] eta, u, v, w, p_nh of the regular theory
+        out[0 * n + p] = rr * f[0 * n + p];
+        out[1 * n + p] = rr * f[1 * n + p];
+        out[2 * n + p] = rr * f[2 * n + p];
+        out[3 * n + p] = rr * f[3 * n + p];
+        out[4 * n + p] = 0.0;
+        out[5 * n + p] = rr * f[4 * n + p];
+    }
+}
+
+// wave_VFrac (CFDwavemaker.cpp:1990-2009) from the ramped elevation.
+__global__ void k_vfrac(long n, const double *z, const double *eta, double dcell, double *out) {
+    long p = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    double w = eta[p], zp = z[p];
+    double v;
+    if (w < zp - (dcell / 2.)) v = 0.0;
+    else if (w > zp + (dcell / 2.)) v = 1.0;
+    else v = (w - (zp - (dcell / 2.))) / dcell;
+    out[p] = v;
+}
+
+RampDev ramp_dev(const RampCfg &r) {
+    RampDev d;
+    d.init = r.init ? 1 : 0;
+    d.flags = r.flags;
+    for (int q = 0; q < 12; q++) d.lim[q] = r.lim[q];
+    return d;
+}
+
+// The device pipeline: out[6][n] of the reference's wave_* functions for
+// the points (x, y, z, t), all device pointers.  want: bit q = output q.
+int eval_api(long n, const double *x, const double *y, const double *z, const double *t, int want,
+             double *out, cudaStream_t s) {
+    Model &M = g_model;
+    if (!M.init) return E_NOT_INITIALIZED;
+    if (n <= 0) return OK;
+    int wt = M.cfg.wavetype;
+    // scratch: clamped z [n], model outputs [5][n] and [4][n]
+    size_t need = sizeof(double) * (size_t)n * 10;
+    Workspace &ws = t_ctx.ws;
+    // irregular_eval uses the same thread workspace; keep a separate buffer
+    static thread_local Workspace api_ws;
+    int rc = workspace_reserve(api_ws, need);
+    if (rc) return rc;
+    double *zc = (double *)api_ws.base, *f = zc + n, *fe = f + 5 * n;
+    k_clamp_z<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, z, M.cfg.depth, zc);
+    CKR(cudaGetLastError());
+    RampDev rd = ramp_dev(M.cfg.ramp);
+    if (wt == WT_IRREGULAR) {
+        int mask = 0;
+        if (want & (1 | 32)) mask |= 1;
+        if (want & 2) mask |= 2;
+        if (want & 4) mask |= 4;
+        if (want & 8) mask |= 8;
+        if (want & (16 | 32)) mask |= 16;
+        CKR(cudaMemsetAsync(f, 0, sizeof(double) * 5 * n, s));
+        rc = irregular_eval(M.sea, n, x, y, zc, t, mask, f, ws, s);
+        if (rc) return rc;
+    } else if (wt == WT_IRR_SGRID) {
+        CKR(cudaMemsetAsync(fe, 0, sizeof(double) * 4 * n, s));
+        if (want & 14) {
+            rc = grid_query(M.grid, n, x, y, zc, t, f, s);
+            if (rc) return rc;
+        }
+        if (want & 1) {
+            CKR(cudaMemsetAsync(zc, 0, sizeof(double) * n, s));
+            rc = grid_query(M.grid, n, x, y, zc, t, fe, s);
+            if (rc) return rc;
+        }
+    } else if (wt == WT_REGULAR) {
+        rc = regular_eval(M.reg, M.cfg, n, x, y, zc, t, f, s);
+        if (rc) return rc;
+    } else {
+        return E_UNSUPPORTED;
+    }
+    k_finish<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(n, wt, rd, M.cfg.rho, M.cfg.gravity, x, y, t,
+                                                         f, fe, out);
+    CKR(cudaGetLastError());
+    return OK;
+}
+
+// Runs eval_api on user arrays, staging host memory as needed.  outs[q]
+// receives row q of the pipeline output (NULL: not wanted).  For VFrac the
+// caller post-processes row 0.
+int run_batch(const double *x, const double *y, const double *z, const double *t, long n,
+              double *const outs[6], int want, double vf_dcell, double *vf_out) {
+    if (!g_model.init) return E_NOT_INITIALIZED;
+    if (n < 0) return E_BAD_ARGUMENT;
+    if (n == 0) return OK;
+    if (!x || !y || !t || (!z && (want & ~1))) return E_BAD_ARGUMENT;
+    cudaStream_t s = stream_of();
+    bool dev = is_device(x) && is_device(y) && is_device(t) && (!z || is_device(z));
+    for (int q = 0; q < 6; q++) if (outs[q] && !is_device(outs[q])) dev = false;
+    if (vf_out && !is_device(vf_out)) dev = false;
+    if (dev) {
+        double *out = nullptr;
+        Workspace &ws = t_ctx.ws;
+        (void)ws;
+        static thread_local Workspace dev_out;
+        int rc = workspace_reserve(dev_out, sizeof(double) * 6 * (size_t)n);
+        if (rc) return rc;
+        out = (double *)dev_out.base;
+        const double *zz = z ? z : t;   // z unused for SurfElev only
+        rc = eval_api(n, x, y, zz, t, want, out, s);
+        if (rc) return rc;
+        for (int q = 0; q < 6; q++)
+            if (outs[q]) CKR(cudaMemcpyAsync(outs[q], out + (long)q * n, sizeof(double) * n,
+                                             cudaMemcpyDeviceToDevice, s));
+        if (vf_out) {
+            k_vfrac<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, z, out, vf_dcell, vf_out);
+            CKR(cudaGetLastError());
+        }
+        if (!t_ctx.user_set) CKR(cudaStreamSynchronize(s));
+        return OK;
+    }
+    // host path: stage in chunks through pinned buffers
+    const long chunk = 1L << 20;
+    int rc = ensure_cap(std::min(n, chunk));
+    if (rc) return rc;
+    for (long b = 0; b < n; b += chunk) {
+        long m = std::min(chunk, n - b);
+        double *hp = t_ctx.h_pin, *din = t_ctx.d_in, *dout = t_ctx.d_out;
+        const double *src[4] = {x, y, z ? z : t, t};
+        for (int q = 0; q < 4; q++) {
+            if (is_device(src[q])) {
+                CKR(cudaMemcpyAsync(din + (long)q * m, src[q] + b, sizeof(double) * m,
+                                    cudaMemcpyDeviceToDevice, s));
+            } else {
+                std::memcpy(hp + (long)q * m, src[q] + b, sizeof(double) * m);
+                CKR(cudaMemcpyAsync(din + (long)q * m, hp + (long)q * m, sizeof(double) * m,
+                                    cudaMemcpyHostToDevice, s));
+            }
+        }
+        rc = eval_api(m, din, din + m, din + 2 * m, din + 3 * m, want, dout, s);
+        if (rc) return rc;
+        if (vf_out) {
+            k_vfrac<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(m, din + 2 * m, dout, vf_dcell, dout + 5 * m);
+            CKR(cudaGetLastError());
+        }
+        CKR(cudaMemcpyAsync(hp + 4 * m, dout, sizeof(double) * 6 * m, cudaMemcpyDeviceToHost, s));
+        CKR(cudaStreamSynchronize(s));
+        for (int q = 0; q < 6; q++)
+            if (outs[q]) std::memcpy(outs[q] + b, hp + (4 + q) * m, sizeof(double) * m);
+        if (vf_out) std::memcpy(vf_out + b, hp + 9 * m, sizeof(double) * m);
+    }
+    return OK;
+}
+
+void free_model() {
+    Model &M = g_model;
+    sea_free(M.sea);
+    grid_free(M.grid);
+    regular_free(M.reg);
+    workspace_free(M.grid_ws);
+    M.cfg = Config();
+    M.init = false;
+}
+
+int initialize_from_text(const std::string &text) {
+    std::lock_guard<std::mutex> lk(g_model_mtx);
+    free_model();
+    Model &M = g_model;
+    Config cfg;
+    int rc = parse_waveinput_text(text, cfg);
+    if (rc) {
+        set_error("waveinput.dat: " + cfg.error);
+        std::fprintf(stderr, "cfdwavemaker_gb300: INPUTFILE ERROR: %s\n", cfg.error.c_str());
+        return rc;
+    }
+    int wt = cfg.wavetype;
+    if (wt != WT_IRREGULAR && wt != WT_IRR_SGRID && wt != WT_REGULAR) {
+        set_error("wave type not served by this build (piston, swd, vtk and slope are not)");
+        std::fprintf(stderr, "cfdwavemaker_gb300: %s\n", t_ctx.err.c_str());
+        return E_UNSUPPORTED;
+    }
+    if ((wt == WT_IRREGULAR || wt == WT_IRR_SGRID) && cfg.vertical_theory == 1) {
+        set_error("vertical_theory smit (experimental upstream) is not served by this build");
+        std::fprintf(stderr, "cfdwavemaker_gb300: %s\n", t_ctx.err.c_str());
+        return E_UNSUPPORTED;
+    }
+    cudaStream_t s = stream_of();
+    M.cfg = cfg;
+    if (wt == WT_IRREGULAR || wt == WT_IRR_SGRID) {
+        dump_spectral_components(cfg);
+        rc = sea_build(cfg, M.sea, wt == WT_IRREGULAR, s);
+        if (rc) { free_model(); return rc; }
+        if (wt == WT_IRR_SGRID) {
+            rc = grid_create(cfg, M.grid, s);
+            if (!rc) rc = grid_initialize(M.grid, M.sea, M.grid_ws, s);
+            if (rc) { free_model(); return rc; }
+        }
+    } else {
+        rc = regular_build(cfg, M.reg, s);
+        if (rc) {
+            set_error("regular-wave setup failed");
+            free_model();
+            return rc;
+        }
+        if (M.reg.status == 3)
+            std::fprintf(stderr, "FentonStream: warning - Newton iteration did not fully converge.\n");
+    }
+    M.init = true;
+    return OK;
+}
+
+double scalar(int q, double x, double y, double z, double t) {
+    if (!g_model.init) return 0.0;
+    double *outs[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    double v = 0.0;
+    outs[q] = &v;
+    int rc = run_batch(&x, &y, &z, &t, 1, outs, 1 << q, 0.0, nullptr);
+    return rc ? 0.0 : v;
+}
+
+}  // namespace
+}  // namespace cfdwm
+
+using namespace cfdwm;
+
+extern "C" {
+
+int CFDwavemaker_is_initialized(void) { return g_model.init ? 1 : 0; }
+
+int wave_Initialize(void) {
+    std::string text, where;
+    if (read_waveinput_file(text, where) != OK) {
+        std::fprintf(stderr, "Could not open file (is it really there?) \n");
+        set_error("waveinput.dat not found");
+        return -1;
+    }
+    return initialize_from_text(text);
+}
+
+int cfdwm_initialize_text(const char *text) {
+    if (!text) return E_BAD_ARGUMENT;
+    return initialize_from_text(std::string(text));
+}
+
+int wave_Cleanup(void) {
+    std::lock_guard<std::mutex> lk(g_model_mtx);
+    free_model();
+    return 0;
+}
+
+double wave_VeloX(double x, double y, double z, double t) { return scalar(1, x, y, z, t); }
+double wave_VeloY(double x, double y, double z, double t) { return scalar(2, x, y, z, t); }
+double wave_VeloZ(double x, double y, double z, double t) { return scalar(3, x, y, z, t); }
+double wave_DynPres(double x, double y, double z, double t) { return scalar(4, x, y, z, t); }
+double wave_nhPres(double x, double y, double z, double t) { return scalar(5, x, y, z, t); }
+double wave_SurfElev(double x, double y, double t) { return scalar(0, x, y, 0.0, t); }
+
+double wave_VFrac(double x, double y, double z, double t, double dcell) {
+    double eta = wave_SurfElev(x, y, t);
+    if (eta < z - (dcell / 2.)) return 0.0;
+    if (eta > z + (dcell / 2.)) return 1.0;
+    return (eta - (z - (dcell / 2.))) / dcell;
+}
+
+double wave_Seabed(double x, double y) {
+    (void)x; (void)y;
+    return -g_model.cfg.depth;
+}
+
+double *wave_Kinematics(double x, double y, double z, double t) {
+    double *k = t_ctx.kin;
+    k[0] = k[1] = k[2] = k[3] = 0.0;
+    int wt = g_model.cfg.wavetype;
+    if (!g_model.init || (wt != WT_IRR_SGRID && wt != WT_IRREGULAR)) return k;
+    double *outs[6] = {&k[0], &k[1], &k[2], &k[3], nullptr, nullptr};
+    if (wt == WT_IRR_SGRID) {
+        // get_kinematics_at_point at the given z (CFDwavemaker.cpp:1625-1635):
+        // eta from the same query, no seabed clamp
+        static thread_local double buf[4];
+        DevGrid &g = g_model.grid;
+        cudaStream_t s = stream_of();
+        double in[4] = {x, y, z, t};
+        double *d = nullptr;
+        if (cudaMalloc(&d, sizeof(double) * 8) != cudaSuccess) return k;
+        cudaMemcpyAsync(d, in, sizeof(in), cudaMemcpyHostToDevice, s);
+        grid_query(g, 1, d, d + 1, d + 2, d + 3, d + 4, s);
+        cudaMemcpyAsync(buf, d + 4, sizeof(double) * 4, cudaMemcpyDeviceToHost, s);
+        cudaStreamSynchronize(s);
+        cudaFree(d);
+        RampCfg &r = g_model.cfg.ramp;
+        double rr = 1.0;
+        if (r.init) {
+            double v[6] = {t, t, x, x, y, y};
+            for (int q = 0; q < 6; q++)
+                if (r.flags & (1 << q)) {
+                    double a = (v[q] - r.lim[2 * q]) / (r.lim[2 * q + 1] - r.lim[2 * q]);
+                    double rq = (q & 1) ? std::max(std::min(1. - a, 1.), 0.) : std::max(std::min(a, 1.), 0.);
+                    rr = std::min(rr, rq);
+                }
+        }
+        for (int q = 0; q < 4; q++) k[q] = buf[q] * rr;
+        return k;
+    }
+    run_batch(&x, &y, &z, &t, 1, outs, 15, 0.0, nullptr);
+    return k;
+}
+
+double wave_piston_position(double t) {
+    (void)t;
+    return 0.;
+}
+
+void wave_force_update(double t) {
+    std::lock_guard<std::mutex> lk(g_model_mtx);
+    Model &M = g_model;
+    if (!M.init || M.cfg.wavetype != WT_IRR_SGRID) return;
+    cudaStream_t s = stream_of();
+    while (grid_check_time(M.grid, t)) {
+        if (grid_update(M.grid, M.sea, M.grid_ws, s) != OK) break;
+    }
+    cudaStreamSynchronize(s);
+}
+
+void wave_set_mpi_comm(int fortran_comm) { (void)fortran_comm; }
+void update_probes(double t) { (void)t; }
+
+double wave_phase_speed(int opt) {
+    return g_model.cfg.wavetype == WT_IRREGULAR ? phase_speed(g_model.cfg, opt) : 0.;
+}
+double wave_mean_length(int opt) {
+    if (g_model.cfg.wavetype == WT_IRREGULAR) return mean_wave_length(g_model.cfg, opt);
+    if (g_model.cfg.wavetype == WT_REGULAR)
+        return g_model.cfg.regular_theory == 1 ? g_model.reg.wave_length : g_model.cfg.wave_length;
+    return 0.;
+}
+double wave_mean_period(int opt) {
+    if (g_model.cfg.wavetype == WT_IRREGULAR) return mean_wave_period(g_model.cfg, opt);
+    if (g_model.cfg.wavetype == WT_REGULAR)
+        return g_model.cfg.regular_theory == 1 ? g_model.reg.wave_period : g_model.cfg.wave_period;
+    return 0.;
+}
+double wave_water_depth(void) { return g_model.cfg.depth; }
+
+double VelocityX(int, int, int, double x, double y, double z, double t) { return wave_VeloX(x, y, z, t); }
+double VelocityY(int, int, int, double x, double y, double z, double t) { return wave_VeloY(x, y, z, t); }
+double VelocityZ(int, int, int, double x, double y, double z, double t) { return wave_VeloZ(x, y, z, t); }
+double DynamicPressure(int, int, int, double x, double y, double z, double t) { return wave_DynPres(x, y, z, t); }
+double SurfaceElevation(int, int, double x, double y, double t) { return wave_SurfElev(x, y, t); }
+double VolumeFraction(double x, double y, double z, double t, double d) { return wave_VFrac(x, y, z, t, d); }
+int Init(void *) { return wave_Initialize(); }
+int Prepare(double, int) { return 0; }
+int Cleanup(void) { return wave_Cleanup(); }
+
+int wave_SurfElev_batch(const double *x, const double *y, const double *t, long n, double *eta) {
+    double *outs[6] = {eta, nullptr, nullptr, nullptr, nullptr, nullptr};
+    return run_batch(x, y, nullptr, t, n, outs, 1, 0.0, nullptr);
+}
+int wave_VeloXYZ_batch(const double *x, const double *y, const double *z, const double *t, long n,
+                       double *u, double *v, double *w) {
+    double *outs[6] = {nullptr, u, v, w, nullptr, nullptr};
+    int want = (u ? 2 : 0) | (v ? 4 : 0) | (w ? 8 : 0);
+    return run_batch(x, y, z, t, n, outs, want, 0.0, nullptr);
+}
+int wave_DynPres_batch(const double *x, const double *y, const double *z, const double *t, long n,
+                       double *p) {
+    double *outs[6] = {nullptr, nullptr, nullptr, nullptr, p, nullptr};
+    return run_batch(x, y, z, t, n, outs, 16, 0.0, nullptr);
+}
+int wave_nhPres_batch(const double *x, const double *y, const double *z, const double *t, long n,
+                      double *p) {
+    double *outs[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, p};
+    return run_batch(x, y, z, t, n, outs, 32, 0.0, nullptr);
+}
+int wave_VFrac_batch(const double *x, const double *y, const double *z, const double *t, double dcell,
+                     long n, double *vf) {
+    double *outs[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    return run_batch(x, y, z, t, n, outs, 1, dcell, vf);
+}
+int wave_Kinematics_batch(const double *x, const double *y, const double *z, const double *t, long n,
+                          double *out) {
+    if (n <= 0) return n == 0 ? 0 : E_BAD_ARGUMENT;
+    std::vector<double> tmp(4 * (size_t)n);
+    bool dev = is_device(out);
+    if (g_model.cfg.wavetype == WT_IRR_SGRID) {
+        // eta and velocities from one query at the given (unclamped) z
+        std::vector<double> hin;
+        cudaStream_t s = stream_of();
+        double *d = nullptr;
+        if (cudaMalloc(&d, sizeof(double) * 8 * (size_t)n) != cudaSuccess) return E_CUDA;
+        const double *src[4] = {x, y, z, t};
+        for (int q = 0; q < 4; q++)
+            cudaMemcpyAsync(d + (long)q * n, src[q], sizeof(double) * n, cudaMemcpyDefault, s);
+        int rc = grid_query(g_model.grid, n, d, d + n, d + 2 * n, d + 3 * n, d + 4 * n, s);
+        if (rc) { cudaFree(d); return rc; }
+        cudaMemcpyAsync(tmp.data(), d + 4 * n, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, s);
+        cudaStreamSynchronize(s);
+        std::vector<double> hx(n), hy(n), ht(n);
+        cudaMemcpy(hx.data(), d, sizeof(double) * n, cudaMemcpyDeviceToHost);
+        cudaMemcpy(hy.data(), d + n, sizeof(double) * n, cudaMemcpyDeviceToHost);
+        cudaMemcpy(ht.data(), d + 3 * n, sizeof(double) * n, cudaMemcpyDeviceToHost);
+        cudaFree(d);
+        const RampCfg &r = g_model.cfg.ramp;
+        std::vector<double> res(4 * (size_t)n);
+        for (long p = 0; p < n; p++) {
+            double rr = 1.0;
+            if (r.init) {
+                double v[6] = {ht[p], ht[p], hx[p], hx[p], hy[p], hy[p]};
+                for (int q = 0; q < 6; q++)
+                    if (r.flags & (1 << q)) {
+                        double a = (v[q] - r.lim[2 * q]) / (r.lim[2 * q + 1] - r.lim[2 * q]);
+                        double rq = (q & 1) ? std::max(std::min(1. - a, 1.), 0.) : std::max(std::min(a, 1.), 0.);
+                        rr = std::min(rr, rq);
+                    }
+            }
+            for (int q = 0; q < 4; q++) res[4 * p + q] = tmp[(long)q * n + p] * rr;
+        }
+        if (dev) cudaMemcpy(out, res.data(), sizeof(double) * 4 * n, cudaMemcpyHostToDevice);
+        else std::memcpy(out, res.data(), sizeof(double) * 4 * n);
+        return OK;
+    }
+    double *o4[6] = {tmp.data(), tmp.data() + n, tmp.data() + 2 * n, tmp.data() + 3 * n, nullptr, nullptr};
+    int rc = run_batch(x, y, z, t, n, o4, 15, 0.0, nullptr);
+    if (rc) return rc;
+    std::vector<double> res(4 * (size_t)n);
+    for (long p = 0; p < n; p++)
+        for (int q = 0; q < 4; q++) res[4 * p + q] = tmp[(long)q * n + p];
+    if (dev) cudaMemcpy(out, res.data(), sizeof(double) * 4 * n, cudaMemcpyHostToDevice);
+    else std::memcpy(out, res.data(), sizeof(double) * 4 * n);
+    return OK;
+}
+
+int cfdwm_set_stream(void *cuda_stream) {
+    t_ctx.user = (cudaStream_t)cuda_stream;
+    t_ctx.user_set = cuda_stream != nullptr;
+    return OK;
+}
+
+int cfdwm_last_error(char *buf, int len) {
+    int n = (int)t_ctx.err.size();
+    if (buf && len > 0) {
+        std::strncpy(buf, t_ctx.err.c_str(), (size_t)len - 1);
+        buf[len - 1] = 0;
+    }
+    return n;
+}
+
+int cfdwm_wavetype(void) { return g_model.init ? g_model.cfg.wavetype : 0; }
+
+int cfdwm_irregular_fields(const double *x, const double *y, const double *z, const double *t, long n,
+                           int mask, double *out) {
+    Model &M = g_model;
+    if (!M.init) return E_NOT_INITIALIZED;
+    if (M.cfg.wavetype != WT_IRREGULAR && M.cfg.wavetype != WT_IRR_SGRID) return E_UNSUPPORTED;
+    if (n <= 0) return n == 0 ? OK : E_BAD_ARGUMENT;
+    if ((mask & 30) && !M.sea.d_tab_point && M.cfg.order == 2) {
+        // the s-grid model has no point-API table; build it on demand
+        int rc = sea_build(M.cfg, M.sea, true, stream_of());
+        if (rc) return rc;
+    }
+    cudaStream_t s = stream_of();
+    double *d = nullptr;
+    CKR(cudaMalloc(&d, sizeof(double) * 9 * (size_t)n));
+    const double *src[4] = {x, y, z ? z : t, t};
+    for (int q = 0; q < 4; q++)
+        CKR(cudaMemcpyAsync(d + (long)q * n, src[q], sizeof(double) * n, cudaMemcpyDefault, s));
+    CKR(cudaMemsetAsync(d + 4 * n, 0, sizeof(double) * 5 * n, s));
+    int rc = irregular_eval(M.sea, n, d, d + n, d + 2 * n, d + 3 * n, mask, d + 4 * n, t_ctx.ws, s);
+    if (rc == OK) {
+        CKR(cudaMemcpyAsync(out, d + 4 * n, sizeof(double) * 5 * n, cudaMemcpyDefault, s));
+        CKR(cudaStreamSynchronize(s));
+    }
+    cudaFree(d);
+    return rc;
+}
+
+long cfdwm_npairs(void) { return g_model.init ? g_model.sea.npairs_grid : 0; }
+
+int cfdwm_components(double *dst) {
+    const Config &c = g_model.cfg;
+    int n = (int)c.omega.size();
+    if (!dst) return n;
+    const std::vector<double> *src[8] = {&c.omega, &c.A, &c.k, &c.phase, &c.theta, &c.ramptime,
+                                         &c.starttime, &c.duration};
+    for (int q = 0; q < 8; q++)
+        for (int i = 0; i < n; i++) dst[(long)q * n + i] = (*src[q])[i];
+    return n;
+}
+
+long cfdwm_sgrid_array(int which, double *dst, long cap) {
+    if (!g_model.init || g_model.cfg.wavetype != WT_IRR_SGRID) return E_UNSUPPORTED;
+    return grid_download(g_model.grid, which, dst, cap, stream_of());
+}
+
+int cfdwm_sgrid_state(double *t0, int *tstep) {
+    if (!g_model.init || g_model.cfg.wavetype != WT_IRR_SGRID) return E_UNSUPPORTED;
+    if (t0) *t0 = g_model.grid.t0;
+    if (tstep) *tstep = g_model.grid.tstep;
+    return OK;
+}
+
+int cfdwm_parse_text(const char *text, double *scalars, double *comps, int cap) {
+    if (!text) return E_BAD_ARGUMENT;
+    Config c;
+    int rc = parse_waveinput_text(std::string(text), c);
+    if (rc) {
+        set_error(c.error);
+        return rc;
+    }
+    double v[16] = {(double)c.wavetype, (double)c.order, c.depth, c.mtheta, c.swl, c.gravity, c.rho,
+                    c.tofmax, c.x_pos, c.y_pos, c.dw_cutoff, c.dw_bandwidth, c.wave_length,
+                    c.wave_period, c.wave_height, (double)c.ndir};
+    if (scalars) for (int q = 0; q < 16; q++) scalars[q] = v[q];
+    int n = (int)c.omega.size();
+    if (comps && n <= cap) {
+        const std::vector<double> *src[8] = {&c.omega, &c.A, &c.k, &c.phase, &c.theta, &c.ramptime,
+                                             &c.starttime, &c.duration};
+        for (int q = 0; q < 8; q++)
+            for (int i = 0; i < n; i++) comps[(long)q * n + i] = (*src[q])[i];
+    }
+    return n;
+}
+
+int cfdwm_regular_solution(double *dst, int cap) {
+    if (!g_model.init || g_model.cfg.wavetype != WT_REGULAR) return E_UNSUPPORTED;
+    return regular_solution(g_model.reg, dst, cap, stream_of());
+}
+
+}  // extern "C"

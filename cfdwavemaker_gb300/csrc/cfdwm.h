@@ -1,0 +1,222 @@
+// Internal declarations of the GB300 build of CFDwavemaker's point-kinematics
+// path: the parsed configuration, the device-resident wave models and the
+// host-side launchers of the CUDA kernels.  Nothing here is exported; the
+// C ABI lives in include/cfdwavemaker_gb300.h.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace cfdwm {
+
+// Wave-type numbering of the reference (CFDwavemaker.cpp:252-258).
+enum WaveType {
+    WT_NONE = 0,
+    WT_IRREGULAR = 1,
+    WT_IRR_SGRID = 5,
+    WT_PISTON = 11,
+    WT_REGULAR = 21,
+    WT_SWD = 31,
+    WT_SWD_SGRID = 34,
+    WT_VTK = 41,
+    WT_SLOPE = 51,
+};
+
+// Status codes of the batched entry points.
+enum Status {
+    OK = 0,
+    E_NOT_INITIALIZED = -1,
+    E_UNSUPPORTED = -2,
+    E_BAD_ARGUMENT = -3,
+    E_CUDA = -4,
+    E_NO_FILE = -5,
+    E_PARSE = -6,
+    E_SOLVER = -7,
+    E_TOO_LARGE = -8,
+};
+
+constexpr double SMALL = 1.e-12;   // Irregular.h:8
+constexpr double HUGE_ = 1.e12;    // Irregular.h:11
+constexpr double PI_IRR = 3.1415926535897;            // Irregular.h:14 (truncated)
+constexpr double PI_FULL = 3.14159265358979323846;    // Stokes5.h:5
+
+struct RampCfg {
+    bool init = false;
+    int flags = 0;        // bit q: time up, time down, x up, x down, y up, y down
+    double lim[12] = {0};
+};
+
+struct LsgridCfg {
+    bool present = false;
+    double domain[4] = {0, 0, 0, 0};
+    int nx = 5, ny = 0, nl = 4;
+    double t0 = 0.0, dt = 0.1, tan_a = 0.0, tan_b = 0.0;
+    double domain_ignore[4] = {1.e12, -1.e12, 1.e12, -1.e12};
+    bool ignore_domain = false, ignore_at_init = false, init_only = false;
+};
+
+struct Config {
+    int wavetype = WT_NONE;
+    double depth = 0.0, mtheta = 0.0, swl = 0.0, gravity = 9.81, rho = 1.0, ampl = 1.0;
+    bool normalize = false, nhpres_kinetic = false;
+    double tofmax = 0.0, x_pos = 0.0, y_pos = 0.0;
+    RampCfg ramp;
+    int extrapolation_met = 0, order = 2;
+    double dw_cutoff = 100000.0, dw_bandwidth = 100.0;
+    bool bw_auto = false, individual_ramp = false;
+    int vertical_theory = 0;
+    int nfreq = 0, ndir = 1;
+    bool property_read = false;
+    std::vector<double> omega, A, k, phase, theta, ramptime, starttime, duration;
+    int regular_theory = 0, wave_order = 16;
+    bool regular_specify_length = true;
+    double wave_length = 0.0, wave_period = 0.0, wave_height = 0.0, current = 0.0;
+    LsgridCfg lsgrid;
+    std::string error;
+};
+
+// waveinput.dat reader (parser.cpp).  Returns OK or E_PARSE (cfg.error set).
+int parse_waveinput_text(const std::string &text, Config &cfg);
+// Search order of wave_Initialize (CFDwavemaker.cpp:2086-2111).
+int read_waveinput_file(std::string &text, std::string &where);
+// Host-side spectral helpers (Irregular.cpp:1336-1452).
+void spectral_moments(const Config &c, double m[3]);
+double phase_speed(const Config &c, int opt);
+double mean_wave_length(const Config &c, int opt);
+double mean_wave_period(const Config &c, int opt);
+double wavenumber_from_period(double T, double depth, double g);
+double wavelength_from_period(double T, double depth, double g);
+double period_from_length(double L, double depth, double g);
+void dump_spectral_components(const Config &c);
+
+// ---------------------------------------------------------------------------
+// Device-resident irregular sea (irregular.cu)
+// ---------------------------------------------------------------------------
+// Per-component FP32 coefficient rows (index * npad + component).
+enum CompCoef {
+    CF_A = 0,     // A                         eta1
+    CF_AU,        // A g k / omega             u1, v1, w1
+    CF_CT,        // cos(theta + mtheta)
+    CF_ST,        // sin(theta + mtheta)
+    CF_K,         // k
+    CF_Q,         // 1 / (1 + exp(-2 k h))     depth-profile normaliser
+    CF_AP,        // A rho g                   dp1
+    CF_GX,        // cos(th) A omega k         phi1_dxdz
+    CF_GY,        // sin(th) A omega k         phi1_dydz
+    CF_GZ,        // A omega k coth(k h)       phi1_dzdz
+    CF_GP,        // A rho g k                 dp1_dz
+    CF_X1,        // rho * -g^2 (2k ct + 2k st) 2 / (2 omega)   dp2 diagonal, times px
+    CF_Z1,        // rho *  g^2 (2k) 2 / (2 omega)              dp2 diagonal, times pz
+    NCF
+};
+
+// Pair-table tile geometry: the upper triangle of the N x N component pairs in
+// square tiles of TILE x TILE, tile (I, M) with I <= M stored at
+// tile_index(I, M), each entry a fixed-size coefficient record.
+// Record sizes are defined with the kernels (irregular.cu).
+constexpr int GRID_TILE = 32;
+constexpr int POINT_TILE = 16;
+
+struct DevSea {
+    int n = 0;              // components
+    int npad_g = 0;         // components padded to GRID_TILE
+    int npad_p = 0;         // components padded to POINT_TILE
+    double depth = 0, swl = 0, g = 9.81, rho = 1, fx = 0, fy = 0;
+    int order = 2;
+    bool trivial_ramp = true;
+    long npairs_grid = 0;   // pairs kept by the reference's pair cache
+    // FP64 phase data, length npad_g: kx, ky, omega, phase0, ramptime, starttime, duration
+    double *d_phase = nullptr;   // [7][npad_g]
+    float *d_cf = nullptr;       // [NCF][npad_g]
+    float *d_tab_eta = nullptr;  // grid-mask pair tiles of eta2 (A, B per pair)
+    float *d_tab_grid = nullptr; // grid-mask pair tiles of uvw2
+    float *d_tab_point = nullptr;// point-API pair tiles (built on demand)
+    int ntile_g = 0, ntile_p = 0;
+};
+
+// Builds the device tables (component coefficients and the FP64 transfer
+// functions of the pair tables, computed on the device).  point_table: also
+// build the unfiltered point-API table.
+int sea_build(const Config &cfg, DevSea &sea, bool point_table, void *stream);
+void sea_free(DevSea &sea);
+
+// Scratch workspace for one batch: phasors and first-order sums.
+struct Workspace {
+    size_t bytes = 0;
+    void *base = nullptr;
+};
+int workspace_reserve(Workspace &ws, size_t bytes);
+void workspace_free(Workspace &ws);
+
+// Evaluate irregular-sea kinematics at n points (device pointers, FP64 in).
+// mask bits: 1 eta, 2 u, 4 v, 8 w, 16 dp.  out is [5][n] FP64 (no ramp, no
+// clamp): the reference's Irregular::eta/u/v/w/dp.
+int irregular_eval(const DevSea &sea, long n, const double *x, const double *y,
+                   const double *z, const double *t, int mask, double *out,
+                   Workspace &ws, void *stream);
+
+// Point-batched second-order sums only (for tests of the pair kernels):
+// which = 0 -> u2,v2,w2,dp2 of the point API at z, 1 -> uvw2 (grid mask).
+int irregular_second_order(const DevSea &sea, long n, const double *x, const double *y,
+                           const double *z, const double *t, int which, double *out,
+                           Workspace &ws, void *stream);
+
+// ---------------------------------------------------------------------------
+// Device-resident s-grid (sgrid.cu)
+// ---------------------------------------------------------------------------
+struct DevGrid {
+    LsgridCfg cfg;
+    int nx = 0, ny = 0, nl = 0;
+    double dx = 0, dy = 0, ds = 0, t0 = 0, dt = 0, depth = 0, swl = 0;
+    int tstep = 0;
+    // FP32 fields, layouts of lsgrid_spline.cpp:35-61 ([slot][i][j][m])
+    float *ETA = nullptr, *ETAdx = nullptr, *ETAdy = nullptr, *ETAdt = nullptr;
+    float *U[3] = {nullptr, nullptr, nullptr};
+    float *Ut[3] = {nullptr, nullptr, nullptr};
+    float *Ux[3] = {nullptr, nullptr, nullptr};
+    float *Uy[3] = {nullptr, nullptr, nullptr};
+    float *Us[3] = {nullptr, nullptr, nullptr};
+    int *IGNORE = nullptr;
+    float *zlev = nullptr;       // scratch: level heights of the slot being written
+    double *colpts = nullptr;    // scratch: column x, y, t (FP64)
+    double *first = nullptr;     // scratch: eta1, gx, gy, gz per column
+    float *second = nullptr;     // scratch: level sums [3][ncol*nl]
+    float *eta2 = nullptr;       // scratch: eta2 per column
+};
+int grid_create(const Config &cfg, DevGrid &g, void *stream);
+void grid_free(DevGrid &g);
+int grid_initialize(DevGrid &g, const DevSea &sea, Workspace &ws, void *stream);
+int grid_update(DevGrid &g, const DevSea &sea, Workspace &ws, void *stream);
+bool grid_check_time(const DevGrid &g, double t);
+// out [4][n] FP64: eta, u, v, w (no ramp)
+int grid_query(const DevGrid &g, long n, const double *x, const double *y, const double *z,
+               const double *t, double *out, void *stream);
+int grid_download(const DevGrid &g, int which, double *dst, long cap, void *stream);
+
+// ---------------------------------------------------------------------------
+// Regular waves (regular.cu)
+// ---------------------------------------------------------------------------
+struct DevRegular {
+    int theory = 0;         // 0 Stokes5, 1 Fenton
+    int N = 0;
+    double *d_sol = nullptr;  // FP64 solution block (coefficients), see regular.cu
+    int status = 0;           // Fenton: 0 converged, 3 not fully converged
+    // host copies of the scalars
+    double k = 0, c = 0, wave_length = 0, wave_period = 0;
+};
+int regular_build(const Config &cfg, DevRegular &r, void *stream);
+void regular_free(DevRegular &r);
+// out [5][n] FP64: eta, u, v, w, nhpres (no ramp); z is used as given.
+int regular_eval(const DevRegular &r, const Config &cfg, long n, const double *x,
+                 const double *y, const double *z, const double *t, double *out, void *stream);
+int regular_solution(const DevRegular &r, double *dst, int cap, void *stream);
+
+// ---------------------------------------------------------------------------
+// Post-processing shared by the API (api_kernels.cu)
+// ---------------------------------------------------------------------------
+// Ramp::ramp applied to [nf][n] fields in place (Utils.cpp:42-68).
+int apply_ramp(const RampCfg &r, long n, const double *x, const double *y, const double *t,
+               double *fields, int nf, void *stream);
+
+}  // namespace cfdwm

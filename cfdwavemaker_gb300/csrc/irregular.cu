@@ -1,0 +1,887 @@
+// Irregular second-order (Sharma & Dean) kinematics on the GPU.
+//
+// What is computed follows the reference (oystelan/CFDwavemaker v3.1.0):
+//   first-order sums     Irregular.cpp:178-198, 394-447, 1107-1192
+//   eta2 (pair cache)    Irregular.cpp:223-293
+//   u2/v2/w2/dp2         Irregular.cpp:450-803   (point API, unfiltered pairs)
+//   uvw2 (pair cache)    Irregular.cpp:975-1102  (s-grid)
+//   pair cache filters   Irregular.cpp:840-967
+//   order dispatch       Irregular.cpp:9-157     (Taylor layer above swl)
+//
+// How it is computed (GB300 design):
+//  * The per-pair transfer functions (D+-, alpha+-) are evaluated ONCE, in FP64
+//    on the device, and stored as FP32 coefficients in tiles of the upper
+//    triangle of the N x N pair matrix (build kernels below).  Each pair
+//    record already folds the amplitudes, 1/(omega_i +- omega_m), the
+//    direction factors and the depth normaliser 1/(1+exp(-2 k+- h)).
+//  * Phases are formed in FP64 (k.x - omega t + phase0 can reach 1e4 rad) and
+//    reduced to [-pi, pi] before an FP32 sincos; the phasors of every
+//    (component, point) are written once to a scratch workspace.
+//  * The pair sums run on FP32 CUDA cores: each thread owns one point (or one
+//    s-grid column with LV levels in registers); the coefficient tile and the
+//    phasors of the streamed component tile are staged in shared memory and
+//    read as warp-wide broadcasts / conflict-free rows.  The depth factors
+//    cosh(k(z+h))/cosh(kh) and sinh(k(z+h))/cosh(kh) use two MUFU ex2 per
+//    wavenumber, exp(kz) and exp(-2k(z+h)), both <= 1 below the surface.
+//  * Accumulation is compensated: a tile row is summed in FP32, then added to
+//    a Kahan (sum, carry) pair per output.
+#include "cfdwm.h"
+
+#include <cuda_runtime.h>
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
+namespace cfdwm {
+
+#define CK(x)                                                  \
+    do {                                                       \
+        cudaError_t e_ = (x);                                  \
+        if (e_ != cudaSuccess) {                               \
+            std::fprintf(stderr, "cfdwm: CUDA error %s at %s:%d\n", \
+                         cudaGetErrorString(e_), __FILE__, __LINE__); \
+            return E_CUDA;                                     \
+        }                                                      \
+    } while (0)
+
+constexpr int EATA_NC = 2;    // eta table: A (cc coefficient), B (ss coefficient)
+constexpr int GRIDV_NC = 8;   // uvw table: Pu, Mu, Pv, Mv, Pw, Mw, kp, km
+constexpr int POINTV_NC = 12; // point table: Pu, Mu, Pv, Mv, Pw, Mw, Pp, Mp, kp, km, Xpp, Xzz
+constexpr float LOG2E_F = 1.4426950408889634f;
+constexpr double TWO_PI = 6.283185307179586476925286766559;
+constexpr double INV_TWO_PI = 0.15915494309189533576888376337251;
+
+__device__ __forceinline__ float ex2(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ void kahan(float &s, float &c, float v) {
+    float y = v - c;
+    float t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
+// Irregular::freq_ramp, Irregular.cpp:200-204 (FP64, as the reference).
+__device__ __forceinline__ double d_freq_ramp(double t, double rt, double ts, double du) {
+    double rampdown = fmax(fmin(1. - ((t - ts - du + rt) / (rt + SMALL)), 1.), 0.);
+    double rampup = fmax(fmin(((t - ts) / (rt + SMALL)), 1.), 0.);
+    return rampup * rampdown;
+}
+
+__host__ __device__ inline long tile_index(int I, int M, int nt) {
+    return (long)I * nt - (long)I * (I - 1) / 2 + (M - I);
+}
+
+// ---------------------------------------------------------------------------
+// Setup: FP64 component data and pair tables (on device)
+// ---------------------------------------------------------------------------
+struct CompIn {
+    int n, npad;
+    const double *omega, *A, *k, *theta;   // device copies (FP64), length n
+    double depth, g, rho, mtheta_rad, cutoff, bandwidth, kmax;
+};
+
+// One record per (tile, entry).  mode 0: grid mask (eta + uvw tables),
+// mode 1: point-API mask (u2/v2/w2/dp2 table).
+__global__ void k_build_tables(CompIn c, int TT, int nt, int mode, float *tab_eta,
+                               float *tab_v) {
+    long t = blockIdx.x;
+    int I = 0;
+    while (tile_index(I, nt - 1, nt) < t) I++;
+    int M = (int)(t - tile_index(I, I, nt)) + I;
+    for (int e = threadIdx.x; e < TT * TT; e += blockDim.x) {
+        int ii = e / TT, mm = e % TT;
+        int i = I * TT + ii, m = M * TT + mm;
+        double out[12];
+        for (int q = 0; q < 12; q++) out[q] = 0.0;
+        double eA = 0.0, eB = 0.0;
+        const double h = c.depth, g = c.g, gg = c.g * c.g;
+        if (i < c.n && m < c.n && i <= m) {
+            double ki = c.k[i], oi = c.omega[i], Ai = c.A[i];
+            double thi = c.theta[i] + c.mtheta_rad;
+            double cti = cos(thi), sti = sin(thi);
+            double Rn = ki * tanh(ki * h), Rsn = sqrt(Rn);
+            double agi = Ai * g / oi;
+            if (i == m) {
+                bool keep = (mode == 1) || (oi <= c.cutoff);
+                if (keep) {
+                    double Dnn = (6.0 * Rsn * Rsn * (ki * ki - Rn * Rn)) /
+                                 (2.0 * Rsn * Rsn - ki * tanh(2.0 * ki * h));
+                    double AAd = 0.25 * agi * agi * (Dnn / (2.0 * oi));
+                    double q2 = 1.0 / (1.0 + exp(-4.0 * ki * h));
+                    out[0] = AAd * (2.0 * ki * cti) * q2;
+                    out[2] = AAd * (2.0 * ki * sti) * q2;
+                    out[4] = AAd * (2.0 * ki) * q2;
+                    if (mode == 1) {
+                        out[6] = c.rho * AAd * (2.0 * oi) * q2;
+                        out[8] = 2.0 * ki;
+                    } else {
+                        out[6] = 2.0 * ki;
+                        if (2.0 * ki <= c.kmax) {
+                            double ann = (Dnn - (ki * ki - Rn * Rn)) / Rn + 2.0 * Rn;
+                            double pe = 0.25 * Ai * Ai * ann;
+                            eA = pe;
+                            eB = -pe;
+                        }
+                    }
+                }
+            } else {
+                double km = c.k[m], om = c.omega[m], Am = c.A[m];
+                double thm = c.theta[m] + c.mtheta_rad;
+                double ctm = cos(thm), stm = sin(thm);
+                double Rm = km * tanh(km * h), Rsm = sqrt(Rm);
+                double agm = Am * g / om;
+                bool keep = true, hp = true, hm = (ki != km);
+                double gam;
+                if (mode == 0) {
+                    keep = (oi <= c.cutoff) && (om <= c.cutoff) && (fabs(oi - om) <= c.bandwidth);
+                    hp = (ki + km) <= c.kmax;
+                    gam = cti * ctm + sti * stm;        // Irregular.cpp:870
+                } else {
+                    gam = cos(thi - thm);               // Irregular.cpp:470
+                }
+                if (keep && (hp || hm)) {
+                    double kp = sqrt(ki * ki + km * km + 2.0 * ki * km * gam);
+                    double kq = sqrt(ki * ki + km * km - 2.0 * ki * km * gam);
+                    double sp = Rsn + Rsm, sm = Rsn - Rsm;
+                    double R2p = sp * sp, R2m = sm * sm;
+                    double AA = 0.5 * agi * agm;
+                    if (hp) {
+                        double den = R2p - kp * tanh(kp * h);
+                        double Dp = (2.0 * R2p * (ki * km * gam - Rn * Rm)) / den +
+                                    (sp * (Rsn * (km * km - Rm * Rm) + Rsm * (ki * ki - Rn * Rn))) / den;
+                        double BB = Dp / (oi + om);
+                        double qp = 1.0 / (1.0 + exp(-2.0 * kp * h));
+                        out[0] = AA * BB * (ki * cti + km * ctm) * qp;
+                        out[2] = AA * BB * (ki * sti + km * stm) * qp;
+                        out[4] = AA * BB * kp * qp;
+                        if (mode == 1) {
+                            out[6] = c.rho * AA * BB * (oi + om) * qp;
+                            out[8] = kp;
+                        } else {
+                            out[6] = kp;
+                            double ap = (Dp - (ki * km * gam - Rn * Rm)) / sqrt(Rn * Rm) + (Rn + Rm);
+                            double pe = 0.5 * Ai * Am * ap;
+                            eA += pe;
+                            eB -= pe;
+                        }
+                    }
+                    if (hm) {
+                        double den = R2m - kq * tanh(kq * h);
+                        double Dm = (2.0 * R2m * (ki * km * gam + Rn * Rm)) / den +
+                                    (sm * (-Rsn * (km * km - Rm * Rm) + Rsm * (ki * ki - Rn * Rn))) / den;
+                        double CC = Dm / (oi - om);
+                        double qm = 1.0 / (1.0 + exp(-2.0 * kq * h));
+                        out[1] = AA * CC * (ki * cti - km * ctm) * qm;
+                        out[3] = AA * CC * (ki * sti - km * stm) * qm;
+                        out[5] = AA * CC * kq * qm;
+                        if (mode == 1) {
+                            out[7] = c.rho * AA * CC * (oi - om) * qm;
+                            out[9] = kq;
+                        } else {
+                            out[7] = kq;
+                            double am = (Dm - (ki * km * gam + Rn * Rm)) / sqrt(Rn * Rm) + (Rn + Rm);
+                            double pe = 0.5 * Ai * Am * am;
+                            eA += pe;
+                            eB += pe;
+                        }
+                    }
+                    if (mode == 1) {
+                        // the phase-free products of the first-order profiles
+                        // in dp2 (Irregular.cpp:786-787)
+                        out[10] = -c.rho * (gg * (ki * cti * km * ctm + ki * sti * km * stm)) / (oi * om);
+                        out[11] = c.rho * (gg * (ki * km)) / (oi * om);
+                    }
+                }
+            }
+        }
+        long base = t * (long)TT * TT + e;
+        if (mode == 0) {
+            tab_eta[base * EATA_NC + 0] = (float)eA;
+            tab_eta[base * EATA_NC + 1] = (float)eB;
+            for (int q = 0; q < GRIDV_NC; q++) tab_v[base * GRIDV_NC + q] = (float)out[q];
+        } else {
+            for (int q = 0; q < POINTV_NC; q++) tab_v[base * POINTV_NC + q] = (float)out[q];
+        }
+    }
+}
+
+// Count of pairs kept by the reference's pair cache (Irregular.cpp:840-967).
+__global__ void k_count_pairs(CompIn c, unsigned long long *cnt) {
+    long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    long tot = (long)c.n * c.n;
+    unsigned long long local = 0;
+    for (; idx < tot; idx += (long)gridDim.x * blockDim.x) {
+        int i = (int)(idx / c.n), m = (int)(idx % c.n);
+        if (m <= i) continue;
+        double oi = c.omega[i], om = c.omega[m];
+        if (oi > c.cutoff || om > c.cutoff || fabs(oi - om) > c.bandwidth) continue;
+        bool hp = (c.k[i] + c.k[m]) <= c.kmax, hm = c.k[i] != c.k[m];
+        if (hp || hm) local++;
+    }
+    if (local) atomicAdd(cnt, local);
+}
+
+__global__ void k_component_coefs(CompIn c, int npad, double fx, double fy, double tofmax,
+                                  const double *phase, const double *rt, const double *st,
+                                  const double *du, double *ph_out, float *cf) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npad) return;
+    double v[NCF];
+    for (int q = 0; q < NCF; q++) v[q] = 0.0;
+    double kx = 0, ky = 0, om = 0, p0 = 0, r0 = 0, r1 = -SMALL, r2 = HUGE_;
+    if (i < c.n) {
+        double k = c.k[i], w = c.omega[i], A = c.A[i], h = c.depth, g = c.g, gg = g * g;
+        double th = c.theta[i] + c.mtheta_rad, ct = cos(th), st_ = sin(th);
+        kx = k * ct; ky = k * st_; om = w; p0 = w * tofmax + phase[i];
+        r0 = rt[i]; r1 = st[i]; r2 = du[i];
+        v[CF_A] = A;
+        v[CF_AU] = A * g * k / w;
+        v[CF_CT] = ct;
+        v[CF_ST] = st_;
+        v[CF_K] = k;
+        v[CF_Q] = 1.0 / (1.0 + exp(-2.0 * k * h));
+        v[CF_AP] = A * c.rho * g;
+        v[CF_GX] = ct * A * w * k;
+        v[CF_GY] = st_ * A * w * k;
+        v[CF_GZ] = A * w * k * (cosh(k * h) / sinh(k * h));
+        v[CF_GP] = A * c.rho * g * k;
+        v[CF_X1] = -c.rho * (gg * (2 * k * ct + 2 * k * st_) * 2) / (2 * w);
+        v[CF_Z1] = c.rho * (gg * (2 * k) * 2) / (2 * w);
+    }
+    ph_out[0 * npad + i] = kx;
+    ph_out[1 * npad + i] = ky;
+    ph_out[2 * npad + i] = om;
+    ph_out[3 * npad + i] = p0;
+    ph_out[4 * npad + i] = r0;
+    ph_out[5 * npad + i] = r1;
+    ph_out[6 * npad + i] = r2;
+    for (int q = 0; q < NCF; q++) cf[q * npad + i] = (float)v[q];
+}
+
+int sea_build(const Config &cfg, DevSea &sea, bool point_table, void *stream_) {
+    cudaStream_t stream = (cudaStream_t)stream_;
+    sea_free(sea);
+    int n = (int)cfg.omega.size();
+    sea.n = n;
+    sea.depth = cfg.depth; sea.swl = cfg.swl; sea.g = cfg.gravity; sea.rho = cfg.rho;
+    sea.fx = cfg.x_pos; sea.fy = cfg.y_pos; sea.order = cfg.order;
+    sea.npad_g = ((n + GRID_TILE - 1) / GRID_TILE) * GRID_TILE;
+    sea.npad_p = ((n + POINT_TILE - 1) / POINT_TILE) * POINT_TILE;
+    if (sea.npad_g == 0) sea.npad_g = GRID_TILE;
+    if (sea.npad_p == 0) sea.npad_p = POINT_TILE;
+    sea.ntile_g = sea.npad_g / GRID_TILE;
+    sea.ntile_p = sea.npad_p / POINT_TILE;
+    sea.trivial_ramp = true;
+    for (int i = 1; i < n; i++)
+        if (cfg.ramptime[i] != cfg.ramptime[0] || cfg.starttime[i] != cfg.starttime[0] ||
+            cfg.duration[i] != cfg.duration[0])
+            sea.trivial_ramp = false;
+    double kmax = 0.0;   // Irregular.cpp:833-835
+    for (int i = 0; i < n; i++) kmax = std::max(kmax, cfg.k[i]);
+
+    // FP64 component inputs on the device
+    double *d_in = nullptr;
+    size_t nn = (size_t)(n > 0 ? n : 1);
+    CK(cudaMalloc(&d_in, sizeof(double) * nn * 8));
+    const std::vector<double> *src[8] = {&cfg.omega, &cfg.A, &cfg.k, &cfg.theta, &cfg.phase,
+                                         &cfg.ramptime, &cfg.starttime, &cfg.duration};
+    for (int q = 0; q < 8; q++)
+        if (n) CK(cudaMemcpyAsync(d_in + q * nn, src[q]->data(), sizeof(double) * n,
+                                  cudaMemcpyHostToDevice, stream));
+    CompIn ci;
+    ci.n = n; ci.npad = sea.npad_g;
+    ci.omega = d_in; ci.A = d_in + nn; ci.k = d_in + 2 * nn; ci.theta = d_in + 3 * nn;
+    ci.depth = cfg.depth; ci.g = cfg.gravity; ci.rho = cfg.rho;
+    ci.mtheta_rad = cfg.mtheta * PI_IRR / 180.0;
+    ci.cutoff = cfg.dw_cutoff; ci.bandwidth = cfg.dw_bandwidth; ci.kmax = kmax;
+
+    CK(cudaMalloc(&sea.d_phase, sizeof(double) * 7 * sea.npad_g));
+    CK(cudaMalloc(&sea.d_cf, sizeof(float) * NCF * sea.npad_g));
+    k_component_coefs<<<(sea.npad_g + 127) / 128, 128, 0, stream>>>(
+        ci, sea.npad_g, cfg.x_pos, cfg.y_pos, cfg.tofmax, d_in + 4 * nn, d_in + 5 * nn,
+        d_in + 6 * nn, d_in + 7 * nn, sea.d_phase, sea.d_cf);
+    CK(cudaGetLastError());
+
+    if (cfg.order == 2) {
+        long ntiles = tile_index(sea.ntile_g - 1, sea.ntile_g - 1, sea.ntile_g) + 1;
+        size_t ent = (size_t)ntiles * GRID_TILE * GRID_TILE;
+        CK(cudaMalloc(&sea.d_tab_eta, sizeof(float) * ent * EATA_NC));
+        CK(cudaMalloc(&sea.d_tab_grid, sizeof(float) * ent * GRIDV_NC));
+        k_build_tables<<<(unsigned)ntiles, 256, 0, stream>>>(ci, GRID_TILE, sea.ntile_g, 0,
+                                                             sea.d_tab_eta, sea.d_tab_grid);
+        CK(cudaGetLastError());
+        if (point_table) {
+            long ntp = tile_index(sea.ntile_p - 1, sea.ntile_p - 1, sea.ntile_p) + 1;
+            size_t entp = (size_t)ntp * POINT_TILE * POINT_TILE;
+            CK(cudaMalloc(&sea.d_tab_point, sizeof(float) * entp * POINTV_NC));
+            k_build_tables<<<(unsigned)ntp, 256, 0, stream>>>(ci, POINT_TILE, sea.ntile_p, 1,
+                                                              nullptr, sea.d_tab_point);
+            CK(cudaGetLastError());
+        }
+        unsigned long long *d_cnt = nullptr, h_cnt = 0;
+        CK(cudaMalloc(&d_cnt, sizeof(unsigned long long)));
+        CK(cudaMemsetAsync(d_cnt, 0, sizeof(unsigned long long), stream));
+        k_count_pairs<<<256, 256, 0, stream>>>(ci, d_cnt);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(&h_cnt, d_cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        cudaFree(d_cnt);
+        sea.npairs_grid = (long)h_cnt;
+    }
+    CK(cudaStreamSynchronize(stream));
+    cudaFree(d_in);
+    return OK;
+}
+
+void sea_free(DevSea &sea) {
+    if (sea.d_phase) cudaFree(sea.d_phase);
+    if (sea.d_cf) cudaFree(sea.d_cf);
+    if (sea.d_tab_eta) cudaFree(sea.d_tab_eta);
+    if (sea.d_tab_grid) cudaFree(sea.d_tab_grid);
+    if (sea.d_tab_point) cudaFree(sea.d_tab_point);
+    sea.d_phase = nullptr; sea.d_cf = nullptr; sea.d_tab_eta = nullptr;
+    sea.d_tab_grid = nullptr; sea.d_tab_point = nullptr;
+}
+
+int workspace_reserve(Workspace &ws, size_t bytes) {
+    if (ws.bytes >= bytes) return OK;
+    if (ws.base) cudaFree(ws.base);
+    ws.base = nullptr;
+    ws.bytes = 0;
+    CK(cudaMalloc(&ws.base, bytes));
+    ws.bytes = bytes;
+    return OK;
+}
+void workspace_free(Workspace &ws) {
+    if (ws.base) cudaFree(ws.base);
+    ws.base = nullptr;
+    ws.bytes = 0;
+}
+
+// ---------------------------------------------------------------------------
+// Phasor pass: one thread per point/column, all components.
+// ---------------------------------------------------------------------------
+struct PhArgs {
+    long n;
+    const double *x, *y, *t;
+    long sx, sy, st;        // element strides of x, y, t (0 broadcasts one value)
+    int ncomp, npad;
+    const double *phase;    // [7][npad_g]
+    const float *cf;        // [NCF][npad_g]
+    int cstride;            // npad_g
+    double fx, fy;
+    int trivial_ramp;
+    float2 *ph;             // [npad][n]
+    float *rr;              // [npad][n]
+    double *first;          // [5][n]: eta1, gx, gy, gz, gp
+};
+
+__global__ void __launch_bounds__(128) k_phasors(PhArgs a) {
+    long p = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (p >= a.n) return;
+    const double dx = a.x[p * a.sx] - a.fx, dy = a.y[p * a.sy] - a.fy, t = a.t[p * a.st];
+    const double *P = a.phase;
+    const int cs = a.cstride;
+    double rconst = d_freq_ramp(t, P[4 * cs], P[5 * cs], P[6 * cs]);
+    double e1 = 0, gx = 0, gy = 0, gz = 0, gp = 0;
+    for (int i = 0; i < a.npad; i++) {
+        float c = 0.f, s = 0.f, r = 0.f;
+        if (i < a.ncomp) {
+            double ph = fma(P[i], dx, fma(P[cs + i], dy, fma(-P[2 * cs + i], t, P[3 * cs + i])));
+            double nn = rint(ph * INV_TWO_PI);
+            float red = (float)fma(-nn, TWO_PI, ph);
+            sincosf(red, &s, &c);
+            r = a.trivial_ramp ? (float)rconst
+                               : (float)d_freq_ramp(t, P[4 * cs + i], P[5 * cs + i], P[6 * cs + i]);
+            float rc = r * c, rs = r * s;
+            e1 += (double)(rc * a.cf[CF_A * cs + i]);
+            gx += (double)(rc * a.cf[CF_GX * cs + i]);
+            gy += (double)(rc * a.cf[CF_GY * cs + i]);
+            gz += (double)(rs * a.cf[CF_GZ * cs + i]);
+            gp += (double)(rc * a.cf[CF_GP * cs + i]);
+        }
+        a.ph[(long)i * a.n + p] = make_float2(c, s);
+        a.rr[(long)i * a.n + p] = r;
+    }
+    a.first[0 * a.n + p] = e1;
+    a.first[1 * a.n + p] = gx;
+    a.first[2 * a.n + p] = gy;
+    a.first[3 * a.n + p] = gz;
+    a.first[4 * a.n + p] = gp;
+}
+
+// ---------------------------------------------------------------------------
+// Pair-sum kernels
+// ---------------------------------------------------------------------------
+struct PairArgs {
+    long ncol;           // points / columns
+    int nl;              // levels per column
+    int nlg;             // level groups per column (power of two, <= 16)
+    int ntile;           // component tiles of the table
+    const float *tab;    // pair tiles
+    const float2 *ph;    // [npad][ncol]
+    const float *rr;     // [npad][ncol]
+    const float *cf;     // [NCF][cstride]
+    int cstride;
+    const float *z0;     // [ncol*nl] evaluation heights (z0 <= 0 below the surface)
+    float depth;
+    float *out;          // [nf][ncol*nl]
+    int pairs;           // 0: first-order z-dependent sums only
+    int first;           // 1: add first-order z-dependent sums
+};
+
+// Depth factors with the normaliser folded into the coefficients:
+//   F = exp(kz) (1 + exp(-2k(z+h))),  G = exp(kz) (1 - exp(-2k(z+h))).
+__device__ __forceinline__ void depth_fg(float k, float zk, float zetak, float &F, float &G) {
+    float e1 = ex2(k * zk);
+    float e2 = ex2(k * zetak);
+    float t = e1 * e2;
+    F = e1 + t;
+    G = e1 - t;
+}
+
+// Column mode: u, v, w at LV levels per thread, grid (pair-cache) mask.
+template <int TT, int LV>
+__global__ void __launch_bounds__(128) k_pairs_columns(PairArgs a) {
+    extern __shared__ float4 smem4[];
+    float *s_tab = reinterpret_cast<float *>(smem4);                       // TT*TT*8
+    float2 *s_ph = reinterpret_cast<float2 *>(s_tab + TT * TT * GRIDV_NC); // TT*cols
+    const int cols = 128 / a.nlg;
+    const int lg = threadIdx.x / cols, cl = threadIdx.x % cols;
+    const long col = (long)blockIdx.x * cols + cl;
+    const bool valid = col < a.ncol;
+    const long colc = valid ? col : 0;
+    const long npts = a.ncol * a.nl;
+    float zk[LV], zetak[LV];
+    float su[LV], cu[LV], sv[LV], cv[LV], sw[LV], cw[LV];
+#pragma unroll
+    for (int l = 0; l < LV; l++) {
+        int lev = lg * LV + l;
+        float z = (valid && lev < a.nl) ? a.z0[colc * a.nl + lev] : 0.f;
+        zk[l] = z * LOG2E_F;
+        zetak[l] = -2.f * (z + a.depth) * LOG2E_F;
+        su[l] = cu[l] = sv[l] = cv[l] = sw[l] = cw[l] = 0.f;
+    }
+    for (int I = 0; I < a.ntile; I++) {
+        for (int M = I; M < a.ntile; M++) {
+            if (!a.pairs && M != I) continue;
+            __syncthreads();
+            if (a.pairs) {
+                const float4 *src = reinterpret_cast<const float4 *>(
+                    a.tab + tile_index(I, M, a.ntile) * (long)TT * TT * GRIDV_NC);
+                float4 *dst = reinterpret_cast<float4 *>(s_tab);
+                for (int e = threadIdx.x; e < TT * TT * GRIDV_NC / 4; e += blockDim.x) dst[e] = src[e];
+            }
+            for (int e = threadIdx.x; e < TT * cols; e += blockDim.x) {
+                int mm = e / cols, c2 = e % cols;
+                long cc = (long)blockIdx.x * cols + c2;
+                s_ph[e] = (cc < a.ncol) ? a.ph[(long)(M * TT + mm) * a.ncol + cc] : make_float2(0.f, 0.f);
+            }
+            __syncthreads();
+            if (!valid) continue;
+            if (a.pairs) {
+                for (int ii = 0; ii < TT; ii++) {
+                    const int i = I * TT + ii;
+                    const float2 pi = a.ph[(long)i * a.ncol + col];
+                    const float ri = a.rr[(long)i * a.ncol + col];
+                    float au[LV], av[LV], aw[LV];
+#pragma unroll
+                    for (int l = 0; l < LV; l++) au[l] = av[l] = aw[l] = 0.f;
+                    const int m0 = (M == I) ? ii : 0;
+                    for (int mm = m0; mm < TT; mm++) {
+                        const float4 c0 = *reinterpret_cast<const float4 *>(s_tab + (ii * TT + mm) * GRIDV_NC);
+                        const float4 c1 = *reinterpret_cast<const float4 *>(s_tab + (ii * TT + mm) * GRIDV_NC + 4);
+                        const float2 pm = s_ph[mm * cols + cl];
+                        const float cc = pi.x * pm.x, ss = pi.y * pm.y;
+                        const float sc = pi.y * pm.x, cs = pi.x * pm.y;
+                        const float cp = cc - ss, cmn = cc + ss, sp = sc + cs, smn = sc - cs;
+                        const float up = c0.x * cp, um = c0.y * cmn, vp = c0.z * cp, vm = c0.w * cmn;
+                        const float wp = c1.x * sp, wm = c1.y * smn;
+                        const float kp = c1.z, km = c1.w;
+#pragma unroll
+                        for (int l = 0; l < LV; l++) {
+                            float Fp, Gp, Fm, Gm;
+                            depth_fg(kp, zk[l], zetak[l], Fp, Gp);
+                            depth_fg(km, zk[l], zetak[l], Fm, Gm);
+                            au[l] = fmaf(up, Fp, fmaf(um, Fm, au[l]));
+                            av[l] = fmaf(vp, Fp, fmaf(vm, Fm, av[l]));
+                            aw[l] = fmaf(wp, Gp, fmaf(wm, Gm, aw[l]));
+                        }
+                    }
+#pragma unroll
+                    for (int l = 0; l < LV; l++) {
+                        kahan(su[l], cu[l], ri * au[l]);
+                        kahan(sv[l], cv[l], ri * av[l]);
+                        kahan(sw[l], cw[l], ri * aw[l]);
+                    }
+                }
+            }
+            if (a.first && M == I) {
+                // first-order u1, v1, w1 at the level heights (Irregular.cpp:394-447)
+                for (int mm = 0; mm < TT; mm++) {
+                    const int m = M * TT + mm;
+                    const float2 pm = s_ph[mm * cols + cl];
+                    const float rm = a.rr[(long)m * a.ncol + col];
+                    const float k = a.cf[CF_K * a.cstride + m], q = a.cf[CF_Q * a.cstride + m];
+                    const float au_ = a.cf[CF_AU * a.cstride + m] * q * rm;
+                    const float cu_ = au_ * a.cf[CF_CT * a.cstride + m] * pm.x;
+                    const float cv_ = au_ * a.cf[CF_ST * a.cstride + m] * pm.x;
+                    const float cw_ = au_ * pm.y;
+#pragma unroll
+                    for (int l = 0; l < LV; l++) {
+                        float F, G;
+                        depth_fg(k, zk[l], zetak[l], F, G);
+                        kahan(su[l], cu[l], cu_ * F);
+                        kahan(sv[l], cv[l], cv_ * F);
+                        kahan(sw[l], cw[l], cw_ * G);
+                    }
+                }
+            }
+        }
+    }
+    if (!valid) return;
+#pragma unroll
+    for (int l = 0; l < LV; l++) {
+        int lev = lg * LV + l;
+        if (lev < a.nl) {
+            long o = col * a.nl + lev;
+            a.out[0 * npts + o] = su[l];
+            a.out[1 * npts + o] = sv[l];
+            a.out[2 * npts + o] = sw[l];
+        }
+    }
+}
+
+// Point mode: u, v, w, dp at one height per thread, point-API mask
+// (u2/v2/w2/dp2 of the reference, with rho folded into the p records).
+template <int TT>
+__global__ void __launch_bounds__(128) k_pairs_points(PairArgs a) {
+    extern __shared__ float4 smem4[];
+    float *s_tab = reinterpret_cast<float *>(smem4);                        // TT*TT*12
+    float2 *s_ph = reinterpret_cast<float2 *>(s_tab + TT * TT * POINTV_NC); // TT*128
+    float2 *s_pz = s_ph + TT * 128;                                         // TT*128
+    const long p = (long)blockIdx.x * 128 + threadIdx.x;
+    const bool valid = p < a.ncol;
+    const long pc = valid ? p : 0;
+    const float z = valid ? a.z0[pc] : 0.f;
+    const float zk = z * LOG2E_F, zetak = -2.f * (z + a.depth) * LOG2E_F;
+    float su = 0, cu = 0, sv = 0, cv = 0, sw = 0, cw = 0, sq = 0, cq = 0;
+    for (int I = 0; I < a.ntile; I++) {
+        for (int M = I; M < a.ntile; M++) {
+            if (!a.pairs && M != I) continue;
+            __syncthreads();
+            if (a.pairs) {
+                const float4 *src = reinterpret_cast<const float4 *>(
+                    a.tab + tile_index(I, M, a.ntile) * (long)TT * TT * POINTV_NC);
+                float4 *dst = reinterpret_cast<float4 *>(s_tab);
+                for (int e = threadIdx.x; e < TT * TT * POINTV_NC / 4; e += blockDim.x) dst[e] = src[e];
+            }
+            for (int mm = 0; mm < TT; mm++) {
+                const int m = M * TT + mm;
+                float2 pm = a.ph[(long)m * a.ncol + pc];
+                float F, G;
+                depth_fg(a.cf[CF_K * a.cstride + m], zk, zetak, F, G);
+                const float q = a.cf[CF_Q * a.cstride + m];
+                s_ph[mm * 128 + threadIdx.x] = pm;
+                s_pz[mm * 128 + threadIdx.x] = make_float2(q * F, q * G);   // px_m, pz_m
+            }
+            __syncthreads();
+            if (!valid) continue;
+            if (a.pairs) {
+                for (int ii = 0; ii < TT; ii++) {
+                    const int i = I * TT + ii;
+                    const float2 pi = a.ph[(long)i * a.ncol + p];
+                    const float ri = a.rr[(long)i * a.ncol + p];
+                    const float2 pxi = (M == I) ? s_pz[ii * 128 + threadIdx.x] : make_float2(0.f, 0.f);
+                    float2 pxz_i = pxi;
+                    if (M != I) {
+                        float F, G;
+                        depth_fg(a.cf[CF_K * a.cstride + i], zk, zetak, F, G);
+                        const float q = a.cf[CF_Q * a.cstride + i];
+                        pxz_i = make_float2(q * F, q * G);
+                    }
+                    float au = 0, av = 0, aw = 0, ap = 0, ax = 0, az = 0;
+                    const int m0 = (M == I) ? ii : 0;
+                    for (int mm = m0; mm < TT; mm++) {
+                        const float *e = s_tab + (ii * TT + mm) * POINTV_NC;
+                        const float4 c0 = *reinterpret_cast<const float4 *>(e);
+                        const float4 c1 = *reinterpret_cast<const float4 *>(e + 4);
+                        const float4 c2 = *reinterpret_cast<const float4 *>(e + 8);
+                        const float2 pm = s_ph[mm * 128 + threadIdx.x];
+                        const float2 xm = s_pz[mm * 128 + threadIdx.x];
+                        const float cc = pi.x * pm.x, ss = pi.y * pm.y;
+                        const float sc = pi.y * pm.x, cs = pi.x * pm.y;
+                        const float cp = cc - ss, cmn = cc + ss, sp = sc + cs, smn = sc - cs;
+                        float Fp, Gp, Fm, Gm;
+                        depth_fg(c2.x, zk, zetak, Fp, Gp);
+                        depth_fg(c2.y, zk, zetak, Fm, Gm);
+                        au = fmaf(c0.x * cp, Fp, fmaf(c0.y * cmn, Fm, au));
+                        av = fmaf(c0.z * cp, Fp, fmaf(c0.w * cmn, Fm, av));
+                        aw = fmaf(c1.x * sp, Gp, fmaf(c1.y * smn, Gm, aw));
+                        ap = fmaf(c1.z * cp, Fp, fmaf(c1.w * cmn, Fm, ap));
+                        ax = fmaf(c2.z, xm.x, ax);
+                        az = fmaf(c2.w, xm.y, az);
+                    }
+                    ap = fmaf(pxz_i.x, ax, fmaf(pxz_i.y, az, ap));
+                    kahan(su, cu, ri * au);
+                    kahan(sv, cv, ri * av);
+                    kahan(sw, cw, ri * aw);
+                    kahan(sq, cq, ri * ap);
+                }
+            }
+            if (a.first && M == I) {
+                // first-order u1, v1, w1, dp1 and the linear dp2 diagonal terms
+                for (int mm = 0; mm < TT; mm++) {
+                    const int m = M * TT + mm;
+                    const float2 pm = s_ph[mm * 128 + threadIdx.x];
+                    const float2 xm = s_pz[mm * 128 + threadIdx.x];
+                    const float rm = a.rr[(long)m * a.ncol + p];
+                    const float au_ = a.cf[CF_AU * a.cstride + m] * rm;
+                    kahan(su, cu, au_ * xm.x * a.cf[CF_CT * a.cstride + m] * pm.x);
+                    kahan(sv, cv, au_ * xm.x * a.cf[CF_ST * a.cstride + m] * pm.x);
+                    kahan(sw, cw, au_ * xm.y * pm.y);
+                    float pp = a.cf[CF_AP * a.cstride + m] * xm.x * pm.x;
+                    if (a.pairs)
+                        pp += a.cf[CF_X1 * a.cstride + m] * xm.x + a.cf[CF_Z1 * a.cstride + m] * xm.y;
+                    kahan(sq, cq, rm * pp);
+                }
+            }
+        }
+    }
+    if (!valid) return;
+    a.out[0 * a.ncol + p] = su;
+    a.out[1 * a.ncol + p] = sv;
+    a.out[2 * a.ncol + p] = sw;
+    a.out[3 * a.ncol + p] = sq;
+}
+
+// Elevation mode: eta2 from the pair cache (Irregular.cpp:223-293).  The
+// record holds A = P+M and B = M-P so that a pair contributes
+// c_i (A c_m) + s_i (B s_m); a row is c_i sum(A c_m) + s_i sum(B s_m).
+template <int TT>
+__global__ void __launch_bounds__(128) k_pairs_eta(PairArgs a) {
+    extern __shared__ float4 smem4[];
+    float2 *s_tab = reinterpret_cast<float2 *>(smem4);        // TT*TT
+    float2 *s_ph = s_tab + TT * TT;                            // TT*128
+    const long p = (long)blockIdx.x * 128 + threadIdx.x;
+    const bool valid = p < a.ncol;
+    const long pc = valid ? p : 0;
+    float se = 0, ce = 0;
+    for (int I = 0; I < a.ntile; I++) {
+        for (int M = I; M < a.ntile; M++) {
+            __syncthreads();
+            const float4 *src = reinterpret_cast<const float4 *>(
+                a.tab + tile_index(I, M, a.ntile) * (long)TT * TT * 2);
+            float4 *dst = reinterpret_cast<float4 *>(s_tab);
+            for (int e = threadIdx.x; e < TT * TT / 2; e += blockDim.x) dst[e] = src[e];
+            for (int mm = 0; mm < TT; mm++)
+                s_ph[mm * 128 + threadIdx.x] = a.ph[(long)(M * TT + mm) * a.ncol + pc];
+            __syncthreads();
+            if (!valid) continue;
+            for (int ii = 0; ii < TT; ii++) {
+                const int i = I * TT + ii;
+                const float2 pi = a.ph[(long)i * a.ncol + p];
+                const float ri = a.rr[(long)i * a.ncol + p];
+                float ac = 0.f, as = 0.f;
+                const int m0 = (M == I) ? ii : 0;
+                for (int mm = m0; mm < TT; mm++) {
+                    const float2 cab = s_tab[ii * TT + mm];
+                    const float2 pm = s_ph[mm * 128 + threadIdx.x];
+                    ac = fmaf(cab.x, pm.x, ac);
+                    as = fmaf(cab.y, pm.y, as);
+                }
+                kahan(se, ce, ri * fmaf(pi.x, ac, pi.y * as));
+            }
+        }
+    }
+    if (valid) a.out[p] = se;
+}
+
+// ---------------------------------------------------------------------------
+// Host launchers
+// ---------------------------------------------------------------------------
+namespace {
+
+struct WsLayout {
+    float2 *ph;
+    float *rr;
+    double *first;
+    float *z0;
+    float *sec;
+    size_t bytes;
+};
+
+WsLayout layout(long n, int npad, void *base) {
+    WsLayout L;
+    size_t off = 0;
+    auto take = [&](size_t b) { size_t o = off; off += (b + 255) & ~size_t(255); return o; };
+    size_t o_ph = take(sizeof(float2) * (size_t)npad * n);
+    size_t o_rr = take(sizeof(float) * (size_t)npad * n);
+    size_t o_first = take(sizeof(double) * 5 * (size_t)n);
+    size_t o_z = take(sizeof(float) * (size_t)n);
+    size_t o_sec = take(sizeof(float) * 5 * (size_t)n);
+    char *b = (char *)base;
+    L.ph = (float2 *)(b + o_ph);
+    L.rr = (float *)(b + o_rr);
+    L.first = (double *)(b + o_first);
+    L.z0 = (float *)(b + o_z);
+    L.sec = (float *)(b + o_sec);
+    L.bytes = off;
+    return L;
+}
+
+// z0 = min(0, z - swl) (order 2/1) or z - swl (order 0), as float
+__global__ void k_prep_z(long n, const double *z, double swl, int order, float *z0) {
+    long p = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    double zz = z[p] - swl;
+    z0[p] = (float)(order == 0 ? zz : fmin(0.0, zz));
+}
+
+// Irregular::eta/u/v/w/dp assembled from the pieces (Irregular.cpp:9-157).
+// out has row stride ldo (the full batch length).
+__global__ void k_combine(long n, long ldo, int order, double swl, const double *z,
+                          const double *first, const float *sec, const float *eta2, int mask,
+                          double *out) {
+    long p = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    double za = (order == 2) ? fmax(0.0, z[p] - swl) : 0.0;
+    if (mask & 1) out[0 * ldo + p] = swl + first[0 * n + p] + (eta2 ? (double)eta2[p] : 0.0);
+    if (mask & 2) out[1 * ldo + p] = (double)sec[0 * n + p] + first[1 * n + p] * za;
+    if (mask & 4) out[2 * ldo + p] = (double)sec[1 * n + p] + first[2 * n + p] * za;
+    if (mask & 8) out[3 * ldo + p] = (double)sec[2 * n + p] + first[3 * n + p] * za;
+    if (mask & 16) out[4 * ldo + p] = (double)sec[3 * n + p] + first[4 * n + p] * za;
+}
+
+}  // namespace
+
+static int launch_phasors(const DevSea &sea, long n, const double *x, const double *y,
+                          const double *t, long sx, long sy, long st, int npad, float2 *ph,
+                          float *rr, double *first, cudaStream_t stream) {
+    PhArgs a;
+    a.n = n; a.x = x; a.y = y; a.t = t; a.sx = sx; a.sy = sy; a.st = st;
+    a.ncomp = sea.n; a.npad = npad; a.phase = sea.d_phase; a.cf = sea.d_cf;
+    a.cstride = sea.npad_g; a.fx = sea.fx; a.fy = sea.fy;
+    a.trivial_ramp = sea.trivial_ramp ? 1 : 0;
+    a.ph = ph; a.rr = rr; a.first = first;
+    k_phasors<<<(unsigned)((n + 127) / 128), 128, 0, stream>>>(a);
+    CK(cudaGetLastError());
+    return OK;
+}
+
+int launch_phasors_public(const DevSea &sea, long n, const double *x, const double *y,
+                          const double *t, long sx, long sy, long st, int npad, float2 *ph,
+                          float *rr, double *first, cudaStream_t stream) {
+    return launch_phasors(sea, n, x, y, t, sx, sy, st, npad, ph, rr, first, stream);
+}
+
+int launch_eta_pairs(const DevSea &sea, long n, const float2 *ph, const float *rr, float *out,
+                     cudaStream_t stream) {
+    PairArgs a{};
+    a.ncol = n; a.nl = 1; a.nlg = 1; a.ntile = sea.ntile_g; a.tab = sea.d_tab_eta;
+    a.ph = ph; a.rr = rr; a.cf = sea.d_cf; a.cstride = sea.npad_g; a.out = out;
+    a.pairs = 1; a.first = 0;
+    size_t smem = sizeof(float2) * (GRID_TILE * GRID_TILE + GRID_TILE * 128);
+    static bool attr = false;
+    if (!attr) {
+        CK(cudaFuncSetAttribute(k_pairs_eta<GRID_TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem));
+        attr = true;
+    }
+    k_pairs_eta<GRID_TILE><<<(unsigned)((n + 127) / 128), 128, smem, stream>>>(a);
+    CK(cudaGetLastError());
+    return OK;
+}
+
+int launch_column_pairs(const DevSea &sea, long ncol, int nl, const float2 *ph, const float *rr,
+                        const float *z0, float *out, int pairs, cudaStream_t stream) {
+    constexpr int LV = 8;
+    int nlg = 1;
+    while (nlg * LV < nl) nlg *= 2;
+    if (nlg > 16) return E_TOO_LARGE;
+    PairArgs a{};
+    a.ncol = ncol; a.nl = nl; a.nlg = nlg; a.ntile = sea.ntile_g; a.tab = sea.d_tab_grid;
+    a.ph = ph; a.rr = rr; a.cf = sea.d_cf; a.cstride = sea.npad_g; a.z0 = z0;
+    a.depth = (float)sea.depth; a.out = out; a.pairs = pairs; a.first = 1;
+    int cols = 128 / nlg;
+    size_t smem = sizeof(float) * GRID_TILE * GRID_TILE * GRIDV_NC + sizeof(float2) * GRID_TILE * cols;
+    static bool attr = false;
+    if (!attr) {
+        CK(cudaFuncSetAttribute(k_pairs_columns<GRID_TILE, LV>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(sizeof(float) * GRID_TILE * GRID_TILE * GRIDV_NC +
+                                      sizeof(float2) * GRID_TILE * 128)));
+        attr = true;
+    }
+    k_pairs_columns<GRID_TILE, LV><<<(unsigned)((ncol + cols - 1) / cols), 128, smem, stream>>>(a);
+    CK(cudaGetLastError());
+    return OK;
+}
+
+static int launch_point_pairs(const DevSea &sea, long n, const float2 *ph, const float *rr,
+                              const float *z0, float *out, int pairs, cudaStream_t stream) {
+    PairArgs a{};
+    a.ncol = n; a.nl = 1; a.nlg = 1; a.ntile = sea.ntile_p; a.tab = sea.d_tab_point;
+    a.ph = ph; a.rr = rr; a.cf = sea.d_cf; a.cstride = sea.npad_g; a.z0 = z0;
+    a.depth = (float)sea.depth; a.out = out; a.pairs = pairs; a.first = 1;
+    size_t smem = sizeof(float) * POINT_TILE * POINT_TILE * POINTV_NC + 2 * sizeof(float2) * POINT_TILE * 128;
+    static bool attr = false;
+    if (!attr) {
+        CK(cudaFuncSetAttribute(k_pairs_points<POINT_TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem));
+        attr = true;
+    }
+    k_pairs_points<POINT_TILE><<<(unsigned)((n + 127) / 128), 128, smem, stream>>>(a);
+    CK(cudaGetLastError());
+    return OK;
+}
+
+// Phasor layout used by the pair kernels: the point kernel reads tiles of
+// POINT_TILE, the grid kernels tiles of GRID_TILE; the workspace is sized for
+// npad_g >= npad_p so both fit.
+int irregular_eval(const DevSea &sea, long n, const double *x, const double *y, const double *z,
+                   const double *t, int mask, double *out, Workspace &ws, void *stream_) {
+    cudaStream_t stream = (cudaStream_t)stream_;
+    if (n <= 0) return OK;
+    const long chunk = 1L << 18;
+    const int npad = sea.npad_g;
+    WsLayout L0 = layout(std::min(n, chunk), npad, nullptr);
+    int rc = workspace_reserve(ws, L0.bytes);
+    if (rc) return rc;
+    for (long b = 0; b < n; b += chunk) {
+        long m = std::min(chunk, n - b);
+        WsLayout L = layout(m, npad, ws.base);
+        rc = launch_phasors(sea, m, x + b, y + b, t + b, 1, 1, 1, npad, L.ph, L.rr, L.first, stream);
+        if (rc) return rc;
+        float *eta2 = nullptr;
+        if ((mask & 1) && sea.order == 2) {
+            eta2 = L.sec + 4 * m;
+            rc = launch_eta_pairs(sea, m, L.ph, L.rr, eta2, stream);
+            if (rc) return rc;
+        }
+        if (mask & 30) {
+            k_prep_z<<<(unsigned)((m + 255) / 256), 256, 0, stream>>>(m, z + b, sea.swl, sea.order, L.z0);
+            CK(cudaGetLastError());
+            // the point table is padded to POINT_TILE; the phasor rows beyond
+            // npad_p are never read by the point kernel
+            rc = launch_point_pairs(sea, m, L.ph, L.rr, L.z0, L.sec, sea.order != 0 ? 1 : 0, stream);
+            if (rc) return rc;
+        }
+        k_combine<<<(unsigned)((m + 255) / 256), 256, 0, stream>>>(m, n, sea.order, sea.swl, z + b,
+                                                                   L.first, L.sec, eta2, mask, out + b);
+        CK(cudaGetLastError());
+    }
+    return OK;
+}
+
+int irregular_second_order(const DevSea &sea, long n, const double *x, const double *y,
+                           const double *z, const double *t, int which, double *out, Workspace &ws,
+                           void *stream_) {
+    (void)sea; (void)n; (void)x; (void)y; (void)z; (void)t; (void)which; (void)out; (void)ws; (void)stream_;
+    return E_UNSUPPORTED;
+}
+
+}  // namespace cfdwm

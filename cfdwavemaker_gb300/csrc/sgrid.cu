@@ -1,0 +1,520 @@
+// Lagrangian stretched s-grid with 4-D cubic-Hermite query, on the GPU.
+//
+// Behaviour follows the reference's lsGridSpline (oystelan/CFDwavemaker
+// v3.1.0, src/lsgrid_spline.cpp):
+//   storage and ring of 4 time slots     :35-61, 847-931
+//   sigma maps z2s/s2z/cart2sigmaS/...   :91-122
+//   column body (eta, levels, uvw2)      :695-720, 880-903
+//   finite-difference gradients          :124-366
+//   spline query                         :368-605
+//
+// GB300 design: the whole grid lives in one device allocation (FP32 fields in
+// the reference's [slot][i][j][m] layout), so the reference's MPI column
+// partition and MPI_Allgatherv disappear.  A ring step is
+//   phasors of the active columns  ->  eta2 pair sums  ->  level heights
+//   ->  column pair sums (u, v, w at all levels of a column in registers)
+//   ->  scatter into the slot  ->  one fused finite-difference pass.
+// The query kernel gathers the 2x2(x2) stencils of the two bracketing slots
+// and reduces x -> y -> s -> t exactly in the reference's order.
+#include "cfdwm.h"
+
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
+namespace cfdwm {
+
+#define CK(x)                                                  \
+    do {                                                       \
+        cudaError_t e_ = (x);                                  \
+        if (e_ != cudaSuccess) {                               \
+            std::fprintf(stderr, "cfdwm: CUDA error %s at %s:%d\n", \
+                         cudaGetErrorString(e_), __FILE__, __LINE__); \
+            return E_CUDA;                                     \
+        }                                                      \
+    } while (0)
+
+// launchers shared with irregular.cu
+int launch_eta_pairs(const DevSea &sea, long n, const float2 *ph, const float *rr, float *out,
+                     cudaStream_t stream);
+int launch_column_pairs(const DevSea &sea, long ncol, int nl, const float2 *ph, const float *rr,
+                        const float *z0, float *out, int pairs, cudaStream_t stream);
+int launch_phasors_public(const DevSea &sea, long n, const double *x, const double *y,
+                          const double *t, long sx, long sy, long st, int npad, float2 *ph,
+                          float *rr, double *first, cudaStream_t stream);
+
+struct GridGeom {
+    int nx, ny, nl;
+    double d0, d2, dx, dy, ds, depth, swl, tan_a, tan_b, dt;
+};
+
+// sigmaS2cart (lsgrid_spline.cpp:117-122) in FP64.
+__device__ __forceinline__ double d_sigmaS2cart(const GridGeom &g, double s, double e) {
+    double sigma = -pow(tan(-(s - 1) * g.tan_a), g.tan_b) / pow(tan(g.tan_a), g.tan_b);
+    return (e - g.swl) + sigma * (g.depth + (e - g.swl));
+}
+
+__global__ void k_column_coords(GridGeom g, long nact, const int *act, double *xy) {
+    long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (q >= nact) return;
+    int c = act[q], i = c / g.ny, j = c % g.ny;
+    xy[q] = g.d0 + g.dx * i;
+    xy[nact + q] = g.d2 + g.dy * j;
+}
+
+// ETA of the slot, the level heights and the level offsets above swl.
+__global__ void k_levels(GridGeom g, long nact, const int *act, const double *first,
+                         const float *eta2, int slot, float *ETA, float *zmin, float *zmax) {
+    long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (q >= nact) return;
+    int c = act[q];
+    double e = first[q] + (double)eta2[q] + g.swl;     // eta1 + eta2 + swl
+    float ef = (float)e;
+    ETA[(long)slot * g.nx * g.ny + c] = ef;
+    for (int m = 0; m < g.nl; m++) {
+        // the reference evaluates the levels from the stored value; the FP32
+        // store is the value the query sees, so use it here too
+        double z = d_sigmaS2cart(g, g.ds * m, (double)ef);
+        zmin[q * g.nl + m] = (float)fmin(0.0, z);
+        zmax[q * g.nl + m] = (float)fmax(0.0, z - g.swl);
+    }
+}
+
+__global__ void k_scatter_levels(GridGeom g, long nact, const int *act, const double *first,
+                                 const float *sec, const float *zmax, int slot, float *UX,
+                                 float *UY, float *UZ) {
+    long e = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    long tot = nact * g.nl;
+    if (e >= tot) return;
+    long q = e / g.nl;
+    int m = (int)(e % g.nl);
+    long c = act[q];
+    float za = zmax[e];
+    long o = (long)slot * g.nx * g.ny * g.nl + c * g.nl + m;
+    UX[o] = sec[0 * tot + e] + (float)first[1 * nact + q] * za;
+    UY[o] = sec[1 * tot + e] + (float)first[2 * nact + q] * za;
+    UZ[o] = sec[2 * tot + e] + (float)first[3 * nact + q] * za;
+}
+
+// All finite differences of lsgrid_spline.cpp:124-366 in one pass over the
+// nodes: x/y/s gradients of slots (tstep+1)%4, (tstep+2)%4 into gradient
+// slots 0/1 and the time gradient of the slot(s) the reference writes.
+struct GradArgs {
+    GridGeom g;
+    int tstep;
+    const float *F[4];      // ETA, UX, UY, UZ
+    float *Fx[4], *Fy[4], *Fs[4], *Ft[4];
+};
+
+__global__ void k_gradients(GradArgs a) {
+    const GridGeom &g = a.g;
+    long nodes = (long)g.nx * g.ny * g.nl, cols = (long)g.nx * g.ny;
+    long e = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    int field = blockIdx.y;                  // 0 ETA (column nodes), 1..3 U, V, W
+    int nl = field == 0 ? 1 : g.nl;
+    long S = field == 0 ? cols : nodes;
+    if (e >= S) return;
+    int m = (int)(e % nl);
+    long c = e / nl;
+    int i = (int)(c / g.ny), j = (int)(c % g.ny);
+    const float *D = a.F[field];
+    int tids[2] = {(a.tstep + 1) % 4, (a.tstep + 2) % 4};
+    long sx = (long)g.ny * nl, sy = nl;
+    for (int q = 0; q < 2; q++) {
+        const float *d = D + tids[q] * S;
+        float gx, gy;
+        if (g.nx == 1) gx = 0.f;
+        else if (i == 0) gx = (float)((d[e + sx] - d[e]) / g.dx);
+        else if (i == g.nx - 1) gx = (float)((d[e] - d[e - sx]) / g.dx);
+        else gx = (float)((d[e + sx] - d[e - sx]) / (2 * g.dx));
+        if (g.ny == 1) gy = 0.f;
+        else if (j == 0) gy = (float)((d[e + sy] - d[e]) / g.dy);
+        else if (j == g.ny - 1) gy = (float)((d[e] - d[e - sy]) / g.dy);
+        else gy = (float)((d[e + sy] - d[e - sy]) / (2 * g.dy));
+        a.Fx[field][q * S + e] = gx;
+        a.Fy[field][q * S + e] = gy;
+        if (field > 0) {
+            float gs;
+            if (nl == 1) gs = 0.f;
+            else if (m == 0) gs = (float)((d[e + 1] - d[e]) / g.ds);
+            else if (m == nl - 1) gs = (float)((d[e] - d[e - 1]) / g.ds);
+            else gs = (float)((d[e + 1] - d[e - 1]) / (2 * g.ds));
+            a.Fs[field][q * S + e] = gs;
+        }
+    }
+    float *T = a.Ft[field];
+    if (a.tstep > 0) {
+        int tid = (a.tstep + 2) % 4, tid1 = (a.tstep + 3) % 4, tid0 = (a.tstep + 1) % 4;
+        T[tid * S + e] = (float)(((double)D[tid1 * S + e] - D[tid0 * S + e]) / (2 * g.dt));
+    } else {
+        T[1 * S + e] = (float)(((double)D[2 * S + e] - D[1 * S + e]) / g.dt);
+        T[2 * S + e] = (float)(((double)D[3 * S + e] - D[1 * S + e]) / (2 * g.dt));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Query
+// ---------------------------------------------------------------------------
+struct QueryArgs {
+    GridGeom g;
+    int tid1, tid2;
+    double t0;
+    const float *ETA, *ETAdt, *ETAdx, *ETAdy;
+    const float *U[3], *Ut[3], *Ux[3], *Uy[3], *Us[3];
+    long n;
+    const double *x, *y, *z, *t;
+    double *out;    // [4][n]
+};
+
+__device__ __forceinline__ float herm(float f0, float f1, float d0, float d1, float h, float r) {
+    float a = h * d0 - (f1 - f0), b = -h * d1 + (f1 - f0);
+    return f0 * (1.f - r) + f1 * r + r * (1.f - r) * (a * (1.f - r) + b * r);
+}
+__device__ __forceinline__ float lin(float f0, float f1, float r) { return f0 * (1.f - r) + f1 * r; }
+
+// cart2sigmaS (lsgrid_spline.cpp:109-113).  The reference takes pow() of a
+// negative base (NaN, then an out-of-range index) for eta - swl < z <= eta
+// when swl != 0; here the base is clamped at zero, i.e. such points are
+// evaluated at the surface level.
+__device__ __forceinline__ float cart2sigmaS(const GridGeom &g, float tanab, float zpt, float e) {
+    float z = fminf(zpt, e);
+    float es = e - (float)g.swl;
+    float sigma = fmaxf((z - es) / ((float)g.depth + es), -1.f);
+    float base = fmaxf(-sigma * tanab, 0.f);
+    return 1.f - atanf(powf(base, 1.f / (float)g.tan_b)) / (float)g.tan_a;
+}
+
+__device__ __forceinline__ int iclamp(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+__device__ float spline_velo(const QueryArgs &a, int f, int xp, int yp, int s0, int s1, float xd,
+                             float yd, float sd0, float sd1, float td) {
+    const GridGeom &g = a.g;
+    const long nn = (long)g.nx * g.ny * g.nl;
+    const int x1 = iclamp(xp + 1, 0, g.nx - 1), y1 = iclamp(yp + 1, 0, g.ny - 1);
+    const int ls[2] = {s0, s1};
+    const int tsl[2] = {a.tid1, a.tid2};
+    float red[2], redt[2];
+    for (int q = 0; q < 2; q++) {            // q = 0: slot tid1 at s0; q = 1: slot tid2 at s1
+        int l0 = ls[q], l1 = iclamp(ls[q] + 1, 0, g.nl - 1);
+        long bv = (long)tsl[q] * nn, bg = (long)q * nn;
+        long idx[8];
+        int xs[8] = {xp, xp, x1, x1, xp, xp, x1, x1};
+        int ys[8] = {yp, y1, yp, y1, yp, y1, yp, y1};
+        int zs[8] = {l0, l0, l0, l0, l1, l1, l1, l1};
+        for (int k = 0; k < 8; k++) idx[k] = ((long)xs[k] * g.ny + ys[k]) * g.nl + zs[k];
+        float C[8], Cx[8], Cy[8], Cs[8], Ct[8];
+        for (int k = 0; k < 8; k++) {
+            C[k] = __ldg(a.U[f] + bv + idx[k]);
+            Ct[k] = __ldg(a.Ut[f] + bv + idx[k]);
+            Cx[k] = __ldg(a.Ux[f] + bg + idx[k]);
+            Cy[k] = __ldg(a.Uy[f] + bg + idx[k]);
+            Cs[k] = __ldg(a.Us[f] + bg + idx[k]);
+        }
+        const float dx = (float)g.dx, dy = (float)g.dy, ds = (float)g.ds;
+        float v00 = herm(C[0], C[2], Cx[0], Cx[2], dx, xd), v10 = herm(C[1], C[3], Cx[1], Cx[3], dx, xd);
+        float v01 = herm(C[4], C[6], Cx[4], Cx[6], dx, xd), v11 = herm(C[5], C[7], Cx[5], Cx[7], dx, xd);
+        float y00 = lin(Cy[0], Cy[2], xd), y10 = lin(Cy[1], Cy[3], xd);
+        float y01 = lin(Cy[4], Cy[6], xd), y11 = lin(Cy[5], Cy[7], xd);
+        float t00 = lin(Ct[0], Ct[2], xd), t10 = lin(Ct[1], Ct[3], xd);
+        float t01 = lin(Ct[4], Ct[6], xd), t11 = lin(Ct[5], Ct[7], xd);
+        float s00 = lin(Cs[0], Cs[2], xd), s10 = lin(Cs[1], Cs[3], xd);
+        float s01 = lin(Cs[4], Cs[6], xd), s11 = lin(Cs[5], Cs[7], xd);
+        float c0 = herm(v00, v10, y00, y10, dy, yd), c1 = herm(v01, v11, y01, y11, dy, yd);
+        float c0s = lin(s00, s10, yd), c1s = lin(s01, s11, yd);
+        float c0t = lin(t00, t10, yd), c1t = lin(t01, t11, yd);
+        float sd = q == 0 ? sd0 : sd1;
+        red[q] = herm(c0, c1, c0s, c1s, ds, sd);
+        redt[q] = lin(c0t, c1t, sd);
+    }
+    return herm(red[0], red[1], redt[0], redt[1], (float)g.dt, td);
+}
+
+__global__ void __launch_bounds__(128) k_query(QueryArgs a) {
+    long p = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (p >= a.n) return;
+    const GridGeom &g = a.g;
+    const double xpt = a.x[p], ypt = a.y[p], zpt = a.z[p], tpt = a.t[p];
+    // std::modf with a float* argument selects the float overload in the
+    // reference (lsgrid_spline.cpp:515-520): the fractions are float.
+    float xi, yi;
+    float xd = modff((float)fmax(0.0, fmin((xpt - g.d0) / g.dx, g.nx - 1.0)), &xi);
+    float yd = modff((float)fmax(0.0, fmin((ypt - g.d2) / g.dy, g.ny - 1.0)), &yi);
+    float td = (float)fmin(1.0, fmax(0.0, (tpt - a.t0) / g.dt));
+    int xp = (int)xi, yp = (int)yi;
+    const long nc = (long)g.nx * g.ny;
+    const int x1 = iclamp(xp + 1, 0, g.nx - 1), y1 = iclamp(yp + 1, 0, g.ny - 1);
+    long cid[4] = {(long)xp * g.ny + yp, (long)xp * g.ny + y1, (long)x1 * g.ny + yp, (long)x1 * g.ny + y1};
+    float C[4], D[4], Ct[4], Dt[4], Cx[4], Dx[4], Cy[4], Dy[4];
+    for (int k = 0; k < 4; k++) {
+        C[k] = __ldg(a.ETA + a.tid1 * nc + cid[k]);
+        D[k] = __ldg(a.ETA + a.tid2 * nc + cid[k]);
+        Ct[k] = __ldg(a.ETAdt + a.tid1 * nc + cid[k]);
+        Dt[k] = __ldg(a.ETAdt + a.tid2 * nc + cid[k]);
+        Cx[k] = __ldg(a.ETAdx + cid[k]);
+        Dx[k] = __ldg(a.ETAdx + nc + cid[k]);
+        Cy[k] = __ldg(a.ETAdy + cid[k]);
+        Dy[k] = __ldg(a.ETAdy + nc + cid[k]);
+    }
+    const float dx = (float)g.dx, dy = (float)g.dy;
+    float C0 = herm(C[0], C[2], Cx[0], Cx[2], dx, xd), C1 = herm(C[1], C[3], Cx[1], Cx[3], dx, xd);
+    float D0 = herm(D[0], D[2], Dx[0], Dx[2], dx, xd), D1 = herm(D[1], D[3], Dx[1], Dx[3], dx, xd);
+    float C0y = lin(Cy[0], Cy[2], xd), C1y = lin(Cy[1], Cy[3], xd);
+    float D0y = lin(Dy[0], Dy[2], xd), D1y = lin(Dy[1], Dy[3], xd);
+    float C0t = lin(Ct[0], Ct[2], xd), C1t = lin(Ct[1], Ct[3], xd);
+    float D0t = lin(Dt[0], Dt[2], xd), D1t = lin(Dt[1], Dt[3], xd);
+    float e0 = herm(C0, C1, C0y, C1y, dy, yd), e1 = herm(D0, D1, D0y, D1y, dy, yd);
+    float CCt = lin(C0t, C1t, yd), DDt = lin(D0t, D1t, yd);
+    float eta = herm(e0, e1, CCt, DDt, (float)g.dt, td);
+    const float tanab = powf(tanf((float)g.tan_a), (float)g.tan_b);
+    float n0 = cart2sigmaS(g, tanab, (float)zpt, e0) / (float)g.ds;
+    float n1 = cart2sigmaS(g, tanab, (float)zpt, e1) / (float)g.ds;
+    float s0i, s1i;
+    float sd0 = modff(n0, &s0i), sd1 = modff(n1, &s1i);
+    int s0 = iclamp((int)s0i, 0, g.nl - 1), s1 = iclamp((int)s1i, 0, g.nl - 1);
+    a.out[p] = eta;
+    for (int f = 0; f < 3; f++)
+        a.out[(long)(f + 1) * a.n + p] = spline_velo(a, f, xp, yp, s0, s1, xd, yd, sd0, sd1, td);
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+static GridGeom geom(const DevGrid &g) {
+    GridGeom G;
+    G.nx = g.nx; G.ny = g.ny; G.nl = g.nl;
+    G.d0 = g.cfg.domain[0]; G.d2 = g.cfg.domain[2];
+    G.dx = g.dx; G.dy = g.dy; G.ds = g.ds; G.depth = g.depth; G.swl = g.swl;
+    G.tan_a = g.cfg.tan_a; G.tan_b = g.cfg.tan_b; G.dt = g.dt;
+    return G;
+}
+
+// Extra per-grid device scratch kept alongside DevGrid (keyed by the grid).
+struct GridExtra {
+    int *act_all = nullptr, *act_live = nullptr;
+    long n_all = 0, n_live = 0;
+    double *xy = nullptr;      // [2][ncol]
+    float *zmin = nullptr, *zmax = nullptr, *sec = nullptr;
+    float *eta2 = nullptr;
+    double *tdev = nullptr;    // the slot time, read with stride 0 by the phasor pass
+};
+static std::vector<std::pair<const DevGrid *, GridExtra>> g_extra;
+static GridExtra *extra(const DevGrid &g) {
+    for (auto &e : g_extra) if (e.first == &g) return &e.second;
+    g_extra.push_back({&g, GridExtra{}});
+    return &g_extra.back().second;
+}
+
+int grid_create(const Config &cfg, DevGrid &g, void *stream_) {
+    cudaStream_t stream = (cudaStream_t)stream_;
+    grid_free(g);
+    g.cfg = cfg.lsgrid;
+    g.nx = cfg.lsgrid.nx; g.ny = cfg.lsgrid.ny; g.nl = cfg.lsgrid.nl;
+    if (g.nx < 1 || g.ny < 1 || g.nl < 1) return E_BAD_ARGUMENT;
+    if (g.nl > 128) return E_TOO_LARGE;
+    // initialize_kinematics (lsgrid_spline.cpp:673-677) and set_ignore (:1406)
+    g.dx = (g.cfg.domain[1] - g.cfg.domain[0]) / std::max(1., double(g.nx - 1));
+    g.dy = (g.cfg.domain[3] - g.cfg.domain[2]) / std::max(1., double(g.ny - 1));
+    g.ds = 1. / std::max(1., double(g.nl - 1));
+    g.t0 = g.cfg.t0; g.dt = g.cfg.dt; g.depth = cfg.depth; g.swl = cfg.swl; g.tstep = 0;
+    long c = (long)g.nx * g.ny, v = c * g.nl;
+    CK(cudaMalloc(&g.ETA, sizeof(float) * 4 * c));
+    CK(cudaMalloc(&g.ETAdt, sizeof(float) * 4 * c));
+    CK(cudaMalloc(&g.ETAdx, sizeof(float) * 2 * c));
+    CK(cudaMalloc(&g.ETAdy, sizeof(float) * 2 * c));
+    CK(cudaMemsetAsync(g.ETA, 0, sizeof(float) * 4 * c, stream));
+    CK(cudaMemsetAsync(g.ETAdt, 0, sizeof(float) * 4 * c, stream));
+    for (int f = 0; f < 3; f++) {
+        CK(cudaMalloc(&g.U[f], sizeof(float) * 4 * v));
+        CK(cudaMalloc(&g.Ut[f], sizeof(float) * 4 * v));
+        CK(cudaMalloc(&g.Ux[f], sizeof(float) * 2 * v));
+        CK(cudaMalloc(&g.Uy[f], sizeof(float) * 2 * v));
+        CK(cudaMalloc(&g.Us[f], sizeof(float) * 2 * v));
+        CK(cudaMemsetAsync(g.U[f], 0, sizeof(float) * 4 * v, stream));
+        CK(cudaMemsetAsync(g.Ut[f], 0, sizeof(float) * 4 * v, stream));
+    }
+    std::vector<int> ign(c), all, live;
+    for (int i = 0; i < g.nx; i++) {
+        double xp = g.cfg.domain[0] + g.dx * i;
+        for (int j = 0; j < g.ny; j++) {
+            double yp = g.cfg.domain[2] + g.dy * j;
+            const double *di = g.cfg.domain_ignore;
+            int ig = (xp >= di[0] && xp <= di[1] && yp >= di[2] && yp <= di[3]) ? 1 : 0;
+            ign[(long)i * g.ny + j] = ig;
+            all.push_back(i * g.ny + j);
+            if (!ig) live.push_back(i * g.ny + j);
+        }
+    }
+    CK(cudaMalloc(&g.IGNORE, sizeof(int) * c));
+    CK(cudaMemcpyAsync(g.IGNORE, ign.data(), sizeof(int) * c, cudaMemcpyHostToDevice, stream));
+    GridExtra *x = extra(g);
+    x->n_all = (long)all.size();
+    x->n_live = (long)live.size();
+    CK(cudaMalloc(&x->act_all, sizeof(int) * std::max<long>(1, x->n_all)));
+    CK(cudaMalloc(&x->act_live, sizeof(int) * std::max<long>(1, x->n_live)));
+    CK(cudaMemcpyAsync(x->act_all, all.data(), sizeof(int) * x->n_all, cudaMemcpyHostToDevice, stream));
+    if (x->n_live)
+        CK(cudaMemcpyAsync(x->act_live, live.data(), sizeof(int) * x->n_live, cudaMemcpyHostToDevice, stream));
+    CK(cudaMalloc(&x->xy, sizeof(double) * 2 * c));
+    CK(cudaMalloc(&x->zmin, sizeof(float) * v));
+    CK(cudaMalloc(&x->zmax, sizeof(float) * v));
+    CK(cudaMalloc(&x->sec, sizeof(float) * 3 * v));
+    CK(cudaMalloc(&x->eta2, sizeof(float) * c));
+    CK(cudaMalloc(&x->tdev, sizeof(double)));
+    CK(cudaStreamSynchronize(stream));
+    return OK;
+}
+
+void grid_free(DevGrid &g) {
+    float *ptrs[] = {g.ETA, g.ETAdx, g.ETAdy, g.ETAdt};
+    for (float *p : ptrs) if (p) cudaFree(p);
+    for (int f = 0; f < 3; f++) {
+        float *q[] = {g.U[f], g.Ut[f], g.Ux[f], g.Uy[f], g.Us[f]};
+        for (float *p : q) if (p) cudaFree(p);
+        g.U[f] = g.Ut[f] = g.Ux[f] = g.Uy[f] = g.Us[f] = nullptr;
+    }
+    if (g.IGNORE) cudaFree(g.IGNORE);
+    g.ETA = g.ETAdx = g.ETAdy = g.ETAdt = nullptr;
+    g.IGNORE = nullptr;
+    for (auto it = g_extra.begin(); it != g_extra.end(); ++it)
+        if (it->first == &g) {
+            GridExtra &x = it->second;
+            void *q[] = {x.act_all, x.act_live, x.xy, x.zmin, x.zmax, x.sec, x.eta2, x.tdev};
+            for (void *p : q) if (p) cudaFree(p);
+            g_extra.erase(it);
+            break;
+        }
+}
+
+// Fill one ring slot at time t for the given column set.
+static int fill_slot(DevGrid &g, const DevSea &sea, Workspace &ws, int slot, double t, bool live_only,
+                     cudaStream_t stream) {
+    GridExtra *x = extra(g);
+    long nact = live_only ? x->n_live : x->n_all;
+    const int *act = live_only ? x->act_live : x->act_all;
+    if (nact == 0) return OK;
+    GridGeom G = geom(g);
+    const int npad = sea.npad_g;
+    // workspace: phasors [npad][nact], ramps [npad][nact], first-order sums [5][nact]
+    auto up = [](size_t b) { return (b + 255) / 256 * 256; };
+    size_t b_ph = up(sizeof(float2) * (size_t)npad * nact), b_rr = up(sizeof(float) * (size_t)npad * nact);
+    int rc = workspace_reserve(ws, b_ph + b_rr + sizeof(double) * 5 * nact);
+    if (rc) return rc;
+    char *b = (char *)ws.base;
+    float2 *ph = (float2 *)b;
+    float *rr = (float *)(b + b_ph);
+    double *first = (double *)(b + b_ph + b_rr);
+    k_column_coords<<<(unsigned)((nact + 255) / 256), 256, 0, stream>>>(G, nact, act, x->xy);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(x->tdev, &t, sizeof(double), cudaMemcpyHostToDevice, stream));
+    rc = launch_phasors_public(sea, nact, x->xy, x->xy + nact, x->tdev, 1, 1, 0, npad, ph, rr, first, stream);
+    if (rc) return rc;
+    rc = launch_eta_pairs(sea, nact, ph, rr, x->eta2, stream);
+    if (rc) return rc;
+    k_levels<<<(unsigned)((nact + 127) / 128), 128, 0, stream>>>(G, nact, act, first, x->eta2, slot, g.ETA,
+                                                                 x->zmin, x->zmax);
+    CK(cudaGetLastError());
+    rc = launch_column_pairs(sea, nact, g.nl, ph, rr, x->zmin, x->sec, 1, stream);
+    if (rc) return rc;
+    long tot = nact * g.nl;
+    k_scatter_levels<<<(unsigned)((tot + 255) / 256), 256, 0, stream>>>(G, nact, act, first, x->sec, x->zmax,
+                                                                        slot, g.U[0], g.U[1], g.U[2]);
+    CK(cudaGetLastError());
+    return OK;
+}
+
+static int gradients(DevGrid &g, cudaStream_t stream) {
+    GradArgs a;
+    a.g = geom(g);
+    a.tstep = g.tstep;
+    a.F[0] = g.ETA; a.Fx[0] = g.ETAdx; a.Fy[0] = g.ETAdy; a.Fs[0] = nullptr; a.Ft[0] = g.ETAdt;
+    for (int f = 0; f < 3; f++) {
+        a.F[f + 1] = g.U[f]; a.Fx[f + 1] = g.Ux[f]; a.Fy[f + 1] = g.Uy[f];
+        a.Fs[f + 1] = g.Us[f]; a.Ft[f + 1] = g.Ut[f];
+    }
+    long nodes = (long)g.nx * g.ny * g.nl;
+    dim3 grid((unsigned)((nodes + 255) / 256), 4);
+    k_gradients<<<grid, 256, 0, stream>>>(a);
+    CK(cudaGetLastError());
+    return OK;
+}
+
+int grid_initialize(DevGrid &g, const DevSea &sea, Workspace &ws, void *stream_) {
+    cudaStream_t stream = (cudaStream_t)stream_;
+    bool wi = g.cfg.ignore_at_init;
+    // initialize_kinematics[_with_ignore] (lsgrid_spline.cpp:679, 758)
+    double tt0[4] = {wi ? g.t0 : g.t0 - g.dt, g.t0, g.t0 + g.dt, g.t0 + 2 * g.dt};
+    g.tstep = 0;
+    for (int tt = 0; tt < 4; tt++) {
+        int rc = fill_slot(g, sea, ws, tt, tt0[tt], wi, stream);
+        if (rc) return rc;
+    }
+    int rc = gradients(g, stream);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(stream));
+    return OK;
+}
+
+int grid_update(DevGrid &g, const DevSea &sea, Workspace &ws, void *stream_) {
+    cudaStream_t stream = (cudaStream_t)stream_;
+    // update (lsgrid_spline.cpp:847-931)
+    g.tstep++;
+    g.t0 += g.dt;
+    double t2 = g.t0 + 2 * g.dt;
+    int slot = (g.tstep + 3) % 4;
+    int rc = fill_slot(g, sea, ws, slot, t2, true, stream);
+    if (rc) return rc;
+    return gradients(g, stream);
+}
+
+bool grid_check_time(const DevGrid &g, double t) { return t > g.t0 + g.dt; }
+
+int grid_query(const DevGrid &g, long n, const double *x, const double *y, const double *z,
+               const double *t, double *out, void *stream_) {
+    cudaStream_t stream = (cudaStream_t)stream_;
+    if (n <= 0) return OK;
+    QueryArgs a;
+    a.g = geom(g);
+    a.tid1 = (g.tstep + 1) % 4; a.tid2 = (g.tstep + 2) % 4; a.t0 = g.t0;
+    a.ETA = g.ETA; a.ETAdt = g.ETAdt; a.ETAdx = g.ETAdx; a.ETAdy = g.ETAdy;
+    for (int f = 0; f < 3; f++) {
+        a.U[f] = g.U[f]; a.Ut[f] = g.Ut[f]; a.Ux[f] = g.Ux[f]; a.Uy[f] = g.Uy[f]; a.Us[f] = g.Us[f];
+    }
+    a.n = n; a.x = x; a.y = y; a.z = z; a.t = t; a.out = out;
+    k_query<<<(unsigned)((n + 127) / 128), 128, 0, stream>>>(a);
+    CK(cudaGetLastError());
+    return OK;
+}
+
+int grid_download(const DevGrid &g, int which, double *dst, long cap, void *stream_) {
+    cudaStream_t stream = (cudaStream_t)stream_;
+    long c = (long)g.nx * g.ny, v = c * g.nl;
+    const float *src = nullptr;
+    long n = 0;
+    switch (which) {
+    case 0: src = g.ETA; n = 4 * c; break;
+    case 1: case 2: case 3: src = g.U[which - 1]; n = 4 * v; break;
+    case 4: src = g.ETAdx; n = 2 * c; break;
+    case 5: src = g.ETAdy; n = 2 * c; break;
+    case 6: src = g.ETAdt; n = 4 * c; break;
+    default:
+        if (which >= 7 && which <= 18) {
+            int f = (which - 7) / 4, k = (which - 7) % 4;
+            const float *arr[4] = {g.Ut[f], g.Ux[f], g.Uy[f], g.Us[f]};
+            src = arr[k];
+            n = (k == 0 ? 4 : 2) * v;
+        } else {
+            return E_BAD_ARGUMENT;
+        }
+    }
+    if (!dst) return (int)std::min<long>(n, 0x7fffffff);
+    if (cap < n) return E_TOO_LARGE;
+    std::vector<float> h(n);
+    CK(cudaMemcpyAsync(h.data(), src, sizeof(float) * n, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    for (long i = 0; i < n; i++) dst[i] = h[i];
+    return (int)n;
+}
+
+}  // namespace cfdwm

@@ -1,0 +1,237 @@
+"""Parity of the CUDA path with the reference.
+
+Every check goes through the C ABI of libcfdwavemaker_gb300.so.  Golden
+values are the reference's own FP64 outputs (tests/golden/, recorded by
+make_golden.py from the unmodified reference) and, at more points, the FP64
+oracle.  The kernels compute in FP32 (phases in FP64), so the bar is the
+normwise relative error max|gpu - ref| / max|ref| per output field:
+
+    TOL = 1e-5   for elevation, velocities and pressures
+    TOL_GRAD = 1e-4  for the s-grid finite-difference arrays (differences of
+                     FP32 node values divided by the spacing)
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import golden_cfg, load_golden, norm_rel_err
+
+import cfdwavemaker_gb300 as cw
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+TOL_GRAD = 1e-4
+API = ["SurfElev", "VeloX", "VeloY", "VeloZ", "DynPres", "nhPres"]
+IRREGULAR = ["t005_focused", "t002_exact", "config1_point", "short_spread", "ramps_swl", "linear"]
+REGULAR = ["stokes5", "fenton24", "stokes5_len", "fenton_len"]
+
+
+@pytest.fixture(scope="module")
+def wm(tmp_path_factory):
+    from cfdwavemaker_gb300 import build
+    build.build()
+    d = tmp_path_factory.mktemp("run")
+    cwd = os.getcwd()
+    os.chdir(d)            # wave_Initialize writes spectral_components.dat here
+    m = cw.CFDwavemaker()
+    yield m
+    m.cleanup()
+    os.chdir(cwd)
+
+
+def init(wm, g):
+    rc = wm.initialize_text(str(g["waveinput"]))
+    assert rc == 0, cw.last_error()
+
+
+def api_all(wm, x, y, z, t):
+    eta = wm.surface_elevation_batch(x, y, t)
+    u, v, w = wm.velocity_batch(x, y, z, t)
+    p = wm.dynamic_pressure_batch(x, y, z, t)
+    nh = wm.nonhydrostatic_pressure_batch(x, y, z, t)
+    return [eta, u, v, w, p, nh]
+
+
+@pytest.mark.parametrize("case", IRREGULAR + REGULAR)
+def test_api_vs_reference(wm, case):
+    g = load_golden(case)
+    init(wm, g)
+    out = api_all(wm, g["pt_x"], g["pt_y"], g["pt_z"], g["pt_t"])
+    for q, name in enumerate(API):
+        ref = g["api_" + name]
+        err = norm_rel_err(out[q], ref)
+        assert err <= TOL, (case, name, err)
+    vf = wm.volume_fraction_batch(g["pt_x"], g["pt_y"], g["pt_z"], g["pt_t"], 0.1)
+    assert np.max(np.abs(vf - g["api_VFrac"])) <= 1e-3
+
+
+@pytest.mark.parametrize("case", ["config1_point", "ramps_swl", "fenton24"])
+def test_scalar_entry_points(wm, case):
+    """The reference's scalar functions are batches of one point here."""
+    g = load_golden(case)
+    init(wm, g)
+    lib = wm.lib
+    idx = np.arange(0, g["pt_x"].size, max(1, g["pt_x"].size // 7))
+    for i in idx:
+        x, y, z, t = (float(g["pt_" + k][i]) for k in "xyzt")
+        vals = [lib.wave_SurfElev(x, y, t), lib.wave_VeloX(x, y, z, t), lib.wave_VeloY(x, y, z, t),
+                lib.wave_VeloZ(x, y, z, t), lib.wave_DynPres(x, y, z, t), lib.wave_nhPres(x, y, z, t)]
+        for q, name in enumerate(API):
+            ref = g["api_" + name]
+            scale = max(np.max(np.abs(ref)), 1e-30)
+            assert abs(vals[q] - ref[i]) / scale <= TOL, (case, name, i)
+        # COMFLOW aliases are the same functions
+        assert lib.VelocityX(0, 0, 0, x, y, z, t) == vals[1]
+        assert lib.SurfaceElevation(0, 0, x, y, t) == vals[0]
+
+
+def test_t005_target_wave(wm):
+    """The reference's own golden elevation series (tests/t005_focused_wave/targetwave.dat)."""
+    g = load_golden("t005_focused")
+    init(wm, g)
+    t = g["extra_targetwave_t"]
+    eta = wm.surface_elevation_batch(np.full_like(t, 10.0), np.zeros_like(t), t)
+    assert norm_rel_err(eta, g["extra_targetwave_eta"]) <= TOL
+
+
+def test_t002_exact_solution(wm):
+    """The reference's own golden momentum integrals (exact_solution.mat)."""
+    g = load_golden("t002_exact")
+    init(wm, g)
+    time = g["extra_time"]
+    dz = 0.1
+    z = np.arange(-20.0, 12, dz)
+    T, Z = np.meshgrid(time, z, indexing="ij")
+    n = T.size
+    u, v, w = wm.velocity_batch(np.zeros(n), np.zeros(n), Z.ravel(), T.ravel())
+    eta = wm.surface_elevation_batch(np.zeros(time.size), np.zeros(time.size), time)
+    ratio = np.clip((eta[:, None] - (z[None, :] - dz / 2.0)) / dz, 0.0, 1.0)
+    for arr, key in ((u, "umom1"), (v, "vmom1"), (w, "wmom1")):
+        a = arr.reshape(time.size, z.size)
+        mom = np.sum(a * np.abs(a) * dz * ratio, axis=1)
+        # the momentum integral is quadratic in the velocity
+        assert norm_rel_err(mom, g["extra_" + key]) <= 2 * TOL, key
+    assert norm_rel_err(eta, g["extra_wave_elev1"]) <= TOL
+
+
+@pytest.mark.parametrize("case", ["config1_point", "short_spread", "ramps_swl"])
+def test_irregular_fields_vs_oracle_random(wm, case):
+    """Irregular::eta/u/v/w/dp (no ramp) at random points against the oracle,
+    including points above swl (Taylor layer), below, and t < 0."""
+    g = load_golden(case)
+    init(wm, g)
+    cfg = golden_cfg(g)
+    rng = np.random.default_rng(3)
+    n = 700
+    x = rng.uniform(-200, 600, n)
+    y = rng.uniform(-100, 100, n)
+    z = rng.uniform(-cfg["depth"], 4.0, n)
+    t = rng.uniform(-1.0, 40.0, n)
+    got = wm.irregular_fields(x, y, z, t)
+    ref = oracle.Sea(cfg).fields(x, y, z, t)
+    for q, name in enumerate(["eta", "u", "v", "w", "dp"]):
+        err = norm_rel_err(got[q], ref[:, q])
+        assert err <= TOL, (case, name, err)
+
+
+def test_config1_workload_vs_oracle(wm):
+    """The 128-component long-crested sea on its 256 x 32 x 8 point set
+    (a sampled subset against the oracle)."""
+    from cfdwavemaker_gb300 import seastate as ss
+    comps = ss.config1_sea()
+    txt = ss.write_irregular(None, comps, 50.0, extrap=2)
+    assert wm.initialize_text(txt) == 0
+    cfg = oracle.waveinput.read_text(txt)
+    xs = np.linspace(0.0, 500.0, 256)
+    ts = np.arange(8.0)
+    X, T = np.meshgrid(xs, ts, indexing="ij")
+    eta = wm.surface_elevation_batch(X.ravel(), np.zeros(X.size), T.ravel())
+    # 32 z-points from the seabed to the local crest
+    zz = -50.0 + (eta[:, None] + 50.0) * np.linspace(0.0, 1.0, 32)[None, :]
+    XX = np.repeat(X.ravel(), 32)
+    TT = np.repeat(T.ravel(), 32)
+    ZZ = zz.ravel()
+    u, v, w = wm.velocity_batch(XX, np.zeros_like(XX), ZZ, TT)
+    p = wm.dynamic_pressure_batch(XX, np.zeros_like(XX), ZZ, TT)
+    sel = np.random.default_rng(0).choice(XX.size, 600, replace=False)
+    ref = oracle.Model(cfg).api(XX[sel], 0.0 * XX[sel], ZZ[sel], TT[sel])
+    for arr, q in ((u, 1), (w, 3), (p, 4)):
+        assert norm_rel_err(arr[sel], ref[:, q]) <= TOL, q
+    refe = oracle.Model(cfg).api(X.ravel(), 0 * X.ravel(), 0 * X.ravel(), T.ravel())[:, 0]
+    assert norm_rel_err(eta, refe) <= TOL
+
+
+@pytest.mark.parametrize("case", ["sgrid_small", "sgrid_ignore"])
+def test_sgrid_vs_reference(wm, case):
+    g = load_golden(case)
+    init(wm, g)
+    cfg = golden_cfg(g)
+    updates = {"sgrid_small": [0.7, 1.6], "sgrid_ignore": [1.5]}[case]
+    for k in range(int(g["nsnap"])):
+        if k > 0:
+            wm.force_update(updates[k - 1])
+        t0, ts = wm.sgrid_state()
+        assert ts == g["s%d_dims" % k][3] and abs(t0 - g["s%d_vals" % k][0]) < 1e-12
+        for which in range(19):
+            ref = g["s%d_arr%d" % (k, which)]
+            got = wm.sgrid_array(which)
+            tol = TOL if which <= 3 else TOL_GRAD
+            if which in (6, 7, 11, 15):
+                nslot = got.size // 4
+                slots = {1, 2} if ts == 0 else {1, 2} | {(s + 2) % 4 for s in range(1, ts + 1)}
+                for s in slots:
+                    a, b = got[s * nslot:(s + 1) * nslot], ref[s * nslot:(s + 1) * nslot]
+                    assert norm_rel_err(a, b) <= tol, (k, which, s)
+            else:
+                assert norm_rel_err(got, ref) <= tol, (k, which, norm_rel_err(got, ref))
+        qt = float(np.ravel(g["s%d_query_t" % k])[0])
+        qx, qy, qz = g["query_x"], g["query_y"], g["query_z"]
+        kin = wm.kinematics_batch(qx, qy, qz, np.full_like(qx, qt))
+        for c in range(4):
+            assert norm_rel_err(kin[:, c], g["s%d_kin" % k][:, c]) <= TOL, (k, c)
+        u, v, w = wm.velocity_batch(qx, qy, qz, np.full_like(qx, qt))
+        for arr, name in ((u, "VeloX"), (v, "VeloY"), (w, "VeloZ")):
+            assert norm_rel_err(arr, g["s%d_api_%s" % (k, name)]) <= TOL, (k, name)
+        e = wm.surface_elevation_batch(qx, qy, np.full_like(qx, qt))
+        assert norm_rel_err(e, g["s%d_api_SurfElev" % k]) <= TOL
+
+
+@pytest.mark.parametrize("case", ["fenton24", "fenton_len"])
+def test_fenton_solution_vs_reference(wm, case):
+    g = load_golden(case)
+    init(wm, g)
+    sol = wm.regular_solution()
+    ref = g["fenton_solution"]
+    np.testing.assert_allclose(sol[:ref.size], ref, rtol=1e-9, atol=1e-12)
+
+
+def test_device_pointer_batch(wm):
+    """Device-resident inputs and outputs (torch tensors on cuda:0)."""
+    torch = pytest.importorskip("torch")
+    g = load_golden("config1_point")
+    init(wm, g)
+    x = torch.tensor(g["pt_x"], device="cuda:0", dtype=torch.float64)
+    y = torch.tensor(g["pt_y"], device="cuda:0", dtype=torch.float64)
+    z = torch.tensor(g["pt_z"], device="cuda:0", dtype=torch.float64)
+    t = torch.tensor(g["pt_t"], device="cuda:0", dtype=torch.float64)
+    u = torch.empty_like(x)
+    n = x.numel()
+    torch.cuda.synchronize()
+    rc = wm.lib.wave_VeloXYZ_batch(cw._ptr(x), cw._ptr(y), cw._ptr(z), cw._ptr(t), n, cw._ptr(u), None, None)
+    assert rc == 0
+    torch.cuda.synchronize()
+    assert norm_rel_err(u.cpu().numpy(), g["api_VeloX"]) <= TOL
+
+
+def test_empty_and_ragged_batches(wm):
+    g = load_golden("config1_point")
+    init(wm, g)
+    assert wm.lib.wave_SurfElev_batch(None, None, None, 0, None) == 0
+    for n in (1, 2, 127, 129, 1000):
+        x = np.linspace(0, 300, n)
+        eta = wm.surface_elevation_batch(x, np.zeros(n), np.full(n, 2.0))
+        ref = np.array([wm.lib.wave_SurfElev(float(a), 0.0, 2.0) for a in x[:3]])
+        np.testing.assert_allclose(eta[:3], ref, rtol=0, atol=1e-12)

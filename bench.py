@@ -1,0 +1,428 @@
+"""Benchmark of the second-order point-kinematics path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload sgrid|point]
+
+Workloads (synthetic seeded sea states of the named shapes; no dataset):
+  sgrid  (default) short-crested JONSWAP Hs=6 m Tp=12 s gamma=2, cos-2s s=10,
+         64 frequencies x 16 directions = 1024 components, depth 100 m; an
+         s-grid of 256 x 256 columns x 16 sigma levels over 1 km x 1 km at
+         dt = 0.5 s.  One step = one ring update (second-order kinematics at
+         all 1,048,576 grid nodes: eta2 + uvw2 pair sums over 521k pairs) plus
+         the 4-D spline query of 1e6 uniformly random (x, y, z, t) points.
+  point  long-crested JONSWAP Hs=4 m Tp=10 s gamma=3.3, 128 components,
+         depth 50 m; eta, u, w, dp on 256 x-points x 32 z-points x 8 times.
+Metric: second-order points per second (grid nodes updated per second for
+sgrid; evaluated points per second for point), FP32 compute with FP64 phases.
+The reference arm times the FP64 CPU restatement (oracle/) on a bounded
+sample of the same workload with all host threads.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import ctypes as C
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "2nd-order pts/s at <=1e-5 rel err vs FP64: split-BF16 TC & surrogate vs plain"
+
+
+def sgrid_config(nx=256, ny=256, nl=16):
+    from cfdwavemaker_gb300 import seastate as ss
+    comps = ss.config3_sea()
+    grid = {"bounds": (0.0, 1000.0, 0.0, 1000.0), "nx": nx, "ny": ny, "nl": nl, "t0": 0.0,
+            "dt": 0.5, "stretch": (0.7, 1.5)}
+    return ss.write_irregular(None, comps, 100.0, extrap=2, lsgrid=grid)
+
+
+def point_config():
+    from cfdwavemaker_gb300 import seastate as ss
+    return ss.write_irregular(None, ss.config1_sea(), 50.0, extrap=2)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if os.environ.get("CFDWM_GLOO") is None else "gloo")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(ws, v):
+    if ws <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def peaks():
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def run_ours(args):
+    import torch
+    import cfdwavemaker_gb300 as cw
+    ws, rank, local = dist_init()
+    torch.cuda.set_device(local)
+    lib = cw.load()
+    work = tempfile.mkdtemp()
+    os.chdir(work)
+    wm = cw.CFDwavemaker()
+    if args.workload == "sgrid":
+        txt = sgrid_config()
+    else:
+        txt = point_config()
+    t_init = time.time()
+    rc = wm.initialize_text(txt)
+    if rc != 0:
+        raise SystemExit("initialize failed: %d %s" % (rc, cw.last_error()))
+    init_s = time.time() - t_init
+    stream = torch.cuda.current_stream()
+    rng = np.random.default_rng(1234 + rank)
+    res = {}
+    if args.workload == "sgrid":
+        nq = 1_000_000
+        qx = rng.uniform(0, 1000, nq)
+        qy = rng.uniform(0, 1000, nq)
+        qz = rng.uniform(-100, 6.0, nq)
+        dt = 0.5
+        state = {"t": 0.0}
+        dq = [torch.tensor(a, device="cuda", dtype=torch.float64) for a in (qx, qy, qz)]
+        dtq = torch.empty(nq, device="cuda", dtype=torch.float64)
+        dout = torch.empty((nq, 4), device="cuda", dtype=torch.float64)
+        hq = [torch.from_numpy(a).pin_memory() for a in (qx, qy, qz)]
+        htq = torch.empty(nq, dtype=torch.float64).pin_memory()
+        hout = np.empty((nq, 4))
+        nodes = 256 * 256 * 16
+
+        def step_device():
+            # one ring update + 1e6 queries at a time inside the new interval
+            state["t"] += dt
+            lib.wave_force_update(state["t"] + 1e-9)
+            t0, _ = wm.sgrid_state()
+            dtq.fill_(t0 + 0.5 * dt)
+            rc = lib.wave_Kinematics_batch(cw._ptr(dq[0]), cw._ptr(dq[1]), cw._ptr(dq[2]), cw._ptr(dtq),
+                                           nq, cw._ptr(dout))
+            assert rc == 0
+
+        def step_host():
+            state["t"] += dt
+            lib.wave_force_update(state["t"] + 1e-9)
+            t0, _ = wm.sgrid_state()
+            htq.fill_(t0 + 0.5 * dt)
+            rc = lib.wave_Kinematics_batch(cw._ptr(hq[0].numpy()), cw._ptr(hq[1].numpy()),
+                                           cw._ptr(hq[2].numpy()), cw._ptr(htq.numpy()), nq, cw._ptr(hout))
+            assert rc == 0
+            return float(hout[0, 1])
+
+        units = nodes
+        h2d = 4 * 8 * nq
+        d2h = 4 * 8 * nq
+    else:
+        xs = np.linspace(0.0, 500.0, 256)
+        ts = np.arange(8.0)
+        X, T = np.meshgrid(xs, ts, indexing="ij")
+        eta = wm.surface_elevation_batch(X.ravel(), np.zeros(X.size), T.ravel())
+        zz = -50.0 + (eta[:, None] + 50.0) * np.linspace(0.0, 1.0, 32)[None, :]
+        XX = np.repeat(X.ravel(), 32)
+        TT = np.repeat(T.ravel(), 32)
+        ZZ = zz.ravel()
+        npt = XX.size
+        d = [torch.tensor(a, device="cuda", dtype=torch.float64) for a in (XX, np.zeros(npt), ZZ, TT)]
+        do = [torch.empty(npt, device="cuda", dtype=torch.float64) for _ in range(4)]
+        hin = [torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in (XX, np.zeros(npt), ZZ, TT)]
+        hout = [np.empty(npt) for _ in range(4)]
+
+        def step_device():
+            p = [cw._ptr(a) for a in d]
+            assert lib.wave_SurfElev_batch(p[0], p[1], p[3], npt, cw._ptr(do[0])) == 0
+            assert lib.wave_VeloXYZ_batch(p[0], p[1], p[2], p[3], npt, cw._ptr(do[1]), None, cw._ptr(do[2])) == 0
+            assert lib.wave_DynPres_batch(p[0], p[1], p[2], p[3], npt, cw._ptr(do[3])) == 0
+
+        def step_host():
+            p = [cw._ptr(a.numpy()) for a in hin]
+            assert lib.wave_SurfElev_batch(p[0], p[1], p[3], npt, cw._ptr(hout[0])) == 0
+            assert lib.wave_VeloXYZ_batch(p[0], p[1], p[2], p[3], npt, cw._ptr(hout[1]), None, cw._ptr(hout[2])) == 0
+            assert lib.wave_DynPres_batch(p[0], p[1], p[2], p[3], npt, cw._ptr(hout[3])) == 0
+            return float(hout[1][0])
+
+        units = npt
+        h2d = 4 * 8 * npt * 3
+        d2h = 8 * npt * 4
+
+    lib.cfdwm_set_stream(C.c_void_p(stream.cuda_stream))
+    for _ in range(args.warmup):
+        step_device()
+    torch.cuda.synchronize()
+    lib.cfdwm_profile_enable(1)
+    for k in range(7):
+        lib.cfdwm_profile_read(k, None)
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier(ws)
+    torch.cuda.synchronize()
+    l0 = lib.cfdwm_kernel_launches()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step_device()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier(ws)
+    launches = lib.cfdwm_kernel_launches() - l0
+    prof = {}
+    for k, name in enumerate(["column_pairs", "eta_pairs", "point_pairs", "phasors", "query",
+                              "gradients", "qform"]):
+        tot = C.c_double(0.0)
+        nk = lib.cfdwm_profile_read(k, C.byref(tot))
+        if nk > 0:
+            prof[name] = {"launches": int(nk), "avg_ms": tot.value / nk, "total_ms": tot.value}
+    lib.cfdwm_profile_enable(0)
+    ms = ev0.elapsed_time(ev1) / args.steps
+    ms = allmax(ws, ms)
+    # end-to-end through the host-buffer API
+    for _ in range(1):
+        step_host()
+    torch.cuda.synchronize()
+    barrier(ws)
+    te0 = time.perf_counter()
+    for _ in range(args.steps):
+        step_host()
+    torch.cuda.synchronize()
+    te = (time.perf_counter() - te0) / args.steps
+    te = allmax(ws, te)
+    clocks = sampler.stop()
+    res.update(ms=ms, e2e_s=te, units=units, launches=launches, init_s=init_s, h2d=h2d, d2h=d2h,
+               clocks=clocks, ws=ws, rank=rank, prof=prof, npairs=int(lib.cfdwm_npairs()),
+               ncomp=int(lib.cfdwm_components(None)))
+    return res
+
+
+def roofline(args, r, pk, src):
+    """Roofline object of the dominant kernel from the in-library CUDA-event
+    timings.  The column pair kernel is bound by the SFU (MUFU ex2) pipe: the
+    depth ratios of both interaction wavenumbers need exp(kz) and
+    exp(-2k(z+h)), i.e. 4 ex2 per (pair, level); a pair costs 22 FP32 flops
+    per level on top (6 FMA for u, v, w and the ratio assembly).  GB300 has
+    152 SMs x 16 MUFU lanes; the peak is that times the median SM clock seen
+    during the run (MEASURED_PEAKS.json holds no SFU or FP32 figure)."""
+    prof = r["prof"]
+    f_mhz = r["clocks"].get("sm_mhz") or pk.get("sm_max_mhz", 2070.0)
+    if args.workload == "sgrid" and "column_pairs" in prof:
+        kp = prof["column_pairs"]
+        units = r["units"]                     # grid nodes per launch (all columns, 16 levels)
+        terms = units * (r["npairs"] + r["ncomp"])
+        t = kp["avg_ms"] / 1e3
+        ex2 = 4.0 * terms / t
+        peak = 152 * 16 * f_mhz * 1e6
+        return {"kernel": "k_pairs_columns", "bound": "sfu", "achieved": ex2 / 1e9, "peak": peak / 1e9,
+                "unit": "Gex2/s", "frac": ex2 / peak, "traffic": traffic_from_profiles("k_pairs_columns"),
+                "algorithmic": "4 ex2 + 22 FP32 flop per (pair, level); %d pairs + %d diagonal terms x %d nodes "
+                               "per launch" % (r["npairs"], r["ncomp"], units),
+                "fp32_tflops": 22.0 * terms / t / 1e12,
+                "fp32_peak_tflops": 152 * 128 * 2 * f_mhz * 1e6 / 1e12,
+                "avg_launch_ms": kp["avg_ms"],
+                "peak_source": "derived: 152 SM x 16 MUFU/clk x median SM clock %.0f MHz" % f_mhz}
+    if "point_pairs" in prof:
+        kp = prof["point_pairs"]
+        n = r["units"]
+        P = r["ncomp"] * (r["ncomp"] + 1) / 2
+        t = kp["avg_ms"] / 1e3
+        ex2 = 4.0 * n * P / t
+        peak = 152 * 16 * f_mhz * 1e6
+        return {"kernel": "k_pairs_points", "bound": "sfu", "achieved": ex2 / 1e9, "peak": peak / 1e9,
+                "unit": "Gex2/s", "frac": ex2 / peak, "traffic": traffic_from_profiles("k_pairs_points"),
+                "avg_launch_ms": kp["avg_ms"],
+                "peak_source": "derived: 152 SM x 16 MUFU/clk x median SM clock %.0f MHz" % f_mhz}
+    return None
+
+
+def traffic_from_profiles(kernel):
+    """DRAM bytes per launch of a kernel from the committed ncu summary."""
+    p = os.path.join(HERE, "profiles", "traffic.json")
+    try:
+        with open(p) as fh:
+            return json.load(fh).get(kernel)
+    except (OSError, ValueError):
+        return None
+
+
+def cpu_baseline(args, budget_s=15.0):
+    """FP64 CPU restatement (oracle/) on a bounded sample, all host threads."""
+    import oracle
+    from oracle import waveinput
+    nthr = os.cpu_count() or 1
+    if args.workload == "sgrid":
+        cfg = waveinput.read_text(sgrid_config())
+        sea = oracle.Sea(cfg)
+        grid = oracle.Sgrid(cfg, sea, init=False)
+        # columns of the next ring slot, timed on a growing sample until the budget
+        ncols = max(4, nthr)
+        t0 = time.perf_counter()
+        grid.update_columns(1.0, 0, ncols, nthr)
+        el = time.perf_counter() - t0
+        if el < budget_s / 4:
+            ncols2 = int(ncols * min(64.0, (budget_s / 2) / max(el, 1e-3)))
+            t0 = time.perf_counter()
+            grid.update_columns(1.0, 0, ncols2, nthr)
+            el = time.perf_counter() - t0
+            ncols = ncols2
+        rate = ncols * 16 / el
+        return {"value": rate, "unit": "grid nodes/s", "cores": nthr, "kind": "port",
+                "sample": "%d columns x 16 levels of one ring update (1024 components, 521k pairs), "
+                          "FP64 oracle restatement of lsGridSpline::update, extrapolates linearly" % ncols}
+    cfg = waveinput.read_text(point_config())
+    m = oracle.Model(cfg)
+    rng = np.random.default_rng(5)
+    n = max(nthr * 8, 64)
+    x = rng.uniform(0, 500, n); z = rng.uniform(-50, 0, n); t = rng.uniform(0, 7, n)
+    t0 = time.perf_counter()
+    m.sea.fields(x, 0 * x, z, t, 1 | 2 | 8 | 16, nthr)
+    el = time.perf_counter() - t0
+    return {"value": n / el, "unit": "points/s", "cores": nthr, "kind": "port",
+            "sample": "%d random points of the 256x32x8 set, eta+u+w+dp, FP64 oracle" % n}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="sgrid", choices=["sgrid", "point"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    unit = "grid nodes/s" if args.workload == "sgrid" else "points/s"
+    workload = ("s-grid second-order update: 1024-component short-crested JONSWAP (64 freq x 16 dir, "
+                "Hs 6 m, Tp 12 s, gamma 2, cos-2s s=10), depth 100 m, 256x256 columns x 16 levels over "
+                "1 km^2, dt 0.5 s, + 1e6 random spline queries per step"
+                if args.workload == "sgrid" else
+                "point API: 128-component JONSWAP (Hs 4 m, Tp 10 s, gamma 3.3), depth 50 m, eta/u/w/dp at "
+                "256 x 32 z x 8 t points")
+    if args.impl == "reference":
+        rank = int(os.environ.get("RANK", "0"))
+        if rank != 0:
+            return
+        steps = []
+        for _ in range(args.steps):
+            steps.append(cpu_baseline(args, budget_s=8.0))
+        v = float(np.median([s["value"] for s in steps]))
+        cb = dict(steps[-1])
+        cb["value"] = v
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": unit, "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": workload}, "cpu_baseline": cb,
+                "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+    r = run_ours(args)
+    if r["rank"] != 0:
+        return
+    n = r["ws"]
+    value = r["units"] * n / (r["ms"] / 1e3)
+    e2e = r["units"] * n / r["e2e_s"]
+    pk, src = peaks()
+    line = {
+        "metric": METRIC, "value": value, "unit": unit, "n_gpus": n, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": r["ms"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (FP64 phases)", "data": "synthetic",
+        "config": {"workload": workload, "l2": "working set > L2 (phasor scratch 805 MB, grid 340 MB)",
+                   "form": "plain FP32 compensated"},
+        "e2e": {"value": e2e, "unit": unit, "h2d_bytes_per_step": r["h2d"], "d2h_bytes_per_step": r["d2h"]},
+        "gpu_launches": r["launches"],
+        "clocks": r["clocks"],
+        "init_s": r["init_s"],
+        "roofline": roofline(args, r, pk, src),
+        "kernels": r["prof"],
+        "peaks_source": src,
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args)
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -68,6 +68,23 @@ def load(path: str | None = None):
     L.wave_water_depth.argtypes = []
     L.wave_set_mpi_comm.restype = None
     L.wave_set_mpi_comm.argtypes = [C.c_int]
+    # COMFLOW aliases (CFDwavemaker.h:61-69)
+    for name in ("VelocityX", "VelocityY", "VelocityZ", "DynamicPressure"):
+        fn = getattr(L, name)
+        fn.restype = _d
+        fn.argtypes = [C.c_int, C.c_int, C.c_int] + _XYZT
+    L.SurfaceElevation.restype = _d
+    L.SurfaceElevation.argtypes = [C.c_int, C.c_int, _d, _d, _d]
+    L.VolumeFraction.restype = _d
+    L.VolumeFraction.argtypes = [_d] * 5
+    L.Init.restype = C.c_int
+    L.Init.argtypes = [C.c_void_p]
+    L.Prepare.restype = C.c_int
+    L.Prepare.argtypes = [_d, C.c_int]
+    L.Cleanup.restype = C.c_int
+    L.Cleanup.argtypes = []
+    L.cfdwm_kernel_launches.restype = C.c_long
+    L.cfdwm_kernel_launches.argtypes = []
     # batched entry points (pointers may be host or device memory)
     vp = C.c_void_p
     L.wave_SurfElev_batch.restype = C.c_int

@@ -22,7 +22,31 @@
 #include <string>
 #include <vector>
 
+#include <atomic>
+
 namespace cfdwm {
+
+static std::atomic<long> g_launches{0};
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+long launch_count() { return g_launches.load(); }
+
+// Per-kernel event profiler (single-threaded use: benchmarks and tests).
+static bool g_prof = false;
+static std::vector<std::pair<cudaEvent_t, cudaEvent_t>> g_prof_ev[PK_COUNT];
+static cudaEvent_t g_prof_open[PK_COUNT];
+bool prof_on() { return g_prof; }
+void prof_begin(int k, void *stream) {
+    if (!g_prof) return;
+    cudaEventCreate(&g_prof_open[k]);
+    cudaEventRecord(g_prof_open[k], (cudaStream_t)stream);
+}
+void prof_end(int k, void *stream) {
+    if (!g_prof) return;
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecord(e, (cudaStream_t)stream);
+    g_prof_ev[k].push_back({g_prof_open[k], e});
+}
 
 #define CKR(x)                                                 \
     do {                                                       \
@@ -176,6 +200,13 @@ __global__ void k_vfrac(long n, const double *z, const double *eta, double dcell
     out[p] = v;
 }
 
+// [4][n] rows -> [n][4] records (wave_Kinematics layout)
+__global__ void k_interleave4(long n, const double *rows, double *rec) {
+    long p = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    for (int q = 0; q < 4; q++) rec[4 * p + q] = rows[(long)q * n + p];
+}
+
 RampDev ramp_dev(const RampCfg &r) {
     RampDev d;
     d.init = r.init ? 1 : 0;
@@ -201,6 +232,7 @@ int eval_api(long n, const double *x, const double *y, const double *z, const do
     if (rc) return rc;
     double *zc = (double *)api_ws.base, *f = zc + n, *fe = f + 5 * n;
     k_clamp_z<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, z, M.cfg.depth, zc);
+    note_launch();
     CKR(cudaGetLastError());
     RampDev rd = ramp_dev(M.cfg.ramp);
     if (wt == WT_IRREGULAR) {
@@ -214,16 +246,12 @@ int eval_api(long n, const double *x, const double *y, const double *z, const do
         rc = irregular_eval(M.sea, n, x, y, zc, t, mask, f, ws, s);
         if (rc) return rc;
     } else if (wt == WT_IRR_SGRID) {
-        CKR(cudaMemsetAsync(fe, 0, sizeof(double) * 4 * n, s));
-        if (want & 14) {
-            rc = grid_query(M.grid, n, x, y, zc, t, f, s);
-            if (rc) return rc;
-        }
-        if (want & 1) {
-            CKR(cudaMemsetAsync(zc, 0, sizeof(double) * n, s));
-            rc = grid_query(M.grid, n, x, y, zc, t, fe, s);
-            if (rc) return rc;
-        }
+        // get_kinematics_at_point forms eta before it looks at z
+        // (lsgrid_spline.cpp:505-571), so one query serves wave_SurfElev
+        // (queried at z = 0) and the velocities (queried at the clamped z)
+        rc = grid_query(M.grid, n, x, y, zc, t, f, s);
+        if (rc) return rc;
+        fe = f;
     } else if (wt == WT_REGULAR) {
         rc = regular_eval(M.reg, M.cfg, n, x, y, zc, t, f, s);
         if (rc) return rc;
@@ -232,6 +260,7 @@ int eval_api(long n, const double *x, const double *y, const double *z, const do
     }
     k_finish<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(n, wt, rd, M.cfg.rho, M.cfg.gravity, x, y, t,
                                                          f, fe, out);
+    note_launch();
     CKR(cudaGetLastError());
     return OK;
 }
@@ -240,7 +269,8 @@ int eval_api(long n, const double *x, const double *y, const double *z, const do
 // receives row q of the pipeline output (NULL: not wanted).  For VFrac the
 // caller post-processes row 0.
 int run_batch(const double *x, const double *y, const double *z, const double *t, long n,
-              double *const outs[6], int want, double vf_dcell, double *vf_out) {
+              double *const outs[6], int want, double vf_dcell, double *vf_out,
+              double *kin_out = nullptr) {
     if (!g_model.init) return E_NOT_INITIALIZED;
     if (n < 0) return E_BAD_ARGUMENT;
     if (n == 0) return OK;
@@ -249,6 +279,7 @@ int run_batch(const double *x, const double *y, const double *z, const double *t
     bool dev = is_device(x) && is_device(y) && is_device(t) && (!z || is_device(z));
     for (int q = 0; q < 6; q++) if (outs[q] && !is_device(outs[q])) dev = false;
     if (vf_out && !is_device(vf_out)) dev = false;
+    if (kin_out && !is_device(kin_out)) dev = false;
     if (dev) {
         double *out = nullptr;
         Workspace &ws = t_ctx.ws;
@@ -265,6 +296,12 @@ int run_batch(const double *x, const double *y, const double *z, const double *t
                                              cudaMemcpyDeviceToDevice, s));
         if (vf_out) {
             k_vfrac<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, z, out, vf_dcell, vf_out);
+            note_launch();
+            CKR(cudaGetLastError());
+        }
+        if (kin_out) {
+            k_interleave4<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, out, kin_out);
+            note_launch();
             CKR(cudaGetLastError());
         }
         if (!t_ctx.user_set) CKR(cudaStreamSynchronize(s));
@@ -292,6 +329,7 @@ int run_batch(const double *x, const double *y, const double *z, const double *t
         if (rc) return rc;
         if (vf_out) {
             k_vfrac<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(m, din + 2 * m, dout, vf_dcell, dout + 5 * m);
+            note_launch();
             CKR(cudaGetLastError());
         }
         CKR(cudaMemcpyAsync(hp + 4 * m, dout, sizeof(double) * 6 * m, cudaMemcpyDeviceToHost, s));
@@ -299,6 +337,9 @@ int run_batch(const double *x, const double *y, const double *z, const double *t
         for (int q = 0; q < 6; q++)
             if (outs[q]) std::memcpy(outs[q] + b, hp + (4 + q) * m, sizeof(double) * m);
         if (vf_out) std::memcpy(vf_out + b, hp + 9 * m, sizeof(double) * m);
+        if (kin_out)
+            for (long p = 0; p < m; p++)
+                for (int q = 0; q < 4; q++) kin_out[4 * (b + p) + q] = hp[(4 + q) * m + p];
     }
     return OK;
 }
@@ -423,36 +464,8 @@ double *wave_Kinematics(double x, double y, double z, double t) {
     k[0] = k[1] = k[2] = k[3] = 0.0;
     int wt = g_model.cfg.wavetype;
     if (!g_model.init || (wt != WT_IRR_SGRID && wt != WT_IRREGULAR)) return k;
-    double *outs[6] = {&k[0], &k[1], &k[2], &k[3], nullptr, nullptr};
-    if (wt == WT_IRR_SGRID) {
-        // get_kinematics_at_point at the given z (CFDwavemaker.cpp:1625-1635):
-        // eta from the same query, no seabed clamp
-        static thread_local double buf[4];
-        DevGrid &g = g_model.grid;
-        cudaStream_t s = stream_of();
-        double in[4] = {x, y, z, t};
-        double *d = nullptr;
-        if (cudaMalloc(&d, sizeof(double) * 8) != cudaSuccess) return k;
-        cudaMemcpyAsync(d, in, sizeof(in), cudaMemcpyHostToDevice, s);
-        grid_query(g, 1, d, d + 1, d + 2, d + 3, d + 4, s);
-        cudaMemcpyAsync(buf, d + 4, sizeof(double) * 4, cudaMemcpyDeviceToHost, s);
-        cudaStreamSynchronize(s);
-        cudaFree(d);
-        RampCfg &r = g_model.cfg.ramp;
-        double rr = 1.0;
-        if (r.init) {
-            double v[6] = {t, t, x, x, y, y};
-            for (int q = 0; q < 6; q++)
-                if (r.flags & (1 << q)) {
-                    double a = (v[q] - r.lim[2 * q]) / (r.lim[2 * q + 1] - r.lim[2 * q]);
-                    double rq = (q & 1) ? std::max(std::min(1. - a, 1.), 0.) : std::max(std::min(a, 1.), 0.);
-                    rr = std::min(rr, rq);
-                }
-        }
-        for (int q = 0; q < 4; q++) k[q] = buf[q] * rr;
-        return k;
-    }
-    run_batch(&x, &y, &z, &t, 1, outs, 15, 0.0, nullptr);
+    double *outs[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    run_batch(&x, &y, &z, &t, 1, outs, 15, 0.0, nullptr, k);
     return k;
 }
 
@@ -529,55 +542,9 @@ int wave_VFrac_batch(const double *x, const double *y, const double *z, const do
 }
 int wave_Kinematics_batch(const double *x, const double *y, const double *z, const double *t, long n,
                           double *out) {
-    if (n <= 0) return n == 0 ? 0 : E_BAD_ARGUMENT;
-    std::vector<double> tmp(4 * (size_t)n);
-    bool dev = is_device(out);
-    if (g_model.cfg.wavetype == WT_IRR_SGRID) {
-        // eta and velocities from one query at the given (unclamped) z
-        std::vector<double> hin;
-        cudaStream_t s = stream_of();
-        double *d = nullptr;
-        if (cudaMalloc(&d, sizeof(double) * 8 * (size_t)n) != cudaSuccess) return E_CUDA;
-        const double *src[4] = {x, y, z, t};
-        for (int q = 0; q < 4; q++)
-            cudaMemcpyAsync(d + (long)q * n, src[q], sizeof(double) * n, cudaMemcpyDefault, s);
-        int rc = grid_query(g_model.grid, n, d, d + n, d + 2 * n, d + 3 * n, d + 4 * n, s);
-        if (rc) { cudaFree(d); return rc; }
-        cudaMemcpyAsync(tmp.data(), d + 4 * n, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, s);
-        cudaStreamSynchronize(s);
-        std::vector<double> hx(n), hy(n), ht(n);
-        cudaMemcpy(hx.data(), d, sizeof(double) * n, cudaMemcpyDeviceToHost);
-        cudaMemcpy(hy.data(), d + n, sizeof(double) * n, cudaMemcpyDeviceToHost);
-        cudaMemcpy(ht.data(), d + 3 * n, sizeof(double) * n, cudaMemcpyDeviceToHost);
-        cudaFree(d);
-        const RampCfg &r = g_model.cfg.ramp;
-        std::vector<double> res(4 * (size_t)n);
-        for (long p = 0; p < n; p++) {
-            double rr = 1.0;
-            if (r.init) {
-                double v[6] = {ht[p], ht[p], hx[p], hx[p], hy[p], hy[p]};
-                for (int q = 0; q < 6; q++)
-                    if (r.flags & (1 << q)) {
-                        double a = (v[q] - r.lim[2 * q]) / (r.lim[2 * q + 1] - r.lim[2 * q]);
-                        double rq = (q & 1) ? std::max(std::min(1. - a, 1.), 0.) : std::max(std::min(a, 1.), 0.);
-                        rr = std::min(rr, rq);
-                    }
-            }
-            for (int q = 0; q < 4; q++) res[4 * p + q] = tmp[(long)q * n + p] * rr;
-        }
-        if (dev) cudaMemcpy(out, res.data(), sizeof(double) * 4 * n, cudaMemcpyHostToDevice);
-        else std::memcpy(out, res.data(), sizeof(double) * 4 * n);
-        return OK;
-    }
-    double *o4[6] = {tmp.data(), tmp.data() + n, tmp.data() + 2 * n, tmp.data() + 3 * n, nullptr, nullptr};
-    int rc = run_batch(x, y, z, t, n, o4, 15, 0.0, nullptr);
-    if (rc) return rc;
-    std::vector<double> res(4 * (size_t)n);
-    for (long p = 0; p < n; p++)
-        for (int q = 0; q < 4; q++) res[4 * p + q] = tmp[(long)q * n + p];
-    if (dev) cudaMemcpy(out, res.data(), sizeof(double) * 4 * n, cudaMemcpyHostToDevice);
-    else std::memcpy(out, res.data(), sizeof(double) * 4 * n);
-    return OK;
+    double *outs[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    if (n > 0 && !out) return E_BAD_ARGUMENT;
+    return run_batch(x, y, z, t, n, outs, 15, 0.0, nullptr, out);
 }
 
 int cfdwm_set_stream(void *cuda_stream) {
@@ -592,6 +559,29 @@ int cfdwm_last_error(char *buf, int len) {
         std::strncpy(buf, t_ctx.err.c_str(), (size_t)len - 1);
         buf[len - 1] = 0;
     }
+    return n;
+}
+
+long cfdwm_kernel_launches(void) { return launch_count(); }
+
+int cfdwm_profile_enable(int on) {
+    g_prof = on != 0;
+    return OK;
+}
+
+long cfdwm_profile_read(int kernel, double *total_ms) {
+    if (kernel < 0 || kernel >= PK_COUNT) return E_BAD_ARGUMENT;
+    double tot = 0.0;
+    long n = 0;
+    for (auto &pr : g_prof_ev[kernel]) {
+        cudaEventSynchronize(pr.second);
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, pr.first, pr.second) == cudaSuccess) { tot += ms; n++; }
+        cudaEventDestroy(pr.first);
+        cudaEventDestroy(pr.second);
+    }
+    g_prof_ev[kernel].clear();
+    if (total_ms) *total_ms = tot;
     return n;
 }
 

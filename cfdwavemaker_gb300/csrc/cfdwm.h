@@ -76,6 +76,18 @@ struct Config {
     std::string error;
 };
 
+// Count of kernel launches issued by the library (process-wide).
+void note_launch();
+long launch_count();
+
+// Optional per-kernel timing with CUDA events recorded on the launching
+// stream around the hot kernels.
+enum ProfKernel { PK_COLUMN_PAIRS = 0, PK_ETA_PAIRS, PK_POINT_PAIRS, PK_PHASORS, PK_QUERY,
+                  PK_GRADIENTS, PK_QFORM, PK_COUNT };
+bool prof_on();
+void prof_begin(int k, void *stream);
+void prof_end(int k, void *stream);
+
 // waveinput.dat reader (parser.cpp).  Returns OK or E_PARSE (cfg.error set).
 int parse_waveinput_text(const std::string &text, Config &cfg);
 // Search order of wave_Initialize (CFDwavemaker.cpp:2086-2111).

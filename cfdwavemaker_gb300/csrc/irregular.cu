@@ -303,6 +303,7 @@ int sea_build(const Config &cfg, DevSea &sea, bool point_table, void *stream_) {
     k_component_coefs<<<(sea.npad_g + 127) / 128, 128, 0, stream>>>(
         ci, sea.npad_g, cfg.x_pos, cfg.y_pos, cfg.tofmax, d_in + 4 * nn, d_in + 5 * nn,
         d_in + 6 * nn, d_in + 7 * nn, sea.d_phase, sea.d_cf);
+    note_launch();
     CK(cudaGetLastError());
 
     if (cfg.order == 2) {
@@ -312,6 +313,7 @@ int sea_build(const Config &cfg, DevSea &sea, bool point_table, void *stream_) {
         CK(cudaMalloc(&sea.d_tab_grid, sizeof(float) * ent * GRIDV_NC));
         k_build_tables<<<(unsigned)ntiles, 256, 0, stream>>>(ci, GRID_TILE, sea.ntile_g, 0,
                                                              sea.d_tab_eta, sea.d_tab_grid);
+        note_launch();
         CK(cudaGetLastError());
         if (point_table) {
             long ntp = tile_index(sea.ntile_p - 1, sea.ntile_p - 1, sea.ntile_p) + 1;
@@ -319,12 +321,14 @@ int sea_build(const Config &cfg, DevSea &sea, bool point_table, void *stream_) {
             CK(cudaMalloc(&sea.d_tab_point, sizeof(float) * entp * POINTV_NC));
             k_build_tables<<<(unsigned)ntp, 256, 0, stream>>>(ci, POINT_TILE, sea.ntile_p, 1,
                                                               nullptr, sea.d_tab_point);
+            note_launch();
             CK(cudaGetLastError());
         }
         unsigned long long *d_cnt = nullptr, h_cnt = 0;
         CK(cudaMalloc(&d_cnt, sizeof(unsigned long long)));
         CK(cudaMemsetAsync(d_cnt, 0, sizeof(unsigned long long), stream));
         k_count_pairs<<<256, 256, 0, stream>>>(ci, d_cnt);
+        note_launch();
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(&h_cnt, d_cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, stream));
         CK(cudaStreamSynchronize(stream));
@@ -767,7 +771,10 @@ static int launch_phasors(const DevSea &sea, long n, const double *x, const doub
     a.cstride = sea.npad_g; a.fx = sea.fx; a.fy = sea.fy;
     a.trivial_ramp = sea.trivial_ramp ? 1 : 0;
     a.ph = ph; a.rr = rr; a.first = first;
+    prof_begin(PK_PHASORS, stream);
     k_phasors<<<(unsigned)((n + 127) / 128), 128, 0, stream>>>(a);
+    note_launch();
+    prof_end(PK_PHASORS, stream);
     CK(cudaGetLastError());
     return OK;
 }
@@ -791,7 +798,10 @@ int launch_eta_pairs(const DevSea &sea, long n, const float2 *ph, const float *r
                                 (int)smem));
         attr = true;
     }
+    prof_begin(PK_ETA_PAIRS, stream);
     k_pairs_eta<GRID_TILE><<<(unsigned)((n + 127) / 128), 128, smem, stream>>>(a);
+    note_launch();
+    prof_end(PK_ETA_PAIRS, stream);
     CK(cudaGetLastError());
     return OK;
 }
@@ -816,7 +826,10 @@ int launch_column_pairs(const DevSea &sea, long ncol, int nl, const float2 *ph, 
                                       sizeof(float2) * GRID_TILE * 128)));
         attr = true;
     }
+    prof_begin(PK_COLUMN_PAIRS, stream);
     k_pairs_columns<GRID_TILE, LV><<<(unsigned)((ncol + cols - 1) / cols), 128, smem, stream>>>(a);
+    note_launch();
+    prof_end(PK_COLUMN_PAIRS, stream);
     CK(cudaGetLastError());
     return OK;
 }
@@ -834,7 +847,10 @@ static int launch_point_pairs(const DevSea &sea, long n, const float2 *ph, const
                                 (int)smem));
         attr = true;
     }
+    prof_begin(PK_POINT_PAIRS, stream);
     k_pairs_points<POINT_TILE><<<(unsigned)((n + 127) / 128), 128, smem, stream>>>(a);
+    note_launch();
+    prof_end(PK_POINT_PAIRS, stream);
     CK(cudaGetLastError());
     return OK;
 }
@@ -864,6 +880,7 @@ int irregular_eval(const DevSea &sea, long n, const double *x, const double *y, 
         }
         if (mask & 30) {
             k_prep_z<<<(unsigned)((m + 255) / 256), 256, 0, stream>>>(m, z + b, sea.swl, sea.order, L.z0);
+            note_launch();
             CK(cudaGetLastError());
             // the point table is padded to POINT_TILE; the phasor rows beyond
             // npad_p are never read by the point kernel
@@ -872,6 +889,7 @@ int irregular_eval(const DevSea &sea, long n, const double *x, const double *y, 
         }
         k_combine<<<(unsigned)((m + 255) / 256), 256, 0, stream>>>(m, n, sea.order, sea.swl, z + b,
                                                                    L.first, L.sec, eta2, mask, out + b);
+        note_launch();
         CK(cudaGetLastError());
     }
     return OK;

@@ -442,6 +442,7 @@ int regular_build(const Config &cfg, DevRegular &r, void *stream_) {
     if (r.theory == 0) {
         if (in.L <= 0 || in.d <= 0) return E_BAD_ARGUMENT;
         k_stokes_setup<<<1, 32, 0, stream>>>(in, r.d_sol);
+        note_launch();
         CK(cudaGetLastError());
         r.N = 5;
     } else {
@@ -453,6 +454,7 @@ int regular_build(const Config &cfg, DevRegular &r, void *stream_) {
         CK(cudaMalloc(&work, sizeof(double) * ((size_t)ld * ld + 128 * 2 * (size_t)ld)));
         CK(cudaMemsetAsync(work, 0, sizeof(double) * (size_t)ld * ld, stream));
         k_fenton_solve<<<1, 128, 0, stream>>>(in, r.d_sol, work);
+        note_launch();
         CK(cudaGetLastError());
         CK(cudaStreamSynchronize(stream));
         cudaFree(work);
@@ -483,6 +485,7 @@ int regular_eval(const DevRegular &r, const Config &cfg, long n, const double *x
     a.x0 = cfg.x_pos; a.y0 = cfg.y_pos; a.t0 = cfg.tofmax; a.z0 = cfg.swl; a.d = cfg.depth;
     a.g = cfg.gravity; a.rho = cfg.rho;
     k_regular_eval<<<(unsigned)((n + 127) / 128), 128, 0, stream>>>(a);
+    note_launch();
     CK(cudaGetLastError());
     return OK;
 }

@@ -50,9 +50,14 @@ struct GridGeom {
     double d0, d2, dx, dy, ds, depth, swl, tan_a, tan_b, dt;
 };
 
-// sigmaS2cart (lsgrid_spline.cpp:117-122) in FP64.
-__device__ __forceinline__ double d_sigmaS2cart(const GridGeom &g, double s, double e) {
-    double sigma = -pow(tan(-(s - 1) * g.tan_a), g.tan_b) / pow(tan(g.tan_a), g.tan_b);
+// sigmaS2cart (lsgrid_spline.cpp:117-122) in FP64 for level m, s = m * ds.
+// s and s - 1 are rounded explicitly: a fused m*ds - 1 leaves +5.6e-17 at the
+// surface level (0.2 * 5 - 1) where the reference's separately rounded
+// product gives exactly 0, and pow() of the then negative tangent is NaN.
+__device__ __forceinline__ double d_sigmaS2cart(const GridGeom &g, int m, double e) {
+    double s = __dmul_rn(g.ds, (double)m);
+    double base = fmax(tan(-__dadd_rn(s, -1.0) * g.tan_a), 0.0);
+    double sigma = -pow(base, g.tan_b) / pow(tan(g.tan_a), g.tan_b);
     return (e - g.swl) + sigma * (g.depth + (e - g.swl));
 }
 
@@ -76,7 +81,7 @@ __global__ void k_levels(GridGeom g, long nact, const int *act, const double *fi
     for (int m = 0; m < g.nl; m++) {
         // the reference evaluates the levels from the stored value; the FP32
         // store is the value the query sees, so use it here too
-        double z = d_sigmaS2cart(g, g.ds * m, (double)ef);
+        double z = d_sigmaS2cart(g, m, (double)ef);
         zmin[q * g.nl + m] = (float)fmin(0.0, z);
         zmax[q * g.nl + m] = (float)fmax(0.0, z - g.swl);
     }
@@ -406,6 +411,7 @@ static int fill_slot(DevGrid &g, const DevSea &sea, Workspace &ws, int slot, dou
     float *rr = (float *)(b + b_ph);
     double *first = (double *)(b + b_ph + b_rr);
     k_column_coords<<<(unsigned)((nact + 255) / 256), 256, 0, stream>>>(G, nact, act, x->xy);
+    note_launch();
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(x->tdev, &t, sizeof(double), cudaMemcpyHostToDevice, stream));
     rc = launch_phasors_public(sea, nact, x->xy, x->xy + nact, x->tdev, 1, 1, 0, npad, ph, rr, first, stream);
@@ -414,12 +420,14 @@ static int fill_slot(DevGrid &g, const DevSea &sea, Workspace &ws, int slot, dou
     if (rc) return rc;
     k_levels<<<(unsigned)((nact + 127) / 128), 128, 0, stream>>>(G, nact, act, first, x->eta2, slot, g.ETA,
                                                                  x->zmin, x->zmax);
+    note_launch();
     CK(cudaGetLastError());
     rc = launch_column_pairs(sea, nact, g.nl, ph, rr, x->zmin, x->sec, 1, stream);
     if (rc) return rc;
     long tot = nact * g.nl;
     k_scatter_levels<<<(unsigned)((tot + 255) / 256), 256, 0, stream>>>(G, nact, act, first, x->sec, x->zmax,
                                                                         slot, g.U[0], g.U[1], g.U[2]);
+    note_launch();
     CK(cudaGetLastError());
     return OK;
 }
@@ -435,7 +443,10 @@ static int gradients(DevGrid &g, cudaStream_t stream) {
     }
     long nodes = (long)g.nx * g.ny * g.nl;
     dim3 grid((unsigned)((nodes + 255) / 256), 4);
+    prof_begin(PK_GRADIENTS, stream);
     k_gradients<<<grid, 256, 0, stream>>>(a);
+    note_launch();
+    prof_end(PK_GRADIENTS, stream);
     CK(cudaGetLastError());
     return OK;
 }
@@ -482,7 +493,10 @@ int grid_query(const DevGrid &g, long n, const double *x, const double *y, const
         a.U[f] = g.U[f]; a.Ut[f] = g.Ut[f]; a.Ux[f] = g.Ux[f]; a.Uy[f] = g.Uy[f]; a.Us[f] = g.Us[f];
     }
     a.n = n; a.x = x; a.y = y; a.z = z; a.t = t; a.out = out;
+    prof_begin(PK_QUERY, stream);
     k_query<<<(unsigned)((n + 127) / 128), 128, 0, stream>>>(a);
+    note_launch();
+    prof_end(PK_QUERY, stream);
     CK(cudaGetLastError());
     return OK;
 }

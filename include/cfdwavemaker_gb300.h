@@ -128,6 +128,15 @@ CFDWM_EXPORT int cfdwm_last_error(char *buf, int len);
 /* ---------------------------------------------------------------------- */
 /* Part 3: introspection hooks for tests and diagnostics                   */
 /* ---------------------------------------------------------------------- */
+/* Number of CUDA kernels the library has launched so far (process-wide). */
+CFDWM_EXPORT long cfdwm_kernel_launches(void);
+/* Per-kernel timing with CUDA events on the launching stream: enable, run,
+ * then read the summed duration (ms) and the launch count of one kernel:
+ * 0 s-grid column pair sums, 1 elevation pair sums, 2 point pair sums,
+ * 3 phasors, 4 s-grid query, 5 s-grid gradients, 6 quadratic-form GEMM.
+ * Reading clears the record. */
+CFDWM_EXPORT int cfdwm_profile_enable(int on);
+CFDWM_EXPORT long cfdwm_profile_read(int kernel, double *total_ms);
 /* Wave type code of the loaded model (1, 5, 21; 0 when none). */
 CFDWM_EXPORT int cfdwm_wavetype(void);
 /* Irregular::eta/u/v/w/dp without ramp or seabed clamp (Irregular.cpp:9-157)

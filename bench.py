@@ -150,7 +150,7 @@ def run_ours(args):
     os.chdir(work)
     wm = cw.CFDwavemaker()
     if args.workload == "sgrid":
-        txt = sgrid_config()
+        txt = sgrid_config(args.grid, args.grid)
     else:
         txt = point_config()
     t_init = time.time()
@@ -174,7 +174,7 @@ def run_ours(args):
         hq = [torch.from_numpy(a).pin_memory() for a in (qx, qy, qz)]
         htq = torch.empty(nq, dtype=torch.float64).pin_memory()
         hout = np.empty((nq, 4))
-        nodes = 256 * 256 * 16
+        nodes = args.grid * args.grid * 16
 
         def step_device():
             # one ring update + 1e6 queries at a time inside the new interval
@@ -373,6 +373,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="sgrid", choices=["sgrid", "point"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--grid", type=int, default=256,
+                    help="columns per side of the s-grid (256 is the named workload; smaller sizes "
+                         "are for profiling captures only)")
     args = ap.parse_args()
     unit = "grid nodes/s" if args.workload == "sgrid" else "points/s"
     workload = ("s-grid second-order update: 1024-component short-crested JONSWAP (64 freq x 16 dir, "

@@ -119,6 +119,14 @@ def load(path: str | None = None):
     L.cfdwm_regular_solution.argtypes = [vp, C.c_int]
     L.cfdwm_parse_text.restype = C.c_int
     L.cfdwm_parse_text.argtypes = [C.c_char_p, vp, vp, C.c_int]
+    L.cfdwm_qform_build.restype = C.c_int
+    L.cfdwm_qform_build.argtypes = [C.c_int]
+    L.cfdwm_qform_eval.restype = C.c_int
+    L.cfdwm_qform_eval.argtypes = [vp, vp, vp, C.c_long, C.c_int, vp]
+    L.cfdwm_profile_enable.restype = C.c_int
+    L.cfdwm_profile_enable.argtypes = [C.c_int]
+    L.cfdwm_profile_read.restype = C.c_long
+    L.cfdwm_profile_read.argtypes = [C.c_int, _dp]
     if path is None:
         _LIB = L
     return L

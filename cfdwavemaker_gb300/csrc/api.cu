@@ -346,6 +346,7 @@ int run_batch(const double *x, const double *y, const double *z, const double *t
 
 void free_model() {
     Model &M = g_model;
+    qform_free();
     sea_free(M.sea);
     grid_free(M.grid);
     regular_free(M.reg);
@@ -411,6 +412,7 @@ double scalar(int q, double x, double y, double z, double t) {
 }
 
 }  // namespace
+
 }  // namespace cfdwm
 
 using namespace cfdwm;
@@ -636,6 +638,36 @@ int cfdwm_sgrid_state(double *t0, int *tstep) {
     if (!g_model.init || g_model.cfg.wavetype != WT_IRR_SGRID) return E_UNSUPPORTED;
     if (t0) *t0 = g_model.grid.t0;
     if (tstep) *tstep = g_model.grid.tstep;
+    return OK;
+}
+
+int cfdwm_qform_build(int fp16) {
+    Model &M = g_model;
+    if (!M.init) return E_NOT_INITIALIZED;
+    if (M.cfg.wavetype != WT_IRREGULAR && M.cfg.wavetype != WT_IRR_SGRID) return E_UNSUPPORTED;
+    if (M.cfg.order != 2) return E_UNSUPPORTED;
+    int rc = qform_build(M.cfg, M.sea, fp16 != 0, stream_of());
+    if (rc) set_error("precision-form set-up failed");
+    return rc;
+}
+
+int cfdwm_qform_eval(const double *x, const double *y, const double *t, long n, int method, float *out) {
+    Model &M = g_model;
+    if (!M.init) return E_NOT_INITIALIZED;
+    if (n <= 0) return n == 0 ? OK : E_BAD_ARGUMENT;
+    if (!is_device(x) || !is_device(y) || !is_device(t) || !is_device(out)) {
+        set_error("cfdwm_qform_eval takes device arrays");
+        return E_BAD_ARGUMENT;
+    }
+    cudaStream_t s = stream_of();
+    int err = 0;
+    int rc = qform_eval(M.sea, n, x, y, t, method, out, s, method == 1 ? &err : nullptr);
+    if (rc) return rc;
+    if (!t_ctx.user_set || method == 1) CKR(cudaStreamSynchronize(s));
+    if (err) {
+        set_error("tensor-core kernel: a bounded wait expired (code " + std::to_string(err) + ")");
+        return E_CUDA;
+    }
     return OK;
 }
 

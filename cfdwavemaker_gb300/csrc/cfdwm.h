@@ -225,6 +225,17 @@ int regular_eval(const DevRegular &r, const Config &cfg, long n, const double *x
 int regular_solution(const DevRegular &r, double *dst, int cap, void *stream);
 
 // ---------------------------------------------------------------------------
+// Precision form (qform.cu): second-order sums at z = 0 as quadratic forms
+// ---------------------------------------------------------------------------
+int qform_build(const Config &cfg, const DevSea &sea, bool fp16, void *stream);
+void qform_free();
+// out [n][4] FP32: eta2, u2, v2, w2 at z0 = 0 (grid mask); method 0 plain
+// FP32 CUDA cores, 1 tcgen05 tensor cores.  *tc_error: nonzero if a bounded
+// wait of the tensor-core kernel expired.
+int qform_eval(const DevSea &sea, long n, const double *x, const double *y, const double *t, int method,
+               float *out, void *stream, int *tc_error);
+
+// ---------------------------------------------------------------------------
 // Post-processing shared by the API (api_kernels.cu)
 // ---------------------------------------------------------------------------
 // Ramp::ramp applied to [nf][n] fields in place (Utils.cpp:42-68).

@@ -1,0 +1,780 @@
+// Precision form: the second-order sums at z = 0 (the surface elevation and
+// the Taylor-layer velocities above the still-water level) as quadratic
+// forms over each point's phasor vector, evaluated on the tcgen05 tensor
+// cores with split 16-bit operands.
+//
+// What is computed: for each point p with phasors c_i = cos(phi_i),
+// s_i = sin(phi_i) and ramps r_i,
+//   eta2 = sum_{i<=m} r_i [A_e c_i c_m + B_e s_i s_m]             (Irregular.cpp:223-293)
+//   u2, v2 at z0 = 0: the same form with A_u = Pu + Mu, B_u = Mu - Pu
+//   w2 at z0 = 0:     sum r_i [C_w s_i c_m + D_w c_i s_m], C,D = Pw' +- Mw'
+// with the uvw2 pair-cache coefficients (Irregular.cpp:975-1102) at z = 0,
+// where cosh(k(z+h))/cosh(kh) = 1 and sinh(k(z+h))/cosh(kh) = tanh(kh).
+// These are the second-order parts the reference evaluates for every point
+// at or above the still-water level (Irregular.cpp:24-39, lsgrid_spline.cpp:890-897).
+//
+// As a GEMM: X = [r c | r s] (rows = points, K = 2N), W = the eight N x N
+// upper-triangular coefficient blocks (eta, u, v, w) x (cos, sin half),
+// T = X W, and each output is the row-wise dot of a T block with c or s.
+//
+// GB300 design:
+//  * X is split into hi + lo 16-bit parts (bf16 or fp16) by a prep kernel
+//    that writes one chunk of rows to a scratch buffer; W is split once at
+//    set-up (stored transposed, K-major, as the B operand).
+//  * k_qform_tc: warp-specialised tcgen05 GEMM, one 128 x 256 output tile
+//    per CTA: warp 0 issues TMA loads (128B swizzle) into a two-stage ring,
+//    one thread of warp 1 issues tcgen05.mma (M=128, N=256, K=16) for the
+//    three split products Xh Wh + Xh Wl + Xl Wh into an FP32 TMEM
+//    accumulator (fp16: the cross products go to a second accumulator with
+//    the lo parts scaled by 2^11), warps 2-5 read TMEM with tcgen05.ld,
+//    multiply by the right-hand phasors and reduce the row, one atomic add
+//    per (row, tile).  Tiles are ordered in groups so that the X and W tiles
+//    in flight stay L2-resident.  Only the K blocks of the upper triangle are
+//    visited.  Every mbarrier wait is bounded; a timeout sets an error word.
+//  * k_qform_plain: the same sums on FP32 CUDA cores (the plain form).
+#include "cfdwm.h"
+
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
+namespace cfdwm {
+
+#define CK(x)                                                  \
+    do {                                                       \
+        cudaError_t e_ = (x);                                  \
+        if (e_ != cudaSuccess) {                               \
+            std::fprintf(stderr, "cfdwm: CUDA error %s at %s:%d\n", \
+                         cudaGetErrorString(e_), __FILE__, __LINE__); \
+            return E_CUDA;                                     \
+        }                                                      \
+    } while (0)
+
+constexpr int QT = 32;          // tile of the plain table (components)
+constexpr int QNC = 8;          // plain record: Ae, Be, Au, Bu, Av, Bv, Cw, Dw
+constexpr double TWO_PI_Q = 6.283185307179586476925286766559;
+constexpr double INV_TWO_PI_Q = 0.15915494309189533576888376337251;
+
+__host__ __device__ inline long qtile_index(int I, int M, int nt) {
+    return (long)I * nt - (long)I * (I - 1) / 2 + (M - I);
+}
+
+__device__ __forceinline__ double q_freq_ramp(double t, double rt, double ts, double du) {
+    double rampdown = fmax(fmin(1. - ((t - ts - du + rt) / (rt + SMALL)), 1.), 0.);
+    double rampup = fmax(fmin(((t - ts) / (rt + SMALL)), 1.), 0.);
+    return rampup * rampdown;
+}
+
+// ---------------------------------------------------------------------------
+// Coefficients at z = 0 from the pair-cache transfer functions (FP64)
+// ---------------------------------------------------------------------------
+struct QIn {
+    int n;
+    const double *omega, *A, *k, *theta;
+    double depth, g, mtheta_rad, cutoff, bandwidth, kmax;
+};
+
+// value of the eight coefficients of entry (i, m), i <= m
+__device__ void q_coefs(const QIn &c, int i, int m, double out[QNC]) {
+    for (int q = 0; q < QNC; q++) out[q] = 0.0;
+    if (i >= c.n || m >= c.n || i > m) return;
+    const double h = c.depth, g = c.g;
+    double ki = c.k[i], oi = c.omega[i], Ai = c.A[i];
+    double thi = c.theta[i] + c.mtheta_rad, cti = cos(thi), sti = sin(thi);
+    double Rn = ki * tanh(ki * h), Rsn = sqrt(Rn), agi = Ai * g / oi;
+    if (i == m) {
+        if (oi > c.cutoff) return;
+        double Dnn = (6.0 * Rsn * Rsn * (ki * ki - Rn * Rn)) / (2.0 * Rsn * Rsn - ki * tanh(2.0 * ki * h));
+        double AAd = 0.25 * agi * agi * (Dnn / (2.0 * oi));
+        if (2.0 * ki <= c.kmax) {
+            double ann = (Dnn - (ki * ki - Rn * Rn)) / Rn + 2.0 * Rn;
+            double pe = 0.25 * Ai * Ai * ann;
+            out[0] = pe; out[1] = -pe;                       // cos(2 phi) = c^2 - s^2
+        }
+        double pu = AAd * 2.0 * ki * cti, pv = AAd * 2.0 * ki * sti;
+        out[2] = pu; out[3] = -pu;
+        out[4] = pv; out[5] = -pv;
+        double pw = AAd * 2.0 * ki * tanh(2.0 * ki * h);    // sin(2 phi) = 2 s c
+        out[6] = pw; out[7] = pw;
+        return;
+    }
+    double km = c.k[m], om = c.omega[m], Am = c.A[m];
+    double thm = c.theta[m] + c.mtheta_rad, ctm = cos(thm), stm = sin(thm);
+    double Rm = km * tanh(km * h), Rsm = sqrt(Rm), agm = Am * g / om;
+    if (oi > c.cutoff || om > c.cutoff || fabs(oi - om) > c.bandwidth) return;
+    bool hp = (ki + km) <= c.kmax, hm = (ki != km);
+    double gam = cti * ctm + sti * stm;
+    double kp = sqrt(ki * ki + km * km + 2.0 * ki * km * gam);
+    double kq = sqrt(ki * ki + km * km - 2.0 * ki * km * gam);
+    double sp = Rsn + Rsm, sm = Rsn - Rsm, R2p = sp * sp, R2m = sm * sm;
+    double AA = 0.5 * agi * agm;
+    double Pe = 0, Me = 0, Pu = 0, Mu = 0, Pv = 0, Mv = 0, Pw = 0, Mw = 0;
+    if (hp) {
+        double den = R2p - kp * tanh(kp * h);
+        double Dp = (2.0 * R2p * (ki * km * gam - Rn * Rm)) / den +
+                    (sp * (Rsn * (km * km - Rm * Rm) + Rsm * (ki * ki - Rn * Rn))) / den;
+        double ap = (Dp - (ki * km * gam - Rn * Rm)) / sqrt(Rn * Rm) + (Rn + Rm);
+        double BB = Dp / (oi + om);
+        Pe = 0.5 * Ai * Am * ap;
+        Pu = AA * BB * (ki * cti + km * ctm);
+        Pv = AA * BB * (ki * sti + km * stm);
+        Pw = AA * BB * kp * tanh(kp * h);
+    }
+    if (hm) {
+        double den = R2m - kq * tanh(kq * h);
+        double Dm = (2.0 * R2m * (ki * km * gam + Rn * Rm)) / den +
+                    (sm * (-Rsn * (km * km - Rm * Rm) + Rsm * (ki * ki - Rn * Rn))) / den;
+        double am = (Dm - (ki * km * gam + Rn * Rm)) / sqrt(Rn * Rm) + (Rn + Rm);
+        double CC = Dm / (oi - om);
+        Me = 0.5 * Ai * Am * am;
+        Mu = AA * CC * (ki * cti - km * ctm);
+        Mv = AA * CC * (ki * sti - km * stm);
+        Mw = AA * CC * kq * tanh(kq * h);
+    }
+    // cos(a+b) = cc - ss, cos(a-b) = cc + ss, sin(a+b) = sc + cs, sin(a-b) = sc - cs
+    out[0] = Pe + Me; out[1] = Me - Pe;
+    out[2] = Pu + Mu; out[3] = Mu - Pu;
+    out[4] = Pv + Mv; out[5] = Mv - Pv;
+    out[6] = Pw + Mw; out[7] = Pw - Mw;
+}
+
+// FP64 coefficients of every pair, once: coef[b][m][i] (W^T layout) for the
+// eight GEMM blocks.  Block b: field (b & 3) -- eta, u, v, w -- and left
+// half (b >> 2): 0 uses X = r c, 1 uses X = r s; the record index of block b
+// is {A_e, A_u, A_v, D_w, B_e, B_u, B_v, C_w}.
+__global__ void k_qform_coef64(QIn c, int npad, double *coef) {
+    long e = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    long tot = (long)npad * npad;
+    if (e >= tot) return;
+    int m = (int)(e / npad), i = (int)(e % npad);
+    static const int idx[8] = {0, 2, 4, 7, 1, 3, 5, 6};
+    double rec[QNC];
+    q_coefs(c, i, m, rec);
+    for (int b = 0; b < 8; b++) coef[((long)b * npad + m) * npad + i] = rec[idx[b]];
+}
+
+// plain table tiles from the FP64 coefficients
+__global__ void k_qform_plain_from64(int npad, int nt, const double *coef, float *tab) {
+    long t = blockIdx.x;
+    int I = 0;
+    while (qtile_index(I, nt - 1, nt) < t) I++;
+    int M = (int)(t - qtile_index(I, I, nt)) + I;
+    static const int rec_of_block[8] = {0, 2, 4, 7, 1, 3, 5, 6};
+    for (int e = threadIdx.x; e < QT * QT; e += blockDim.x) {
+        int ii = e / QT, mm = e % QT, i = I * QT + ii, m = M * QT + mm;
+        long base = (t * QT * QT + e) * QNC;
+        for (int b = 0; b < 8; b++)
+            tab[base + rec_of_block[b]] = (float)coef[((long)b * npad + m) * npad + i];
+    }
+}
+
+// B operand of the tensor-core form, split into hi and lo 16-bit parts.
+// For fp16 each column m is scaled by 2^e_m (column maximum near 2^14) and
+// the lo part by a further 2^11; colscale[b][m] holds 2^-e_m (1 for bf16).
+template <typename T16>
+__global__ void k_qform_split(int npad, int fp16, const double *coef, T16 *Whi, T16 *Wlo, float *colscale) {
+    const int b = blockIdx.y, m = blockIdx.x;
+    const double *row = coef + ((long)b * npad + m) * npad;
+    __shared__ double red[32];
+    __shared__ double smax;
+    double lmax = 0.0;
+    for (int i = threadIdx.x; i < npad; i += blockDim.x) lmax = fmax(lmax, fabs(row[i]));
+    for (int o = 16; o > 0; o >>= 1) lmax = fmax(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = lmax;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double mx = 0.0;
+        for (int w = 0; w < (int)(blockDim.x + 31) / 32; w++) mx = fmax(mx, red[w]);
+        smax = mx;
+    }
+    __syncthreads();
+    double scale = 1.0;
+    if (fp16 && smax > 0.0) {
+        int ex;
+        frexp(smax, &ex);               // smax = f 2^ex, f in [0.5, 1)
+        scale = ldexp(1.0, 14 - ex);
+    }
+    if (threadIdx.x == 0) colscale[(long)b * npad + m] = (float)(1.0 / scale);
+    for (int i = threadIdx.x; i < npad; i += blockDim.x) {
+        double v = row[i] * scale;
+        T16 hi, lo;
+        if (fp16) {
+            __half h = __float2half_rn((float)v);
+            __half l = __float2half_rn((float)((v - (double)__half2float(h)) * 2048.0));
+            hi = *reinterpret_cast<T16 *>(&h);
+            lo = *reinterpret_cast<T16 *>(&l);
+        } else {
+            __nv_bfloat16 h = __float2bfloat16_rn((float)v);
+            __nv_bfloat16 l = __float2bfloat16_rn((float)(v - (double)__bfloat162float(h)));
+            hi = *reinterpret_cast<T16 *>(&h);
+            lo = *reinterpret_cast<T16 *>(&l);
+        }
+        long o = ((long)b * npad + m) * npad + i;
+        Whi[o] = hi;
+        Wlo[o] = lo;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Phasor prep for a chunk of rows: X hi/lo (16-bit, [rows][2 npad]) and the
+// right-hand phasors Y (FP32, [rows][2 npad]).
+// ---------------------------------------------------------------------------
+struct QPrep {
+    long rows;
+    const double *x, *y, *t;
+    const double *phase;       // [7][cstride] kx, ky, omega, phase0, ramp params
+    int cstride, ncomp, npad;
+    double fx, fy;
+    int trivial_ramp, fp16;
+    void *Xhi, *Xlo;           // [rows][2 npad]
+    float *Y;                  // [rows][2 npad]
+};
+
+__global__ void __launch_bounds__(256) k_qform_prep(QPrep a) {
+    long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    long tot = a.rows * a.npad;
+    if (idx >= tot) return;
+    long p = idx / a.npad;
+    int i = (int)(idx % a.npad);
+    float c = 0.f, s = 0.f, r = 0.f;
+    if (i < a.ncomp) {
+        const double *P = a.phase;
+        const int cs = a.cstride;
+        double dx = a.x[p] - a.fx, dy = a.y[p] - a.fy, t = a.t[p];
+        double ph = fma(P[i], dx, fma(P[cs + i], dy, fma(-P[2 * cs + i], t, P[3 * cs + i])));
+        double nn = rint(ph * INV_TWO_PI_Q);
+        float red = (float)fma(-nn, TWO_PI_Q, ph);
+        sincosf(red, &s, &c);
+        int ir = a.trivial_ramp ? 0 : i;
+        r = (float)q_freq_ramp(t, P[4 * cs + ir], P[5 * cs + ir], P[6 * cs + ir]);
+    }
+    long o = p * 2 * a.npad + i;
+    a.Y[o] = c;
+    a.Y[o + a.npad] = s;
+    float xc = r * c, xs = r * s;
+    if (a.fp16) {
+        __half *H = (__half *)a.Xhi, *L = (__half *)a.Xlo;
+        __half hc = __float2half_rn(xc), hs = __float2half_rn(xs);
+        H[o] = hc;
+        H[o + a.npad] = hs;
+        L[o] = __float2half_rn((xc - __half2float(hc)) * 2048.0f);
+        L[o + a.npad] = __float2half_rn((xs - __half2float(hs)) * 2048.0f);
+    } else {
+        __nv_bfloat16 *H = (__nv_bfloat16 *)a.Xhi, *L = (__nv_bfloat16 *)a.Xlo;
+        __nv_bfloat16 hc = __float2bfloat16_rn(xc), hs = __float2bfloat16_rn(xs);
+        H[o] = hc;
+        H[o + a.npad] = hs;
+        L[o] = __float2bfloat16_rn(xc - __bfloat162float(hc));
+        L[o + a.npad] = __float2bfloat16_rn(xs - __bfloat162float(hs));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Plain FP32 form (CUDA cores): thread per point, tiles staged in smem.
+// ---------------------------------------------------------------------------
+struct QPlain {
+    long rows;
+    int ntile;
+    const float *tab;        // plain tiles
+    const float2 *ph;        // [npad][rows] (c, s)
+    const float *rr;         // [npad][rows]
+    float *out;              // [rows][4]
+};
+
+constexpr int QPLAIN_SMEM = QT * QT * QNC * 4 + QT * 128 * 8;
+
+__global__ void __launch_bounds__(128) k_qform_plain(QPlain a) {
+    extern __shared__ float4 q_smem[];
+    float4 *s_tab = q_smem;                                         // QT*QT*QNC/4
+    float2 *s_ph = reinterpret_cast<float2 *>(q_smem + QT * QT * QNC / 4);   // QT*128
+    const long p = (long)blockIdx.x * 128 + threadIdx.x;
+    const bool valid = p < a.rows;
+    const long pc = valid ? p : 0;
+    float S[4] = {0, 0, 0, 0}, Cc[4] = {0, 0, 0, 0};
+    for (int I = 0; I < a.ntile; I++) {
+        for (int M = I; M < a.ntile; M++) {
+            __syncthreads();
+            const float4 *src = reinterpret_cast<const float4 *>(a.tab + qtile_index(I, M, a.ntile) * (long)QT * QT * QNC);
+            for (int e = threadIdx.x; e < QT * QT * QNC / 4; e += blockDim.x) s_tab[e] = src[e];
+            for (int mm = 0; mm < QT; mm++) s_ph[mm * 128 + threadIdx.x] = a.ph[(long)(M * QT + mm) * a.rows + pc];
+            __syncthreads();
+            if (!valid) continue;
+            for (int ii = 0; ii < QT; ii++) {
+                const int i = I * QT + ii;
+                const float2 pi = a.ph[(long)i * a.rows + p];
+                const float ri = a.rr[(long)i * a.rows + p];
+                float ec = 0, es = 0, uc = 0, us = 0, vc = 0, vs = 0, wc = 0, ws = 0;
+                const int m0 = (M == I) ? ii : 0;
+                for (int mm = m0; mm < QT; mm++) {
+                    const float4 c0 = s_tab[(ii * QT + mm) * 2];
+                    const float4 c1 = s_tab[(ii * QT + mm) * 2 + 1];
+                    const float2 pm = s_ph[mm * 128 + threadIdx.x];
+                    ec = fmaf(c0.x, pm.x, ec); es = fmaf(c0.y, pm.y, es);
+                    uc = fmaf(c0.z, pm.x, uc); us = fmaf(c0.w, pm.y, us);
+                    vc = fmaf(c1.x, pm.x, vc); vs = fmaf(c1.y, pm.y, vs);
+                    wc = fmaf(c1.z, pm.x, wc); ws = fmaf(c1.w, pm.y, ws);
+                }
+                float v[4] = {fmaf(pi.x, ec, pi.y * es), fmaf(pi.x, uc, pi.y * us),
+                              fmaf(pi.x, vc, pi.y * vs), fmaf(pi.y, wc, pi.x * ws)};
+                for (int f = 0; f < 4; f++) {
+                    float y = ri * v[f] - Cc[f];
+                    float tt = S[f] + y;
+                    Cc[f] = (tt - S[f]) - y;
+                    S[f] = tt;
+                }
+            }
+        }
+    }
+    if (valid)
+        for (int f = 0; f < 4; f++) a.out[p * 4 + f] = S[f];
+}
+
+// ---------------------------------------------------------------------------
+// tcgen05 tensor-core form
+// ---------------------------------------------------------------------------
+constexpr int TBM = 128, TBN = 256, TBK = 64, TSTAGES = 2;
+constexpr int A_TILE = TBM * TBK * 2;     // 16 KiB
+constexpr int B_TILE = TBN * TBK * 2;     // 32 KiB
+constexpr int STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;
+constexpr int TC_SMEM = TSTAGES * STAGE_BYTES + 1024 + 256;
+constexpr long long WAIT_LIMIT = 4000000000LL;   // clock cycles (about 2 s)
+
+__device__ __forceinline__ uint32_t su32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *b, uint32_t n) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(b)), "r"(n));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *b, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint64_t *b, uint32_t parity) {
+    uint32_t ok;
+    asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(ok) : "r"(su32(b)), "r"(parity) : "memory");
+    return ok != 0;
+}
+// bounded wait: false (and the error word set) after WAIT_LIMIT cycles
+__device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity, int *err, int code) {
+    long long t0 = clock64();
+    while (!mbar_try(b, parity)) {
+        if (clock64() - t0 > WAIT_LIMIT) {
+            atomicExch(err, code);
+            return false;
+        }
+    }
+    return true;
+}
+__device__ __forceinline__ void tma_2d(void *dst, const CUtensorMap *m, uint64_t *bar, int x, int y) {
+    asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];"
+                 ::"r"(su32(dst)), "l"(m), "r"(su32(bar)), "r"(x), "r"(y) : "memory");
+}
+// K-major operand in the 128-byte swizzle layout: 8-row groups 1024 B apart
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
+    uint64_t d = (uint64_t)((saddr & 0x3FFFF) >> 4);
+    d |= (uint64_t)1 << 16;
+    d |= (uint64_t)(1024 >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)2 << 61;
+    return d;
+}
+__device__ __forceinline__ void umma(uint32_t dt, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+    asm volatile("{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}"
+                 ::"r"(dt), "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+__device__ __forceinline__ void umma_commit(uint64_t *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(bar)) : "memory");
+}
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7]),
+          "=f"(v[8]), "=f"(v[9]), "=f"(v[10]), "=f"(v[11]), "=f"(v[12]), "=f"(v[13]), "=f"(v[14]), "=f"(v[15]),
+          "=f"(v[16]), "=f"(v[17]), "=f"(v[18]), "=f"(v[19]), "=f"(v[20]), "=f"(v[21]), "=f"(v[22]), "=f"(v[23]),
+          "=f"(v[24]), "=f"(v[25]), "=f"(v[26]), "=f"(v[27]), "=f"(v[28]), "=f"(v[29]), "=f"(v[30]), "=f"(v[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+struct QTC {
+    long rows;               // rows of this chunk
+    int npad;                // components (multiple of 256)
+    int ntn;                 // column tiles per block (npad / 256)
+    int group_m;             // row blocks per tile group
+    const float *Y;          // [rows][2 npad]
+    const float *colscale;   // [8][npad] (1 for bf16)
+    float *out;              // [rows][4] accumulated with atomics
+    int fp16;
+    int *err;
+};
+
+// Grid: one CTA per (row block, column tile).  Column tiles: 8 blocks x ntn.
+__global__ void __launch_bounds__(192, 1) k_qform_tc(const __grid_constant__ CUtensorMap mXh,
+                                                     const __grid_constant__ CUtensorMap mXl,
+                                                     const __grid_constant__ CUtensorMap mWh,
+                                                     const __grid_constant__ CUtensorMap mWl, QTC a) {
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t *full = (uint64_t *)(smem + TSTAGES * STAGE_BYTES);
+    uint64_t *empty = full + TSTAGES;
+    uint64_t *accf = empty + TSTAGES;
+    uint32_t *tmem_slot = (uint32_t *)(accf + 1);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    // grouped tile order: a group of group_m row blocks sweeps all column tiles
+    const long nrb = (a.rows + TBM - 1) / TBM;
+    const int ncol = 8 * a.ntn;
+    long bid = blockIdx.x;
+    long per_group = (long)a.group_m * ncol;
+    long grp = bid / per_group;
+    long in = bid % per_group;
+    long gm0 = grp * a.group_m;
+    long gsz = nrb - gm0 < a.group_m ? nrb - gm0 : a.group_m;
+    long rb = gm0 + in % gsz;
+    int ct = (int)(in / gsz);
+    if (rb >= nrb || ct >= ncol) return;
+    const int blk = ct / a.ntn, tn = ct % a.ntn;
+    const int field = blk & 3, khalf = blk >> 2;
+    const int m0 = tn * TBN;
+    const int nkb = (m0 + TBN) / TBK;            // upper triangle: i < m0 + 256
+    // right-hand multiplier half: eta/u/v take their own half, w the other
+    const int yhalf = (field == 3) ? (1 - khalf) : khalf;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < TSTAGES; s++) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
+        mbar_init(accf, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    const uint32_t ncols_tmem = a.fp16 ? 512 : 256;
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(tmem_slot)),
+                     "r"(ncols_tmem));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    __shared__ int issued_s, consumed_s;
+    if (threadIdx.x == 0) { issued_s = 0; consumed_s = 0; }
+    __syncthreads();
+    if (warp == 0) {
+        if (lane == 0) {
+            for (int kb = 0; kb < nkb; kb++) {
+                int s = kb % TSTAGES;
+                uint32_t ph = (kb / TSTAGES) & 1;
+                if (!mbar_wait(&empty[s], ph ^ 1, a.err, 1)) break;
+                uint8_t *st = smem + s * STAGE_BYTES;
+                mbar_expect_tx(&full[s], STAGE_BYTES);
+                int kx = khalf * a.npad + kb * TBK;
+                int ky = (int)(rb * TBM);
+                tma_2d(st, &mXh, &full[s], kx, ky);
+                tma_2d(st + A_TILE, &mXl, &full[s], kx, ky);
+                int wy = blk * a.npad + m0;
+                tma_2d(st + 2 * A_TILE, &mWh, &full[s], kb * TBK, wy);
+                tma_2d(st + 2 * A_TILE + B_TILE, &mWl, &full[s], kb * TBK, wy);
+                issued_s = kb + 1;
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            // kind::f16, D = F32, A/B = bf16 (1) or f16 (0), both K-major, N = 256, M = 128
+            const uint32_t fmt = a.fp16 ? 0u : 1u;
+            const uint32_t idesc = (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(TBN >> 3) << 17) |
+                                   ((uint32_t)(TBM >> 4) << 24);
+            const uint32_t acc_lo = a.fp16 ? tmem + 256 : tmem;
+            for (int kb = 0; kb < nkb; kb++) {
+                int s = kb % TSTAGES;
+                uint32_t ph = (kb / TSTAGES) & 1;
+                if (!mbar_wait(&full[s], ph, a.err, 2)) break;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                uint32_t base = su32(smem + s * STAGE_BYTES);
+                uint64_t dXh = sdesc(base), dXl = sdesc(base + A_TILE);
+                uint64_t dWh = sdesc(base + 2 * A_TILE), dWl = sdesc(base + 2 * A_TILE + B_TILE);
+                for (int k = 0; k < TBK / 16; k++) {
+                    uint64_t o = (uint64_t)(k * 32) >> 4;     // 16 elements = 32 bytes per step
+                    uint32_t first = (kb == 0 && k == 0) ? 0u : 1u;
+                    umma(tmem, dXh + o, dWh + o, idesc, first);
+                    umma(acc_lo, dXh + o, dWl + o, idesc, a.fp16 ? first : 1u);
+                    umma(acc_lo, dXl + o, dWh + o, idesc, 1u);
+                }
+                umma_commit(&empty[s]);
+                consumed_s = kb + 1;
+            }
+            umma_commit(accf);
+        }
+    } else {
+        // epilogue: warps 2..5 own TMEM lane quarters (warp % 4)
+        const int q = warp & 3;
+        const long row = rb * TBM + q * 32 + lane;
+        bool ok = mbar_wait(accf, 0, a.err, 3);
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        float part = 0.f;
+        if (ok) {
+            const float *Yr = a.Y + (row < a.rows ? row : 0) * 2L * a.npad + (long)yhalf * a.npad + m0;
+            const float *cs = a.colscale + (long)blk * a.npad + m0;
+            for (int c = 0; c < TBN / 32; c++) {
+                float v[32], w[32];
+                tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + c * 32, v);
+                if (a.fp16) {
+                    tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + 256 + c * 32, w);
+                    for (int j = 0; j < 32; j++) v[j] = fmaf(w[j], 1.0f / 2048.0f, v[j]);
+                }
+                if (row < a.rows) {
+                    for (int j = 0; j < 32; j += 4) {
+                        float4 y4 = *reinterpret_cast<const float4 *>(Yr + c * 32 + j);
+                        float4 s4 = *reinterpret_cast<const float4 *>(cs + c * 32 + j);
+                        part = fmaf(v[j] * s4.x, y4.x, part);
+                        part = fmaf(v[j + 1] * s4.y, y4.y, part);
+                        part = fmaf(v[j + 2] * s4.z, y4.z, part);
+                        part = fmaf(v[j + 3] * s4.w, y4.w, part);
+                    }
+                }
+            }
+            if (row < a.rows) atomicAdd(a.out + row * 4 + field, part);
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && consumed_s < issued_s) {
+        // error path only: wait (bounded) for the copies still in flight
+        for (int kb = consumed_s; kb < issued_s; kb++)
+            mbar_wait(&full[kb % TSTAGES], (kb / TSTAGES) & 1, a.err, 4);
+    }
+    __syncthreads();
+    if (warp == 1) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols_tmem));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+typedef CUresult (*EncodeTiled)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiled get_encode() {
+    static EncodeTiled fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess && q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiled)p;
+    }
+    return fn;
+}
+
+// 2-D K-major map of a [rows][cols] 16-bit matrix, box {64, box_rows}, 128B swizzle
+static int make_map(CUtensorMap *m, const void *base, long rows, long cols, int box_rows, bool fp16) {
+    EncodeTiled enc = get_encode();
+    if (!enc) return E_CUDA;
+    cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)cols * 2};
+    cuuint32_t box[2] = {(cuuint32_t)TBK, (cuuint32_t)box_rows};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = enc(m, fp16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+                     const_cast<void *>(base), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                     CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? OK : E_CUDA;
+}
+
+struct QformState {
+    bool built = false;
+    int n = 0, npad = 0, ntile_plain = 0;
+    bool fp16 = false;
+    float *plain_tab = nullptr;
+    void *Whi = nullptr, *Wlo = nullptr;
+    float *colscale = nullptr;
+    int *err = nullptr;
+    void *scratch = nullptr;   // chunk buffers
+    size_t scratch_bytes = 0;
+};
+static QformState g_q;
+
+int launch_phasors_public(const DevSea &sea, long n, const double *x, const double *y, const double *t,
+                          long sx, long sy, long st, int npad, float2 *ph, float *rr, double *first,
+                          cudaStream_t stream);
+
+int qform_build(const Config &cfg, const DevSea &sea, bool fp16, void *stream_) {
+    cudaStream_t stream = (cudaStream_t)stream_;
+    if (g_q.plain_tab) cudaFree(g_q.plain_tab);
+    if (g_q.Whi) cudaFree(g_q.Whi);
+    if (g_q.Wlo) cudaFree(g_q.Wlo);
+    if (g_q.colscale) cudaFree(g_q.colscale);
+    g_q = QformState();
+    int n = (int)cfg.omega.size();
+    int npad = ((n + TBN - 1) / TBN) * TBN;
+    if (npad == 0) npad = TBN;
+    g_q.n = n;
+    g_q.npad = npad;
+    g_q.fp16 = fp16;
+    double kmax = 0;
+    for (double k : cfg.k) kmax = std::max(kmax, k);
+    double *d_in = nullptr;
+    size_t nn = (size_t)std::max(n, 1);
+    CK(cudaMalloc(&d_in, sizeof(double) * nn * 4));
+    const std::vector<double> *src[4] = {&cfg.omega, &cfg.A, &cfg.k, &cfg.theta};
+    for (int q = 0; q < 4; q++)
+        CK(cudaMemcpyAsync(d_in + q * nn, src[q]->data(), sizeof(double) * n, cudaMemcpyHostToDevice, stream));
+    QIn qi;
+    qi.n = n; qi.omega = d_in; qi.A = d_in + nn; qi.k = d_in + 2 * nn; qi.theta = d_in + 3 * nn;
+    qi.depth = cfg.depth; qi.g = cfg.gravity; qi.mtheta_rad = cfg.mtheta * PI_IRR / 180.0;
+    qi.cutoff = cfg.dw_cutoff; qi.bandwidth = cfg.dw_bandwidth; qi.kmax = kmax;
+    // FP64 coefficients of all pairs (temporary), then the plain tiles and
+    // the split tensor-core operand from them
+    size_t wel = (size_t)8 * npad * npad;
+    double *coef = nullptr;
+    CK(cudaMalloc(&coef, sizeof(double) * wel));
+    long tot = (long)npad * npad;
+    k_qform_coef64<<<(unsigned)((tot + 255) / 256), 256, 0, stream>>>(qi, npad, coef);
+    note_launch();
+    CK(cudaGetLastError());
+    int nt = npad / QT;
+    g_q.ntile_plain = nt;
+    long ntiles = qtile_index(nt - 1, nt - 1, nt) + 1;
+    CK(cudaMalloc(&g_q.plain_tab, sizeof(float) * ntiles * QT * QT * QNC));
+    k_qform_plain_from64<<<(unsigned)ntiles, 256, 0, stream>>>(npad, nt, coef, g_q.plain_tab);
+    note_launch();
+    CK(cudaGetLastError());
+    CK(cudaMalloc(&g_q.Whi, 2 * wel));
+    CK(cudaMalloc(&g_q.Wlo, 2 * wel));
+    CK(cudaMalloc(&g_q.colscale, sizeof(float) * 8 * npad));
+    dim3 gt((unsigned)npad, 8);
+    if (fp16)
+        k_qform_split<__half><<<gt, 256, 0, stream>>>(npad, 1, coef, (__half *)g_q.Whi, (__half *)g_q.Wlo,
+                                                      g_q.colscale);
+    else
+        k_qform_split<__nv_bfloat16><<<gt, 256, 0, stream>>>(npad, 0, coef, (__nv_bfloat16 *)g_q.Whi,
+                                                             (__nv_bfloat16 *)g_q.Wlo, g_q.colscale);
+    note_launch();
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(stream));
+    cudaFree(coef);
+    CK(cudaMalloc(&g_q.err, sizeof(int)));
+    CK(cudaMemsetAsync(g_q.err, 0, sizeof(int), stream));
+    CK(cudaStreamSynchronize(stream));
+    cudaFree(d_in);
+    g_q.built = true;
+    (void)sea;
+    return OK;
+}
+
+void qform_free() {
+    if (g_q.plain_tab) cudaFree(g_q.plain_tab);
+    if (g_q.Whi) cudaFree(g_q.Whi);
+    if (g_q.Wlo) cudaFree(g_q.Wlo);
+    if (g_q.colscale) cudaFree(g_q.colscale);
+    if (g_q.err) cudaFree(g_q.err);
+    if (g_q.scratch) cudaFree(g_q.scratch);
+    g_q = QformState();
+}
+
+static int reserve_scratch(size_t bytes) {
+    if (g_q.scratch_bytes >= bytes) return OK;
+    if (g_q.scratch) cudaFree(g_q.scratch);
+    g_q.scratch = nullptr;
+    g_q.scratch_bytes = 0;
+    CK(cudaMalloc(&g_q.scratch, bytes));
+    g_q.scratch_bytes = bytes;
+    return OK;
+}
+
+// out [rows][4] FP32: eta2, u2, v2, w2 at z0 = 0 (no ramp of the API, no
+// first order).  method 0 plain FP32, 1 tensor cores.
+int qform_eval(const DevSea &sea, long n, const double *x, const double *y, const double *t, int method,
+               float *out, void *stream_, int *tc_error) {
+    cudaStream_t stream = (cudaStream_t)stream_;
+    if (!g_q.built) return E_NOT_INITIALIZED;
+    if (n <= 0) return OK;
+    const int npad = g_q.npad;
+    CK(cudaMemsetAsync(out, 0, sizeof(float) * 4 * n, stream));
+    if (method == 0) {
+        const long chunk = 1L << 16;
+        static bool pattr = false;
+        if (!pattr) {
+            CK(cudaFuncSetAttribute(k_qform_plain, cudaFuncAttributeMaxDynamicSharedMemorySize, QPLAIN_SMEM));
+            pattr = true;
+        }
+        long m = std::min(n, chunk);
+        size_t bytes = (sizeof(float2) + sizeof(float)) * (size_t)npad * m + sizeof(double) * 5 * m + 4096;
+        int rc = reserve_scratch(bytes);
+        if (rc) return rc;
+        for (long b = 0; b < n; b += chunk) {
+            long mm = std::min(chunk, n - b);
+            float2 *ph = (float2 *)g_q.scratch;
+            float *rr = (float *)((char *)g_q.scratch + ((sizeof(float2) * npad * mm + 255) / 256) * 256);
+            double *first = (double *)((char *)rr + ((sizeof(float) * npad * mm + 255) / 256) * 256);
+            rc = launch_phasors_public(sea, mm, x + b, y + b, t + b, 1, 1, 1, npad, ph, rr, first, stream);
+            if (rc) return rc;
+            QPlain q;
+            q.rows = mm; q.ntile = g_q.ntile_plain; q.tab = g_q.plain_tab; q.ph = ph; q.rr = rr;
+            q.out = out + 4 * b;
+            prof_begin(PK_QFORM, stream);
+            k_qform_plain<<<(unsigned)((mm + 127) / 128), 128, QPLAIN_SMEM, stream>>>(q);
+            note_launch();
+            prof_end(PK_QFORM, stream);
+            CK(cudaGetLastError());
+        }
+        return OK;
+    }
+    // tensor cores: chunks of rows with X hi/lo and Y in scratch
+    const long chunk = 1L << 16;
+    long m = std::min(n, chunk);
+    long mpad = ((m + TBM - 1) / TBM) * TBM;
+    size_t xb = (size_t)mpad * 2 * npad * 2;     // one 16-bit matrix
+    size_t yb = (size_t)mpad * 2 * npad * 4;
+    int rc = reserve_scratch(2 * xb + yb + 4096);
+    if (rc) return rc;
+    static bool attr = false;
+    if (!attr) {
+        CK(cudaFuncSetAttribute(k_qform_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
+        attr = true;
+    }
+    for (long b = 0; b < n; b += chunk) {
+        long mm = std::min(chunk, n - b);
+        char *base = (char *)g_q.scratch;
+        void *Xh = base, *Xl = base + xb;
+        float *Y = (float *)(base + 2 * xb);
+        QPrep pp;
+        pp.rows = mm; pp.x = x + b; pp.y = y + b; pp.t = t + b; pp.phase = sea.d_phase;
+        pp.cstride = sea.npad_g; pp.ncomp = sea.n; pp.npad = npad; pp.fx = sea.fx; pp.fy = sea.fy;
+        pp.trivial_ramp = sea.trivial_ramp ? 1 : 0; pp.fp16 = g_q.fp16 ? 1 : 0;
+        pp.Xhi = Xh; pp.Xlo = Xl; pp.Y = Y;
+        long tot = mm * (long)npad;
+        k_qform_prep<<<(unsigned)((tot + 255) / 256), 256, 0, stream>>>(pp);
+        note_launch();
+        CK(cudaGetLastError());
+        CUtensorMap mXh, mXl, mWh, mWl;
+        if (make_map(&mXh, Xh, mm, 2L * npad, TBM, g_q.fp16) || make_map(&mXl, Xl, mm, 2L * npad, TBM, g_q.fp16) ||
+            make_map(&mWh, g_q.Whi, 8L * npad, npad, TBN, g_q.fp16) ||
+            make_map(&mWl, g_q.Wlo, 8L * npad, npad, TBN, g_q.fp16))
+            return E_CUDA;
+        QTC q;
+        q.rows = mm; q.npad = npad; q.ntn = npad / TBN; q.group_m = 8; q.Y = Y; q.colscale = g_q.colscale;
+        q.out = out + 4 * b; q.fp16 = g_q.fp16 ? 1 : 0; q.err = g_q.err;
+        long nrb = (mm + TBM - 1) / TBM;
+        long nblk = nrb * 8L * q.ntn;
+        prof_begin(PK_QFORM, stream);
+        k_qform_tc<<<(unsigned)nblk, 192, TC_SMEM, stream>>>(mXh, mXl, mWh, mWl, q);
+        note_launch();
+        prof_end(PK_QFORM, stream);
+        CK(cudaGetLastError());
+    }
+    if (tc_error) {
+        int h = 0;
+        CK(cudaMemcpyAsync(&h, g_q.err, sizeof(int), cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        *tc_error = h;
+    }
+    return OK;
+}
+
+}  // namespace cfdwm

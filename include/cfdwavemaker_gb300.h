@@ -163,6 +163,16 @@ CFDWM_EXPORT int cfdwm_regular_solution(double *dst, int cap);
  * Returns n (>= 0) or a negative status. */
 CFDWM_EXPORT int cfdwm_parse_text(const char *text, double *scalars, double *comps, int cap);
 
+/* Precision form (no counterpart in the reference): the second-order sums
+ * at z0 = 0 -- eta2 and the Taylor-layer u2, v2, w2 of the pair cache
+ * (Irregular.cpp:223-293, 975-1102) -- as quadratic forms over the phasor
+ * vectors.  build: fp16 != 0 splits operands into fp16 hi/lo parts, else
+ * bf16 hi/lo.  eval: device arrays x, y, t (n points), out [n][4] FP32;
+ * method 0 plain FP32 CUDA cores, 1 tcgen05 tensor cores. */
+CFDWM_EXPORT int cfdwm_qform_build(int fp16);
+CFDWM_EXPORT int cfdwm_qform_eval(const double *x, const double *y, const double *t, long n, int method,
+                                  float *out);
+
 #ifdef __cplusplus
 }
 #endif

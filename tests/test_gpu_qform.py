@@ -1,0 +1,102 @@
+"""Parity of the precision form (second-order sums at z0 = 0 as quadratic
+forms) with the FP64 oracle: eta2 from the pair cache (Irregular.cpp:223-293)
+and the uvw2 velocities at z = 0 (Irregular.cpp:975-1102).
+
+Tolerance: normwise relative error max|gpu - ref| / max|ref| per field,
+TOL = 1e-5 for the plain FP32 form and the fp16-split tensor-core form.
+The bf16-split form keeps 16 significant bits per operand (8 + 8), about
+2^-16 relative, so its bar is TOL_BF16 = 1e-4 and the measured error is
+printed.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import norm_rel_err
+
+import cfdwavemaker_gb300 as cw
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+TOL_BF16 = 1e-4
+
+
+def _sea(ncomp_freq, ndir, seed):
+    from cfdwavemaker_gb300 import seastate as ss
+    comps = ss.irregular_components(6.0, 12.0, 2.0, ncomp_freq, 0.25, 1.6, 100.0, seed, ndir=ndir,
+                                    spreading_s=10.0)
+    return ss.write_irregular(None, comps, 100.0, extrap=2)
+
+
+@pytest.fixture(scope="module")
+def torch():
+    return pytest.importorskip("torch")
+
+
+def _run(wm, torch, txt, n, method, fp16, seed=5):
+    assert wm.initialize_text(txt) == 0, cw.last_error()
+    assert wm.lib.cfdwm_qform_build(int(fp16)) == 0, cw.last_error()
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(0, 1000, n)
+    y = rng.uniform(0, 1000, n)
+    t = rng.uniform(0, 100, n)
+    d = [torch.tensor(a, device="cuda:0", dtype=torch.float64) for a in (x, y, t)]
+    out = torch.zeros((n, 4), device="cuda:0", dtype=torch.float32)
+    torch.cuda.synchronize()
+    rc = wm.lib.cfdwm_qform_eval(*[cw._ptr(a) for a in d], n, method, cw._ptr(out))
+    assert rc == 0, cw.last_error()
+    return x, y, t, out.cpu().numpy().astype(np.float64)
+
+
+def _reference(txt, x, y, t):
+    cfg = oracle.waveinput.read_text(txt)
+    sea = oracle.Sea(cfg)
+    eta2 = sea.eta2(x, y, t)
+    uvw = sea.uvw2(x, y, np.zeros_like(x), t)
+    return np.stack([eta2, uvw[:, 0], uvw[:, 1], uvw[:, 2]], axis=1)
+
+
+@pytest.fixture(scope="module")
+def wm(tmp_path_factory):
+    from cfdwavemaker_gb300 import build
+    build.build()
+    cwd = os.getcwd()
+    os.chdir(tmp_path_factory.mktemp("qf"))
+    m = cw.CFDwavemaker()
+    yield m
+    m.cleanup()
+    os.chdir(cwd)
+
+
+@pytest.mark.parametrize("nf,nd", [(12, 4), (40, 8)])
+def test_plain_form(wm, torch, nf, nd):
+    txt = _sea(nf, nd, 17)
+    x, y, t, got = _run(wm, torch, txt, 333, 0, False)
+    ref = _reference(txt, x, y, t)
+    for f in range(4):
+        assert norm_rel_err(got[:, f], ref[:, f]) <= TOL, (f, norm_rel_err(got[:, f], ref[:, f]))
+
+
+@pytest.mark.parametrize("nf,nd", [(12, 4), (40, 8)])
+def test_tensor_core_fp16_split(wm, torch, nf, nd):
+    txt = _sea(nf, nd, 17)
+    x, y, t, got = _run(wm, torch, txt, 333, 1, True)
+    ref = _reference(txt, x, y, t)
+    for f in range(4):
+        err = norm_rel_err(got[:, f], ref[:, f])
+        print("fp16x3 field", f, "err", err)
+        assert err <= TOL, (f, err)
+
+
+@pytest.mark.parametrize("nf,nd", [(12, 4), (40, 8)])
+def test_tensor_core_bf16_split(wm, torch, nf, nd):
+    txt = _sea(nf, nd, 17)
+    x, y, t, got = _run(wm, torch, txt, 333, 1, False)
+    ref = _reference(txt, x, y, t)
+    for f in range(4):
+        err = norm_rel_err(got[:, f], ref[:, f])
+        print("bf16x3 field", f, "err", err)
+        assert err <= TOL_BF16, (f, err)

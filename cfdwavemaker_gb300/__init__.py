@@ -119,6 +119,8 @@ def load(path: str | None = None):
     L.cfdwm_regular_solution.argtypes = [vp, C.c_int]
     L.cfdwm_parse_text.restype = C.c_int
     L.cfdwm_parse_text.argtypes = [C.c_char_p, vp, vp, C.c_int]
+    L.cfdwm_irregular_fields_noalloc.restype = C.c_int
+    L.cfdwm_irregular_fields_noalloc.argtypes = [vp, vp, vp, vp, C.c_long, C.c_int, vp]
     L.cfdwm_qform_build.restype = C.c_int
     L.cfdwm_qform_build.argtypes = [C.c_int]
     L.cfdwm_qform_eval.restype = C.c_int

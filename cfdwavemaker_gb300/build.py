@@ -21,7 +21,7 @@ NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden",
          "-I" + os.path.join(os.path.dirname(HERE), "include")]
-SOURCES = ["parser.cpp", "irregular.cu", "sgrid.cu", "regular.cu", "api.cu", "qform.cu"]
+SOURCES = ["parser.cpp", "irregular.cu", "sgrid.cu", "regular.cu", "api.cu", "noalloc.cu", "qform.cu"]
 
 
 def _compile(src):

@@ -413,6 +413,14 @@ double scalar(int q, double x, double y, double z, double t) {
 
 }  // namespace
 
+// Accessors for entry points defined in other translation units.
+const DevSea *api_loaded_sea(int *wavetype) {
+    if (wavetype) *wavetype = g_model.init ? g_model.cfg.wavetype : 0;
+    return g_model.init ? &g_model.sea : nullptr;
+}
+void api_set_error(const char *msg) { set_error(msg); }
+void *api_user_stream() { return t_ctx.user_set ? (void *)t_ctx.user : nullptr; }
+
 }  // namespace cfdwm
 
 using namespace cfdwm;

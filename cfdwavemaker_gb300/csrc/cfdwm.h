@@ -168,6 +168,9 @@ int irregular_eval(const DevSea &sea, long n, const double *x, const double *y,
                    const double *z, const double *t, int mask, double *out,
                    Workspace &ws, void *stream);
 
+// Workspace bytes irregular_eval needs for a batch of n points.
+size_t irregular_eval_scratch_bytes(const DevSea &sea, long n);
+
 // Point-batched second-order sums only (for tests of the pair kernels):
 // which = 0 -> u2,v2,w2,dp2 of the point API at z, 1 -> uvw2 (grid mask).
 int irregular_second_order(const DevSea &sea, long n, const double *x, const double *y,

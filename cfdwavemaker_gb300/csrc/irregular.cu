@@ -895,6 +895,11 @@ int irregular_eval(const DevSea &sea, long n, const double *x, const double *y, 
     return OK;
 }
 
+size_t irregular_eval_scratch_bytes(const DevSea &sea, long n) {
+    const long chunk = 1L << 18;
+    return layout(std::min(n, chunk), sea.npad_g, nullptr).bytes;
+}
+
 int irregular_second_order(const DevSea &sea, long n, const double *x, const double *y,
                            const double *z, const double *t, int which, double *out, Workspace &ws,
                            void *stream_) {

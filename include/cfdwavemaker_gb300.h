@@ -173,6 +173,27 @@ CFDWM_EXPORT int cfdwm_qform_build(int fp16);
 CFDWM_EXPORT int cfdwm_qform_eval(const double *x, const double *y, const double *t, long n, int method,
                                   float *out);
 
+/* ---------------------------------------------------------------------- */
+/* Part 4: allocation-free evaluation                                      */
+/* ---------------------------------------------------------------------- */
+/* No counterpart in the reference.  Same results as cfdwm_irregular_fields,
+ * for host codes that cannot let the library allocate device memory while
+ * they run (solvers that reserve all device memory for their own pool at
+ * start-up, or run under a fixed device-memory budget): this call performs
+ * no cudaMalloc/cudaFree or other allocation.  x, y, z, t and out ([5][n])
+ * must be device memory of the current device.  The workspace is one fixed
+ * 32 MiB device array per GPU, held from library load until process exit;
+ * a batch needs about (12 * Npad + 64) bytes per point, Npad = component
+ * count rounded up to a multiple of 32, and larger batches are rejected with
+ * -8 (message in cfdwm_last_error).  The first call on a device looks up the
+ * array's device address, so make it before any stream capture.  All calls
+ * share the array: calls that overlap on the GPU (several host threads or
+ * streams at once) race.  The call returns after the results are written.
+ * Wave type 5 models need one cfdwm_irregular_fields call first (it builds
+ * the point-API pair table); without it the call returns -2. */
+CFDWM_EXPORT int cfdwm_irregular_fields_noalloc(const double *x, const double *y, const double *z,
+                                                const double *t, long n, int mask, double *out);
+
 #ifdef __cplusplus
 }
 #endif

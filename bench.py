@@ -47,6 +47,106 @@ def sgrid_config(nx=256, ny=256, nl=16):
     return ss.write_irregular(None, comps, 100.0, extrap=2, lsgrid=grid)
 
 
+def qform_config():
+    from cfdwavemaker_gb300 import seastate as ss
+    comps = ss.config3_sea(nfreq=256, ndir=16)
+    return ss.write_irregular(None, comps, 100.0, extrap=2)
+
+
+def run_qform(args):
+    """Precision form: eta2 and the Taylor-layer u2, v2, w2 at z0 = 0 of the
+    4096-component sea (256 frequencies x 16 directions) at 4e6 points, as
+    split 16-bit tcgen05 GEMMs; the plain FP32 CUDA-core form is timed on a
+    row subset (its time is linear in rows) and the error of both against
+    the FP64 oracle is taken on a sample of rows."""
+    import torch
+    import cfdwavemaker_gb300 as cw
+    ws, rank, local = dist_init()
+    torch.cuda.set_device(local)
+    lib = cw.load()
+    os.chdir(tempfile.mkdtemp())
+    wm = cw.CFDwavemaker()
+    txt = qform_config()
+    t0 = time.time()
+    assert wm.initialize_text(txt) == 0, cw.last_error()
+    init_s = time.time() - t0
+    R = args.rows
+    rng = np.random.default_rng(99 + rank)
+    x = rng.uniform(0, 1000, R); y = rng.uniform(0, 1000, R); t = rng.uniform(0, 100, R)
+    d = [torch.tensor(a, device="cuda", dtype=torch.float64) for a in (x, y, t)]
+    out = torch.zeros((R, 4), device="cuda", dtype=torch.float32)
+    stream = torch.cuda.current_stream()
+    lib.cfdwm_set_stream(C.c_void_p(stream.cuda_stream))
+    ptr = [cw._ptr(a) for a in d]
+    res = {"init_s": init_s, "forms": {}}
+    # FP64 oracle on a sample of rows
+    import oracle
+    cfg = oracle.waveinput.read_text(txt)
+    sea = oracle.Sea(cfg)
+    ns = 24
+    refE = sea.eta2(x[:ns], y[:ns], t[:ns])
+    refU = sea.uvw2(x[:ns], y[:ns], np.zeros(ns), t[:ns])
+    ref = np.stack([refE, refU[:, 0], refU[:, 1], refU[:, 2]], axis=1)
+
+    def errs(o):
+        g = o[:ns].astype(np.float64)
+        return [float(np.max(np.abs(g[:, f] - ref[:, f])) / np.max(np.abs(ref[:, f]))) for f in range(4)]
+
+    def timed(method, rows, steps, warm):
+        for _ in range(warm):
+            assert lib.cfdwm_qform_eval(ptr[0], ptr[1], ptr[2], rows, method, cw._ptr(out)) == 0, cw.last_error()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            assert lib.cfdwm_qform_eval(ptr[0], ptr[1], ptr[2], rows, method, cw._ptr(out)) == 0, cw.last_error()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    for fp16 in (0, 1):
+        name = "tc_fp16x3" if fp16 else "tc_bf16x3"
+        tb = time.time()
+        assert lib.cfdwm_qform_build(fp16) == 0, cw.last_error()
+        build_s = time.time() - tb
+        if fp16 == 0:
+            sub = min(R, args.plain_rows)
+            ms = timed(0, sub, 1, 1)
+            res["forms"]["plain_fp32"] = {"ms_rows": ms, "rows": sub, "pts_per_s": sub / (ms / 1e3),
+                                          "err": errs(out.cpu().numpy())}
+        lib.cfdwm_profile_enable(1)
+        lib.cfdwm_profile_read(6, None)
+        sampler = ClockSampler(local)
+        sampler.start()
+        ms = timed(1, R, args.steps, args.warmup)
+        clocks = sampler.stop()
+        tot = C.c_double(0.0)
+        nk = lib.cfdwm_profile_read(6, C.byref(tot))
+        lib.cfdwm_profile_enable(0)
+        res["forms"][name] = {"ms": ms, "rows": R, "pts_per_s": R / (ms / 1e3), "err": errs(out.cpu().numpy()),
+                              "build_s": build_s, "gemm_launches": int(nk),
+                              "gemm_ms_per_step": tot.value / max(1, args.steps), "clocks": clocks}
+    # end to end: host arrays in pinned memory, copies inside the timed region
+    hx = [torch.from_numpy(a).pin_memory() for a in (x, y, t)]
+    hout = torch.empty((R, 4), dtype=torch.float32).pin_memory()
+    torch.cuda.synchronize()
+    te0 = time.perf_counter()
+    for _ in range(args.steps):
+        for a, b in zip(d, hx):
+            a.copy_(b, non_blocking=True)
+        assert lib.cfdwm_qform_eval(ptr[0], ptr[1], ptr[2], R, 1, cw._ptr(out)) == 0
+        hout.copy_(out, non_blocking=True)
+        torch.cuda.synchronize()
+    te = (time.perf_counter() - te0) / args.steps
+    res["e2e_s"] = te
+    res["h2d"] = 3 * 8 * R
+    res["d2h"] = 4 * 4 * R
+    res["ws"] = ws
+    res["rank"] = rank
+    res["npad"] = 4096
+    return res
+
+
 def point_config():
     from cfdwavemaker_gb300 import seastate as ss
     return ss.write_irregular(None, ss.config1_sea(), 50.0, extrap=2)
@@ -285,9 +385,11 @@ def roofline(args, r, pk, src):
     timings.  The column pair kernel is bound by the SFU (MUFU ex2) pipe: the
     depth ratios of both interaction wavenumbers need exp(kz) and
     exp(-2k(z+h)), i.e. 4 ex2 per (pair, level); a pair costs 22 FP32 flops
-    per level on top (6 FMA for u, v, w and the ratio assembly).  GB300 has
-    152 SMs x 16 MUFU lanes; the peak is that times the median SM clock seen
-    during the run (MEASURED_PEAKS.json holds no SFU or FP32 figure)."""
+    per level on top (6 FMA for u, v, w and the ratio assembly).  The SFU
+    (XU) pipe of a GB300 SM executes 32 lanes of ex2 per clock (ncu:
+    the kernel's ex2 rate of 4.46 T/s was 49.4% of the XU peak at 2070 MHz);
+    the peak is 152 SMs x 32 lanes x the median SM clock seen during the run
+    (MEASURED_PEAKS.json holds no SFU or FP32 figure)."""
     prof = r["prof"]
     f_mhz = r["clocks"].get("sm_mhz") or pk.get("sm_max_mhz", 2070.0)
     if args.workload == "sgrid" and "column_pairs" in prof:
@@ -296,7 +398,7 @@ def roofline(args, r, pk, src):
         terms = units * (r["npairs"] + r["ncomp"])
         t = kp["avg_ms"] / 1e3
         ex2 = 4.0 * terms / t
-        peak = 152 * 16 * f_mhz * 1e6
+        peak = 152 * 32 * f_mhz * 1e6
         return {"kernel": "k_pairs_columns", "bound": "sfu", "achieved": ex2 / 1e9, "peak": peak / 1e9,
                 "unit": "Gex2/s", "frac": ex2 / peak, "traffic": traffic_from_profiles("k_pairs_columns"),
                 "algorithmic": "4 ex2 + 22 FP32 flop per (pair, level); %d pairs + %d diagonal terms x %d nodes "
@@ -304,18 +406,18 @@ def roofline(args, r, pk, src):
                 "fp32_tflops": 22.0 * terms / t / 1e12,
                 "fp32_peak_tflops": 152 * 128 * 2 * f_mhz * 1e6 / 1e12,
                 "avg_launch_ms": kp["avg_ms"],
-                "peak_source": "derived: 152 SM x 16 MUFU/clk x median SM clock %.0f MHz" % f_mhz}
+                "peak_source": "derived: 152 SM x 32 XU lanes/clk x median SM clock %.0f MHz" % f_mhz}
     if "point_pairs" in prof:
         kp = prof["point_pairs"]
         n = r["units"]
         P = r["ncomp"] * (r["ncomp"] + 1) / 2
         t = kp["avg_ms"] / 1e3
         ex2 = 4.0 * n * P / t
-        peak = 152 * 16 * f_mhz * 1e6
+        peak = 152 * 32 * f_mhz * 1e6
         return {"kernel": "k_pairs_points", "bound": "sfu", "achieved": ex2 / 1e9, "peak": peak / 1e9,
                 "unit": "Gex2/s", "frac": ex2 / peak, "traffic": traffic_from_profiles("k_pairs_points"),
                 "avg_launch_ms": kp["avg_ms"],
-                "peak_source": "derived: 152 SM x 16 MUFU/clk x median SM clock %.0f MHz" % f_mhz}
+                "peak_source": "derived: 152 SM x 32 XU lanes/clk x median SM clock %.0f MHz" % f_mhz}
     return None
 
 
@@ -324,7 +426,8 @@ def traffic_from_profiles(kernel):
     p = os.path.join(HERE, "profiles", "traffic.json")
     try:
         with open(p) as fh:
-            return json.load(fh).get(kernel)
+            v = json.load(fh).get(kernel)
+            return v.get("bytes_per_launch") if isinstance(v, dict) else v
     except (OSError, ValueError):
         return None
 
@@ -371,7 +474,10 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="sgrid", choices=["sgrid", "point"])
+    ap.add_argument("--workload", default="sgrid", choices=["sgrid", "point", "qform"])
+    ap.add_argument("--rows", type=int, default=4_000_000, help="points of the precision-form workload")
+    ap.add_argument("--plain-rows", type=int, default=65536,
+                    help="row subset on which the plain FP32 form of the precision workload is timed")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--grid", type=int, default=256,
                     help="columns per side of the s-grid (256 is the named workload; smaller sizes "
@@ -400,6 +506,12 @@ def main():
                 "config": {"workload": workload}, "cpu_baseline": cb,
                 "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
+        return
+    if args.workload == "qform":
+        r = run_qform(args)
+        if r["rank"] != 0:
+            return
+        print(json.dumps({"workload": "qform", **r}))
         return
     r = run_ours(args)
     if r["rank"] != 0:

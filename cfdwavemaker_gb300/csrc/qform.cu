@@ -341,7 +341,7 @@ constexpr int A_TILE = TBM * TBK * 2;     // 16 KiB
 constexpr int B_TILE = TBN * TBK * 2;     // 32 KiB
 constexpr int STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;
 constexpr int TC_SMEM = TSTAGES * STAGE_BYTES + 1024 + 256;
-constexpr long long WAIT_LIMIT = 4000000000LL;   // clock cycles (about 2 s)
+constexpr long long WAIT_LIMIT = 1000000000LL;   // clock cycles (about 0.5 s)
 
 __device__ __forceinline__ uint32_t su32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -437,6 +437,8 @@ __global__ void __launch_bounds__(192, 1) k_qform_tc(const __grid_constant__ CUt
     long rb = gm0 + in % gsz;
     int ct = (int)(in / gsz);
     if (rb >= nrb || ct >= ncol) return;
+    // a CTA that finds the error word set leaves before touching any resource
+    if (*(volatile int *)a.err != 0) return;
     const int blk = ct / a.ntn, tn = ct % a.ntn;
     const int field = blk & 3, khalf = blk >> 2;
     const int m0 = tn * TBN;
@@ -512,6 +514,8 @@ __global__ void __launch_bounds__(192, 1) k_qform_tc(const __grid_constant__ CUt
         const int q = warp & 3;
         const long row = rb * TBM + q * 32 + lane;
         bool ok = mbar_wait(accf, 0, a.err, 3);
+        // tcgen05.ld is warp-collective (.sync.aligned): decide per warp
+        ok = __all_sync(0xffffffffu, ok);
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         float part = 0.f;
         if (ok) {

@@ -459,7 +459,10 @@ __global__ void __launch_bounds__(128) k_pairs_columns(PairArgs a) {
     const bool valid = col < a.ncol;
     const long colc = valid ? col : 0;
     const long npts = a.ncol * a.nl;
-    float zk[LV], zetak[LV];
+    static_assert(LV % 2 == 0, "levels are processed in pairs");
+    constexpr int LP = LV / 2;
+    float zk[LV], zetak[LV], yk[LV];   // z log2(e), -2(z + h) log2(e), -(z + 2h) log2(e)
+    float2 zk2[LP], yk2[LP];
     float su[LV], cu[LV], sv[LV], cv[LV], sw[LV], cw[LV];
 #pragma unroll
     for (int l = 0; l < LV; l++) {
@@ -467,7 +470,13 @@ __global__ void __launch_bounds__(128) k_pairs_columns(PairArgs a) {
         float z = (valid && lev < a.nl) ? a.z0[colc * a.nl + lev] : 0.f;
         zk[l] = z * LOG2E_F;
         zetak[l] = -2.f * (z + a.depth) * LOG2E_F;
+        yk[l] = -(z + 2.f * a.depth) * LOG2E_F;
         su[l] = cu[l] = sv[l] = cv[l] = sw[l] = cw[l] = 0.f;
+    }
+#pragma unroll
+    for (int j = 0; j < LP; j++) {
+        zk2[j] = make_float2(zk[2 * j], zk[2 * j + 1]);
+        yk2[j] = make_float2(yk[2 * j], yk[2 * j + 1]);
     }
     for (int I = 0; I < a.ntile; I++) {
         for (int M = I; M < a.ntile; M++) {
@@ -491,9 +500,13 @@ __global__ void __launch_bounds__(128) k_pairs_columns(PairArgs a) {
                     const int i = I * TT + ii;
                     const float2 pi = a.ph[(long)i * a.ncol + col];
                     const float ri = a.rr[(long)i * a.ncol + col];
-                    float au[LV], av[LV], aw[LV];
+                    // packed FP32x2 over level pairs: per pair and level,
+                    // E = exp(k z), Y = exp(-k(z + 2h)) = E exp(-2k(z+h)),
+                    // F = E + Y, G = E - Y (the normaliser is in the record)
+                    float2 au[LP], av[LP], aw[LP];
 #pragma unroll
-                    for (int l = 0; l < LV; l++) au[l] = av[l] = aw[l] = 0.f;
+                    for (int j = 0; j < LP; j++) au[j] = av[j] = aw[j] = make_float2(0.f, 0.f);
+                    const float2 neg1 = make_float2(-1.f, -1.f);
                     const int m0 = (M == I) ? ii : 0;
                     for (int mm = m0; mm < TT; mm++) {
                         const float4 c0 = *reinterpret_cast<const float4 *>(s_tab + (ii * TT + mm) * GRIDV_NC);
@@ -504,22 +517,33 @@ __global__ void __launch_bounds__(128) k_pairs_columns(PairArgs a) {
                         const float cp = cc - ss, cmn = cc + ss, sp = sc + cs, smn = sc - cs;
                         const float up = c0.x * cp, um = c0.y * cmn, vp = c0.z * cp, vm = c0.w * cmn;
                         const float wp = c1.x * sp, wm = c1.y * smn;
-                        const float kp = c1.z, km = c1.w;
+                        const float2 up2 = make_float2(up, up), um2 = make_float2(um, um);
+                        const float2 vp2 = make_float2(vp, vp), vm2 = make_float2(vm, vm);
+                        const float2 wp2 = make_float2(wp, wp), wm2 = make_float2(wm, wm);
+                        const float2 kp2 = make_float2(c1.z, c1.z), km2 = make_float2(c1.w, c1.w);
 #pragma unroll
-                        for (int l = 0; l < LV; l++) {
-                            float Fp, Gp, Fm, Gm;
-                            depth_fg(kp, zk[l], zetak[l], Fp, Gp);
-                            depth_fg(km, zk[l], zetak[l], Fm, Gm);
-                            au[l] = fmaf(up, Fp, fmaf(um, Fm, au[l]));
-                            av[l] = fmaf(vp, Fp, fmaf(vm, Fm, av[l]));
-                            aw[l] = fmaf(wp, Gp, fmaf(wm, Gm, aw[l]));
+                        for (int j = 0; j < LP; j++) {
+                            const float2 ap = __fmul2_rn(kp2, zk2[j]), bp = __fmul2_rn(kp2, yk2[j]);
+                            const float2 am = __fmul2_rn(km2, zk2[j]), bm = __fmul2_rn(km2, yk2[j]);
+                            const float2 Ep = make_float2(ex2(ap.x), ex2(ap.y));
+                            const float2 Yp = make_float2(ex2(bp.x), ex2(bp.y));
+                            const float2 Em = make_float2(ex2(am.x), ex2(am.y));
+                            const float2 Ym = make_float2(ex2(bm.x), ex2(bm.y));
+                            const float2 Fp = __fadd2_rn(Ep, Yp), Gp = __ffma2_rn(Yp, neg1, Ep);
+                            const float2 Fm = __fadd2_rn(Em, Ym), Gm = __ffma2_rn(Ym, neg1, Em);
+                            au[j] = __ffma2_rn(up2, Fp, __ffma2_rn(um2, Fm, au[j]));
+                            av[j] = __ffma2_rn(vp2, Fp, __ffma2_rn(vm2, Fm, av[j]));
+                            aw[j] = __ffma2_rn(wp2, Gp, __ffma2_rn(wm2, Gm, aw[j]));
                         }
                     }
 #pragma unroll
-                    for (int l = 0; l < LV; l++) {
-                        kahan(su[l], cu[l], ri * au[l]);
-                        kahan(sv[l], cv[l], ri * av[l]);
-                        kahan(sw[l], cw[l], ri * aw[l]);
+                    for (int j = 0; j < LP; j++) {
+                        kahan(su[2 * j], cu[2 * j], ri * au[j].x);
+                        kahan(su[2 * j + 1], cu[2 * j + 1], ri * au[j].y);
+                        kahan(sv[2 * j], cv[2 * j], ri * av[j].x);
+                        kahan(sv[2 * j + 1], cv[2 * j + 1], ri * av[j].y);
+                        kahan(sw[2 * j], cw[2 * j], ri * aw[j].x);
+                        kahan(sw[2 * j + 1], cw[2 * j + 1], ri * aw[j].y);
                     }
                 }
             }

@@ -1,21 +1,25 @@
 """Benchmark of the second-order point-kinematics path on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload sgrid|point]
+                    [--workload qform|sgrid|point]
 
 Workloads (synthetic seeded sea states of the named shapes; no dataset):
-  sgrid  (default) short-crested JONSWAP Hs=6 m Tp=12 s gamma=2, cos-2s s=10,
-         64 frequencies x 16 directions = 1024 components, depth 100 m; an
-         s-grid of 256 x 256 columns x 16 sigma levels over 1 km x 1 km at
-         dt = 0.5 s.  One step = one ring update (second-order kinematics at
-         all 1,048,576 grid nodes: eta2 + uvw2 pair sums over 521k pairs) plus
-         the 4-D spline query of 1e6 uniformly random (x, y, z, t) points.
+  qform  (default) precision form: short-crested JONSWAP Hs=6 m Tp=12 s
+         gamma=2, cos-2s s=10, 256 frequencies x 16 directions = 4096
+         components, depth 100 m; second-order eta and z=0 / Taylor-layer
+         u, v, w at 4e6 random (x, y, t) points as split 16-bit tcgen05 GEMMs
+         (fp16x3 and bf16x3), beside the plain FP32 CUDA-core form; errors of
+         every field against the FP64 oracle on a row sample.
+  sgrid  the same sea at 64 x 16 = 1024 components; an s-grid of 256 x 256
+         columns x 16 sigma levels over 1 km x 1 km at dt = 0.5 s.  One step
+         = one ring update (second-order kinematics at all 1,048,576 grid
+         nodes: eta2 + uvw2 pair sums over 521k pairs) plus the 4-D spline
+         query of 1e6 uniformly random (x, y, z, t) points.
   point  long-crested JONSWAP Hs=4 m Tp=10 s gamma=3.3, 128 components,
          depth 50 m; eta, u, w, dp on 256 x-points x 32 z-points x 8 times.
 Metric: second-order points per second (grid nodes updated per second for
-sgrid; evaluated points per second for point), FP32 compute with FP64 phases.
-The reference arm times the FP64 CPU restatement (oracle/) on a bounded
-sample of the same workload with all host threads.
+sgrid).  The reference arm times the FP64 CPU restatement (oracle/) on a
+bounded sample of the same workload with all host threads.
 """
 from __future__ import annotations
 
@@ -45,6 +49,11 @@ def sgrid_config(nx=256, ny=256, nl=16):
     grid = {"bounds": (0.0, 1000.0, 0.0, 1000.0), "nx": nx, "ny": ny, "nl": nl, "t0": 0.0,
             "dt": 0.5, "stretch": (0.7, 1.5)}
     return ss.write_irregular(None, comps, 100.0, extrap=2, lsgrid=grid)
+
+
+QFORM_WORKLOAD = ("precision form: second-order eta and z=0/Taylor-layer u, v, w (pair-cache coefficients) of "
+                  "a 4096-component short-crested JONSWAP sea (256 freq x 16 dir, Hs 6 m, Tp 12 s, gamma 2, "
+                  "cos-2s s=10, depth 100 m) at %d random (x, y, t) points")
 
 
 def qform_config():
@@ -96,12 +105,15 @@ def run_qform(args):
         for _ in range(warm):
             assert lib.cfdwm_qform_eval(ptr[0], ptr[1], ptr[2], rows, method, cw._ptr(out)) == 0, cw.last_error()
         torch.cuda.synchronize()
+        lib.cfdwm_profile_read(6, None)      # drop the warm-up launches
         e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+        l0 = lib.cfdwm_kernel_launches()
         e0.record(stream)
         for _ in range(steps):
             assert lib.cfdwm_qform_eval(ptr[0], ptr[1], ptr[2], rows, method, cw._ptr(out)) == 0, cw.last_error()
         e1.record(stream)
         torch.cuda.synchronize()
+        timed.launches = lib.cfdwm_kernel_launches() - l0
         return e0.elapsed_time(e1) / steps
 
     for fp16 in (0, 1):
@@ -124,7 +136,7 @@ def run_qform(args):
         nk = lib.cfdwm_profile_read(6, C.byref(tot))
         lib.cfdwm_profile_enable(0)
         res["forms"][name] = {"ms": ms, "rows": R, "pts_per_s": R / (ms / 1e3), "err": errs(out.cpu().numpy()),
-                              "build_s": build_s, "gemm_launches": int(nk),
+                              "build_s": build_s, "gemm_launches": int(nk), "launches": int(timed.launches),
                               "gemm_ms_per_step": tot.value / max(1, args.steps), "clocks": clocks}
     # end to end: host arrays in pinned memory, copies inside the timed region
     hx = [torch.from_numpy(a).pin_memory() for a in (x, y, t)]
@@ -170,15 +182,12 @@ def qform_line(args, r):
         "metric": METRIC, "value": value, "unit": "points/s", "n_gpus": n, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": f["ms"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": head.replace("tc_", "") + " split, FP32 accumulate", "data": "synthetic",
-        "config": {"workload": "precision form: second-order eta and z=0/Taylor-layer u, v, w (pair-cache "
-                               "coefficients) of a 4096-component short-crested JONSWAP sea (256 freq x 16 dir, "
-                               "Hs 6 m, Tp 12 s, gamma 2, cos-2s s=10, depth 100 m) at %d random (x, y, t) points"
-                               % f["rows"],
+        "config": {"workload": QFORM_WORKLOAD % f["rows"],
                    "l2": "inputs larger than L2 (split operands 4 GB per 65,536-row chunk, W 537 MB)",
                    "form": head},
         "e2e": {"value": f["rows"] * n / r["e2e_s"], "unit": "points/s", "h2d_bytes_per_step": r["h2d"],
                 "d2h_bytes_per_step": r["d2h"]},
-        "gpu_launches": 2 * ((f["rows"] + 65535) // 65536) * args.steps,
+        "gpu_launches": f["launches"],
         "clocks": f["clocks"],
         "roofline": {"kernel": "k_qform_tc", "bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops"],
                      "unit": "TFLOP/s", "frac": (achieved / pk["bf16_tflops"]) if achieved else None,
@@ -539,7 +548,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="sgrid", choices=["sgrid", "point", "qform"])
+    ap.add_argument("--workload", default="qform", choices=["qform", "sgrid", "point"])
     ap.add_argument("--rows", type=int, default=4_000_000, help="points of the precision-form workload")
     ap.add_argument("--plain-rows", type=int, default=65536,
                     help="row subset on which the plain FP32 form of the precision workload is timed")
@@ -549,19 +558,24 @@ def main():
                          "are for profiling captures only)")
     args = ap.parse_args()
     unit = "grid nodes/s" if args.workload == "sgrid" else "points/s"
-    workload = ("s-grid second-order update: 1024-component short-crested JONSWAP (64 freq x 16 dir, "
-                "Hs 6 m, Tp 12 s, gamma 2, cos-2s s=10), depth 100 m, 256x256 columns x 16 levels over "
-                "1 km^2, dt 0.5 s, + 1e6 random spline queries per step"
-                if args.workload == "sgrid" else
-                "point API: 128-component JONSWAP (Hs 4 m, Tp 10 s, gamma 3.3), depth 50 m, eta/u/w/dp at "
-                "256 x 32 z x 8 t points")
+    workload = {
+        "sgrid": "s-grid second-order update: 1024-component short-crested JONSWAP (64 freq x 16 dir, "
+                 "Hs 6 m, Tp 12 s, gamma 2, cos-2s s=10), depth 100 m, 256x256 columns x 16 levels over "
+                 "1 km^2, dt 0.5 s, + 1e6 random spline queries per step",
+        "point": "point API: 128-component JONSWAP (Hs 4 m, Tp 10 s, gamma 3.3), depth 50 m, eta/u/w/dp at "
+                 "256 x 32 z x 8 t points",
+        "qform": QFORM_WORKLOAD % args.rows,
+    }[args.workload]
     if args.impl == "reference":
         rank = int(os.environ.get("RANK", "0"))
         if rank != 0:
             return
         steps = []
         for _ in range(args.steps):
-            steps.append(cpu_baseline(args, budget_s=8.0))
+            if args.workload == "qform":
+                steps.append(qform_cpu_baseline())
+            else:
+                steps.append(cpu_baseline(args, budget_s=8.0))
         v = float(np.median([s["value"] for s in steps]))
         cb = dict(steps[-1])
         cb["value"] = v

@@ -56,8 +56,6 @@ namespace cfdwm {
 
 constexpr int QT = 32;          // tile of the plain table (components)
 constexpr int QNC = 8;          // plain record: Ae, Be, Au, Bu, Av, Bv, Cw, Dw
-constexpr double TWO_PI_Q = 6.283185307179586476925286766559;
-constexpr double INV_TWO_PI_Q = 0.15915494309189533576888376337251;
 
 __host__ __device__ inline long qtile_index(int I, int M, int nt) {
     return (long)I * nt - (long)I * (I - 1) / 2 + (M - I);
@@ -222,35 +220,97 @@ __global__ void k_qform_split(int npad, int fp16, const double *coef, T16 *Whi, 
 // ---------------------------------------------------------------------------
 // Phasor prep for a chunk of rows: X hi/lo (16-bit, [rows][2 npad]) and the
 // right-hand phasors Y (FP32, [rows][2 npad]).
+//
+// The phase k.x - omega t + phase0 reaches 1e3-1e4 rad, so it is formed in
+// float-float arithmetic (Dekker's exact product via FMA and Knuth's
+// two-sum) from per-component (hi, lo) coefficient pairs and per-row (hi,
+// lo) coordinates, then reduced by a three-part 2 pi (Cody-Waite) before the
+// FP32 sincos.  Error: a few 1e-7 rad at |phase| ~ 1e4.
 // ---------------------------------------------------------------------------
+struct QRow {     // per row: dx, dy, t as float pairs and the ramp (trivial ramps)
+    float dxh, dxl, dyh, dyl, th, tl, ramp, pad;
+};
+struct QComp {    // per component: kx, ky, -omega, phase0 as float pairs
+    float kxh, kxl, kyh, kyl, wh, wl, ph, pl;
+};
+
+__global__ void k_qform_rows(long rows, const double *x, const double *y, const double *t, double fx, double fy,
+                             const double *phase, int cstride, QRow *out) {
+    long p = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (p >= rows) return;
+    double dx = x[p] - fx, dy = y[p] - fy, tt = t[p];
+    QRow r;
+    r.dxh = (float)dx; r.dxl = (float)(dx - (double)r.dxh);
+    r.dyh = (float)dy; r.dyl = (float)(dy - (double)r.dyh);
+    r.th = (float)tt; r.tl = (float)(tt - (double)r.th);
+    r.ramp = (float)q_freq_ramp(tt, phase[4 * cstride], phase[5 * cstride], phase[6 * cstride]);
+    r.pad = 0.f;
+    out[p] = r;
+}
+
+__global__ void k_qform_comps(int n, int npad, const double *phase, int cstride, QComp *out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npad) return;
+    QComp c = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (i < n) {
+        double v[4] = {phase[i], phase[cstride + i], -phase[2 * cstride + i], phase[3 * cstride + i]};
+        float h[4], l[4];
+        for (int q = 0; q < 4; q++) { h[q] = (float)v[q]; l[q] = (float)(v[q] - (double)h[q]); }
+        c = {h[0], l[0], h[1], l[1], h[2], l[2], h[3], l[3]};
+    }
+    out[i] = c;
+}
+
+// a*b as an unevaluated float pair (products of the lo parts dropped)
+__device__ __forceinline__ float2 ff_mul(float ah, float al, float bh, float bl) {
+    float p = ah * bh;
+    float e = fmaf(ah, bh, -p);
+    e = fmaf(ah, bl, fmaf(al, bh, e));
+    return make_float2(p, e);
+}
+// Knuth two-sum of the hi parts, error folded into the lo part
+__device__ __forceinline__ float2 ff_add(float2 a, float2 b) {
+    float s = a.x + b.x;
+    float bb = s - a.x;
+    float e = (a.x - (s - bb)) + (b.x - bb);
+    return make_float2(s, e + a.y + b.y);
+}
+
 struct QPrep {
     long rows;
-    const double *x, *y, *t;
-    const double *phase;       // [7][cstride] kx, ky, omega, phase0, ramp params
+    const QRow *row;
+    const QComp *comp;
+    const double *phase;       // [7][cstride] (ramp parameters for non-trivial ramps)
+    const double *t;
     int cstride, ncomp, npad;
-    double fx, fy;
     int trivial_ramp, fp16;
     void *Xhi, *Xlo;           // [rows][2 npad]
     float *Y;                  // [rows][2 npad]
 };
 
 __global__ void __launch_bounds__(256) k_qform_prep(QPrep a) {
-    long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    long tot = a.rows * a.npad;
-    if (idx >= tot) return;
-    long p = idx / a.npad;
-    int i = (int)(idx % a.npad);
+    // grid: x over rows, y over blocks of 256 components
+    const int i = blockIdx.y * blockDim.x + threadIdx.x;
+    const long p = blockIdx.x;
+    if (i >= a.npad || p >= a.rows) return;
     float c = 0.f, s = 0.f, r = 0.f;
     if (i < a.ncomp) {
-        const double *P = a.phase;
-        const int cs = a.cstride;
-        double dx = a.x[p] - a.fx, dy = a.y[p] - a.fy, t = a.t[p];
-        double ph = fma(P[i], dx, fma(P[cs + i], dy, fma(-P[2 * cs + i], t, P[3 * cs + i])));
-        double nn = rint(ph * INV_TWO_PI_Q);
-        float red = (float)fma(-nn, TWO_PI_Q, ph);
-        sincosf(red, &s, &c);
-        int ir = a.trivial_ramp ? 0 : i;
-        r = (float)q_freq_ramp(t, P[4 * cs + ir], P[5 * cs + ir], P[6 * cs + ir]);
+        const QRow R = a.row[p];
+        const QComp K = a.comp[i];
+        float2 ph = ff_add(ff_mul(K.kxh, K.kxl, R.dxh, R.dxl), ff_mul(K.kyh, K.kyl, R.dyh, R.dyl));
+        ph = ff_add(ph, ff_mul(K.wh, K.wl, R.th, R.tl));
+        ph = ff_add(ph, make_float2(K.ph, K.pl));
+        // 2 pi = P1 + P2 + P3: P1 = 201/32 has 8 significant bits, so n P1 is exact for |n| < 2^16
+        const float P1 = 6.28125f, P2 = 1.9353071693331003e-3f, P3 = 1.0253376273028358e-11f;
+        float n = rintf(ph.x * 0.15915494309189535f);
+        float red = fmaf(-n, P1, ph.x);
+        red = fmaf(-n, P2, red);
+        red = fmaf(-n, P3, red);
+        red += ph.y;
+        __sincosf(red, &s, &c);
+        r = a.trivial_ramp ? R.ramp
+                           : (float)q_freq_ramp(a.t[p], a.phase[4 * a.cstride + i], a.phase[5 * a.cstride + i],
+                                                a.phase[6 * a.cstride + i]);
     }
     long o = p * 2 * a.npad + i;
     a.Y[o] = c;
@@ -735,7 +795,7 @@ int qform_eval(const DevSea &sea, long n, const double *x, const double *y, cons
     long mpad = ((m + TBM - 1) / TBM) * TBM;
     size_t xb = (size_t)mpad * 2 * npad * 2;     // one 16-bit matrix
     size_t yb = (size_t)mpad * 2 * npad * 4;
-    int rc = reserve_scratch(2 * xb + yb + 4096);
+    int rc = reserve_scratch(2 * xb + yb + sizeof(QRow) * chunk + sizeof(QComp) * npad + 4096);
     if (rc) return rc;
     static bool attr = false;
     if (!attr) {
@@ -747,13 +807,21 @@ int qform_eval(const DevSea &sea, long n, const double *x, const double *y, cons
         char *base = (char *)g_q.scratch;
         void *Xh = base, *Xl = base + xb;
         float *Y = (float *)(base + 2 * xb);
+        QRow *rowrec = (QRow *)(base + 2 * xb + yb);
+        QComp *comprec = (QComp *)(base + 2 * xb + yb + sizeof(QRow) * chunk);
+        k_qform_rows<<<(unsigned)((mm + 255) / 256), 256, 0, stream>>>(mm, x + b, y + b, t + b, sea.fx, sea.fy,
+                                                                       sea.d_phase, sea.npad_g, rowrec);
+        note_launch();
+        k_qform_comps<<<(unsigned)((npad + 255) / 256), 256, 0, stream>>>(sea.n, npad, sea.d_phase, sea.npad_g,
+                                                                          comprec);
+        note_launch();
         QPrep pp;
-        pp.rows = mm; pp.x = x + b; pp.y = y + b; pp.t = t + b; pp.phase = sea.d_phase;
-        pp.cstride = sea.npad_g; pp.ncomp = sea.n; pp.npad = npad; pp.fx = sea.fx; pp.fy = sea.fy;
+        pp.rows = mm; pp.row = rowrec; pp.comp = comprec; pp.phase = sea.d_phase; pp.t = t + b;
+        pp.cstride = sea.npad_g; pp.ncomp = sea.n; pp.npad = npad;
         pp.trivial_ramp = sea.trivial_ramp ? 1 : 0; pp.fp16 = g_q.fp16 ? 1 : 0;
         pp.Xhi = Xh; pp.Xlo = Xl; pp.Y = Y;
-        long tot = mm * (long)npad;
-        k_qform_prep<<<(unsigned)((tot + 255) / 256), 256, 0, stream>>>(pp);
+        dim3 pg((unsigned)mm, (unsigned)(npad / 256));
+        k_qform_prep<<<pg, 256, 0, stream>>>(pp);
         note_launch();
         CK(cudaGetLastError());
         CUtensorMap mXh, mXl, mWh, mWl;

@@ -43,12 +43,200 @@ sys.path.insert(0, HERE)
 METRIC = "2nd-order pts/s at <=1e-5 rel err vs FP64: split-BF16 TC & surrogate vs plain"
 
 
-def sgrid_config(nx=256, ny=256, nl=16):
+def sgrid_config(nx=256, ny=256, nl=16, dt=0.5):
     from cfdwavemaker_gb300 import seastate as ss
     comps = ss.config3_sea()
     grid = {"bounds": (0.0, 1000.0, 0.0, 1000.0), "nx": nx, "ny": ny, "nl": nl, "t0": 0.0,
-            "dt": 0.5, "stretch": (0.7, 1.5)}
+            "dt": dt, "stretch": (0.7, 1.5)}
     return ss.write_irregular(None, comps, 100.0, extrap=2, lsgrid=grid)
+
+
+SURR_WORKLOAD = ("learned s-grid update: the 1024-component short-crested JONSWAP sea (Hs 6 m, Tp 12 s, gamma 2, "
+                 "cos-2s s=10, depth 100 m) on the 256x256x16 s-grid over 1 km^2, %d ring steps at dt 0.1 s, "
+                 "a full plain update every %d steps, the others predicted by the conv operator (4 layers, 32 "
+                 "channels, 3x3, BF16 weights) and checked on %d sampled columns against the plain method "
+                 "(fallback above tol %g); + 1e5 random spline queries per step")
+
+
+def run_surrogate(args):
+    """Learned s-grid update against the plain update on the same grid.
+
+    value: grid nodes updated per second over the surrogate-assisted loop
+    (plain every --plain-every steps, the others predicted and checked,
+    routed through wave_force_update with cfdwm_surrogate_enable); the plain
+    rate is the same loop with every update plain (timed on fewer steps,
+    its cost per step is constant).  Accuracy: max errors of eta and U
+    against a full plain fill at 4 points of a 20-step window (unchecked
+    prediction).  The target tolerance 1e-3 is run too, on a short loop, and
+    its fallback fraction reported."""
+    import torch
+    import cfdwavemaker_gb300 as cw
+    from cfdwavemaker_gb300 import surrogate as S
+    ws, rank, local = dist_init()
+    torch.cuda.set_device(local)
+    lib = cw.load()
+    os.chdir(tempfile.mkdtemp())
+    wm = cw.CFDwavemaker()
+    txt = sgrid_config(256, 256, 16, dt=0.1)
+    nodes = 256 * 256 * 16
+    stream = torch.cuda.current_stream()
+    lib.cfdwm_set_stream(C.c_void_p(stream.cuda_stream))
+    nq = 100_000
+    rng = np.random.default_rng(4321 + rank)
+    qx, qy, qz = rng.uniform(0, 1000, nq), rng.uniform(0, 1000, nq), rng.uniform(-100, 6.0, nq)
+    dq = [torch.tensor(a, device="cuda", dtype=torch.float64) for a in (qx, qy, qz)]
+    dtq = torch.empty(nq, device="cuda", dtype=torch.float64)
+    dout = torch.empty((nq, 4), device="cuda", dtype=torch.float64)
+    hq = [np.ascontiguousarray(a) for a in (qx, qy, qz)]
+    htq = np.empty(nq)
+    hout = np.empty((nq, 4))
+
+    def ok(rc):
+        assert rc == 0, (rc, cw.last_error())
+
+    def fresh(weights=True):
+        ok(wm.initialize_text(txt))
+        if weights:
+            ok(lib.cfdwm_surrogate_load(S.WEIGHTS.encode()))
+
+    def loop(nsteps, host=False):
+        t0, _ = wm.sgrid_state()
+        t = t0
+        for _ in range(nsteps):
+            t += 0.1
+            lib.wave_force_update(t + 1e-9)
+            ts, _ = wm.sgrid_state()
+            if host:
+                htq.fill(ts + 0.05)
+                ok(lib.wave_Kinematics_batch(*[cw._ptr(a) for a in hq], cw._ptr(htq), nq, cw._ptr(hout)))
+            else:
+                dtq.fill_(ts + 0.05)
+                ok(lib.wave_Kinematics_batch(*[cw._ptr(a) for a in dq], cw._ptr(dtq), nq, cw._ptr(dout)))
+
+    def timed(nsteps, host=False):
+        torch.cuda.synchronize()
+        l0 = lib.cfdwm_kernel_launches()
+        if host:
+            c0 = time.perf_counter()
+            loop(nsteps, host=True)
+            torch.cuda.synchronize()
+            return (time.perf_counter() - c0) * 1e3 / nsteps, lib.cfdwm_kernel_launches() - l0
+        e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        loop(nsteps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / nsteps, lib.cfdwm_kernel_launches() - l0
+
+    res = {"ws": ws, "rank": rank}
+    # plain every step
+    fresh(weights=False)
+    ok(lib.cfdwm_surrogate_enable(0, 1, 0.0, 0))
+    loop(max(1, args.warmup))
+    lib.cfdwm_profile_enable(1)
+    lib.cfdwm_profile_read(0, None)
+    ms_plain, _ = timed(args.plain_steps)
+    tot = C.c_double(0.0)
+    nk = lib.cfdwm_profile_read(0, C.byref(tot))
+    lib.cfdwm_profile_enable(0)
+    res["plain"] = {"ms_per_step": ms_plain, "steps": args.plain_steps, "nodes_per_s": nodes / (ms_plain / 1e3),
+                    "column_pairs": {"launches": int(nk), "avg_ms": tot.value / max(1, nk)}}
+    res["npairs"] = int(lib.cfdwm_npairs())
+    res["ncomp"] = int(lib.cfdwm_components(None))
+    # surrogate-assisted loop at the working tolerance
+    fresh()
+    ok(lib.cfdwm_surrogate_enable(1, args.plain_every, args.surr_tol, args.nsample))
+    loop(max(1, args.warmup))
+    ok(lib.cfdwm_surrogate_enable(1, args.plain_every, args.surr_tol, args.nsample))
+    lib.cfdwm_profile_enable(1)
+    for k in range(9):
+        lib.cfdwm_profile_read(k, None)
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier(ws)
+    ms, launches = timed(args.surr_steps)
+    clocks = sampler.stop()
+    prof = {}
+    for k, name in enumerate(["column_pairs", "eta_pairs", "point_pairs", "phasors", "query", "gradients",
+                              "qform", "surr_features", "surr_net"]):
+        tot = C.c_double(0.0)
+        nk = lib.cfdwm_profile_read(k, C.byref(tot))
+        if nk > 0:
+            prof[name] = {"launches": int(nk), "avg_ms": tot.value / nk, "total_ms": tot.value}
+    lib.cfdwm_profile_enable(0)
+    st = [C.c_long(0) for _ in range(3)]
+    ok(lib.cfdwm_surrogate_stats(*[C.byref(v) for v in st]))
+    res.update(ms=ms, launches=launches, clocks=clocks, prof=prof,
+               stats={"predicted": st[0].value, "fell_back": st[1].value, "plain": st[2].value})
+    # end to end (host query arrays), same loop
+    fresh()
+    ok(lib.cfdwm_surrogate_enable(1, args.plain_every, args.surr_tol, args.nsample))
+    res["e2e_ms"], _ = timed(args.surr_steps, host=True)
+    # the target tolerance, short loop
+    fresh()
+    ok(lib.cfdwm_surrogate_enable(1, args.plain_every, 1e-3, args.nsample))
+    ms3, _ = timed(args.plain_every * 2)
+    ok(lib.cfdwm_surrogate_stats(*[C.byref(v) for v in st]))
+    res["tol_1e-3"] = {"ms_per_step": ms3, "steps": args.plain_every * 2, "predicted": st[0].value,
+                       "fell_back": st[1].value, "nodes_per_s": nodes / (ms3 / 1e3)}
+    ok(lib.cfdwm_surrogate_enable(0, 1, 0.0, 0))
+    # accuracy over one window: unchecked predictions against full plain fills
+    acc = {}
+    for name, zero in (("network", False), ("first_order_only", True)):
+        fresh()
+        if zero:
+            n = lib.cfdwm_surrogate_nparams()
+            z = np.zeros(n, np.float32)
+            ok(lib.cfdwm_surrogate_set_params(z.ctypes.data, n))
+        rows = []
+        for i in range(args.plain_every):
+            ok(lib.cfdwm_surrogate_step(0 if i == 0 else 2, 0.0, 0, None, None))
+            if i in (1, args.plain_every // 4, args.plain_every // 2, args.plain_every - 1):
+                err = (C.c_double * 4)()
+                ok(lib.cfdwm_surrogate_compare(err))
+                rows.append([i] + [float(v) for v in err])
+        acc[name] = {"rows_step_eta_u_v_w": rows,
+                     "max_eta": max(r[1] for r in rows), "max_u": max(r[2] for r in rows),
+                     "max_uvw": max(max(r[2:]) for r in rows)}
+    res["accuracy"] = acc
+    res["nodes"] = nodes
+    res["h2d"] = 3 * 8 * nq + 8 * nq
+    res["d2h"] = 4 * 8 * nq
+    return res
+
+
+def surrogate_line(args, r):
+    pk, src = peaks()
+    n = r["ws"]
+    value = r["nodes"] * n / (r["ms"] / 1e3)
+    plain = r["plain"]["nodes_per_s"] * n
+    prof = r["prof"]
+    line = {
+        "metric": METRIC, "value": value, "unit": "grid nodes/s", "n_gpus": n, "steps": args.surr_steps,
+        "warmup": args.warmup, "ms_per_step": r["ms"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (FP64 phases); network bf16 weights, f32 accumulate",
+        "data": "synthetic",
+        "config": {"workload": SURR_WORKLOAD % (args.surr_steps, args.plain_every, args.nsample, args.surr_tol),
+                   "l2": "working set > L2 (grid 340 MB, phasor scratch 856 MB)"},
+        "e2e": {"value": r["nodes"] * n / (r["e2e_ms"] / 1e3), "unit": "grid nodes/s",
+                "h2d_bytes_per_step": r["h2d"], "d2h_bytes_per_step": r["d2h"]},
+        "gpu_launches": r["launches"],
+        "clocks": r["clocks"],
+        "plain_every_step": {"value": plain, "ms_per_step": r["plain"]["ms_per_step"],
+                             "steps": r["plain"]["steps"]},
+        "speedup_vs_plain": value / plain,
+        "surrogate_steps": r["stats"],
+        "tol_1e-3": r["tol_1e-3"],
+        "accuracy": r["accuracy"],
+        "kernels": prof,
+        "peaks_source": src,
+    }
+    # the dominant kernel is still the plain column pair sum (every plain-every-th
+    # step); its roofline is taken from the plain loop's full-grid launches
+    fake = {"prof": {"column_pairs": r["plain"]["column_pairs"]}, "clocks": r["clocks"], "units": r["nodes"],
+            "npairs": r["npairs"], "ncomp": r["ncomp"]}
+    line["roofline"] = roofline(argparse.Namespace(workload="sgrid", grid=256), fake, pk, src)
+    return line
 
 
 QFORM_WORKLOAD = ("precision form: second-order eta and z=0/Taylor-layer u, v, w (pair-cache coefficients) of "
@@ -511,7 +699,7 @@ def cpu_baseline(args, budget_s=15.0):
     import oracle
     from oracle import waveinput
     nthr = os.cpu_count() or 1
-    if args.workload == "sgrid":
+    if args.workload in ("sgrid", "surrogate"):
         cfg = waveinput.read_text(sgrid_config())
         sea = oracle.Sea(cfg)
         grid = oracle.Sgrid(cfg, sea, init=False)
@@ -548,7 +736,13 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="qform", choices=["qform", "sgrid", "point"])
+    ap.add_argument("--workload", default="qform", choices=["qform", "sgrid", "point", "surrogate"])
+    ap.add_argument("--surr-steps", type=int, default=600, help="ring steps of the learned-update loop")
+    ap.add_argument("--plain-every", type=int, default=20)
+    ap.add_argument("--plain-steps", type=int, default=20, help="steps on which the plain loop is timed")
+    ap.add_argument("--surr-tol", type=float, default=5e-2,
+                    help="fallback tolerance of the sampled check in the timed loop")
+    ap.add_argument("--nsample", type=int, default=64)
     ap.add_argument("--rows", type=int, default=4_000_000, help="points of the precision-form workload")
     ap.add_argument("--plain-rows", type=int, default=65536,
                     help="row subset on which the plain FP32 form of the precision workload is timed")
@@ -557,7 +751,7 @@ def main():
                     help="columns per side of the s-grid (256 is the named workload; smaller sizes "
                          "are for profiling captures only)")
     args = ap.parse_args()
-    unit = "grid nodes/s" if args.workload == "sgrid" else "points/s"
+    unit = "grid nodes/s" if args.workload in ("sgrid", "surrogate") else "points/s"
     workload = {
         "sgrid": "s-grid second-order update: 1024-component short-crested JONSWAP (64 freq x 16 dir, "
                  "Hs 6 m, Tp 12 s, gamma 2, cos-2s s=10), depth 100 m, 256x256 columns x 16 levels over "
@@ -565,6 +759,7 @@ def main():
         "point": "point API: 128-component JONSWAP (Hs 4 m, Tp 10 s, gamma 3.3), depth 50 m, eta/u/w/dp at "
                  "256 x 32 z x 8 t points",
         "qform": QFORM_WORKLOAD % args.rows,
+        "surrogate": SURR_WORKLOAD % (args.surr_steps, args.plain_every, args.nsample, args.surr_tol),
     }[args.workload]
     if args.impl == "reference":
         rank = int(os.environ.get("RANK", "0"))
@@ -591,6 +786,15 @@ def main():
         if r["rank"] != 0:
             return
         print(json.dumps(qform_line(args, r)))
+        return
+    if args.workload == "surrogate":
+        r = run_surrogate(args)
+        if r["rank"] != 0:
+            return
+        line = surrogate_line(args, r)
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(argparse.Namespace(workload="sgrid"))
+        print(json.dumps(line))
         return
     r = run_ours(args)
     if r["rank"] != 0:

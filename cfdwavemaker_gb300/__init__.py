@@ -129,6 +129,41 @@ def load(path: str | None = None):
     L.cfdwm_profile_enable.argtypes = [C.c_int]
     L.cfdwm_profile_read.restype = C.c_long
     L.cfdwm_profile_read.argtypes = [C.c_int, _dp]
+    # learned s-grid update
+    ip = C.POINTER(C.c_int)
+    lp = C.POINTER(C.c_long)
+    L.cfdwm_surrogate_create.restype = C.c_int
+    L.cfdwm_surrogate_create.argtypes = [C.c_int, C.c_ulonglong]
+    L.cfdwm_surrogate_nparams.restype = C.c_long
+    L.cfdwm_surrogate_nparams.argtypes = []
+    L.cfdwm_surrogate_get_params.restype = C.c_int
+    L.cfdwm_surrogate_get_params.argtypes = [vp, C.c_long]
+    L.cfdwm_surrogate_set_params.restype = C.c_int
+    L.cfdwm_surrogate_set_params.argtypes = [vp, C.c_long]
+    L.cfdwm_surrogate_save.restype = C.c_int
+    L.cfdwm_surrogate_save.argtypes = [C.c_char_p]
+    L.cfdwm_surrogate_load.restype = C.c_int
+    L.cfdwm_surrogate_load.argtypes = [C.c_char_p]
+    L.cfdwm_surrogate_features.restype = C.c_int
+    L.cfdwm_surrogate_features.argtypes = [_d, vp, vp, vp]
+    L.cfdwm_surrogate_targets.restype = C.c_int
+    L.cfdwm_surrogate_targets.argtypes = [C.c_int, vp, vp, vp]
+    L.cfdwm_surrogate_forward.restype = C.c_int
+    L.cfdwm_surrogate_forward.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp]
+    L.cfdwm_surrogate_loss_grad.restype = C.c_int
+    L.cfdwm_surrogate_loss_grad.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, _dp, vp]
+    L.cfdwm_surrogate_train_step.restype = C.c_int
+    L.cfdwm_surrogate_train_step.argtypes = [vp, vp, C.c_long, vp, C.c_int, C.c_int, C.c_int, C.c_float, _dp]
+    L.cfdwm_surrogate_step.restype = C.c_int
+    L.cfdwm_surrogate_step.argtypes = [C.c_int, _d, C.c_int, ip, _dp]
+    L.cfdwm_surrogate_compare.restype = C.c_int
+    L.cfdwm_surrogate_compare.argtypes = [_dp]
+    L.cfdwm_surrogate_enable.restype = C.c_int
+    L.cfdwm_surrogate_enable.argtypes = [C.c_int, C.c_int, _d, C.c_int]
+    L.cfdwm_surrogate_set_carry.restype = C.c_int
+    L.cfdwm_surrogate_set_carry.argtypes = [_d]
+    L.cfdwm_surrogate_stats.restype = C.c_int
+    L.cfdwm_surrogate_stats.argtypes = [lp, lp, lp]
     if path is None:
         _LIB = L
     return L

@@ -70,6 +70,17 @@ struct Model {
 Model g_model;
 std::mutex g_model_mtx;
 
+// Ring updates through the learned update (cfdwm_surrogate_enable): every
+// plain_every-th update is plain, the others are predicted and checked.
+struct SurrUse {
+    bool on = false;
+    int plain_every = 20;
+    double tol = 1e-3;
+    int nsample = 64;
+    long count = 0;
+};
+SurrUse g_surr_use;
+
 // Per-thread execution context: stream, workspace and staging buffers.
 struct ThreadCtx {
     cudaStream_t own = nullptr;
@@ -490,7 +501,14 @@ void wave_force_update(double t) {
     if (!M.init || M.cfg.wavetype != WT_IRR_SGRID) return;
     cudaStream_t s = stream_of();
     while (grid_check_time(M.grid, t)) {
-        if (grid_update(M.grid, M.sea, M.grid_ws, s) != OK) break;
+        if (g_surr_use.on && surrogate_levels() == M.grid.nl) {
+            int mode = (g_surr_use.count++ % g_surr_use.plain_every == 0) ? 0 : 1;
+            if (surrogate_step(M.cfg, M.sea, M.grid, M.grid_ws, mode, g_surr_use.tol, g_surr_use.nsample,
+                               nullptr, nullptr, s) != OK)
+                break;
+        } else if (grid_update(M.grid, M.sea, M.grid_ws, s) != OK) {
+            break;
+        }
     }
     cudaStreamSynchronize(s);
 }
@@ -704,6 +722,159 @@ int cfdwm_parse_text(const char *text, double *scalars, double *comps, int cap) 
 int cfdwm_regular_solution(double *dst, int cap) {
     if (!g_model.init || g_model.cfg.wavetype != WT_REGULAR) return E_UNSUPPORTED;
     return regular_solution(g_model.reg, dst, cap, stream_of());
+}
+
+// ---- learned s-grid update ------------------------------------------------
+static bool sgrid_loaded() { return g_model.init && g_model.cfg.wavetype == WT_IRR_SGRID; }
+
+int cfdwm_surrogate_create(int nl, unsigned long long seed) {
+    std::lock_guard<std::mutex> lk(g_model_mtx);
+    int rc = surrogate_create(nl, seed, stream_of());
+    if (rc) set_error("surrogate: create failed (levels must be 1..32)");
+    return rc;
+}
+
+long cfdwm_surrogate_nparams(void) { return surrogate_nparams(); }
+
+int cfdwm_surrogate_get_params(float *dst, long n) { return surrogate_get_params(dst, n, stream_of()); }
+
+int cfdwm_surrogate_set_params(const float *src, long n) {
+    std::lock_guard<std::mutex> lk(g_model_mtx);
+    return surrogate_set_params(src, n, stream_of());
+}
+
+static const char SURR_MAGIC[8] = {'C', 'F', 'D', 'W', 'M', 'S', 'R', '1'};
+
+int cfdwm_surrogate_save(const char *path) {
+    long n = surrogate_nparams();
+    if (n <= 0) return E_NOT_INITIALIZED;
+    if (!path) return E_BAD_ARGUMENT;
+    std::vector<float> w(n);
+    int rc = surrogate_get_params(w.data(), n, stream_of());
+    if (rc) return rc;
+    FILE *f = std::fopen(path, "wb");
+    if (!f) {
+        set_error(std::string("surrogate: cannot write ") + path);
+        return E_NO_FILE;
+    }
+    int32_t hdr[2] = {surrogate_levels(), 0};
+    int64_t nn = n;
+    bool ok = std::fwrite(SURR_MAGIC, 1, 8, f) == 8 && std::fwrite(hdr, 4, 2, f) == 2 &&
+              std::fwrite(&nn, 8, 1, f) == 1 && std::fwrite(w.data(), 4, n, f) == (size_t)n;
+    std::fclose(f);
+    return ok ? OK : E_NO_FILE;
+}
+
+int cfdwm_surrogate_load(const char *path) {
+    if (!path) return E_BAD_ARGUMENT;
+    FILE *f = std::fopen(path, "rb");
+    if (!f) {
+        set_error(std::string("surrogate: cannot read ") + path);
+        return E_NO_FILE;
+    }
+    char mg[8];
+    int32_t hdr[2];
+    int64_t nn = 0;
+    bool ok = std::fread(mg, 1, 8, f) == 8 && std::memcmp(mg, SURR_MAGIC, 8) == 0 &&
+              std::fread(hdr, 4, 2, f) == 2 && std::fread(&nn, 8, 1, f) == 1 && nn > 0 && nn < (1L << 28);
+    std::vector<float> w(ok ? nn : 0);
+    if (ok) ok = std::fread(w.data(), 4, nn, f) == (size_t)nn;
+    std::fclose(f);
+    if (!ok) {
+        set_error(std::string("surrogate: not a weight file: ") + path);
+        return E_PARSE;
+    }
+    std::lock_guard<std::mutex> lk(g_model_mtx);
+    int rc = surrogate_levels() == hdr[0] ? OK : surrogate_create(hdr[0], 0, stream_of());
+    if (rc) return rc;
+    if (surrogate_nparams() != nn) {
+        set_error("surrogate: weight file does not match the network shape");
+        return E_PARSE;
+    }
+    return surrogate_set_params(w.data(), (long)nn, stream_of());
+}
+
+int cfdwm_surrogate_features(double t, float *feat, float *base, float *eta1) {
+    std::lock_guard<std::mutex> lk(g_model_mtx);
+    Model &M = g_model;
+    if (!sgrid_loaded()) return E_UNSUPPORTED;
+    if (!is_device(feat) || !is_device(base) || !is_device(eta1)) return E_BAD_ARGUMENT;
+    cudaStream_t s = stream_of();
+    int rc = surrogate_features(M.cfg, M.sea, M.grid, M.grid_ws, t, feat, base, eta1, s);
+    if (!rc) CKR(cudaStreamSynchronize(s));
+    return rc;
+}
+
+int cfdwm_surrogate_targets(int slot, const float *base, const float *eta1, float *tgt) {
+    std::lock_guard<std::mutex> lk(g_model_mtx);
+    if (!sgrid_loaded()) return E_UNSUPPORTED;
+    if (!tgt || !is_device(tgt) || !is_device(base) || !is_device(eta1)) return E_BAD_ARGUMENT;
+    cudaStream_t s = stream_of();
+    int rc = surrogate_targets(g_model.cfg, g_model.grid, slot, base, eta1, tgt, s);
+    if (!rc) CKR(cudaStreamSynchronize(s));
+    return rc;
+}
+
+int cfdwm_surrogate_forward(const float *x, int B, int H, int W, float *y) {
+    if (!x || !y || !is_device(x) || !is_device(y)) return E_BAD_ARGUMENT;
+    cudaStream_t s = stream_of();
+    int rc = surrogate_forward(x, B, H, W, y, s);
+    if (!rc) CKR(cudaStreamSynchronize(s));
+    return rc;
+}
+
+int cfdwm_surrogate_loss_grad(const float *x, const float *tgt, int B, int H, int W, double *loss, float *grad) {
+    if (!x || !tgt || !is_device(x) || !is_device(tgt) || (grad && !is_device(grad))) return E_BAD_ARGUMENT;
+    return surrogate_loss_grad(x, tgt, B, H, W, loss, grad, stream_of());
+}
+
+int cfdwm_surrogate_train_step(const float *xs, const float *ts, long nsamples, const int *idx, int B, int H, int W,
+                               float lr, double *loss) {
+    if (!xs || !ts || !is_device(xs) || !is_device(ts)) return E_BAD_ARGUMENT;
+    return surrogate_train_step(xs, ts, nsamples, idx, B, H, W, lr, loss, stream_of());
+}
+
+int cfdwm_surrogate_step(int mode, double tol, int nsample, int *fell_back, double *err4) {
+    std::lock_guard<std::mutex> lk(g_model_mtx);
+    Model &M = g_model;
+    if (!sgrid_loaded()) return E_UNSUPPORTED;
+    cudaStream_t s = stream_of();
+    int rc = surrogate_step(M.cfg, M.sea, M.grid, M.grid_ws, mode, tol, nsample, fell_back, err4, s);
+    if (rc) set_error("surrogate: ring step failed");
+    return rc;
+}
+
+int cfdwm_surrogate_compare(double *err4) {
+    std::lock_guard<std::mutex> lk(g_model_mtx);
+    Model &M = g_model;
+    if (!sgrid_loaded()) return E_UNSUPPORTED;
+    if (!err4) return E_BAD_ARGUMENT;
+    return surrogate_compare_newest(M.cfg, M.sea, M.grid, M.grid_ws, err4, stream_of());
+}
+
+int cfdwm_surrogate_enable(int on, int plain_every, double tol, int nsample) {
+    std::lock_guard<std::mutex> lk(g_model_mtx);
+    if (on && (surrogate_nparams() <= 0 || plain_every < 1 || nsample < 0 || nsample > 4096))
+        return on && surrogate_nparams() <= 0 ? E_NOT_INITIALIZED : E_BAD_ARGUMENT;
+    g_surr_use.on = on != 0;
+    g_surr_use.plain_every = plain_every;
+    g_surr_use.tol = tol;
+    g_surr_use.nsample = nsample;
+    g_surr_use.count = 0;
+    surrogate_reset_stats();
+    return OK;
+}
+
+int cfdwm_surrogate_set_carry(double wavelengths) {
+    if (!(wavelengths >= 0.0)) return E_BAD_ARGUMENT;
+    std::lock_guard<std::mutex> lk(g_model_mtx);
+    surrogate_set_carry(wavelengths);
+    return OK;
+}
+
+int cfdwm_surrogate_stats(long *steps, long *fallbacks, long *plain_steps) {
+    surrogate_stats(steps, fallbacks, plain_steps);
+    return OK;
 }
 
 }  // extern "C"

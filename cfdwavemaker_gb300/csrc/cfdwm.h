@@ -83,7 +83,7 @@ long launch_count();
 // Optional per-kernel timing with CUDA events recorded on the launching
 // stream around the hot kernels.
 enum ProfKernel { PK_COLUMN_PAIRS = 0, PK_ETA_PAIRS, PK_POINT_PAIRS, PK_PHASORS, PK_QUERY,
-                  PK_GRADIENTS, PK_QFORM, PK_COUNT };
+                  PK_GRADIENTS, PK_QFORM, PK_SURR_FEATURES, PK_SURR_NET, PK_COUNT };
 bool prof_on();
 void prof_begin(int k, void *stream);
 void prof_end(int k, void *stream);
@@ -208,6 +208,40 @@ bool grid_check_time(const DevGrid &g, double t);
 int grid_query(const DevGrid &g, long n, const double *x, const double *y, const double *z,
                const double *t, double *out, void *stream);
 int grid_download(const DevGrid &g, int which, double *dst, long cap, void *stream);
+// Plain fill of a column subset into ring slot `slot` of the given arrays
+// (the grid's own ETA/U or a scratch copy with the same layout).
+int grid_fill_columns(DevGrid &g, const DevSea &sea, Workspace &ws, const int *act, long nact, double t,
+                      float *ETA, float *const U[3], int slot, void *stream);
+// Plain fill of all live columns of slot `slot` of the grid at time t.
+int grid_fill_slot(DevGrid &g, const DevSea &sea, Workspace &ws, int slot, double t, void *stream);
+int grid_gradients(DevGrid &g, void *stream);
+void grid_live_columns(DevGrid &g, const int **act, long *n);
+
+// ---------------------------------------------------------------------------
+// Learned s-grid update (surrogate.cu)
+// ---------------------------------------------------------------------------
+int surrogate_create(int nl, unsigned long long seed, void *stream);
+void surrogate_destroy();
+long surrogate_nparams();
+int surrogate_levels();
+int surrogate_get_params(float *dst, long n, void *stream);
+int surrogate_set_params(const float *src, long n, void *stream);
+int surrogate_features(const Config &cfg, const DevSea &sea, DevGrid &g, Workspace &ws, double t, float *feat,
+                       float *base, float *eta1, void *stream);
+int surrogate_targets(const Config &cfg, DevGrid &g, int slot, const float *base, const float *eta1, float *tg,
+                      void *stream);
+int surrogate_forward(const float *x, int B, int H, int W, float *y, void *stream);
+int surrogate_loss_grad(const float *x, const float *tg, int B, int H, int W, double *loss, float *grad,
+                        void *stream);
+int surrogate_train_step(const float *xs, const float *ts, long nsamples, const int *idx_host, int B, int H, int W,
+                         float lr, double *loss, void *stream);
+int surrogate_step(const Config &cfg, const DevSea &sea, DevGrid &g, Workspace &ws, int mode, double tol,
+                   int nsample, int *fell_back, double *err, void *stream);
+int surrogate_compare_newest(const Config &cfg, const DevSea &sea, DevGrid &g, Workspace &ws, double *err,
+                             void *stream);
+void surrogate_stats(long *steps, long *fallbacks, long *plain_steps);
+void surrogate_set_carry(double wavelengths);
+void surrogate_reset_stats();
 
 // ---------------------------------------------------------------------------
 // Regular waves (regular.cu)

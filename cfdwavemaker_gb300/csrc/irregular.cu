@@ -28,6 +28,7 @@
 #include "cfdwm.h"
 
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <vector>
@@ -48,6 +49,7 @@ constexpr int EATA_NC = 2;    // eta table: A (cc coefficient), B (ss coefficien
 constexpr int GRIDV_NC = 8;   // uvw table: Pu, Mu, Pv, Mv, Pw, Mw, kp, km
 constexpr int POINTV_NC = 12; // point table: Pu, Mu, Pv, Mv, Pw, Mw, Pp, Mp, kp, km, Xpp, Xzz
 constexpr float LOG2E_F = 1.4426950408889634f;
+constexpr long SPLIT_TARGET_BLOCKS = 4 * 152;   // blocks a column-pair launch aims for
 constexpr double TWO_PI = 6.283185307179586476925286766559;
 constexpr double INV_TWO_PI = 0.15915494309189533576888376337251;
 
@@ -82,6 +84,12 @@ struct CompIn {
     const double *omega, *A, *k, *theta;   // device copies (FP64), length n
     double depth, g, rho, mtheta_rad, cutoff, bandwidth, kmax;
 };
+
+// ki^2 + km^2 + 2 ki km gam, each product rounded separately (as the
+// reference's FP64 expression without contraction)
+__device__ __forceinline__ double pair_k2(double ki, double km, double gam) {
+    return __dadd_rn(__dadd_rn(__dmul_rn(ki, ki), __dmul_rn(km, km)), __dmul_rn(__dmul_rn(2.0 * ki, km), gam));
+}
 
 // One record per (tile, entry).  mode 0: grid mask (eta + uvw tables),
 // mode 1: point-API mask (u2/v2/w2/dp2 table).
@@ -138,13 +146,17 @@ __global__ void k_build_tables(CompIn c, int TT, int nt, int mode, float *tab_et
                 if (mode == 0) {
                     keep = (oi <= c.cutoff) && (om <= c.cutoff) && (fabs(oi - om) <= c.bandwidth);
                     hp = (ki + km) <= c.kmax;
-                    gam = cti * ctm + sti * stm;        // Irregular.cpp:870
+                    // Irregular.cpp:870, rounded as the reference rounds it (no FMA)
+                    gam = __dadd_rn(__dmul_rn(cti, ctm), __dmul_rn(sti, stm));
                 } else {
                     gam = cos(thi - thm);               // Irregular.cpp:470
                 }
                 if (keep && (hp || hm)) {
-                    double kp = sqrt(ki * ki + km * km + 2.0 * ki * km * gam);
-                    double kq = sqrt(ki * ki + km * km - 2.0 * ki * km * gam);
+                    // |k_i +- k_m|; for opposite (equal) directions of equal k the
+                    // radicand is 0 up to rounding: clamped so that a -1e-16 does
+                    // not turn the whole table into NaN
+                    double kp = sqrt(fmax(0.0, pair_k2(ki, km, gam)));
+                    double kq = sqrt(fmax(0.0, pair_k2(ki, km, -gam)));
                     double sp = Rsn + Rsm, sm = Rsn - Rsm;
                     double R2p = sp * sp, R2m = sm * sm;
                     double AA = 0.5 * agi * agm;
@@ -435,6 +447,8 @@ struct PairArgs {
     float *out;          // [nf][ncol*nl]
     int pairs;           // 0: first-order z-dependent sums only
     int first;           // 1: add first-order z-dependent sums
+    int tp_per;          // tile pairs per blockIdx.y (split of the pair loop; partial sums
+                         // of slice y go to out + y * nf * ncol * nl)
 };
 
 // Depth factors with the normaliser folded into the coefficients:
@@ -478,9 +492,14 @@ __global__ void __launch_bounds__(128) k_pairs_columns(PairArgs a) {
         zk2[j] = make_float2(zk[2 * j], zk[2 * j + 1]);
         yk2[j] = make_float2(yk[2 * j], yk[2 * j + 1]);
     }
+    // slice of the tile-pair loop owned by this blockIdx.y (block-uniform)
+    const int tp_lo = blockIdx.y * a.tp_per, tp_hi = tp_lo + a.tp_per;
+    int tp = -1;
     for (int I = 0; I < a.ntile; I++) {
         for (int M = I; M < a.ntile; M++) {
             if (!a.pairs && M != I) continue;
+            tp++;
+            if (tp < tp_lo || tp >= tp_hi) continue;
             __syncthreads();
             if (a.pairs) {
                 const float4 *src = reinterpret_cast<const float4 *>(
@@ -571,16 +590,26 @@ __global__ void __launch_bounds__(128) k_pairs_columns(PairArgs a) {
         }
     }
     if (!valid) return;
+    float *out = a.out + (long)blockIdx.y * 3 * npts;
 #pragma unroll
     for (int l = 0; l < LV; l++) {
         int lev = lg * LV + l;
         if (lev < a.nl) {
             long o = col * a.nl + lev;
-            a.out[0 * npts + o] = su[l];
-            a.out[1 * npts + o] = sv[l];
-            a.out[2 * npts + o] = sw[l];
+            out[0 * npts + o] = su[l];
+            out[1 * npts + o] = sv[l];
+            out[2 * npts + o] = sw[l];
         }
     }
+}
+
+// Sum of the split slices of the column kernel, in slice order.
+__global__ void k_sum_slices(long n, int nslice, const float *part, float *out) {
+    long e = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    float s = 0.f, c = 0.f;
+    for (int k = 0; k < nslice; k++) kahan(s, c, part[(long)k * n + e]);
+    out[e] = s;
 }
 
 // Point mode: u, v, w, dp at one height per thread, point-API mask
@@ -830,8 +859,17 @@ int launch_eta_pairs(const DevSea &sea, long n, const float2 *ph, const float *r
     return OK;
 }
 
+long column_pairs_split_floats(int nl) {
+    constexpr int LV = 8;
+    int nlg = 1;
+    while (nlg * LV < nl) nlg *= 2;
+    long cols = 128 / nlg;
+    return 3L * nl * cols * 2 * SPLIT_TARGET_BLOCKS;
+}
+
 int launch_column_pairs(const DevSea &sea, long ncol, int nl, const float2 *ph, const float *rr,
-                        const float *z0, float *out, int pairs, cudaStream_t stream) {
+                        const float *z0, float *out, int pairs, cudaStream_t stream, float *split_buf,
+                        long split_cap) {
     constexpr int LV = 8;
     int nlg = 1;
     while (nlg * LV < nl) nlg *= 2;
@@ -841,6 +879,23 @@ int launch_column_pairs(const DevSea &sea, long ncol, int nl, const float2 *ph, 
     a.ph = ph; a.rr = rr; a.cf = sea.d_cf; a.cstride = sea.npad_g; a.z0 = z0;
     a.depth = (float)sea.depth; a.out = out; a.pairs = pairs; a.first = 1;
     int cols = 128 / nlg;
+    // Few columns (a small grid, a column sample): split the tile-pair loop
+    // over blockIdx.y so that the launch still fills the GPU, and sum the
+    // slices in a fixed order afterwards.
+    const long nblk = (ncol + cols - 1) / cols;
+    const int ntp = pairs ? sea.ntile_g * (sea.ntile_g + 1) / 2 : sea.ntile_g;
+    int nslice = 1;
+    a.tp_per = ntp;
+    if (pairs && split_buf && nblk < SPLIT_TARGET_BLOCKS) {
+        int want = (int)std::min<long>(ntp, (SPLIT_TARGET_BLOCKS + nblk - 1) / nblk);
+        int per = (ntp + want - 1) / want;
+        int ns = (ntp + per - 1) / per;
+        if ((long)ns * 3 * ncol * nl <= split_cap && ns > 1) {
+            nslice = ns;
+            a.tp_per = per;
+            a.out = split_buf;
+        }
+    }
     size_t smem = sizeof(float) * GRID_TILE * GRID_TILE * GRIDV_NC + sizeof(float2) * GRID_TILE * cols;
     static bool attr = false;
     if (!attr) {
@@ -851,10 +906,16 @@ int launch_column_pairs(const DevSea &sea, long ncol, int nl, const float2 *ph, 
         attr = true;
     }
     prof_begin(PK_COLUMN_PAIRS, stream);
-    k_pairs_columns<GRID_TILE, LV><<<(unsigned)((ncol + cols - 1) / cols), 128, smem, stream>>>(a);
+    k_pairs_columns<GRID_TILE, LV><<<dim3((unsigned)nblk, (unsigned)nslice), 128, smem, stream>>>(a);
     note_launch();
     prof_end(PK_COLUMN_PAIRS, stream);
     CK(cudaGetLastError());
+    if (nslice > 1) {
+        long n = 3 * ncol * nl;
+        k_sum_slices<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(n, nslice, split_buf, out);
+        note_launch();
+        CK(cudaGetLastError());
+    }
     return OK;
 }
 

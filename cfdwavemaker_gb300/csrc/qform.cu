@@ -105,9 +105,13 @@ __device__ void q_coefs(const QIn &c, int i, int m, double out[QNC]) {
     double Rm = km * tanh(km * h), Rsm = sqrt(Rm), agm = Am * g / om;
     if (oi > c.cutoff || om > c.cutoff || fabs(oi - om) > c.bandwidth) return;
     bool hp = (ki + km) <= c.kmax, hm = (ki != km);
-    double gam = cti * ctm + sti * stm;
-    double kp = sqrt(ki * ki + km * km + 2.0 * ki * km * gam);
-    double kq = sqrt(ki * ki + km * km - 2.0 * ki * km * gam);
+    // rounded as the reference rounds it; radicands clamped at 0 (opposite
+    // directions of equal k give 0 up to rounding)
+    double gam = __dadd_rn(__dmul_rn(cti, ctm), __dmul_rn(sti, stm));
+    double kp = sqrt(fmax(0.0, __dadd_rn(__dadd_rn(__dmul_rn(ki, ki), __dmul_rn(km, km)),
+                                          __dmul_rn(__dmul_rn(2.0 * ki, km), gam))));
+    double kq = sqrt(fmax(0.0, __dadd_rn(__dadd_rn(__dmul_rn(ki, ki), __dmul_rn(km, km)),
+                                          -__dmul_rn(__dmul_rn(2.0 * ki, km), gam))));
     double sp = Rsn + Rsm, sm = Rsn - Rsm, R2p = sp * sp, R2m = sm * sm;
     double AA = 0.5 * agi * agm;
     double Pe = 0, Me = 0, Pu = 0, Mu = 0, Pv = 0, Mv = 0, Pw = 0, Mw = 0;

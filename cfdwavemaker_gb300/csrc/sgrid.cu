@@ -17,6 +17,7 @@
 // The query kernel gathers the 2x2(x2) stencils of the two bracketing slots
 // and reduces x -> y -> s -> t exactly in the reference's order.
 #include "cfdwm.h"
+#include "sgrid_geom.cuh"
 
 #include <cuda_runtime.h>
 #include <algorithm>
@@ -40,26 +41,12 @@ namespace cfdwm {
 int launch_eta_pairs(const DevSea &sea, long n, const float2 *ph, const float *rr, float *out,
                      cudaStream_t stream);
 int launch_column_pairs(const DevSea &sea, long ncol, int nl, const float2 *ph, const float *rr,
-                        const float *z0, float *out, int pairs, cudaStream_t stream);
+                        const float *z0, float *out, int pairs, cudaStream_t stream, float *split_buf,
+                        long split_cap);
+long column_pairs_split_floats(int nl);
 int launch_phasors_public(const DevSea &sea, long n, const double *x, const double *y,
                           const double *t, long sx, long sy, long st, int npad, float2 *ph,
                           float *rr, double *first, cudaStream_t stream);
-
-struct GridGeom {
-    int nx, ny, nl;
-    double d0, d2, dx, dy, ds, depth, swl, tan_a, tan_b, dt;
-};
-
-// sigmaS2cart (lsgrid_spline.cpp:117-122) in FP64 for level m, s = m * ds.
-// s and s - 1 are rounded explicitly: a fused m*ds - 1 leaves +5.6e-17 at the
-// surface level (0.2 * 5 - 1) where the reference's separately rounded
-// product gives exactly 0, and pow() of the then negative tangent is NaN.
-__device__ __forceinline__ double d_sigmaS2cart(const GridGeom &g, int m, double e) {
-    double s = __dmul_rn(g.ds, (double)m);
-    double base = fmax(tan(-__dadd_rn(s, -1.0) * g.tan_a), 0.0);
-    double sigma = -pow(base, g.tan_b) / pow(tan(g.tan_a), g.tan_b);
-    return (e - g.swl) + sigma * (g.depth + (e - g.swl));
-}
 
 __global__ void k_column_coords(GridGeom g, long nact, const int *act, double *xy) {
     long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
@@ -303,6 +290,8 @@ struct GridExtra {
     float *zmin = nullptr, *zmax = nullptr, *sec = nullptr;
     float *eta2 = nullptr;
     double *tdev = nullptr;    // the slot time, read with stride 0 by the phasor pass
+    float *split = nullptr;    // slices of a split column-pair launch
+    long split_cap = 0;
 };
 static std::vector<std::pair<const DevGrid *, GridExtra>> g_extra;
 static GridExtra *extra(const DevGrid &g) {
@@ -367,6 +356,8 @@ int grid_create(const Config &cfg, DevGrid &g, void *stream_) {
     CK(cudaMalloc(&x->sec, sizeof(float) * 3 * v));
     CK(cudaMalloc(&x->eta2, sizeof(float) * c));
     CK(cudaMalloc(&x->tdev, sizeof(double)));
+    x->split_cap = column_pairs_split_floats(g.nl);
+    CK(cudaMalloc(&x->split, sizeof(float) * x->split_cap));
     CK(cudaStreamSynchronize(stream));
     return OK;
 }
@@ -385,19 +376,18 @@ void grid_free(DevGrid &g) {
     for (auto it = g_extra.begin(); it != g_extra.end(); ++it)
         if (it->first == &g) {
             GridExtra &x = it->second;
-            void *q[] = {x.act_all, x.act_live, x.xy, x.zmin, x.zmax, x.sec, x.eta2, x.tdev};
+            void *q[] = {x.act_all, x.act_live, x.xy, x.zmin, x.zmax, x.sec, x.eta2, x.tdev, x.split};
             for (void *p : q) if (p) cudaFree(p);
             g_extra.erase(it);
             break;
         }
 }
 
-// Fill one ring slot at time t for the given column set.
-static int fill_slot(DevGrid &g, const DevSea &sea, Workspace &ws, int slot, double t, bool live_only,
-                     cudaStream_t stream) {
+// Plain second-order fill of the columns act[0..nact) at time t into ring
+// slot `slot` of the arrays ETA ([slot][nx*ny]) and U[f] ([slot][nx*ny*nl]).
+static int fill_cols(DevGrid &g, const DevSea &sea, Workspace &ws, const int *act, long nact, double t,
+                     float *ETA, float *const U[3], int slot, cudaStream_t stream) {
     GridExtra *x = extra(g);
-    long nact = live_only ? x->n_live : x->n_all;
-    const int *act = live_only ? x->act_live : x->act_all;
     if (nact == 0) return OK;
     GridGeom G = geom(g);
     const int npad = sea.npad_g;
@@ -418,19 +408,46 @@ static int fill_slot(DevGrid &g, const DevSea &sea, Workspace &ws, int slot, dou
     if (rc) return rc;
     rc = launch_eta_pairs(sea, nact, ph, rr, x->eta2, stream);
     if (rc) return rc;
-    k_levels<<<(unsigned)((nact + 127) / 128), 128, 0, stream>>>(G, nact, act, first, x->eta2, slot, g.ETA,
+    k_levels<<<(unsigned)((nact + 127) / 128), 128, 0, stream>>>(G, nact, act, first, x->eta2, slot, ETA,
                                                                  x->zmin, x->zmax);
     note_launch();
     CK(cudaGetLastError());
-    rc = launch_column_pairs(sea, nact, g.nl, ph, rr, x->zmin, x->sec, 1, stream);
+    rc = launch_column_pairs(sea, nact, g.nl, ph, rr, x->zmin, x->sec, 1, stream, x->split, x->split_cap);
     if (rc) return rc;
     long tot = nact * g.nl;
     k_scatter_levels<<<(unsigned)((tot + 255) / 256), 256, 0, stream>>>(G, nact, act, first, x->sec, x->zmax,
-                                                                        slot, g.U[0], g.U[1], g.U[2]);
+                                                                        slot, U[0], U[1], U[2]);
     note_launch();
     CK(cudaGetLastError());
     return OK;
 }
+
+// Fill one ring slot at time t for the given column set.
+static int fill_slot(DevGrid &g, const DevSea &sea, Workspace &ws, int slot, double t, bool live_only,
+                     cudaStream_t stream) {
+    GridExtra *x = extra(g);
+    long nact = live_only ? x->n_live : x->n_all;
+    const int *act = live_only ? x->act_live : x->act_all;
+    return fill_cols(g, sea, ws, act, nact, t, g.ETA, g.U, slot, stream);
+}
+
+int grid_fill_columns(DevGrid &g, const DevSea &sea, Workspace &ws, const int *act, long nact, double t,
+                      float *ETA, float *const U[3], int slot, void *stream) {
+    if (nact < 0 || nact > (long)g.nx * g.ny) return E_BAD_ARGUMENT;
+    return fill_cols(g, sea, ws, act, nact, t, ETA, U, slot, (cudaStream_t)stream);
+}
+
+int grid_fill_slot(DevGrid &g, const DevSea &sea, Workspace &ws, int slot, double t, void *stream) {
+    return fill_slot(g, sea, ws, slot, t, true, (cudaStream_t)stream);
+}
+
+void grid_live_columns(DevGrid &g, const int **act, long *n) {
+    GridExtra *x = extra(g);
+    *act = x->act_live;
+    *n = x->n_live;
+}
+
+GridGeom grid_geom(const DevGrid &g) { return geom(g); }
 
 static int gradients(DevGrid &g, cudaStream_t stream) {
     GradArgs a;
@@ -466,6 +483,8 @@ int grid_initialize(DevGrid &g, const DevSea &sea, Workspace &ws, void *stream_)
     CK(cudaStreamSynchronize(stream));
     return OK;
 }
+
+int grid_gradients(DevGrid &g, void *stream) { return gradients(g, (cudaStream_t)stream); }
 
 int grid_update(DevGrid &g, const DevSea &sea, Workspace &ws, void *stream_) {
     cudaStream_t stream = (cudaStream_t)stream_;

@@ -133,7 +133,8 @@ CFDWM_EXPORT long cfdwm_kernel_launches(void);
 /* Per-kernel timing with CUDA events on the launching stream: enable, run,
  * then read the summed duration (ms) and the launch count of one kernel:
  * 0 s-grid column pair sums, 1 elevation pair sums, 2 point pair sums,
- * 3 phasors, 4 s-grid query, 5 s-grid gradients, 6 quadratic-form GEMM.
+ * 3 phasors, 4 s-grid query, 5 s-grid gradients, 6 quadratic-form GEMM,
+ * 7 learned-update first-order channels, 8 learned-update network forward.
  * Reading clears the record. */
 CFDWM_EXPORT int cfdwm_profile_enable(int on);
 CFDWM_EXPORT long cfdwm_profile_read(int kernel, double *total_ms);
@@ -193,6 +194,73 @@ CFDWM_EXPORT int cfdwm_qform_eval(const double *x, const double *y, const double
  * the point-API pair table); without it the call returns -2. */
 CFDWM_EXPORT int cfdwm_irregular_fields_noalloc(const double *x, const double *y, const double *z,
                                                 const double *t, long n, int mask, double *out);
+
+/* ===========================================================================
+ * Part 5 -- learned s-grid update (new; no counterpart in the reference).
+ *
+ * Between full plain ring updates (lsgrid_spline.cpp:847-931) a small
+ * convolutional network predicts the second-order part of the new slot from
+ * first-order channels of the columns.  Network: 4 valid 3x3 convolutions,
+ * 8 nl -> 32 -> 32 -> 32 -> 1 + 3 nl channels, SiLU between them, BF16
+ * weights, FP32 accumulation; nl = sigma levels of the grid (1..32).
+ * Tensors are [B][C][H][W] FP32 planes in device memory; the network maps
+ * H x W inputs to (H - 8) x (W - 8) outputs.
+ *   input channel  8 m + q, level m, q = u, u~, v, v~, w, w~, p, p~ (first
+ *                  order at the levels placed under eta1; ~ = the quadrature
+ *                  sum, phase - pi/2), over the grid plus a 4-column halo,
+ *                  scaled by 1/(sigma omega_m) (u, v, w) and 1/sigma (p);
+ *   output channel 0 = (eta - swl - eta1) / (k_m sigma^2),
+ *                  1 + f nl + m = (U_f - U1_f) / (k_m sigma^2 omega_m),
+ *                  U1 = first order with the Taylor term at the eta1 levels;
+ * sigma^2 = sum A^2 / 2; omega_m, k_m = A^2-weighted means.
+ * All calls return 0 or a negative status. */
+/* Creates the network for nl levels with seeded He-normal weights. */
+CFDWM_EXPORT int cfdwm_surrogate_create(int nl, unsigned long long seed);
+CFDWM_EXPORT long cfdwm_surrogate_nparams(void);
+/* Parameters (FP32 master copy; host or device pointers), n = nparams. */
+CFDWM_EXPORT int cfdwm_surrogate_get_params(float *dst, long n);
+CFDWM_EXPORT int cfdwm_surrogate_set_params(const float *src, long n);
+/* Weight file: "CFDWMSR1", int32 nl, int32 0, int64 n, n float32. */
+CFDWM_EXPORT int cfdwm_surrogate_save(const char *path);
+CFDWM_EXPORT int cfdwm_surrogate_load(const char *path);
+/* Of the loaded wave type 5 model at time t: feat [8 nl][nx+8][ny+8],
+ * base [3][nx ny nl] (U1), eta1 [nx ny]; device pointers. */
+CFDWM_EXPORT int cfdwm_surrogate_features(double t, float *feat, float *base, float *eta1);
+/* Normalised targets of ring slot `slot` (filled by the plain method, with
+ * base/eta1 from cfdwm_surrogate_features at that slot's time):
+ * tgt [1 + 3 nl][nx][ny]. */
+CFDWM_EXPORT int cfdwm_surrogate_targets(int slot, const float *base, const float *eta1, float *tgt);
+/* y [B][1 + 3 nl][H-8][W-8] = network(x [B][8 nl][H][W]). */
+CFDWM_EXPORT int cfdwm_surrogate_forward(const float *x, int B, int H, int W, float *y);
+/* Loss L = sum_c w_c (y - tgt)^2 / (B P sum w), w_0 = nl, w_c = 1 otherwise,
+ * P = (H-8)(W-8), and dL/dparams into grad [nparams] (device, may be NULL). */
+CFDWM_EXPORT int cfdwm_surrogate_loss_grad(const float *x, const float *tgt, int B, int H, int W, double *loss,
+                                           float *grad);
+/* One Adam step (beta 0.9/0.999, eps 1e-8) on samples idx[0..B) (host ints,
+ * each in [0, S)) of the datasets xs [S][8 nl][H][W] and
+ * ts [S][1 + 3 nl][H-8][W-8], S = nsamples. */
+CFDWM_EXPORT int cfdwm_surrogate_train_step(const float *xs, const float *ts, long nsamples, const int *idx,
+                                            int B, int H, int W, float lr, double *loss);
+/* One ring update of the loaded s-grid: mode 0 plain, 1 predicted and
+ * checked against the plain method on nsample random live columns (the plain
+ * method fills the slot when the error exceeds tol), 2 predicted unchecked.
+ * A predicted slot is first order + network output + the low-passed
+ * residual (plain - network) of the last plain slot, carried forward (see
+ * cfdwm_surrogate_set_carry); adding 4 to the mode leaves the residual out
+ * (network alone).  err4 (may be
+ * NULL): the check's max errors of eta, u, v, w, each relative to the
+ * max |eta - swl| / max |U| of the last plain slot. */
+CFDWM_EXPORT int cfdwm_surrogate_step(int mode, double tol, int nsample, int *fell_back, double *err4);
+/* Errors of the newest slot against a full plain fill at its time
+ * (normalised as in cfdwm_surrogate_step, by the plain slot's own maxima). */
+CFDWM_EXPORT int cfdwm_surrogate_compare(double *err4);
+/* Route wave_force_update through the learned update: every plain_every-th
+ * ring update is plain, the others mode 1 with (tol, nsample). */
+CFDWM_EXPORT int cfdwm_surrogate_enable(int on, int plain_every, double tol, int nsample);
+CFDWM_EXPORT int cfdwm_surrogate_stats(long *steps, long *fallbacks, long *plain_steps);
+/* Low-pass scale of the carried residual, in mean wavelengths 2 pi / k_m
+ * (Gaussian standard deviation; default 0: nothing is carried). */
+CFDWM_EXPORT int cfdwm_surrogate_set_carry(double wavelengths);
 
 #ifdef __cplusplus
 }

@@ -199,6 +199,27 @@ def test_sgrid_vs_reference(wm, case):
         assert norm_rel_err(e, g["s%d_api_SurfElev" % k]) <= TOL
 
 
+def test_sgrid_opposite_directions_vs_oracle(wm):
+    """Directions exactly opposite at equal frequency (theta = -90 and +90 deg
+    of a spread rotated by mtheta = 228.70473821303267 deg): the radicand of
+    |k_i + k_m| is zero up to rounding.  The grid must stay finite and match
+    the FP64 oracle (compiled without contraction, as the reference)."""
+    from cfdwavemaker_gb300 import seastate as ss
+    comps = ss.irregular_components(2.2, 7.2, 1.7, 8, 0.25, 1.6, 100.0, 714772915, ndir=16, spreading_s=6.4)
+    grid = {"bounds": (435.0, 470.0, 442.0, 470.0), "nx": 8, "ny": 7, "nl": 6, "t0": 164.4, "dt": 1.7,
+            "stretch": (0.7, 1.5)}
+    txt = ss.write_irregular(None, comps, 100.0, extrap=2, lsgrid=grid, mtheta=228.70473821303267)
+    assert wm.initialize_text(txt) == 0, cw.last_error()
+    cfg = oracle.waveinput.read_text(txt)
+    sea = oracle.Sea(cfg)
+    og = oracle.Sgrid(cfg, sea)
+    for which in range(4):
+        got, ref = wm.sgrid_array(which), og.array(which)
+        assert np.all(np.isfinite(got)), which
+        assert np.all(np.isfinite(ref)), which
+        assert norm_rel_err(got, ref) <= TOL, (which, norm_rel_err(got, ref))
+
+
 @pytest.mark.parametrize("case", ["fenton24", "fenton_len"])
 def test_fenton_solution_vs_reference(wm, case):
     g = load_golden(case)

@@ -519,6 +519,13 @@ def run_ours(args):
     rc = wm.initialize_text(txt)
     if rc != 0:
         raise SystemExit("initialize failed: %d %s" % (rc, cw.last_error()))
+    depth_rank = 0
+    if args.workload == "sgrid" and args.sgrid_method:
+        R = C.c_int(0)
+        rc = lib.cfdwm_sgrid_method(args.sgrid_method, C.byref(R))
+        if rc != 0:
+            raise SystemExit("tensor-core s-grid form unavailable: %s" % cw.last_error())
+        depth_rank = R.value
     init_s = time.time() - t_init
     stream = torch.cuda.current_stream()
     rng = np.random.default_rng(1234 + rank)
@@ -636,6 +643,7 @@ def run_ours(args):
     te = (time.perf_counter() - te0) / args.steps
     te = allmax(ws, te)
     clocks = sampler.stop()
+    res.update(depth_rank=depth_rank)
     res.update(ms=ms, e2e_s=te, units=units, launches=launches, init_s=init_s, h2d=h2d, d2h=d2h,
                clocks=clocks, ws=ws, rank=rank, prof=prof, npairs=int(lib.cfdwm_npairs()),
                ncomp=int(lib.cfdwm_components(None)))
@@ -654,6 +662,23 @@ def roofline(args, r, pk, src):
     (MEASURED_PEAKS.json holds no SFU or FP32 figure)."""
     prof = r["prof"]
     f_mhz = r["clocks"].get("sm_mhz") or pk.get("sm_max_mhz", 2070.0)
+    if args.workload == "sgrid" and r.get("depth_rank") and "qform" in prof:
+        # depth-separable form: eta2 and 3R quadratic forms per column, each
+        # 2 flop per nonzero coefficient of two N x N upper triangles
+        kp = prof["qform"]
+        N = r["ncomp"]
+        nout = 1 + 3 * r["depth_rank"]
+        flops = 2.0 * nout * N * (N + 1) * r["units"] / 16    # units = nodes; one row per column
+        t = kp["avg_ms"] / 1e3
+        ach = flops / t / 1e12
+        return {"kernel": "k_qform_tc (depth-separable s-grid form)", "bound": "tensor", "achieved": ach,
+                "peak": pk["bf16_tflops"], "unit": "TFLOP/s", "frac": ach / pk["bf16_tflops"],
+                "traffic": traffic_from_profiles("k_qform_tc_sgrid"),
+                "issued_frac": 3 * ach / pk["bf16_tflops"],
+                "algorithmic": "2 flop x (1 + 3R) forms x N (N+1) coefficients per column, N = %d, R = %d, "
+                               "%d columns" % (N, r["depth_rank"], r["units"] // 16),
+                "avg_launch_ms": kp["avg_ms"],
+                "peak_source": "measured bf16 burst (dense), MEASURED_PEAKS.json"}
     if args.workload == "sgrid" and "column_pairs" in prof:
         kp = prof["column_pairs"]
         units = r["units"]                     # grid nodes per launch (all columns, 16 levels)
@@ -743,6 +768,8 @@ def main():
     ap.add_argument("--surr-tol", type=float, default=5e-2,
                     help="fallback tolerance of the sampled check in the timed loop")
     ap.add_argument("--nsample", type=int, default=64)
+    ap.add_argument("--sgrid-method", type=int, default=1, choices=[0, 1],
+                    help="s-grid column sums: 0 plain FP32 CUDA cores, 1 depth-separable tensor-core form")
     ap.add_argument("--rows", type=int, default=4_000_000, help="points of the precision-form workload")
     ap.add_argument("--plain-rows", type=int, default=65536,
                     help="row subset on which the plain FP32 form of the precision workload is timed")
@@ -806,9 +833,12 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": unit, "n_gpus": n, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": r["ms"], "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 (FP64 phases)", "data": "synthetic",
+        "vs_baseline": None,
+        "dtype": "fp16x3 split tcgen05, FP32 accumulate (FP64 phases)" if r.get("depth_rank") else
+                 "f32 (FP64 phases)", "data": "synthetic",
         "config": {"workload": workload, "l2": "working set > L2 (phasor scratch 805 MB, grid 340 MB)",
-                   "form": "plain FP32 compensated"},
+                   "form": ("depth-separable tensor-core form, R = %d (fp16x3 split GEMM)" % r["depth_rank"])
+                   if r.get("depth_rank") else "plain FP32 compensated"},
         "e2e": {"value": e2e, "unit": unit, "h2d_bytes_per_step": r["h2d"], "d2h_bytes_per_step": r["d2h"]},
         "gpu_launches": r["launches"],
         "clocks": r["clocks"],

@@ -160,6 +160,10 @@ def load(path: str | None = None):
     L.cfdwm_surrogate_compare.argtypes = [_dp]
     L.cfdwm_surrogate_enable.restype = C.c_int
     L.cfdwm_surrogate_enable.argtypes = [C.c_int, C.c_int, _d, C.c_int]
+    L.cfdwm_sgrid_method.restype = C.c_int
+    L.cfdwm_sgrid_method.argtypes = [C.c_int, ip]
+    L.cfdwm_depth_basis.restype = C.c_int
+    L.cfdwm_depth_basis.argtypes = [_d, _d, ip, _dp]
     L.cfdwm_surrogate_set_carry.restype = C.c_int
     L.cfdwm_surrogate_set_carry.argtypes = [_d]
     L.cfdwm_surrogate_stats.restype = C.c_int

@@ -865,6 +865,21 @@ int cfdwm_surrogate_enable(int on, int plain_every, double tol, int nsample) {
     return OK;
 }
 
+int cfdwm_sgrid_method(int method, int *rank) {
+    std::lock_guard<std::mutex> lk(g_model_mtx);
+    Model &M = g_model;
+    if (!sgrid_loaded()) return E_UNSUPPORTED;
+    int rc = grid_set_method(M.grid, M.cfg, M.sea, method, stream_of());
+    if (rc) {
+        set_error("s-grid: the tensor-core form is not available for this sea (depth basis)");
+        return rc;
+    }
+    if (rank) *rank = method == 1 ? depthform_rank(M.grid) : 0;
+    return OK;
+}
+
+int cfdwm_depth_basis(double K, double h, int *rank, double *err) { return depthform_basis_info(K, h, rank, err); }
+
 int cfdwm_surrogate_set_carry(double wavelengths) {
     if (!(wavelengths >= 0.0)) return E_BAD_ARGUMENT;
     std::lock_guard<std::mutex> lk(g_model_mtx);

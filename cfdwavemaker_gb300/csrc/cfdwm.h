@@ -138,6 +138,7 @@ struct DevSea {
     int order = 2;
     bool trivial_ramp = true;
     long npairs_grid = 0;   // pairs kept by the reference's pair cache
+    double kmax = 0;        // largest component wavenumber
     // FP64 phase data, length npad_g: kx, ky, omega, phase0, ramptime, starttime, duration
     double *d_phase = nullptr;   // [7][npad_g]
     float *d_cf = nullptr;       // [NCF][npad_g]
@@ -198,7 +199,13 @@ struct DevGrid {
     double *first = nullptr;     // scratch: eta1, gx, gy, gz per column
     float *second = nullptr;     // scratch: level sums [3][ncol*nl]
     float *eta2 = nullptr;       // scratch: eta2 per column
+    int method = 0;              // 0 plain FP32 column sums, 1 depth-separable tensor-core form
 };
+// Selects the method of the column sums (builds the tensor-core form).
+int grid_set_method(DevGrid &g, const Config &cfg, const DevSea &sea, int method, void *stream);
+// The error word of the tensor-core form (0: no bounded wait expired).
+int grid_tc_error(DevGrid &g, void *stream);
+int depthform_rank(DevGrid &g);
 int grid_create(const Config &cfg, DevGrid &g, void *stream);
 void grid_free(DevGrid &g);
 int grid_initialize(DevGrid &g, const DevSea &sea, Workspace &ws, void *stream);
@@ -264,6 +271,45 @@ int regular_solution(const DevRegular &r, double *dst, int cap, void *stream);
 // ---------------------------------------------------------------------------
 // Precision form (qform.cu): second-order sums at z = 0 as quadratic forms
 // ---------------------------------------------------------------------------
+// A quadratic form over each point's phasor vector on the tcgen05 tensor
+// cores (qform.cu): nblk upper-triangular N x N coefficient blocks, split
+// into 16-bit hi/lo parts, each block feeding one output column.
+struct TcForm {
+    bool built = false;
+    int npad = 0, nblk = 0, nout = 0;
+    bool fp16 = true;
+    void *Whi = nullptr, *Wlo = nullptr;
+    float *colscale = nullptr;
+    int *bmap = nullptr;        // per block: X half, Y half, output column
+    int *err = nullptr;
+    void *scratch = nullptr;
+    size_t scratch_bytes = 0;
+};
+int tcform_split(TcForm &f, const double *coef64, const int *bmap_host, int nblk, int nout, int npad, bool fp16,
+                 void *stream);
+int tcform_eval(TcForm &f, const DevSea &sea, long n, const double *x, const double *y, const double *t, long st,
+                float *out, void *stream, int *tc_error);
+void tcform_free(TcForm &f);
+constexpr int TC_NPAD = 256;    // the component count of a TcForm is a multiple of this
+
+// Depth-separable tensor-core form of the s-grid column sums (depthform.cu).
+struct DepthForm {
+    bool built = false;
+    int R = 0, nout = 0;
+    double K = 0, h = 0;
+    TcForm tc;
+    float *bz = nullptr;        // b_r(z) on a uniform table over [-h, 0]
+    float *qout = nullptr;      // [ncol][1 + 3R] GEMM outputs
+    long qcap = 0;
+};
+int depthform_build(const Config &cfg, const DevSea &sea, DepthForm &df, void *stream);
+void depthform_free(DepthForm &df);
+int depthform_columns(DepthForm &df, const DevSea &sea, long nact, const double *x, const double *y,
+                      const double *tdev, float *eta2, void *stream);
+int depthform_combine(DepthForm &df, long nact, int nl, const float *z0, float *sec, void *stream);
+int depthform_error(DepthForm &df, void *stream);
+int depthform_basis_info(double K, double h, int *R, double *err);
+
 int qform_build(const Config &cfg, const DevSea &sea, bool fp16, void *stream);
 void qform_free();
 // out [n][4] FP32: eta2, u2, v2, w2 at z0 = 0 (grid mask); method 0 plain

@@ -1,0 +1,497 @@
+// Depth-separable form of the s-grid column pair sums, on the tensor cores.
+//
+// The column update (lsgrid_spline.cpp:880-903 -> Irregular::uvw2,
+// Irregular.cpp:975-1102) sums, at every level height z of a column,
+//   u2(z) = sum_pairs r_i [Pu F(k+, z) cos(phi_i + phi_m) + Mu F(k-, z) cos(phi_i - phi_m)]
+// (and v2 alike, w2 with G and sines), with the depth profiles
+//   F(k, z) = q(k) (e^{kz} + e^{-k(z + 2h)}),  G(k, z) = q(k) (e^{kz} - e^{-k(z + 2h)}),
+// q folded into the pair coefficients.  F and G do not factor into a part of
+// the pair and a part of the level, which is why the plain form evaluates
+// them per (pair, level).  Over k in [0, K] and z in [-h, 0] the two
+// exponential families have a low numerical rank, though: with an
+// orthonormal basis b_r(z) of their span (the eigenfunctions of the kernel
+//   C(z, z') = int_0^K [e^{k(z+z')} + e^{-k(z+z'+4h)}] dk ),
+//   e^{kz} + e^{-k(z+2h)} = sum_r f_r(k) b_r(z),  e^{kz} - e^{-k(z+2h)} = sum_r g_r(k) b_r(z)
+// to 1e-8 with R of about 16 terms (a Karhunen-Loeve expansion).  Then
+//   u2(z) = sum_r b_r(z) Q^u_r,   Q^u_r = sum_pairs r_i [Pu f_r(k+) cos(.+.) + Mu f_r(k-) cos(.-.)],
+// and every Q_r is a quadratic form in the column's phasor vector -- the
+// same shape as the precision form at z = 0 -- so the 3R forms and eta2 run
+// as one tcgen05 GEMM over all columns (qform.cu), and the levels only
+// combine R numbers per field.  The first-order sums stay exact
+// (k_pairs_columns with pairs = 0).
+//
+// Set-up (host, FP64): Gauss-Legendre nodes on [-h, 0], the weighted kernel
+// matrix, its eigenvectors by cyclic Jacobi rotations, b_r on a fine z table
+// (barycentric interpolation through the nodes), f_r and g_r on a fine k
+// table (quadrature).  The rank is the smallest R whose reconstruction error
+// over a test set of (k, z) is below 2e-8 of max F.
+#include "cfdwm.h"
+#include "sgrid_geom.cuh"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
+namespace cfdwm {
+
+#define CK(x)                                                  \
+    do {                                                       \
+        cudaError_t e_ = (x);                                  \
+        if (e_ != cudaSuccess) {                               \
+            std::fprintf(stderr, "cfdwm: CUDA error %s at %s:%d\n", \
+                         cudaGetErrorString(e_), __FILE__, __LINE__); \
+            return E_CUDA;                                     \
+        }                                                      \
+    } while (0)
+
+constexpr int DF_RMAX = 32;
+constexpr int DF_NK = 4097;      // k table points over [0, K]
+constexpr int DF_NZ = 8193;      // z table points over [-h, 0]
+constexpr int DF_TT = 32;        // pair-table tile of the grid tables (GRID_TILE)
+constexpr int GRIDV_NC_DF = 8;   // grid uvw record: Pu, Mu, Pv, Mv, Pw, Mw, kp, km
+constexpr int EATA_NC_DF = 2;    // grid eta record: A, B
+
+// ---------------------------------------------------------------------------
+// Host: basis construction
+// ---------------------------------------------------------------------------
+static void gauss_legendre(int n, double a, double b, std::vector<double> &x, std::vector<double> &w) {
+    x.assign(n, 0.0);
+    w.assign(n, 0.0);
+    for (int i = 0; i < n; i++) {
+        double t = std::cos(3.141592653589793 * (i + 0.75) / (n + 0.5));
+        double dp = 1.0;
+        for (int it = 0; it < 100; it++) {
+            double p0 = 1.0, p1 = t;
+            for (int k = 2; k <= n; k++) {
+                double p2 = ((2.0 * k - 1.0) * t * p1 - (k - 1.0) * p0) / k;
+                p0 = p1;
+                p1 = p2;
+            }
+            dp = n * (t * p1 - p0) / (t * t - 1.0);
+            double dt = p1 / dp;
+            t -= dt;
+            if (std::fabs(dt) < 1e-16) break;
+        }
+        {
+            double p0 = 1.0, p1 = t;
+            for (int k = 2; k <= n; k++) {
+                double p2 = ((2.0 * k - 1.0) * t * p1 - (k - 1.0) * p0) / k;
+                p0 = p1;
+                p1 = p2;
+            }
+            dp = n * (t * p1 - p0) / (t * t - 1.0);
+        }
+        x[i] = 0.5 * (a + b) + 0.5 * (b - a) * t;
+        w[i] = (b - a) / ((1.0 - t * t) * dp * dp);
+    }
+}
+
+// One-sided (Hestenes) Jacobi SVD of an m x n matrix G (column-major): the
+// columns are rotated until mutually orthogonal.  On return sv holds the
+// column norms (the singular values) and V (n x n, column-major) the right
+// singular vectors.  It resolves small singular values to relative
+// accuracy, which a Gram-matrix eigen-decomposition (squared condition)
+// does not.
+static void jacobi_svd(int m, int n, std::vector<double> &G, std::vector<double> &sv, std::vector<double> &V) {
+    V.assign((size_t)n * n, 0.0);
+    for (int i = 0; i < n; i++) V[(size_t)i * n + i] = 1.0;
+    for (int sweep = 0; sweep < 80; sweep++) {
+        bool rotated = false;
+        for (int p = 0; p < n; p++) {
+            double *gp = &G[(size_t)p * m];
+            for (int q = p + 1; q < n; q++) {
+                double *gq = &G[(size_t)q * m];
+                double al = 0, be = 0, ga = 0;
+                for (int i = 0; i < m; i++) {
+                    al += gp[i] * gp[i];
+                    be += gq[i] * gq[i];
+                    ga += gp[i] * gq[i];
+                }
+                if (std::fabs(ga) <= 1e-15 * std::sqrt(al * be) || ga == 0.0) continue;
+                rotated = true;
+                double ze = (be - al) / (2.0 * ga);
+                double t = (ze >= 0 ? 1.0 : -1.0) / (std::fabs(ze) + std::sqrt(1.0 + ze * ze));
+                double c = 1.0 / std::sqrt(1.0 + t * t), s = c * t;
+                for (int i = 0; i < m; i++) {
+                    double a1 = gp[i], a2 = gq[i];
+                    gp[i] = c * a1 - s * a2;
+                    gq[i] = s * a1 + c * a2;
+                }
+                double *vp = &V[(size_t)p * n], *vq = &V[(size_t)q * n];
+                for (int i = 0; i < n; i++) {
+                    double a1 = vp[i], a2 = vq[i];
+                    vp[i] = c * a1 - s * a2;
+                    vq[i] = s * a1 + c * a2;
+                }
+            }
+        }
+        if (!rotated) break;
+    }
+    sv.assign(n, 0.0);
+    for (int j = 0; j < n; j++) {
+        double a = 0;
+        for (int i = 0; i < m; i++) a += G[(size_t)j * m + i] * G[(size_t)j * m + i];
+        sv[j] = std::sqrt(a);
+    }
+}
+
+struct DfBasis {
+    int R = 0, nz = 0;
+    double K = 0, h = 0, err = 0;
+    std::vector<double> zj, wj, b;   // b[r][j] = b_r(z_j)
+};
+
+// Barycentric interpolation weights of Gauss-Legendre nodes on [a, b]
+// (monotone order): (-1)^j sqrt((1 - t_j^2) W_j), t_j the nodes and W_j the
+// weights on [-1, 1] (Wang and Xiang, 2012), free of the over- and underflow
+// of the product formula.
+static std::vector<double> bary_weights(const std::vector<double> &x, const std::vector<double> &w, double a,
+                                        double b) {
+    int n = (int)x.size();
+    std::vector<double> lw(n);
+    for (int j = 0; j < n; j++) {
+        double t = (2.0 * x[j] - (a + b)) / (b - a);
+        double W = w[j] * 2.0 / (b - a);
+        lw[j] = ((j & 1) ? -1.0 : 1.0) * std::sqrt((1.0 - t * t) * W);
+    }
+    return lw;
+}
+
+static double bary_eval(const std::vector<double> &x, const std::vector<double> &lw, const double *f, double z) {
+    int n = (int)x.size();
+    double num = 0.0, den = 0.0;
+    for (int j = 0; j < n; j++) {
+        double dz = z - x[j];
+        if (dz == 0.0) return f[j];
+        double t = lw[j] / dz;
+        num += t * f[j];
+        den += t;
+    }
+    return num / den;
+}
+
+static int build_basis(double K, double h, DfBasis &B) {
+    const int nz = std::min(512, std::max(96, (int)std::ceil(0.75 * K * h) + 64));
+    std::vector<double> z, w, kq, wq;
+    gauss_legendre(nz, -h, 0.0, z, w);
+    const int nk = 64;
+    gauss_legendre(nk, 0.0, K, kq, wq);
+    // rows: the two exponential families at the k nodes, columns: the z nodes,
+    // both with the square roots of their quadrature weights
+    const int m = 2 * nk;
+    std::vector<double> G((size_t)m * nz);
+    for (int j = 0; j < nz; j++)
+        for (int a = 0; a < nk; a++) {
+            double sw = std::sqrt(wq[a] * w[j]);
+            G[(size_t)j * m + a] = sw * std::exp(kq[a] * z[j]);
+            G[(size_t)j * m + nk + a] = sw * std::exp(-kq[a] * (z[j] + 2.0 * h));
+        }
+    std::vector<double> d, V;
+    jacobi_svd(m, nz, G, d, V);
+    std::vector<int> ord(nz);
+    for (int i = 0; i < nz; i++) ord[i] = i;
+    std::sort(ord.begin(), ord.end(), [&](int a, int b) { return d[a] > d[b]; });
+    // candidate basis (descending), b_r(z_j) = V_jr / sqrt(w_j)
+    std::vector<double> bb((size_t)DF_RMAX * nz);
+    for (int r = 0; r < DF_RMAX && r < nz; r++)
+        for (int j = 0; j < nz; j++) bb[(size_t)r * nz + j] = V[(size_t)ord[r] * nz + j] / std::sqrt(w[j]);
+    // smallest R with max |F - sum_r f_r b_r| <= 2e-8 * 2 over a test set
+    std::vector<double> lw = bary_weights(z, w, -h, 0.0);
+    const int nkt = 48, nzt = 160;
+    const int rmax = std::min(DF_RMAX, nz);
+    std::vector<double> zt(nzt), bt((size_t)rmax * nzt), ft((size_t)nkt * rmax), Ft((size_t)nkt * nzt);
+    for (int c = 0; c < nzt; c++) zt[c] = -h + h * std::sqrt((double)c / (nzt - 1));   // dense near z = 0
+    for (int r = 0; r < rmax; r++)
+        for (int c = 0; c < nzt; c++) bt[(size_t)r * nzt + c] = bary_eval(z, lw, &bb[(size_t)r * nz], zt[c]);
+    for (int a = 0; a < nkt; a++) {
+        double k = K * a / (nkt - 1);
+        for (int r = 0; r < rmax; r++) {
+            double acc = 0.0;
+            for (int j = 0; j < nz; j++)
+                acc += w[j] * (std::exp(k * z[j]) + std::exp(-k * (z[j] + 2.0 * h))) * bb[(size_t)r * nz + j];
+            ft[(size_t)a * rmax + r] = acc;
+        }
+        for (int c = 0; c < nzt; c++) Ft[(size_t)a * nzt + c] = std::exp(k * zt[c]) + std::exp(-k * (zt[c] + 2.0 * h));
+    }
+    int R = 0;
+    double e_at_R = 0.0;
+    for (int Rt = 8; Rt <= rmax; Rt += 2) {
+        double emax = 0.0;
+        for (int a = 0; a < nkt; a++)
+            for (int c = 0; c < nzt; c++) {
+                double Fa = 0.0;
+                for (int r = 0; r < Rt; r++) Fa += ft[(size_t)a * rmax + r] * bt[(size_t)r * nzt + c];
+                emax = std::max(emax, std::fabs(Ft[(size_t)a * nzt + c] - Fa));
+            }
+        if (emax <= 4e-8) {
+            R = Rt;
+            e_at_R = emax;
+            break;
+        }
+    }
+    if (R == 0) return E_UNSUPPORTED;
+    B.err = e_at_R;
+    B.R = R;
+    B.nz = nz;
+    B.K = K;
+    B.h = h;
+    B.zj = z;
+    B.wj = w;
+    B.b.assign(bb.begin(), bb.begin() + (size_t)R * nz);
+    return OK;
+}
+
+// ---------------------------------------------------------------------------
+// Device
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ long df_tile_index(int I, int M, int nt) {
+    return (long)I * nt - (long)I * (I - 1) / 2 + (M - I);
+}
+
+// cubic Lagrange interpolation on a uniform table (4 points, clamped)
+__device__ __forceinline__ void cubic_w(double t, int n, int &i0, double wt[4]) {
+    int i = (int)floor(t);
+    i = max(1, min(n - 3, i));
+    double u = t - i;              // in [0, 1] between points i and i+1
+    i0 = i - 1;
+    wt[0] = -u * (u - 1.0) * (u - 2.0) / 6.0;
+    wt[1] = (u + 1.0) * (u - 1.0) * (u - 2.0) / 2.0;
+    wt[2] = -(u + 1.0) * u * (u - 2.0) / 2.0;
+    wt[3] = (u + 1.0) * u * (u - 1.0) / 6.0;
+}
+
+struct DfCoefArgs {
+    int n, npad, ntile, R;
+    const float *tab_grid, *tab_eta;
+    const double *fk, *gk;    // [R][DF_NK]
+    double inv_dk;
+    double *coef;             // [2 + 6R][npad][npad]
+};
+
+// One thread per (m, i): the coefficient of every block at W^T[m][i].
+__global__ void k_depth_coef(DfCoefArgs a) {
+    long e = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    long tot = (long)a.npad * a.npad;
+    if (e >= tot) return;
+    const int m = (int)(e / a.npad), i = (int)(e % a.npad);
+    const long nn = tot;
+    const int nb = 2 + 6 * a.R;
+    if (i > m || i >= a.n || m >= a.n) {
+        for (int b = 0; b < nb; b++) a.coef[(long)b * nn + e] = 0.0;
+        return;
+    }
+    const int I = i / DF_TT, M = m / DF_TT, ii = i % DF_TT, mm = m % DF_TT;
+    const long rec = df_tile_index(I, M, a.ntile) * DF_TT * DF_TT + ii * DF_TT + mm;
+    const float *g = a.tab_grid + rec * GRIDV_NC_DF;
+    const double Pu = g[0], Mu = g[1], Pv = g[2], Mv = g[3], Pw = g[4], Mw = g[5];
+    const double kp = g[6], km = g[7];
+    a.coef[e] = a.tab_eta[rec * EATA_NC_DF + 0];
+    a.coef[nn + e] = a.tab_eta[rec * EATA_NC_DF + 1];
+    int ip, im;
+    double wp[4], wm[4];
+    cubic_w(kp * a.inv_dk, DF_NK, ip, wp);
+    cubic_w(km * a.inv_dk, DF_NK, im, wm);
+    for (int r = 0; r < a.R; r++) {
+        const double *fr = a.fk + (long)r * DF_NK, *gr = a.gk + (long)r * DF_NK;
+        double fp = 0, fm = 0, gp = 0, gm = 0;
+        for (int q = 0; q < 4; q++) {
+            fp += wp[q] * fr[ip + q];
+            gp += wp[q] * gr[ip + q];
+            fm += wm[q] * fr[im + q];
+            gm += wm[q] * gr[im + q];
+        }
+        double *c = a.coef + (long)(2 + 6 * r) * nn + e;
+        c[0] = Pu * fp + Mu * fm;          // u, c c
+        c[nn] = Mu * fm - Pu * fp;         // u, s s
+        c[2 * nn] = Pv * fp + Mv * fm;     // v, c c
+        c[3 * nn] = Mv * fm - Pv * fp;     // v, s s
+        c[4 * nn] = Pw * gp - Mw * gm;     // w, c s
+        c[5 * nn] = Pw * gp + Mw * gm;     // w, s c
+    }
+}
+
+// eta2 of the columns from output column 0
+__global__ void k_df_take(long n, int nout, const float *out, float *eta2) {
+    long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (q < n) eta2[q] = out[q * nout];
+}
+
+// sec[f][e] += sum_r b_r(z0[e]) Q[q][1 + 3 r + f], e = q nl + m
+__global__ void k_df_combine(long nact, int nl, int R, int nout, const float *z0, const float *out,
+                             const float *bz, float h, float inv_dz, float *sec) {
+    long e = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    long tot = nact * nl;
+    if (e >= tot) return;
+    long q = e / nl;
+    float t = (z0[e] + h) * inv_dz;
+    int i = (int)floorf(t);
+    i = max(1, min(DF_NZ - 3, i));
+    float u = t - i;
+    float w0 = -u * (u - 1.f) * (u - 2.f) * (1.f / 6.f);
+    float w1 = (u + 1.f) * (u - 1.f) * (u - 2.f) * 0.5f;
+    float w2 = -(u + 1.f) * u * (u - 2.f) * 0.5f;
+    float w3 = (u + 1.f) * u * (u - 1.f) * (1.f / 6.f);
+    const float *Q = out + q * nout + 1;
+    float su = 0.f, sv = 0.f, sw = 0.f;
+    for (int r = 0; r < R; r++) {
+        const float *b = bz + (long)r * DF_NZ + i - 1;
+        float br = w0 * b[0] + w1 * b[1] + w2 * b[2] + w3 * b[3];
+        su = fmaf(br, Q[3 * r], su);
+        sv = fmaf(br, Q[3 * r + 1], sv);
+        sw = fmaf(br, Q[3 * r + 2], sw);
+    }
+    sec[e] += su;
+    sec[tot + e] += sv;
+    sec[2 * tot + e] += sw;
+}
+
+// ---------------------------------------------------------------------------
+// Host
+// ---------------------------------------------------------------------------
+int depthform_build(const Config &cfg, const DevSea &sea, DepthForm &df, void *stream_) {
+    cudaStream_t stream = (cudaStream_t)stream_;
+    depthform_free(df);
+    if (sea.n < 1 || !sea.d_tab_grid || !sea.d_tab_eta) return E_NOT_INITIALIZED;
+    double kmax = sea.kmax;
+    for (double k : cfg.k) kmax = std::max(kmax, k);
+    // the pair wavenumbers |k_i +- k_m| and the diagonal 2 k are <= 2 kmax
+    const double K = 2.0 * kmax * (1.0 + 1e-9) + 1e-12;
+    const double h = cfg.depth;
+    DfBasis B;
+    int rc = build_basis(K, h, B);
+    if (rc) return rc;
+    const int R = B.R, nz = B.nz;
+    // k tables f_r(k), g_r(k) by quadrature; z table b_r(z) by barycentric interpolation
+    std::vector<double> fk((size_t)R * DF_NK), gk((size_t)R * DF_NK);
+    const double dk = K / (DF_NK - 1);
+    for (int a = 0; a < DF_NK; a++) {
+        double k = dk * a;
+        std::vector<double> E(nz), Y(nz);
+        for (int j = 0; j < nz; j++) {
+            E[j] = std::exp(k * B.zj[j]);
+            Y[j] = std::exp(-k * (B.zj[j] + 2.0 * h));
+        }
+        for (int r = 0; r < R; r++) {
+            double f = 0.0, g = 0.0;
+            for (int j = 0; j < nz; j++) {
+                double wb = B.wj[j] * B.b[(size_t)r * nz + j];
+                f += wb * (E[j] + Y[j]);
+                g += wb * (E[j] - Y[j]);
+            }
+            fk[(size_t)r * DF_NK + a] = f;
+            gk[(size_t)r * DF_NK + a] = g;
+        }
+    }
+    std::vector<double> lw = bary_weights(B.zj, B.wj, -h, 0.0);
+    std::vector<float> bz((size_t)R * DF_NZ);
+    const double dz = h / (DF_NZ - 1);
+    for (int r = 0; r < R; r++)
+        for (int c = 0; c < DF_NZ; c++)
+            bz[(size_t)r * DF_NZ + c] = (float)bary_eval(B.zj, lw, &B.b[(size_t)r * nz], -h + dz * c);
+    df.R = R;
+    df.K = K;
+    df.h = h;
+    df.nout = 1 + 3 * R;
+    CK(cudaMalloc(&df.bz, sizeof(float) * bz.size()));
+    CK(cudaMemcpyAsync(df.bz, bz.data(), sizeof(float) * bz.size(), cudaMemcpyHostToDevice, stream));
+    double *d_fk = nullptr, *d_gk = nullptr, *coef = nullptr;
+    CK(cudaMalloc(&d_fk, sizeof(double) * fk.size()));
+    CK(cudaMalloc(&d_gk, sizeof(double) * gk.size()));
+    CK(cudaMemcpyAsync(d_fk, fk.data(), sizeof(double) * fk.size(), cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d_gk, gk.data(), sizeof(double) * gk.size(), cudaMemcpyHostToDevice, stream));
+    const int npad = ((sea.n + TC_NPAD - 1) / TC_NPAD) * TC_NPAD;
+    const int nblk = 2 + 6 * R;
+    CK(cudaMalloc(&coef, sizeof(double) * (size_t)nblk * npad * npad));
+    DfCoefArgs a;
+    a.n = sea.n; a.npad = npad; a.ntile = sea.ntile_g; a.R = R;
+    a.tab_grid = sea.d_tab_grid; a.tab_eta = sea.d_tab_eta; a.fk = d_fk; a.gk = d_gk;
+    a.inv_dk = 1.0 / dk; a.coef = coef;
+    long tot = (long)npad * npad;
+    k_depth_coef<<<(unsigned)((tot + 255) / 256), 256, 0, stream>>>(a);
+    note_launch();
+    CK(cudaGetLastError());
+    // blocks: eta (c c, s s), then per r: u (c c, s s), v (c c, s s), w (c s, s c)
+    std::vector<int> bmap(3 * nblk);
+    auto setb = [&](int b, int kh, int yh, int col) { bmap[3 * b] = kh; bmap[3 * b + 1] = yh; bmap[3 * b + 2] = col; };
+    setb(0, 0, 0, 0);
+    setb(1, 1, 1, 0);
+    for (int r = 0; r < R; r++) {
+        int b = 2 + 6 * r, o = 1 + 3 * r;
+        setb(b + 0, 0, 0, o);
+        setb(b + 1, 1, 1, o);
+        setb(b + 2, 0, 0, o + 1);
+        setb(b + 3, 1, 1, o + 1);
+        setb(b + 4, 0, 1, o + 2);
+        setb(b + 5, 1, 0, o + 2);
+    }
+    rc = tcform_split(df.tc, coef, bmap.data(), nblk, df.nout, npad, true, stream);
+    cudaFree(coef);
+    cudaFree(d_fk);
+    cudaFree(d_gk);
+    if (rc) return rc;
+    df.built = true;
+    return OK;
+}
+
+// Host-only check of the basis construction (no device work).
+int depthform_basis_info(double K, double h, int *R, double *err) {
+    if (!(K > 0) || !(h > 0)) return E_BAD_ARGUMENT;
+    DfBasis B;
+    int rc = build_basis(K, h, B);
+    if (rc) return rc;
+    if (R) *R = B.R;
+    if (err) *err = B.err;
+    return OK;
+}
+
+void depthform_free(DepthForm &df) {
+    tcform_free(df.tc);
+    if (df.bz) cudaFree(df.bz);
+    if (df.qout) cudaFree(df.qout);
+    df = DepthForm();
+}
+
+// second-order sums of the columns act[0..nact) at the level heights z0:
+// eta2 [nact] and sec [3][nact nl] (+=, after the first-order sums)
+int depthform_columns(DepthForm &df, const DevSea &sea, long nact, const double *x, const double *y,
+                      const double *tdev, float *eta2, void *stream_) {
+    cudaStream_t stream = (cudaStream_t)stream_;
+    if (!df.built) return E_NOT_INITIALIZED;
+    if (df.qcap < nact) {
+        if (df.qout) cudaFree(df.qout);
+        df.qout = nullptr;
+        df.qcap = 0;
+        CK(cudaMalloc(&df.qout, sizeof(float) * df.nout * nact));
+        df.qcap = nact;
+    }
+    int rc = tcform_eval(df.tc, sea, nact, x, y, tdev, 0, df.qout, stream, nullptr);
+    if (rc) return rc;
+    k_df_take<<<(unsigned)((nact + 255) / 256), 256, 0, stream>>>(nact, df.nout, df.qout, eta2);
+    note_launch();
+    CK(cudaGetLastError());
+    return OK;
+}
+
+int depthform_combine(DepthForm &df, long nact, int nl, const float *z0, float *sec, void *stream_) {
+    cudaStream_t stream = (cudaStream_t)stream_;
+    long tot = nact * nl;
+    k_df_combine<<<(unsigned)((tot + 255) / 256), 256, 0, stream>>>(nact, nl, df.R, df.nout, z0, df.qout, df.bz,
+                                                                    (float)df.h,
+                                                                    (float)((DF_NZ - 1) / df.h), sec);
+    note_launch();
+    CK(cudaGetLastError());
+    return OK;
+}
+
+int depthform_error(DepthForm &df, void *stream_) {
+    if (!df.built) return OK;
+    int h = 0;
+    CK(cudaMemcpyAsync(&h, df.tc.err, sizeof(int), cudaMemcpyDeviceToHost, (cudaStream_t)stream_));
+    CK(cudaStreamSynchronize((cudaStream_t)stream_));
+    return h;
+}
+
+}  // namespace cfdwm

@@ -293,6 +293,7 @@ int sea_build(const Config &cfg, DevSea &sea, bool point_table, void *stream_) {
             sea.trivial_ramp = false;
     double kmax = 0.0;   // Irregular.cpp:833-835
     for (int i = 0; i < n; i++) kmax = std::max(kmax, cfg.k[i]);
+    sea.kmax = kmax;
 
     // FP64 component inputs on the device
     double *d_in = nullptr;
@@ -727,8 +728,12 @@ __global__ void __launch_bounds__(128) k_pairs_eta(PairArgs a) {
     const bool valid = p < a.ncol;
     const long pc = valid ? p : 0;
     float se = 0, ce = 0;
+    const int tp_lo = blockIdx.y * a.tp_per, tp_hi = tp_lo + a.tp_per;
+    int tp = -1;
     for (int I = 0; I < a.ntile; I++) {
         for (int M = I; M < a.ntile; M++) {
+            tp++;
+            if (tp < tp_lo || tp >= tp_hi) continue;   // block-uniform
             __syncthreads();
             const float4 *src = reinterpret_cast<const float4 *>(
                 a.tab + tile_index(I, M, a.ntile) * (long)TT * TT * 2);
@@ -754,7 +759,7 @@ __global__ void __launch_bounds__(128) k_pairs_eta(PairArgs a) {
             }
         }
     }
-    if (valid) a.out[p] = se;
+    if (valid) a.out[(long)blockIdx.y * a.ncol + p] = se;
 }
 
 // ---------------------------------------------------------------------------
@@ -839,11 +844,26 @@ int launch_phasors_public(const DevSea &sea, long n, const double *x, const doub
 }
 
 int launch_eta_pairs(const DevSea &sea, long n, const float2 *ph, const float *rr, float *out,
-                     cudaStream_t stream) {
+                     cudaStream_t stream, float *split_buf = nullptr, long split_cap = 0) {
     PairArgs a{};
     a.ncol = n; a.nl = 1; a.nlg = 1; a.ntile = sea.ntile_g; a.tab = sea.d_tab_eta;
     a.ph = ph; a.rr = rr; a.cf = sea.d_cf; a.cstride = sea.npad_g; a.out = out;
     a.pairs = 1; a.first = 0;
+    // few columns: split the tile-pair loop over blockIdx.y (as the column kernel)
+    const long nblk = (n + 127) / 128;
+    const int ntp = sea.ntile_g * (sea.ntile_g + 1) / 2;
+    int nslice = 1;
+    a.tp_per = ntp;
+    if (split_buf && nblk < SPLIT_TARGET_BLOCKS) {
+        int want = (int)std::min<long>(ntp, (SPLIT_TARGET_BLOCKS + nblk - 1) / nblk);
+        int per = (ntp + want - 1) / want;
+        int ns = (ntp + per - 1) / per;
+        if ((long)ns * n <= split_cap && ns > 1) {
+            nslice = ns;
+            a.tp_per = per;
+            a.out = split_buf;
+        }
+    }
     size_t smem = sizeof(float2) * (GRID_TILE * GRID_TILE + GRID_TILE * 128);
     static bool attr = false;
     if (!attr) {
@@ -852,10 +872,15 @@ int launch_eta_pairs(const DevSea &sea, long n, const float2 *ph, const float *r
         attr = true;
     }
     prof_begin(PK_ETA_PAIRS, stream);
-    k_pairs_eta<GRID_TILE><<<(unsigned)((n + 127) / 128), 128, smem, stream>>>(a);
+    k_pairs_eta<GRID_TILE><<<dim3((unsigned)nblk, (unsigned)nslice), 128, smem, stream>>>(a);
     note_launch();
     prof_end(PK_ETA_PAIRS, stream);
     CK(cudaGetLastError());
+    if (nslice > 1) {
+        k_sum_slices<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(n, nslice, split_buf, out);
+        note_launch();
+        CK(cudaGetLastError());
+    }
     return OK;
 }
 

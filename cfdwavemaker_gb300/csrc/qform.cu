@@ -238,11 +238,11 @@ struct QComp {    // per component: kx, ky, -omega, phase0 as float pairs
     float kxh, kxl, kyh, kyl, wh, wl, ph, pl;
 };
 
-__global__ void k_qform_rows(long rows, const double *x, const double *y, const double *t, double fx, double fy,
-                             const double *phase, int cstride, QRow *out) {
+__global__ void k_qform_rows(long rows, const double *x, const double *y, const double *t, long st, double fx,
+                             double fy, const double *phase, int cstride, QRow *out) {
     long p = blockIdx.x * (long)blockDim.x + threadIdx.x;
     if (p >= rows) return;
-    double dx = x[p] - fx, dy = y[p] - fy, tt = t[p];
+    double dx = x[p] - fx, dy = y[p] - fy, tt = t[p * st];
     QRow r;
     r.dxh = (float)dx; r.dxl = (float)(dx - (double)r.dxh);
     r.dyh = (float)dy; r.dyl = (float)(dy - (double)r.dyh);
@@ -286,6 +286,7 @@ struct QPrep {
     const QComp *comp;
     const double *phase;       // [7][cstride] (ramp parameters for non-trivial ramps)
     const double *t;
+    long st;                   // element stride of t
     int cstride, ncomp, npad;
     int trivial_ramp, fp16;
     void *Xhi, *Xlo;           // [rows][2 npad]
@@ -313,7 +314,7 @@ __global__ void __launch_bounds__(256) k_qform_prep(QPrep a) {
         red += ph.y;
         __sincosf(red, &s, &c);
         r = a.trivial_ramp ? R.ramp
-                           : (float)q_freq_ramp(a.t[p], a.phase[4 * a.cstride + i], a.phase[5 * a.cstride + i],
+                           : (float)q_freq_ramp(a.t[p * a.st], a.phase[4 * a.cstride + i], a.phase[5 * a.cstride + i],
                                                 a.phase[6 * a.cstride + i]);
     }
     long o = p * 2 * a.npad + i;
@@ -469,14 +470,17 @@ struct QTC {
     int npad;                // components (multiple of 256)
     int ntn;                 // column tiles per block (npad / 256)
     int group_m;             // row blocks per tile group
+    int nblk;                // coefficient blocks of W
+    int nout;                // outputs per row
+    const int *bmap;         // per block: X half, Y half, output column
     const float *Y;          // [rows][2 npad]
-    const float *colscale;   // [8][npad] (1 for bf16)
-    float *out;              // [rows][4] accumulated with atomics
+    const float *colscale;   // [nblk][npad] (1 for bf16)
+    float *out;              // [rows][nout] accumulated with atomics
     int fp16;
     int *err;
 };
 
-// Grid: one CTA per (row block, column tile).  Column tiles: 8 blocks x ntn.
+// Grid: one CTA per (row block, column tile).  Column tiles: nblk blocks x ntn.
 __global__ void __launch_bounds__(192, 1) k_qform_tc(const __grid_constant__ CUtensorMap mXh,
                                                      const __grid_constant__ CUtensorMap mXl,
                                                      const __grid_constant__ CUtensorMap mWh,
@@ -491,7 +495,7 @@ __global__ void __launch_bounds__(192, 1) k_qform_tc(const __grid_constant__ CUt
 
     // grouped tile order: a group of group_m row blocks sweeps all column tiles
     const long nrb = (a.rows + TBM - 1) / TBM;
-    const int ncol = 8 * a.ntn;
+    const int ncol = a.nblk * a.ntn;
     long bid = blockIdx.x;
     long per_group = (long)a.group_m * ncol;
     long grp = bid / per_group;
@@ -504,11 +508,9 @@ __global__ void __launch_bounds__(192, 1) k_qform_tc(const __grid_constant__ CUt
     // a CTA that finds the error word set leaves before touching any resource
     if (*(volatile int *)a.err != 0) return;
     const int blk = ct / a.ntn, tn = ct % a.ntn;
-    const int field = blk & 3, khalf = blk >> 2;
+    const int khalf = a.bmap[3 * blk], yhalf = a.bmap[3 * blk + 1], outcol = a.bmap[3 * blk + 2];
     const int m0 = tn * TBN;
     const int nkb = (m0 + TBN) / TBK;            // upper triangle: i < m0 + 256
-    // right-hand multiplier half: eta/u/v take their own half, w the other
-    const int yhalf = (field == 3) ? (1 - khalf) : khalf;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < TSTAGES; s++) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
@@ -603,7 +605,7 @@ __global__ void __launch_bounds__(192, 1) k_qform_tc(const __grid_constant__ CUt
                     }
                 }
             }
-            if (row < a.rows) atomicAdd(a.out + row * 4 + field, part);
+            if (row < a.rows) atomicAdd(a.out + row * a.nout + outcol, part);
         }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     }
@@ -654,36 +656,150 @@ static int make_map(CUtensorMap *m, const void *base, long rows, long cols, int 
     return r == CUDA_SUCCESS ? OK : E_CUDA;
 }
 
-struct QformState {
-    bool built = false;
-    int n = 0, npad = 0, ntile_plain = 0;
-    bool fp16 = false;
-    float *plain_tab = nullptr;
-    void *Whi = nullptr, *Wlo = nullptr;
-    float *colscale = nullptr;
-    int *err = nullptr;
-    void *scratch = nullptr;   // chunk buffers
-    size_t scratch_bytes = 0;
-};
-static QformState g_q;
-
+// ---------------------------------------------------------------------------
+// A quadratic form on the tensor cores: the split W operand of nblk blocks
+// and the per-block map (X half, Y half, output column).
+// ---------------------------------------------------------------------------
 int launch_phasors_public(const DevSea &sea, long n, const double *x, const double *y, const double *t,
                           long sx, long sy, long st, int npad, float2 *ph, float *rr, double *first,
                           cudaStream_t stream);
 
+void tcform_free(TcForm &f) {
+    void *q[] = {f.Whi, f.Wlo, f.colscale, f.bmap, f.err, f.scratch};
+    for (void *p : q) if (p) cudaFree(p);
+    f = TcForm();
+}
+
+// coef64: [nblk][npad (output column m)][npad (K index i)] FP64, W transposed.
+int tcform_split(TcForm &f, const double *coef64, const int *bmap_host, int nblk, int nout, int npad, bool fp16,
+                 void *stream_) {
+    cudaStream_t stream = (cudaStream_t)stream_;
+    tcform_free(f);
+    if (npad % TBN != 0 || nblk < 1) return E_BAD_ARGUMENT;
+    f.npad = npad; f.nblk = nblk; f.nout = nout; f.fp16 = fp16;
+    size_t wel = (size_t)nblk * npad * npad;
+    CK(cudaMalloc(&f.Whi, 2 * wel));
+    CK(cudaMalloc(&f.Wlo, 2 * wel));
+    CK(cudaMalloc(&f.colscale, sizeof(float) * nblk * npad));
+    CK(cudaMalloc(&f.bmap, sizeof(int) * 3 * nblk));
+    CK(cudaMemcpyAsync(f.bmap, bmap_host, sizeof(int) * 3 * nblk, cudaMemcpyHostToDevice, stream));
+    dim3 gt((unsigned)npad, (unsigned)nblk);
+    if (fp16)
+        k_qform_split<__half><<<gt, 256, 0, stream>>>(npad, 1, coef64, (__half *)f.Whi, (__half *)f.Wlo,
+                                                      f.colscale);
+    else
+        k_qform_split<__nv_bfloat16><<<gt, 256, 0, stream>>>(npad, 0, coef64, (__nv_bfloat16 *)f.Whi,
+                                                             (__nv_bfloat16 *)f.Wlo, f.colscale);
+    note_launch();
+    CK(cudaGetLastError());
+    CK(cudaMalloc(&f.err, sizeof(int)));
+    CK(cudaMemsetAsync(f.err, 0, sizeof(int), stream));
+    CK(cudaStreamSynchronize(stream));
+    f.built = true;
+    return OK;
+}
+
+static int tc_reserve(TcForm &f, size_t bytes) {
+    if (f.scratch_bytes >= bytes) return OK;
+    if (f.scratch) cudaFree(f.scratch);
+    f.scratch = nullptr;
+    f.scratch_bytes = 0;
+    CK(cudaMalloc(&f.scratch, bytes));
+    f.scratch_bytes = bytes;
+    return OK;
+}
+
+// out [n][nout] FP32 (zeroed here, then accumulated): the nout quadratic forms
+// of the points (x, y, t[p * st]).
+int tcform_eval(TcForm &f, const DevSea &sea, long n, const double *x, const double *y, const double *t, long st,
+                float *out, void *stream_, int *tc_error) {
+    cudaStream_t stream = (cudaStream_t)stream_;
+    if (!f.built) return E_NOT_INITIALIZED;
+    if (n <= 0) return OK;
+    const int npad = f.npad;
+    if (npad < sea.n) return E_BAD_ARGUMENT;
+    CK(cudaMemsetAsync(out, 0, sizeof(float) * f.nout * n, stream));
+    const long chunk = 1L << 16;
+    long m = std::min(n, chunk);
+    long mpad = ((m + TBM - 1) / TBM) * TBM;
+    size_t xb = (size_t)mpad * 2 * npad * 2;     // one 16-bit matrix
+    size_t yb = (size_t)mpad * 2 * npad * 4;
+    int rc = tc_reserve(f, 2 * xb + yb + sizeof(QRow) * chunk + sizeof(QComp) * npad + 4096);
+    if (rc) return rc;
+    static bool attr = false;
+    if (!attr) {
+        CK(cudaFuncSetAttribute(k_qform_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
+        attr = true;
+    }
+    for (long b = 0; b < n; b += chunk) {
+        long mm = std::min(chunk, n - b);
+        char *base = (char *)f.scratch;
+        void *Xh = base, *Xl = base + xb;
+        float *Y = (float *)(base + 2 * xb);
+        QRow *rowrec = (QRow *)(base + 2 * xb + yb);
+        QComp *comprec = (QComp *)(base + 2 * xb + yb + sizeof(QRow) * chunk);
+        k_qform_rows<<<(unsigned)((mm + 255) / 256), 256, 0, stream>>>(mm, x + b, y + b, t + b * st, st, sea.fx,
+                                                                       sea.fy, sea.d_phase, sea.npad_g, rowrec);
+        note_launch();
+        k_qform_comps<<<(unsigned)((npad + 255) / 256), 256, 0, stream>>>(sea.n, npad, sea.d_phase, sea.npad_g,
+                                                                          comprec);
+        note_launch();
+        QPrep pp;
+        pp.rows = mm; pp.row = rowrec; pp.comp = comprec; pp.phase = sea.d_phase; pp.t = t + b * st; pp.st = st;
+        pp.cstride = sea.npad_g; pp.ncomp = sea.n; pp.npad = npad;
+        pp.trivial_ramp = sea.trivial_ramp ? 1 : 0; pp.fp16 = f.fp16 ? 1 : 0;
+        pp.Xhi = Xh; pp.Xlo = Xl; pp.Y = Y;
+        dim3 pg((unsigned)mm, (unsigned)(npad / 256));
+        k_qform_prep<<<pg, 256, 0, stream>>>(pp);
+        note_launch();
+        CK(cudaGetLastError());
+        CUtensorMap mXh, mXl, mWh, mWl;
+        if (make_map(&mXh, Xh, mm, 2L * npad, TBM, f.fp16) || make_map(&mXl, Xl, mm, 2L * npad, TBM, f.fp16) ||
+            make_map(&mWh, f.Whi, (long)f.nblk * npad, npad, TBN, f.fp16) ||
+            make_map(&mWl, f.Wlo, (long)f.nblk * npad, npad, TBN, f.fp16))
+            return E_CUDA;
+        QTC q;
+        q.rows = mm; q.npad = npad; q.ntn = npad / TBN; q.group_m = 8; q.nblk = f.nblk; q.nout = f.nout;
+        q.bmap = f.bmap; q.Y = Y; q.colscale = f.colscale;
+        q.out = out + (long)f.nout * b; q.fp16 = f.fp16 ? 1 : 0; q.err = f.err;
+        long nrb = (mm + TBM - 1) / TBM;
+        long nctas = nrb * (long)f.nblk * q.ntn;
+        prof_begin(PK_QFORM, stream);
+        k_qform_tc<<<(unsigned)nctas, 192, TC_SMEM, stream>>>(mXh, mXl, mWh, mWl, q);
+        note_launch();
+        prof_end(PK_QFORM, stream);
+        CK(cudaGetLastError());
+    }
+    if (tc_error) {
+        int h = 0;
+        CK(cudaMemcpyAsync(&h, f.err, sizeof(int), cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        *tc_error = h;
+    }
+    return OK;
+}
+
+// ---------------------------------------------------------------------------
+// The precision form of the API: eight blocks (eta, u, v, w) x (cos, sin half)
+// ---------------------------------------------------------------------------
+struct QformState {
+    bool built = false;
+    int n = 0, npad = 0, ntile_plain = 0;
+    float *plain_tab = nullptr;
+    TcForm tc;
+    void *scratch = nullptr;   // plain-form chunk buffers
+    size_t scratch_bytes = 0;
+};
+static QformState g_q;
+
 int qform_build(const Config &cfg, const DevSea &sea, bool fp16, void *stream_) {
     cudaStream_t stream = (cudaStream_t)stream_;
-    if (g_q.plain_tab) cudaFree(g_q.plain_tab);
-    if (g_q.Whi) cudaFree(g_q.Whi);
-    if (g_q.Wlo) cudaFree(g_q.Wlo);
-    if (g_q.colscale) cudaFree(g_q.colscale);
-    g_q = QformState();
+    qform_free();
     int n = (int)cfg.omega.size();
     int npad = ((n + TBN - 1) / TBN) * TBN;
     if (npad == 0) npad = TBN;
     g_q.n = n;
     g_q.npad = npad;
-    g_q.fp16 = fp16;
     double kmax = 0;
     for (double k : cfg.k) kmax = std::max(kmax, k);
     double *d_in = nullptr;
@@ -712,24 +828,19 @@ int qform_build(const Config &cfg, const DevSea &sea, bool fp16, void *stream_) 
     k_qform_plain_from64<<<(unsigned)ntiles, 256, 0, stream>>>(npad, nt, coef, g_q.plain_tab);
     note_launch();
     CK(cudaGetLastError());
-    CK(cudaMalloc(&g_q.Whi, 2 * wel));
-    CK(cudaMalloc(&g_q.Wlo, 2 * wel));
-    CK(cudaMalloc(&g_q.colscale, sizeof(float) * 8 * npad));
-    dim3 gt((unsigned)npad, 8);
-    if (fp16)
-        k_qform_split<__half><<<gt, 256, 0, stream>>>(npad, 1, coef, (__half *)g_q.Whi, (__half *)g_q.Wlo,
-                                                      g_q.colscale);
-    else
-        k_qform_split<__nv_bfloat16><<<gt, 256, 0, stream>>>(npad, 0, coef, (__nv_bfloat16 *)g_q.Whi,
-                                                             (__nv_bfloat16 *)g_q.Wlo, g_q.colscale);
-    note_launch();
-    CK(cudaGetLastError());
-    CK(cudaStreamSynchronize(stream));
+    // block b: field (b & 3) -- eta, u, v, w -- X half (b >> 2); the w blocks
+    // take the other half of Y (sin(a +- b) = s c +- c s)
+    int bmap[24];
+    for (int b = 0; b < 8; b++) {
+        int field = b & 3, kh = b >> 2;
+        bmap[3 * b] = kh;
+        bmap[3 * b + 1] = field == 3 ? 1 - kh : kh;
+        bmap[3 * b + 2] = field;
+    }
+    int rc = tcform_split(g_q.tc, coef, bmap, 8, 4, npad, fp16, stream);
     cudaFree(coef);
-    CK(cudaMalloc(&g_q.err, sizeof(int)));
-    CK(cudaMemsetAsync(g_q.err, 0, sizeof(int), stream));
-    CK(cudaStreamSynchronize(stream));
     cudaFree(d_in);
+    if (rc) return rc;
     g_q.built = true;
     (void)sea;
     return OK;
@@ -737,11 +848,8 @@ int qform_build(const Config &cfg, const DevSea &sea, bool fp16, void *stream_) 
 
 void qform_free() {
     if (g_q.plain_tab) cudaFree(g_q.plain_tab);
-    if (g_q.Whi) cudaFree(g_q.Whi);
-    if (g_q.Wlo) cudaFree(g_q.Wlo);
-    if (g_q.colscale) cudaFree(g_q.colscale);
-    if (g_q.err) cudaFree(g_q.err);
     if (g_q.scratch) cudaFree(g_q.scratch);
+    tcform_free(g_q.tc);
     g_q = QformState();
 }
 
@@ -763,92 +871,33 @@ int qform_eval(const DevSea &sea, long n, const double *x, const double *y, cons
     if (!g_q.built) return E_NOT_INITIALIZED;
     if (n <= 0) return OK;
     const int npad = g_q.npad;
+    if (method == 1) return tcform_eval(g_q.tc, sea, n, x, y, t, 1, out, stream, tc_error);
     CK(cudaMemsetAsync(out, 0, sizeof(float) * 4 * n, stream));
-    if (method == 0) {
-        const long chunk = 1L << 16;
-        static bool pattr = false;
-        if (!pattr) {
-            CK(cudaFuncSetAttribute(k_qform_plain, cudaFuncAttributeMaxDynamicSharedMemorySize, QPLAIN_SMEM));
-            pattr = true;
-        }
-        long m = std::min(n, chunk);
-        size_t bytes = (sizeof(float2) + sizeof(float)) * (size_t)npad * m + sizeof(double) * 5 * m + 4096;
-        int rc = reserve_scratch(bytes);
-        if (rc) return rc;
-        for (long b = 0; b < n; b += chunk) {
-            long mm = std::min(chunk, n - b);
-            float2 *ph = (float2 *)g_q.scratch;
-            float *rr = (float *)((char *)g_q.scratch + ((sizeof(float2) * npad * mm + 255) / 256) * 256);
-            double *first = (double *)((char *)rr + ((sizeof(float) * npad * mm + 255) / 256) * 256);
-            rc = launch_phasors_public(sea, mm, x + b, y + b, t + b, 1, 1, 1, npad, ph, rr, first, stream);
-            if (rc) return rc;
-            QPlain q;
-            q.rows = mm; q.ntile = g_q.ntile_plain; q.tab = g_q.plain_tab; q.ph = ph; q.rr = rr;
-            q.out = out + 4 * b;
-            prof_begin(PK_QFORM, stream);
-            k_qform_plain<<<(unsigned)((mm + 127) / 128), 128, QPLAIN_SMEM, stream>>>(q);
-            note_launch();
-            prof_end(PK_QFORM, stream);
-            CK(cudaGetLastError());
-        }
-        return OK;
-    }
-    // tensor cores: chunks of rows with X hi/lo and Y in scratch
     const long chunk = 1L << 16;
-    long m = std::min(n, chunk);
-    long mpad = ((m + TBM - 1) / TBM) * TBM;
-    size_t xb = (size_t)mpad * 2 * npad * 2;     // one 16-bit matrix
-    size_t yb = (size_t)mpad * 2 * npad * 4;
-    int rc = reserve_scratch(2 * xb + yb + sizeof(QRow) * chunk + sizeof(QComp) * npad + 4096);
-    if (rc) return rc;
-    static bool attr = false;
-    if (!attr) {
-        CK(cudaFuncSetAttribute(k_qform_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
-        attr = true;
+    static bool pattr = false;
+    if (!pattr) {
+        CK(cudaFuncSetAttribute(k_qform_plain, cudaFuncAttributeMaxDynamicSharedMemorySize, QPLAIN_SMEM));
+        pattr = true;
     }
+    long m = std::min(n, chunk);
+    size_t bytes = (sizeof(float2) + sizeof(float)) * (size_t)npad * m + sizeof(double) * 5 * m + 4096;
+    int rc = reserve_scratch(bytes);
+    if (rc) return rc;
     for (long b = 0; b < n; b += chunk) {
         long mm = std::min(chunk, n - b);
-        char *base = (char *)g_q.scratch;
-        void *Xh = base, *Xl = base + xb;
-        float *Y = (float *)(base + 2 * xb);
-        QRow *rowrec = (QRow *)(base + 2 * xb + yb);
-        QComp *comprec = (QComp *)(base + 2 * xb + yb + sizeof(QRow) * chunk);
-        k_qform_rows<<<(unsigned)((mm + 255) / 256), 256, 0, stream>>>(mm, x + b, y + b, t + b, sea.fx, sea.fy,
-                                                                       sea.d_phase, sea.npad_g, rowrec);
-        note_launch();
-        k_qform_comps<<<(unsigned)((npad + 255) / 256), 256, 0, stream>>>(sea.n, npad, sea.d_phase, sea.npad_g,
-                                                                          comprec);
-        note_launch();
-        QPrep pp;
-        pp.rows = mm; pp.row = rowrec; pp.comp = comprec; pp.phase = sea.d_phase; pp.t = t + b;
-        pp.cstride = sea.npad_g; pp.ncomp = sea.n; pp.npad = npad;
-        pp.trivial_ramp = sea.trivial_ramp ? 1 : 0; pp.fp16 = g_q.fp16 ? 1 : 0;
-        pp.Xhi = Xh; pp.Xlo = Xl; pp.Y = Y;
-        dim3 pg((unsigned)mm, (unsigned)(npad / 256));
-        k_qform_prep<<<pg, 256, 0, stream>>>(pp);
-        note_launch();
-        CK(cudaGetLastError());
-        CUtensorMap mXh, mXl, mWh, mWl;
-        if (make_map(&mXh, Xh, mm, 2L * npad, TBM, g_q.fp16) || make_map(&mXl, Xl, mm, 2L * npad, TBM, g_q.fp16) ||
-            make_map(&mWh, g_q.Whi, 8L * npad, npad, TBN, g_q.fp16) ||
-            make_map(&mWl, g_q.Wlo, 8L * npad, npad, TBN, g_q.fp16))
-            return E_CUDA;
-        QTC q;
-        q.rows = mm; q.npad = npad; q.ntn = npad / TBN; q.group_m = 8; q.Y = Y; q.colscale = g_q.colscale;
-        q.out = out + 4 * b; q.fp16 = g_q.fp16 ? 1 : 0; q.err = g_q.err;
-        long nrb = (mm + TBM - 1) / TBM;
-        long nblk = nrb * 8L * q.ntn;
+        float2 *ph = (float2 *)g_q.scratch;
+        float *rr = (float *)((char *)g_q.scratch + ((sizeof(float2) * npad * mm + 255) / 256) * 256);
+        double *first = (double *)((char *)rr + ((sizeof(float) * npad * mm + 255) / 256) * 256);
+        rc = launch_phasors_public(sea, mm, x + b, y + b, t + b, 1, 1, 1, npad, ph, rr, first, stream);
+        if (rc) return rc;
+        QPlain q;
+        q.rows = mm; q.ntile = g_q.ntile_plain; q.tab = g_q.plain_tab; q.ph = ph; q.rr = rr;
+        q.out = out + 4 * b;
         prof_begin(PK_QFORM, stream);
-        k_qform_tc<<<(unsigned)nblk, 192, TC_SMEM, stream>>>(mXh, mXl, mWh, mWl, q);
+        k_qform_plain<<<(unsigned)((mm + 127) / 128), 128, QPLAIN_SMEM, stream>>>(q);
         note_launch();
         prof_end(PK_QFORM, stream);
         CK(cudaGetLastError());
-    }
-    if (tc_error) {
-        int h = 0;
-        CK(cudaMemcpyAsync(&h, g_q.err, sizeof(int), cudaMemcpyDeviceToHost, stream));
-        CK(cudaStreamSynchronize(stream));
-        *tc_error = h;
     }
     return OK;
 }

@@ -39,7 +39,7 @@ namespace cfdwm {
 
 // launchers shared with irregular.cu
 int launch_eta_pairs(const DevSea &sea, long n, const float2 *ph, const float *rr, float *out,
-                     cudaStream_t stream);
+                     cudaStream_t stream, float *split_buf, long split_cap);
 int launch_column_pairs(const DevSea &sea, long ncol, int nl, const float2 *ph, const float *rr,
                         const float *z0, float *out, int pairs, cudaStream_t stream, float *split_buf,
                         long split_cap);
@@ -292,6 +292,7 @@ struct GridExtra {
     double *tdev = nullptr;    // the slot time, read with stride 0 by the phasor pass
     float *split = nullptr;    // slices of a split column-pair launch
     long split_cap = 0;
+    DepthForm df;              // tensor-core form of the column sums (method 1)
 };
 static std::vector<std::pair<const DevGrid *, GridExtra>> g_extra;
 static GridExtra *extra(const DevGrid &g) {
@@ -378,6 +379,7 @@ void grid_free(DevGrid &g) {
             GridExtra &x = it->second;
             void *q[] = {x.act_all, x.act_live, x.xy, x.zmin, x.zmax, x.sec, x.eta2, x.tdev, x.split};
             for (void *p : q) if (p) cudaFree(p);
+            depthform_free(x.df);
             g_extra.erase(it);
             break;
         }
@@ -406,14 +408,26 @@ static int fill_cols(DevGrid &g, const DevSea &sea, Workspace &ws, const int *ac
     CK(cudaMemcpyAsync(x->tdev, &t, sizeof(double), cudaMemcpyHostToDevice, stream));
     rc = launch_phasors_public(sea, nact, x->xy, x->xy + nact, x->tdev, 1, 1, 0, npad, ph, rr, first, stream);
     if (rc) return rc;
-    rc = launch_eta_pairs(sea, nact, ph, rr, x->eta2, stream);
+    const bool tc = g.method == 1 && x->df.built;
+    if (tc) {
+        // eta2 and the 3R depth-separated quadratic forms of every column in one GEMM
+        rc = depthform_columns(x->df, sea, nact, x->xy, x->xy + nact, x->tdev, x->eta2, stream);
+    } else {
+        rc = launch_eta_pairs(sea, nact, ph, rr, x->eta2, stream, x->split, x->split_cap);
+    }
     if (rc) return rc;
     k_levels<<<(unsigned)((nact + 127) / 128), 128, 0, stream>>>(G, nact, act, first, x->eta2, slot, ETA,
                                                                  x->zmin, x->zmax);
     note_launch();
     CK(cudaGetLastError());
-    rc = launch_column_pairs(sea, nact, g.nl, ph, rr, x->zmin, x->sec, 1, stream, x->split, x->split_cap);
+    // plain: first and second order per (pair, level); tc: first order here,
+    // the second order from the R basis functions of the level heights
+    rc = launch_column_pairs(sea, nact, g.nl, ph, rr, x->zmin, x->sec, tc ? 0 : 1, stream, x->split, x->split_cap);
     if (rc) return rc;
+    if (tc) {
+        rc = depthform_combine(x->df, nact, g.nl, x->zmin, x->sec, stream);
+        if (rc) return rc;
+    }
     long tot = nact * g.nl;
     k_scatter_levels<<<(unsigned)((tot + 255) / 256), 256, 0, stream>>>(G, nact, act, first, x->sec, x->zmax,
                                                                         slot, U[0], U[1], U[2]);
@@ -485,6 +499,21 @@ int grid_initialize(DevGrid &g, const DevSea &sea, Workspace &ws, void *stream_)
 }
 
 int grid_gradients(DevGrid &g, void *stream) { return gradients(g, (cudaStream_t)stream); }
+
+int grid_set_method(DevGrid &g, const Config &cfg, const DevSea &sea, int method, void *stream) {
+    if (method != 0 && method != 1) return E_BAD_ARGUMENT;
+    GridExtra *x = extra(g);
+    if (method == 1 && !x->df.built) {
+        int rc = depthform_build(cfg, sea, x->df, stream);
+        if (rc) return rc;
+    }
+    g.method = method;
+    return OK;
+}
+
+int grid_tc_error(DevGrid &g, void *stream) { return depthform_error(extra(g)->df, stream); }
+
+int depthform_rank(DevGrid &g) { return extra(g)->df.built ? extra(g)->df.R : 0; }
 
 int grid_update(DevGrid &g, const DevSea &sea, Workspace &ws, void *stream_) {
     cudaStream_t stream = (cudaStream_t)stream_;

@@ -196,6 +196,21 @@ CFDWM_EXPORT int cfdwm_irregular_fields_noalloc(const double *x, const double *y
                                                 const double *t, long n, int mask, double *out);
 
 /* ===========================================================================
+ * Part 4b -- method of the s-grid column sums (new).
+ * 0: the plain form, FP32 CUDA-core pair sums per (pair, level) with
+ *    compensated accumulation (default).
+ * 1: the depth-separable tensor-core form: the depth profiles
+ *    e^{kz} +- e^{-k(z+2h)} are expanded in R orthonormal functions of z
+ *    (R chosen so that the expansion error is <= 4e-8 of max F), each
+ *    coefficient sum is a quadratic form over the column's phasors, and all
+ *    of them with eta2 run as one split-fp16 tcgen05 GEMM over the columns.
+ * rank (may be NULL) receives R.  Applies to the ring updates that follow. */
+CFDWM_EXPORT int cfdwm_sgrid_method(int method, int *rank);
+/* Host-only check of the depth basis for wavenumbers up to K and depth h:
+ * R and the max reconstruction error over a test set of (k, z). */
+CFDWM_EXPORT int cfdwm_depth_basis(double K, double h, int *rank, double *err);
+
+/* ===========================================================================
  * Part 5 -- learned s-grid update (new; no counterpart in the reference).
  *
  * Between full plain ring updates (lsgrid_spline.cpp:847-931) a small

@@ -111,3 +111,15 @@ def test_spectral_helpers_match_reference_formulas(lib):
     cfg = golden_cfg(g)
     m0, m1, m2 = waveinput.spectral_moments(cfg)
     assert m0 > 0 and m1 > 0 and m2 > 0
+
+
+def test_depth_basis_host(lib):
+    """The depth basis of the tensor-core s-grid form is built on the host:
+    rank and reconstruction error for a few (K, h)."""
+    import ctypes as C
+    for K, h, rmax in ((0.52, 100.0, 18), (0.3, 50.0, 16), (1.2, 100.0, 24), (0.05, 30.0, 12)):
+        R = C.c_int(0)
+        e = C.c_double(1.0)
+        assert lib.cfdwm_depth_basis(K, h, C.byref(R), C.byref(e)) == 0
+        assert 8 <= R.value <= rmax and e.value <= 4e-8, (K, h, R.value, e.value)
+    assert lib.cfdwm_depth_basis(-1.0, 10.0, None, None) != 0

@@ -164,10 +164,18 @@ def test_config1_workload_vs_oracle(wm):
     assert norm_rel_err(eta, refe) <= TOL
 
 
+@pytest.mark.parametrize("method", [0, 1])
 @pytest.mark.parametrize("case", ["sgrid_small", "sgrid_ignore"])
-def test_sgrid_vs_reference(wm, case):
+def test_sgrid_vs_reference(wm, case, method):
+    """method 0: plain FP32 column sums; 1: the depth-separable tensor-core
+    form, switched on after the initial fill (every update after it)."""
     g = load_golden(case)
     init(wm, g)
+    if method:
+        import ctypes as C
+        R = C.c_int(0)
+        assert wm.lib.cfdwm_sgrid_method(1, C.byref(R)) == 0, cw.last_error()
+        assert R.value >= 8
     cfg = golden_cfg(g)
     updates = {"sgrid_small": [0.7, 1.6], "sgrid_ignore": [1.5]}[case]
     for k in range(int(g["nsnap"])):
@@ -197,6 +205,32 @@ def test_sgrid_vs_reference(wm, case):
             assert norm_rel_err(arr, g["s%d_api_%s" % (k, name)]) <= TOL, (k, name)
         e = wm.surface_elevation_batch(qx, qy, np.full_like(qx, qt))
         assert norm_rel_err(e, g["s%d_api_SurfElev" % k]) <= TOL
+
+
+def test_sgrid_tensor_core_method_vs_plain(wm):
+    """The depth-separable tensor-core form against the plain form on the
+    1024-component short-crested sea (64 x 16) on a 40 x 36 x 16 patch:
+    every slot array of the ring after the initial fill and two updates."""
+    import ctypes as C
+    from cfdwavemaker_gb300 import seastate as ss
+    comps = ss.config3_sea()
+    grid = {"bounds": (100.0, 100.0 + 39 * 3.92, 200.0, 200.0 + 35 * 3.92), "nx": 40, "ny": 36, "nl": 16,
+            "t0": 5.0, "dt": 0.5, "stretch": (0.7, 1.5)}
+    txt = ss.write_irregular(None, comps, 100.0, extrap=2, lsgrid=grid)
+    arrs = {}
+    for method in (0, 1):
+        assert wm.initialize_text(txt) == 0, cw.last_error()
+        R = C.c_int(0)
+        assert wm.lib.cfdwm_sgrid_method(method, C.byref(R)) == 0, cw.last_error()
+        for k in range(4):           # refill the ring with this method
+            wm.lib.cfdwm_surrogate_step(0, 0.0, 0, None, None)
+        arrs[method] = [wm.sgrid_array(w) for w in range(19)]
+        if method:
+            print("depth basis rank", R.value)
+    for w in range(19):
+        tol = TOL if w <= 3 else TOL_GRAD
+        err = norm_rel_err(arrs[1][w], arrs[0][w])
+        assert err <= tol, (w, err)
 
 
 def test_sgrid_opposite_directions_vs_oracle(wm):

@@ -94,8 +94,11 @@ def run_surrogate(args):
     def ok(rc):
         assert rc == 0, (rc, cw.last_error())
 
-    def fresh(weights=True):
+    def fresh(weights=True, method=0):
+        # the plain steps of this workload are the plain FP32 form (method 0)
+        # unless the tensor-core s-grid form is asked for
         ok(wm.initialize_text(txt))
+        ok(lib.cfdwm_sgrid_method(method, None))
         if weights:
             ok(lib.cfdwm_surrogate_load(S.WEIGHTS.encode()))
 
@@ -143,6 +146,20 @@ def run_surrogate(args):
                     "column_pairs": {"launches": int(nk), "avg_ms": tot.value / max(1, nk)}}
     res["npairs"] = int(lib.cfdwm_npairs())
     res["ncomp"] = int(lib.cfdwm_components(None))
+    # the tensor-core s-grid form every step, and the learned update with its
+    # plain steps on that form (context for the comparison above)
+    fresh(weights=False, method=1)
+    loop(max(1, args.warmup))
+    ms_tc, _ = timed(args.plain_steps)
+    res["tc_every_step"] = {"ms_per_step": ms_tc, "nodes_per_s": nodes / (ms_tc / 1e3)}
+    fresh(method=1)
+    ok(lib.cfdwm_surrogate_enable(1, args.plain_every, args.surr_tol, args.nsample))
+    loop(max(1, args.warmup))
+    ok(lib.cfdwm_surrogate_enable(1, args.plain_every, args.surr_tol, args.nsample))
+    ms_stc, _ = timed(args.surr_steps)
+    res["surrogate_tc_plain"] = {"ms_per_step": ms_stc, "nodes_per_s": nodes / (ms_stc / 1e3),
+                                 "speedup_vs_tc_every_step": ms_tc / ms_stc}
+    ok(lib.cfdwm_surrogate_enable(0, 1, 0.0, 0))
     # surrogate-assisted loop at the working tolerance
     fresh()
     ok(lib.cfdwm_surrogate_enable(1, args.plain_every, args.surr_tol, args.nsample))
@@ -205,6 +222,133 @@ def run_surrogate(args):
     return res
 
 
+REG_WORKLOAD = ("regular waves: Stokes 5th H=6 m T=10 s depth 30 m and Fenton stream function order 24 H=8 m "
+                "T=12 s depth 20 m (FP64 Newton solve on the device), each evaluated (eta, u, v, w) at 1e7 points "
+                "of a uniform x-z-t grid (500 x in [0, 2L], 100 z from the seabed to the crest, 200 t in [0, T))")
+
+
+def regular_cases():
+    from cfdwavemaker_gb300 import seastate as ss
+    return [("stokes5", ss.write_regular(None, "stokes", 6.0, 30.0, period=10.0), 30.0, 6.0),
+            ("fenton24", ss.write_regular(None, "stream", 8.0, 20.0, period=12.0, order=24), 20.0, 8.0)]
+
+
+def run_regular(args):
+    """configs[1]: both regular theories at 1e7 points each per step, through
+    wave_Kinematics_batch (device arrays for value; host arrays for e2e)."""
+    import torch
+    import cfdwavemaker_gb300 as cw
+    ws, rank, local = dist_init()
+    torch.cuda.set_device(local)
+    lib = cw.load()
+    os.chdir(tempfile.mkdtemp())
+    wm = cw.CFDwavemaker()
+    stream = torch.cuda.current_stream()
+    lib.cfdwm_set_stream(C.c_void_p(stream.cuda_stream))
+    nx, nz, nt = 500, 100, 200
+    cases = []
+    for name, txt, depth, H in regular_cases():
+        assert wm.initialize_text(txt) == 0, cw.last_error()
+        L, T = wm.mean_length(1), wm.mean_period(1)
+        xs = np.linspace(0.0, 2.0 * L, nx)
+        zs = np.linspace(-depth, 0.75 * H, nz)
+        ts = np.linspace(0.0, T, nt, endpoint=False)
+        X, Z, TT = np.meshgrid(xs, zs, ts, indexing="ij")
+        host = [np.ascontiguousarray(a.ravel()) for a in (X, np.zeros_like(X), Z, TT)]
+        dev = [torch.tensor(a, device="cuda", dtype=torch.float64) for a in host]
+        cases.append({"name": name, "txt": txt, "host": host, "dev": dev, "L": L, "T": T})
+    n = nx * nz * nt
+    dout = torch.empty((n, 4), device="cuda", dtype=torch.float64)
+    hout = np.empty((n, 4))
+
+    res = {"ws": ws, "rank": rank, "cases": {}}
+    tot_ms, tot_e2e = 0.0, 0.0
+    launches = 0
+    clocks = None
+    for c in cases:
+        assert wm.initialize_text(c["txt"]) == 0, cw.last_error()
+        p = [cw._ptr(a) for a in c["dev"]]
+        for _ in range(args.warmup):
+            assert lib.wave_Kinematics_batch(*p, n, cw._ptr(dout)) == 0
+        torch.cuda.synchronize()
+        lib.cfdwm_profile_enable(1)
+        lib.cfdwm_profile_read(9, None)
+        sampler = ClockSampler(local)
+        sampler.start()
+        l0 = lib.cfdwm_kernel_launches()
+        e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            assert lib.wave_Kinematics_batch(*p, n, cw._ptr(dout)) == 0
+        e1.record(stream)
+        torch.cuda.synchronize()
+        launches += lib.cfdwm_kernel_launches() - l0
+        ms = e0.elapsed_time(e1) / args.steps
+        kt = C.c_double(0.0)
+        nk = lib.cfdwm_profile_read(9, C.byref(kt))
+        lib.cfdwm_profile_enable(0)
+        ck = sampler.stop()
+        clocks = ck if clocks is None else clocks
+        hp = [cw._ptr(a) for a in c["host"]]
+        t0 = time.perf_counter()
+        for _ in range(max(1, args.steps // 2)):
+            assert lib.wave_Kinematics_batch(*hp, n, cw._ptr(hout)) == 0
+        e2e_ms = (time.perf_counter() - t0) * 1e3 / max(1, args.steps // 2)
+        res["cases"][c["name"]] = {"ms_per_eval": ms, "kernel_ms": kt.value / max(1, nk), "e2e_ms": e2e_ms,
+                                   "pts_per_s": n / (ms / 1e3), "wave_length": c["L"], "period": c["T"]}
+        tot_ms += ms
+        tot_e2e += e2e_ms
+    res.update(ms=tot_ms, e2e_ms=tot_e2e, n=n, launches=launches, clocks=clocks)
+    return res
+
+
+def regular_line(args, r):
+    pk, src = peaks()
+    ws = r["ws"]
+    units = 2 * r["n"]
+    value = units * ws / (r["ms"] / 1e3)
+    # algorithmic bytes per point: x, y, z, t in (4 x 8 B) and eta, u, v, w out (4 x 8 B)
+    kms = sum(c["kernel_ms"] for c in r["cases"].values())
+    bytes_pt = 64.0
+    ach = bytes_pt * units / (kms / 1e3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": "points/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": r["ms"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (FP64 phase; FP64 Newton set-up)", "data": "synthetic",
+        "config": {"workload": REG_WORKLOAD, "l2": "inputs larger than L2 (640 MB in, 320 MB out per case)"},
+        "e2e": {"value": units * ws / (r["e2e_ms"] / 1e3), "unit": "points/s",
+                "h2d_bytes_per_step": 2 * 32 * r["n"], "d2h_bytes_per_step": 2 * 32 * r["n"]},
+        "gpu_launches": r["launches"],
+        "clocks": r["clocks"],
+        "cases": r["cases"],
+        "roofline": {"kernel": "k_regular_eval", "bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"],
+                     "unit": "GB/s", "frac": ach / pk["hbm_gbs"], "traffic": traffic_from_profiles("k_regular_eval"),
+                     "algorithmic": "64 B per point (x, y, z, t in; eta, u, v, w out; FP64)",
+                     "peak_source": src + " HBM copy, MEASURED_PEAKS.json"},
+        "peaks_source": src,
+    }
+    return line
+
+
+def regular_cpu_baseline(budget_s=10.0):
+    import oracle
+    from oracle import waveinput
+    nthr = os.cpu_count() or 1
+    tot, npts = 0.0, 0
+    for name, txt, depth, H in regular_cases():
+        cfg = waveinput.read_text(txt)
+        m = oracle.Model(cfg)
+        rng = np.random.default_rng(3)
+        n = 20000
+        x = rng.uniform(0, 200, n); z = rng.uniform(-depth, 0, n); t = rng.uniform(0, 10, n)
+        t0 = time.perf_counter()
+        m.api(x, 0 * x, z, t, nthr)
+        tot += time.perf_counter() - t0
+        npts += n
+    return {"value": npts / tot, "unit": "points/s", "cores": nthr, "kind": "port",
+            "sample": "2 x 20000 random points, all API fields (Stokes5, Fenton 24), FP64 oracle"}
+
+
 def surrogate_line(args, r):
     pk, src = peaks()
     n = r["ws"]
@@ -223,7 +367,9 @@ def surrogate_line(args, r):
         "gpu_launches": r["launches"],
         "clocks": r["clocks"],
         "plain_every_step": {"value": plain, "ms_per_step": r["plain"]["ms_per_step"],
-                             "steps": r["plain"]["steps"]},
+                             "steps": r["plain"]["steps"], "form": "plain FP32 column sums"},
+        "tensor_core_every_step": r["tc_every_step"],
+        "surrogate_with_tensor_core_plain_steps": r["surrogate_tc_plain"],
         "speedup_vs_plain": value / plain,
         "surrogate_steps": r["stats"],
         "tol_1e-3": r["tol_1e-3"],
@@ -520,11 +666,11 @@ def run_ours(args):
     if rc != 0:
         raise SystemExit("initialize failed: %d %s" % (rc, cw.last_error()))
     depth_rank = 0
-    if args.workload == "sgrid" and args.sgrid_method:
+    if args.workload == "sgrid":
         R = C.c_int(0)
         rc = lib.cfdwm_sgrid_method(args.sgrid_method, C.byref(R))
         if rc != 0:
-            raise SystemExit("tensor-core s-grid form unavailable: %s" % cw.last_error())
+            raise SystemExit("s-grid method %d unavailable: %s" % (args.sgrid_method, cw.last_error()))
         depth_rank = R.value
     init_s = time.time() - t_init
     stream = torch.cuda.current_stream()
@@ -761,7 +907,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="qform", choices=["qform", "sgrid", "point", "surrogate"])
+    ap.add_argument("--workload", default="qform", choices=["qform", "sgrid", "point", "surrogate", "regular"])
     ap.add_argument("--surr-steps", type=int, default=600, help="ring steps of the learned-update loop")
     ap.add_argument("--plain-every", type=int, default=20)
     ap.add_argument("--plain-steps", type=int, default=20, help="steps on which the plain loop is timed")
@@ -787,6 +933,7 @@ def main():
                  "256 x 32 z x 8 t points",
         "qform": QFORM_WORKLOAD % args.rows,
         "surrogate": SURR_WORKLOAD % (args.surr_steps, args.plain_every, args.nsample, args.surr_tol),
+        "regular": REG_WORKLOAD,
     }[args.workload]
     if args.impl == "reference":
         rank = int(os.environ.get("RANK", "0"))
@@ -796,6 +943,8 @@ def main():
         for _ in range(args.steps):
             if args.workload == "qform":
                 steps.append(qform_cpu_baseline())
+            elif args.workload == "regular":
+                steps.append(regular_cpu_baseline())
             else:
                 steps.append(cpu_baseline(args, budget_s=8.0))
         v = float(np.median([s["value"] for s in steps]))
@@ -813,6 +962,15 @@ def main():
         if r["rank"] != 0:
             return
         print(json.dumps(qform_line(args, r)))
+        return
+    if args.workload == "regular":
+        r = run_regular(args)
+        if r["rank"] != 0:
+            return
+        line = regular_line(args, r)
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = regular_cpu_baseline()
+        print(json.dumps(line))
         return
     if args.workload == "surrogate":
         r = run_surrogate(args)

@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -396,6 +397,15 @@ int initialize_from_text(const std::string &text) {
         if (rc) { free_model(); return rc; }
         if (wt == WT_IRR_SGRID) {
             rc = grid_create(cfg, M.grid, s);
+            // column sums: the depth-separable tensor-core form unless
+            // CFDWM_SGRID_METHOD=0 asks for the plain form (or the depth basis
+            // cannot be built for this sea, in which case the plain form is kept)
+            const char *env = std::getenv("CFDWM_SGRID_METHOD");
+            int method = (env && env[0] == '0') ? 0 : 1;
+            if (!rc && method == 1 && grid_set_method(M.grid, cfg, M.sea, 1, s) != OK) {
+                cudaGetLastError();
+                grid_set_method(M.grid, cfg, M.sea, 0, s);
+            }
             if (!rc) rc = grid_initialize(M.grid, M.sea, M.grid_ws, s);
             if (rc) { free_model(); return rc; }
         }
@@ -869,11 +879,15 @@ int cfdwm_sgrid_method(int method, int *rank) {
     std::lock_guard<std::mutex> lk(g_model_mtx);
     Model &M = g_model;
     if (!sgrid_loaded()) return E_UNSUPPORTED;
-    int rc = grid_set_method(M.grid, M.cfg, M.sea, method, stream_of());
+    cudaStream_t s = stream_of();
+    int rc = grid_set_method(M.grid, M.cfg, M.sea, method, s);
     if (rc) {
         set_error("s-grid: the tensor-core form is not available for this sea (depth basis)");
         return rc;
     }
+    // the ring is refilled at the current t0 with the selected method
+    rc = grid_initialize(M.grid, M.sea, M.grid_ws, s);
+    if (rc) return rc;
     if (rank) *rank = method == 1 ? depthform_rank(M.grid) : 0;
     return OK;
 }

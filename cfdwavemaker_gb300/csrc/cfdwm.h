@@ -83,7 +83,7 @@ long launch_count();
 // Optional per-kernel timing with CUDA events recorded on the launching
 // stream around the hot kernels.
 enum ProfKernel { PK_COLUMN_PAIRS = 0, PK_ETA_PAIRS, PK_POINT_PAIRS, PK_PHASORS, PK_QUERY,
-                  PK_GRADIENTS, PK_QFORM, PK_SURR_FEATURES, PK_SURR_NET, PK_COUNT };
+                  PK_GRADIENTS, PK_QFORM, PK_SURR_FEATURES, PK_SURR_NET, PK_REGULAR, PK_COUNT };
 bool prof_on();
 void prof_begin(int k, void *stream);
 void prof_end(int k, void *stream);

@@ -177,6 +177,9 @@ __global__ void k_qform_plain_from64(int npad, int nt, const double *coef, float
 // B operand of the tensor-core form, split into hi and lo 16-bit parts.
 // For fp16 each column m is scaled by 2^e_m (column maximum near 2^14) and
 // the lo part by a further 2^11; colscale[b][m] holds 2^-e_m (1 for bf16).
+// The fp16 cross products go to their own accumulator: the tensor cores'
+// FP32 accumulation keeps few guard bits, and adding terms 2^-11 smaller to
+// the hi-hi sum lost them (1.5e-5 at N = 4096 against 7e-6 with two).
 template <typename T16>
 __global__ void k_qform_split(int npad, int fp16, const double *coef, T16 *Whi, T16 *Wlo, float *colscale) {
     const int b = blockIdx.y, m = blockIdx.x;
@@ -401,11 +404,19 @@ __global__ void __launch_bounds__(128) k_qform_plain(QPlain a) {
 // ---------------------------------------------------------------------------
 // tcgen05 tensor-core form
 // ---------------------------------------------------------------------------
-constexpr int TBM = 128, TBN = 256, TBK = 64, TSTAGES = 2;
+constexpr int TBM = 128, TBK = 64;
+// two variants: bf16 (one accumulator, N = 256, 2 stages) and fp16 (hi and
+// cross accumulators, N = 128, 3 stages); either way two accumulator buffers
+// of 256 TMEM columns
+constexpr int TBN = 256;                  // component padding unit
 constexpr int A_TILE = TBM * TBK * 2;     // 16 KiB
-constexpr int B_TILE = TBN * TBK * 2;     // 32 KiB
-constexpr int STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;
-constexpr int TC_SMEM = TSTAGES * STAGE_BYTES + 1024 + 256;
+template <int BN> struct TcCfg {
+    static constexpr int B_TILE = BN * TBK * 2;
+    static constexpr int STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;
+    static constexpr int STAGES = BN == 128 ? 3 : 2;
+    static constexpr int SMEM = STAGES * STAGE_BYTES + 1024 + 256;
+    static constexpr bool TWO_ACC = BN == 128;
+};
 constexpr long long WAIT_LIMIT = 1000000000LL;   // clock cycles (about 0.5 s)
 
 __device__ __forceinline__ uint32_t su32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -480,44 +491,76 @@ struct QTC {
     int *err;
 };
 
-// Grid: one CTA per (row block, column tile).  Column tiles: nblk blocks x ntn.
+// bounded wait that also gives up as soon as another role has set the error word
+__device__ __forceinline__ bool mbar_wait_e(uint64_t *b, uint32_t parity, int *err, int code) {
+    long long t0 = clock64();
+    int n = 0;
+    while (!mbar_try(b, parity)) {
+        if ((++n & 255) == 0 && *(volatile int *)err != 0) return false;
+        if (clock64() - t0 > WAIT_LIMIT) {
+            atomicExch(err, code);
+            return false;
+        }
+    }
+    return true;
+}
+
+struct TileInfo {
+    long rb;
+    int blk, tn, nkb;
+};
+
+// grouped tile order: a group of group_m row blocks sweeps all column tiles
+template <int BN>
+__device__ __forceinline__ bool tile_of(const QTC &a, long nrb, long t, TileInfo &ti) {
+    const int ncol = a.nblk * a.ntn;
+    const long per_group = (long)a.group_m * ncol;
+    long grp = t / per_group, in = t % per_group;
+    long gm0 = grp * a.group_m;
+    long gsz = nrb - gm0 < a.group_m ? nrb - gm0 : a.group_m;
+    if (gsz <= 0) return false;
+    ti.rb = gm0 + in % gsz;
+    int ct = (int)(in / gsz);
+    if (ti.rb >= nrb || ct >= ncol) return false;
+    ti.blk = ct / a.ntn;
+    ti.tn = ct % a.ntn;
+    ti.nkb = (ti.tn * BN + BN) / TBK;          // upper triangle: i < m0 + BN
+    return true;
+}
+
+// Persistent: CTA c takes tiles c, c + gridDim.x, ...  Warp 0 streams the
+// operand tiles through the stage ring (continuously across tiles), one
+// thread of warp 1 issues the MMAs into TMEM accumulator buffer (j & 1) of
+// its j-th tile, warps 2-5 drain the other buffer meanwhile: the epilogue of
+// tile j overlaps the MMAs of tile j + 1.
+template <int BN>
 __global__ void __launch_bounds__(192, 1) k_qform_tc(const __grid_constant__ CUtensorMap mXh,
                                                      const __grid_constant__ CUtensorMap mXl,
                                                      const __grid_constant__ CUtensorMap mWh,
                                                      const __grid_constant__ CUtensorMap mWl, QTC a) {
+    using CF = TcCfg<BN>;
+    constexpr int TSTAGES = CF::STAGES, STAGE_BYTES = CF::STAGE_BYTES, B_TILE = CF::B_TILE;
+    constexpr bool TWO = CF::TWO_ACC;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *full = (uint64_t *)(smem + TSTAGES * STAGE_BYTES);
     uint64_t *empty = full + TSTAGES;
-    uint64_t *accf = empty + TSTAGES;
-    uint32_t *tmem_slot = (uint32_t *)(accf + 1);
+    uint64_t *accf = empty + TSTAGES;         // [2] accumulator buffer full
+    uint64_t *acce = accf + 2;                // [2] accumulator buffer drained
+    uint64_t *mdone = acce + 2;               // all MMAs of this CTA complete
+    uint32_t *tmem_slot = (uint32_t *)(mdone + 1);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-
-    // grouped tile order: a group of group_m row blocks sweeps all column tiles
     const long nrb = (a.rows + TBM - 1) / TBM;
-    const int ncol = a.nblk * a.ntn;
-    long bid = blockIdx.x;
-    long per_group = (long)a.group_m * ncol;
-    long grp = bid / per_group;
-    long in = bid % per_group;
-    long gm0 = grp * a.group_m;
-    long gsz = nrb - gm0 < a.group_m ? nrb - gm0 : a.group_m;
-    long rb = gm0 + in % gsz;
-    int ct = (int)(in / gsz);
-    if (rb >= nrb || ct >= ncol) return;
-    // a CTA that finds the error word set leaves before touching any resource
+    const long ntiles = nrb * (long)a.nblk * a.ntn;
     if (*(volatile int *)a.err != 0) return;
-    const int blk = ct / a.ntn, tn = ct % a.ntn;
-    const int khalf = a.bmap[3 * blk], yhalf = a.bmap[3 * blk + 1], outcol = a.bmap[3 * blk + 2];
-    const int m0 = tn * TBN;
-    const int nkb = (m0 + TBN) / TBK;            // upper triangle: i < m0 + 256
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < TSTAGES; s++) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
-        mbar_init(accf, 1);
+        for (int b = 0; b < 2; b++) { mbar_init(&accf[b], 1); mbar_init(&acce[b], 4); }
+        mbar_init(mdone, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    const uint32_t ncols_tmem = a.fp16 ? 512 : 256;
+    const uint32_t ncols_tmem = 512;          // two buffers of 256 FP32 columns (one or two accumulators)
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(tmem_slot)),
                      "r"(ncols_tmem));
@@ -527,93 +570,132 @@ __global__ void __launch_bounds__(192, 1) k_qform_tc(const __grid_constant__ CUt
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
 
-    __shared__ int issued_s, consumed_s;
+    __shared__ long issued_s, consumed_s;
     if (threadIdx.x == 0) { issued_s = 0; consumed_s = 0; }
     __syncthreads();
     if (warp == 0) {
         if (lane == 0) {
-            for (int kb = 0; kb < nkb; kb++) {
-                int s = kb % TSTAGES;
-                uint32_t ph = (kb / TSTAGES) & 1;
-                if (!mbar_wait(&empty[s], ph ^ 1, a.err, 1)) break;
-                uint8_t *st = smem + s * STAGE_BYTES;
-                mbar_expect_tx(&full[s], STAGE_BYTES);
-                int kx = khalf * a.npad + kb * TBK;
-                int ky = (int)(rb * TBM);
-                tma_2d(st, &mXh, &full[s], kx, ky);
-                tma_2d(st + A_TILE, &mXl, &full[s], kx, ky);
-                int wy = blk * a.npad + m0;
-                tma_2d(st + 2 * A_TILE, &mWh, &full[s], kb * TBK, wy);
-                tma_2d(st + 2 * A_TILE + B_TILE, &mWl, &full[s], kb * TBK, wy);
-                issued_s = kb + 1;
+            long g = 0;
+            bool ok = true;
+            for (long t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+                TileInfo ti;
+                if (!tile_of<BN>(a, nrb, t, ti)) continue;
+                const int khalf = a.bmap[3 * ti.blk];
+                const int m0 = ti.tn * BN;
+                for (int kb = 0; kb < ti.nkb; kb++, g++) {
+                    int s = (int)(g % TSTAGES);
+                    uint32_t ph = (uint32_t)((g / TSTAGES) & 1);
+                    if (!mbar_wait_e(&empty[s], ph ^ 1, a.err, 1)) { ok = false; break; }
+                    uint8_t *st = smem + s * STAGE_BYTES;
+                    mbar_expect_tx(&full[s], STAGE_BYTES);
+                    int kx = khalf * a.npad + kb * TBK;
+                    int ky = (int)(ti.rb * TBM);
+                    tma_2d(st, &mXh, &full[s], kx, ky);
+                    tma_2d(st + A_TILE, &mXl, &full[s], kx, ky);
+                    int wy = ti.blk * a.npad + m0;
+                    tma_2d(st + 2 * A_TILE, &mWh, &full[s], kb * TBK, wy);
+                    tma_2d(st + 2 * A_TILE + B_TILE, &mWl, &full[s], kb * TBK, wy);
+                    issued_s = g + 1;
+                }
             }
         }
     } else if (warp == 1) {
         if (lane == 0) {
             // kind::f16, D = F32, A/B = bf16 (1) or f16 (0), both K-major, N = 256, M = 128
             const uint32_t fmt = a.fp16 ? 0u : 1u;
-            const uint32_t idesc = (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(TBN >> 3) << 17) |
+            const uint32_t idesc = (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(BN >> 3) << 17) |
                                    ((uint32_t)(TBM >> 4) << 24);
-            const uint32_t acc_lo = a.fp16 ? tmem + 256 : tmem;
-            for (int kb = 0; kb < nkb; kb++) {
-                int s = kb % TSTAGES;
-                uint32_t ph = (kb / TSTAGES) & 1;
-                if (!mbar_wait(&full[s], ph, a.err, 2)) break;
+            long g = 0;
+            int j = 0;
+            bool ok = true;
+            for (long t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+                TileInfo ti;
+                if (!tile_of<BN>(a, nrb, t, ti)) continue;
+                const int buf = j & 1;
+                const uint32_t use = (uint32_t)(j >> 1);
+                // the epilogue has drained this buffer's previous tile
+                if (!mbar_wait_e(&acce[buf], (use & 1) ^ 1, a.err, 5)) break;
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                uint32_t base = su32(smem + s * STAGE_BYTES);
-                uint64_t dXh = sdesc(base), dXl = sdesc(base + A_TILE);
-                uint64_t dWh = sdesc(base + 2 * A_TILE), dWl = sdesc(base + 2 * A_TILE + B_TILE);
-                for (int k = 0; k < TBK / 16; k++) {
-                    uint64_t o = (uint64_t)(k * 32) >> 4;     // 16 elements = 32 bytes per step
-                    uint32_t first = (kb == 0 && k == 0) ? 0u : 1u;
-                    umma(tmem, dXh + o, dWh + o, idesc, first);
-                    umma(acc_lo, dXh + o, dWl + o, idesc, a.fp16 ? first : 1u);
-                    umma(acc_lo, dXl + o, dWh + o, idesc, 1u);
+                const uint32_t acc = tmem + (uint32_t)(buf * 256);
+                const uint32_t acc2 = TWO ? acc + BN : acc;     // fp16: cross products
+                for (int kb = 0; kb < ti.nkb; kb++, g++) {
+                    int s = (int)(g % TSTAGES);
+                    uint32_t ph = (uint32_t)((g / TSTAGES) & 1);
+                    if (!mbar_wait_e(&full[s], ph, a.err, 2)) { ok = false; break; }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    uint32_t base = su32(smem + s * STAGE_BYTES);
+                    uint64_t dXh = sdesc(base), dXl = sdesc(base + A_TILE);
+                    uint64_t dWh = sdesc(base + 2 * A_TILE), dWl = sdesc(base + 2 * A_TILE + B_TILE);
+                    for (int k = 0; k < TBK / 16; k++) {
+                        uint64_t o = (uint64_t)(k * 32) >> 4;     // 16 elements = 32 bytes per step
+                        uint32_t first = (kb == 0 && k == 0) ? 0u : 1u;
+                        umma(acc, dXh + o, dWh + o, idesc, first);
+                        umma(acc2, dXh + o, dWl + o, idesc, TWO ? first : 1u);
+                        umma(acc2, dXl + o, dWh + o, idesc, 1u);
+                    }
+                    umma_commit(&empty[s]);
+                    consumed_s = g + 1;
                 }
-                umma_commit(&empty[s]);
-                consumed_s = kb + 1;
+                if (!ok) break;
+                umma_commit(&accf[buf]);
+                j++;
             }
-            umma_commit(accf);
+            umma_commit(mdone);
         }
     } else {
         // epilogue: warps 2..5 own TMEM lane quarters (warp % 4)
         const int q = warp & 3;
-        const long row = rb * TBM + q * 32 + lane;
-        bool ok = mbar_wait(accf, 0, a.err, 3);
-        // tcgen05.ld is warp-collective (.sync.aligned): decide per warp
-        ok = __all_sync(0xffffffffu, ok);
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        float part = 0.f;
-        if (ok) {
+        int j = 0;
+        for (long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+            TileInfo ti;
+            if (!tile_of<BN>(a, nrb, t, ti)) continue;
+            const int buf = j & 1;
+            const uint32_t use = (uint32_t)(j >> 1);
+            bool ok = mbar_wait_e(&accf[buf], use & 1, a.err, 3);
+            // tcgen05.ld is warp-collective (.sync.aligned): decide per warp
+            ok = __all_sync(0xffffffffu, ok);
+            if (!ok) break;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const int yhalf = a.bmap[3 * ti.blk + 1], outcol = a.bmap[3 * ti.blk + 2];
+            const int m0 = ti.tn * BN;
+            const long row = ti.rb * TBM + q * 32 + lane;
             const float *Yr = a.Y + (row < a.rows ? row : 0) * 2L * a.npad + (long)yhalf * a.npad + m0;
-            const float *cs = a.colscale + (long)blk * a.npad + m0;
-            for (int c = 0; c < TBN / 32; c++) {
-                float v[32], w[32];
-                tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + c * 32, v);
-                if (a.fp16) {
-                    tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + 256 + c * 32, w);
-                    for (int j = 0; j < 32; j++) v[j] = fmaf(w[j], 1.0f / 2048.0f, v[j]);
+            const float *cs = a.colscale + (long)ti.blk * a.npad + m0;
+            const uint32_t acc = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * 256);
+            float part = 0.f;
+            for (int c = 0; c < BN / 32; c++) {
+                float v[32];
+                tmem_ld32(acc + c * 32, v);
+                if (TWO) {
+                    float w[32];
+                    tmem_ld32(acc + BN + c * 32, w);
+                    for (int jj = 0; jj < 32; jj++) v[jj] = fmaf(w[jj], 1.0f / 2048.0f, v[jj]);
                 }
                 if (row < a.rows) {
-                    for (int j = 0; j < 32; j += 4) {
-                        float4 y4 = *reinterpret_cast<const float4 *>(Yr + c * 32 + j);
-                        float4 s4 = *reinterpret_cast<const float4 *>(cs + c * 32 + j);
-                        part = fmaf(v[j] * s4.x, y4.x, part);
-                        part = fmaf(v[j + 1] * s4.y, y4.y, part);
-                        part = fmaf(v[j + 2] * s4.z, y4.z, part);
-                        part = fmaf(v[j + 3] * s4.w, y4.w, part);
+                    for (int jj = 0; jj < 32; jj += 4) {
+                        float4 y4 = *reinterpret_cast<const float4 *>(Yr + c * 32 + jj);
+                        float4 s4 = *reinterpret_cast<const float4 *>(cs + c * 32 + jj);
+                        part = fmaf(v[jj] * s4.x, y4.x, part);
+                        part = fmaf(v[jj + 1] * s4.y, y4.y, part);
+                        part = fmaf(v[jj + 2] * s4.z, y4.z, part);
+                        part = fmaf(v[jj + 3] * s4.w, y4.w, part);
                     }
                 }
             }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(&acce[buf])) : "memory");
             if (row < a.rows) atomicAdd(a.out + row * a.nout + outcol, part);
+            j++;
         }
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     }
     __syncthreads();
-    if (threadIdx.x == 0 && consumed_s < issued_s) {
+    if (threadIdx.x == 0) {
+        // every MMA issued has completed before the accumulators are freed
+        mbar_wait(mdone, 0, a.err, 6);
         // error path only: wait (bounded) for the copies still in flight
-        for (int kb = consumed_s; kb < issued_s; kb++)
-            mbar_wait(&full[kb % TSTAGES], (kb / TSTAGES) & 1, a.err, 4);
+        for (long g = consumed_s; g < issued_s; g++)
+            mbar_wait(&full[g % TSTAGES], (uint32_t)((g / TSTAGES) & 1), a.err, 4);
     }
     __syncthreads();
     if (warp == 1) {
@@ -728,9 +810,11 @@ int tcform_eval(TcForm &f, const DevSea &sea, long n, const double *x, const dou
     if (rc) return rc;
     static bool attr = false;
     if (!attr) {
-        CK(cudaFuncSetAttribute(k_qform_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
+        CK(cudaFuncSetAttribute(k_qform_tc<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcCfg<128>::SMEM));
+        CK(cudaFuncSetAttribute(k_qform_tc<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcCfg<256>::SMEM));
         attr = true;
     }
+    const int BN = f.fp16 ? 128 : 256;
     for (long b = 0; b < n; b += chunk) {
         long mm = std::min(chunk, n - b);
         char *base = (char *)f.scratch;
@@ -755,17 +839,27 @@ int tcform_eval(TcForm &f, const DevSea &sea, long n, const double *x, const dou
         CK(cudaGetLastError());
         CUtensorMap mXh, mXl, mWh, mWl;
         if (make_map(&mXh, Xh, mm, 2L * npad, TBM, f.fp16) || make_map(&mXl, Xl, mm, 2L * npad, TBM, f.fp16) ||
-            make_map(&mWh, f.Whi, (long)f.nblk * npad, npad, TBN, f.fp16) ||
-            make_map(&mWl, f.Wlo, (long)f.nblk * npad, npad, TBN, f.fp16))
+            make_map(&mWh, f.Whi, (long)f.nblk * npad, npad, BN, f.fp16) ||
+            make_map(&mWl, f.Wlo, (long)f.nblk * npad, npad, BN, f.fp16))
             return E_CUDA;
         QTC q;
-        q.rows = mm; q.npad = npad; q.ntn = npad / TBN; q.group_m = 8; q.nblk = f.nblk; q.nout = f.nout;
+        q.rows = mm; q.npad = npad; q.ntn = npad / BN; q.group_m = 8; q.nblk = f.nblk; q.nout = f.nout;
         q.bmap = f.bmap; q.Y = Y; q.colscale = f.colscale;
         q.out = out + (long)f.nout * b; q.fp16 = f.fp16 ? 1 : 0; q.err = f.err;
         long nrb = (mm + TBM - 1) / TBM;
-        long nctas = nrb * (long)f.nblk * q.ntn;
+        long ntiles = nrb * (long)f.nblk * q.ntn;
+        static int nsm = 0;
+        if (!nsm) {
+            int dev = 0;
+            CK(cudaGetDevice(&dev));
+            CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+        }
+        long nctas = std::min<long>(ntiles, nsm);
         prof_begin(PK_QFORM, stream);
-        k_qform_tc<<<(unsigned)nctas, 192, TC_SMEM, stream>>>(mXh, mXl, mWh, mWl, q);
+        if (BN == 128)
+            k_qform_tc<128><<<(unsigned)nctas, 192, TcCfg<128>::SMEM, stream>>>(mXh, mXl, mWh, mWl, q);
+        else
+            k_qform_tc<256><<<(unsigned)nctas, 192, TcCfg<256>::SMEM, stream>>>(mXh, mXl, mWh, mWl, q);
         note_launch();
         prof_end(PK_QFORM, stream);
         CK(cudaGetLastError());

@@ -484,8 +484,10 @@ int regular_eval(const DevRegular &r, const Config &cfg, long n, const double *x
     a.finite = (cfg.depth > 0.0 && cfg.depth < 1e8) ? 1 : 0;
     a.x0 = cfg.x_pos; a.y0 = cfg.y_pos; a.t0 = cfg.tofmax; a.z0 = cfg.swl; a.d = cfg.depth;
     a.g = cfg.gravity; a.rho = cfg.rho;
+    prof_begin(PK_REGULAR, stream);
     k_regular_eval<<<(unsigned)((n + 127) / 128), 128, 0, stream>>>(a);
     note_launch();
+    prof_end(PK_REGULAR, stream);
     CK(cudaGetLastError());
     return OK;
 }

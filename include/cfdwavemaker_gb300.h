@@ -134,7 +134,8 @@ CFDWM_EXPORT long cfdwm_kernel_launches(void);
  * then read the summed duration (ms) and the launch count of one kernel:
  * 0 s-grid column pair sums, 1 elevation pair sums, 2 point pair sums,
  * 3 phasors, 4 s-grid query, 5 s-grid gradients, 6 quadratic-form GEMM,
- * 7 learned-update first-order channels, 8 learned-update network forward.
+ * 7 learned-update first-order channels, 8 learned-update network forward,
+ * 9 regular-wave (Stokes5 / Fenton) point evaluation.
  * Reading clears the record. */
 CFDWM_EXPORT int cfdwm_profile_enable(int on);
 CFDWM_EXPORT long cfdwm_profile_read(int kernel, double *total_ms);
@@ -198,13 +199,15 @@ CFDWM_EXPORT int cfdwm_irregular_fields_noalloc(const double *x, const double *y
 /* ===========================================================================
  * Part 4b -- method of the s-grid column sums (new).
  * 0: the plain form, FP32 CUDA-core pair sums per (pair, level) with
- *    compensated accumulation (default).
- * 1: the depth-separable tensor-core form: the depth profiles
+ *    compensated accumulation.
+ * 1: (default; environment CFDWM_SGRID_METHOD=0 at wave_Initialize selects
+ *    the plain form) the depth-separable tensor-core form: the depth profiles
  *    e^{kz} +- e^{-k(z+2h)} are expanded in R orthonormal functions of z
  *    (R chosen so that the expansion error is <= 4e-8 of max F), each
  *    coefficient sum is a quadratic form over the column's phasors, and all
  *    of them with eta2 run as one split-fp16 tcgen05 GEMM over the columns.
- * rank (may be NULL) receives R.  Applies to the ring updates that follow. */
+ * rank (may be NULL) receives R.  The ring is refilled at the current t0
+ * (tstep restarts at 0) and the updates that follow use the method. */
 CFDWM_EXPORT int cfdwm_sgrid_method(int method, int *rank);
 /* Host-only check of the depth basis for wavenumbers up to K and depth h:
  * R and the max reconstruction error over a test set of (k, z). */

@@ -169,13 +169,12 @@ def test_config1_workload_vs_oracle(wm):
 def test_sgrid_vs_reference(wm, case, method):
     """method 0: plain FP32 column sums; 1: the depth-separable tensor-core
     form, switched on after the initial fill (every update after it)."""
+    import ctypes as C
     g = load_golden(case)
     init(wm, g)
-    if method:
-        import ctypes as C
-        R = C.c_int(0)
-        assert wm.lib.cfdwm_sgrid_method(1, C.byref(R)) == 0, cw.last_error()
-        assert R.value >= 8
+    R = C.c_int(0)
+    assert wm.lib.cfdwm_sgrid_method(method, C.byref(R)) == 0, cw.last_error()
+    assert (R.value >= 8) if method else (R.value == 0)
     cfg = golden_cfg(g)
     updates = {"sgrid_small": [0.7, 1.6], "sgrid_ignore": [1.5]}[case]
     for k in range(int(g["nsnap"])):
@@ -221,8 +220,8 @@ def test_sgrid_tensor_core_method_vs_plain(wm):
     for method in (0, 1):
         assert wm.initialize_text(txt) == 0, cw.last_error()
         R = C.c_int(0)
-        assert wm.lib.cfdwm_sgrid_method(method, C.byref(R)) == 0, cw.last_error()
-        for k in range(4):           # refill the ring with this method
+        assert wm.lib.cfdwm_sgrid_method(method, C.byref(R)) == 0, cw.last_error()   # refills the ring
+        for k in range(2):
             wm.lib.cfdwm_surrogate_step(0, 0.0, 0, None, None)
         arrs[method] = [wm.sgrid_array(w) for w in range(19)]
         if method:

@@ -172,7 +172,9 @@ def test_fallback_restores_plain(env, torch):
     assert max(err) > 1e-9
     e2 = (C.c_double * 4)()
     _ok(lib.cfdwm_surrogate_compare(e2))
-    assert max(e2) <= 1e-7, list(e2)
+    # the slot is the plain method's own (summation order of the tensor-core
+    # form's atomics aside)
+    assert max(e2) <= 1e-6, list(e2)
     # routed through wave_force_update: every update falls back at this tolerance
     _ok(lib.cfdwm_surrogate_enable(1, 3, 1e-9, 8))
     t0 = C.c_double(0.0)

@@ -405,17 +405,21 @@ __global__ void __launch_bounds__(128) k_qform_plain(QPlain a) {
 // tcgen05 tensor-core form
 // ---------------------------------------------------------------------------
 constexpr int TBM = 128, TBK = 64;
-// two variants: bf16 (one accumulator, N = 256, 2 stages) and fp16 (hi and
-// cross accumulators, N = 128, 3 stages); either way two accumulator buffers
-// of 256 TMEM columns
+// two variants (TMEM holds 512 FP32 columns), each with two accumulator
+// buffers so that the epilogue of one tile hides behind the next tile's MMAs:
+//   bf16, one accumulator, N = 256, 2 stages;
+//   fp16, hi and cross accumulators, N = 128, 3 stages.
+// (An fp16 variant with N = 256 and a single buffer measured no faster at
+// N = 4096: 1207 ms against 1161 ms per 4e6 points.)
 constexpr int TBN = 256;                  // component padding unit
 constexpr int A_TILE = TBM * TBK * 2;     // 16 KiB
-template <int BN> struct TcCfg {
+template <int BN, bool TWO> struct TcCfg {
     static constexpr int B_TILE = BN * TBK * 2;
     static constexpr int STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;
     static constexpr int STAGES = BN == 128 ? 3 : 2;
     static constexpr int SMEM = STAGES * STAGE_BYTES + 1024 + 256;
-    static constexpr bool TWO_ACC = BN == 128;
+    static constexpr int ACOLS = TWO ? 2 * BN : BN;     // TMEM columns of one tile
+    static constexpr int NBUF = 512 / ACOLS;             // accumulator buffers
 };
 constexpr long long WAIT_LIMIT = 1000000000LL;   // clock cycles (about 0.5 s)
 
@@ -533,14 +537,14 @@ __device__ __forceinline__ bool tile_of(const QTC &a, long nrb, long t, TileInfo
 // thread of warp 1 issues the MMAs into TMEM accumulator buffer (j & 1) of
 // its j-th tile, warps 2-5 drain the other buffer meanwhile: the epilogue of
 // tile j overlaps the MMAs of tile j + 1.
-template <int BN>
+template <int BN, bool TWO>
 __global__ void __launch_bounds__(192, 1) k_qform_tc(const __grid_constant__ CUtensorMap mXh,
                                                      const __grid_constant__ CUtensorMap mXl,
                                                      const __grid_constant__ CUtensorMap mWh,
                                                      const __grid_constant__ CUtensorMap mWl, QTC a) {
-    using CF = TcCfg<BN>;
+    using CF = TcCfg<BN, TWO>;
     constexpr int TSTAGES = CF::STAGES, STAGE_BYTES = CF::STAGE_BYTES, B_TILE = CF::B_TILE;
-    constexpr bool TWO = CF::TWO_ACC;
+    constexpr int ACOLS = CF::ACOLS, NBUF = CF::NBUF;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *full = (uint64_t *)(smem + TSTAGES * STAGE_BYTES);
@@ -611,12 +615,12 @@ __global__ void __launch_bounds__(192, 1) k_qform_tc(const __grid_constant__ CUt
             for (long t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
                 TileInfo ti;
                 if (!tile_of<BN>(a, nrb, t, ti)) continue;
-                const int buf = j & 1;
-                const uint32_t use = (uint32_t)(j >> 1);
+                const int buf = j % NBUF;
+                const uint32_t use = (uint32_t)(j / NBUF);
                 // the epilogue has drained this buffer's previous tile
                 if (!mbar_wait_e(&acce[buf], (use & 1) ^ 1, a.err, 5)) break;
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                const uint32_t acc = tmem + (uint32_t)(buf * 256);
+                const uint32_t acc = tmem + (uint32_t)(buf * ACOLS);
                 const uint32_t acc2 = TWO ? acc + BN : acc;     // fp16: cross products
                 for (int kb = 0; kb < ti.nkb; kb++, g++) {
                     int s = (int)(g % TSTAGES);
@@ -649,8 +653,8 @@ __global__ void __launch_bounds__(192, 1) k_qform_tc(const __grid_constant__ CUt
         for (long t = blockIdx.x; t < ntiles; t += gridDim.x) {
             TileInfo ti;
             if (!tile_of<BN>(a, nrb, t, ti)) continue;
-            const int buf = j & 1;
-            const uint32_t use = (uint32_t)(j >> 1);
+            const int buf = j % NBUF;
+            const uint32_t use = (uint32_t)(j / NBUF);
             bool ok = mbar_wait_e(&accf[buf], use & 1, a.err, 3);
             // tcgen05.ld is warp-collective (.sync.aligned): decide per warp
             ok = __all_sync(0xffffffffu, ok);
@@ -661,7 +665,7 @@ __global__ void __launch_bounds__(192, 1) k_qform_tc(const __grid_constant__ CUt
             const long row = ti.rb * TBM + q * 32 + lane;
             const float *Yr = a.Y + (row < a.rows ? row : 0) * 2L * a.npad + (long)yhalf * a.npad + m0;
             const float *cs = a.colscale + (long)ti.blk * a.npad + m0;
-            const uint32_t acc = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * 256);
+            const uint32_t acc = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * ACOLS);
             float part = 0.f;
             for (int c = 0; c < BN / 32; c++) {
                 float v[32];
@@ -810,8 +814,10 @@ int tcform_eval(TcForm &f, const DevSea &sea, long n, const double *x, const dou
     if (rc) return rc;
     static bool attr = false;
     if (!attr) {
-        CK(cudaFuncSetAttribute(k_qform_tc<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcCfg<128>::SMEM));
-        CK(cudaFuncSetAttribute(k_qform_tc<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcCfg<256>::SMEM));
+        CK(cudaFuncSetAttribute(k_qform_tc<128, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                TcCfg<128, true>::SMEM));
+        CK(cudaFuncSetAttribute(k_qform_tc<256, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                TcCfg<256, false>::SMEM));
         attr = true;
     }
     const int BN = f.fp16 ? 128 : 256;
@@ -856,10 +862,10 @@ int tcform_eval(TcForm &f, const DevSea &sea, long n, const double *x, const dou
         }
         long nctas = std::min<long>(ntiles, nsm);
         prof_begin(PK_QFORM, stream);
-        if (BN == 128)
-            k_qform_tc<128><<<(unsigned)nctas, 192, TcCfg<128>::SMEM, stream>>>(mXh, mXl, mWh, mWl, q);
+        if (!f.fp16)
+            k_qform_tc<256, false><<<(unsigned)nctas, 192, TcCfg<256, false>::SMEM, stream>>>(mXh, mXl, mWh, mWl, q);
         else
-            k_qform_tc<256><<<(unsigned)nctas, 192, TcCfg<256>::SMEM, stream>>>(mXh, mXl, mWh, mWl, q);
+            k_qform_tc<128, true><<<(unsigned)nctas, 192, TcCfg<128, true>::SMEM, stream>>>(mXh, mXl, mWh, mWl, q);
         note_launch();
         prof_end(PK_QFORM, stream);
         CK(cudaGetLastError());

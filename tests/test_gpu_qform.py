@@ -100,3 +100,14 @@ def test_tensor_core_bf16_split(wm, torch, nf, nd):
         err = norm_rel_err(got[:, f], ref[:, f])
         print("bf16x3 field", f, "err", err)
         assert err <= TOL_BF16, (f, err)
+
+
+def test_tensor_core_fp16_split_wide(wm, torch):
+    """2048 components: long K-loops with both accumulator buffers in turn."""
+    txt = _sea(128, 16, 23)
+    x, y, t, got = _run(wm, torch, txt, 64, 1, True)
+    ref = _reference(txt, x, y, t)
+    for f in range(4):
+        err = norm_rel_err(got[:, f], ref[:, f])
+        print("fp16x3 N=2048 field", f, "err", err)
+        assert err <= TOL, (f, err)

@@ -28,7 +28,7 @@ SOURCES = ["parser.cpp", "irregular.cu", "sgrid.cu", "regular.cu", "api.cu", "no
 def _compile(src):
     obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
     path = os.path.join(CSRC, src)
-    deps = [path, os.path.join(CSRC, "cfdwm.h"), os.path.join(CSRC, "sgrid_geom.cuh"),
+    deps = [path, os.path.join(CSRC, "cfdwm.h"), os.path.join(CSRC, "sgrid_geom.cuh"), os.path.join(CSRC, "ffmath.cuh"),
             os.path.join(os.path.dirname(HERE), "include", "cfdwavemaker_gb300.h")]
     if os.path.exists(obj) and all(os.path.getmtime(obj) >= os.path.getmtime(d) for d in deps):
         return obj, ""

@@ -307,6 +307,10 @@ void depthform_free(DepthForm &df);
 int depthform_columns(DepthForm &df, const DevSea &sea, long nact, const double *x, const double *y,
                       const double *tdev, float *eta2, void *stream);
 int depthform_combine(DepthForm &df, long nact, int nl, const float *z0, float *sec, void *stream);
+// First-order sums of the tensor-core path (float-float phases): first [5][n]
+// (eta1 and the Taylor gradients) and/or sec [3][n nl] (u1, v1, w1 at z0).
+int depthform_first(const DevSea &sea, long nact, int nl, const double *xy, double t, const float *z0,
+                    double *first, float *sec, void *stream);
 int depthform_error(DepthForm &df, void *stream);
 int depthform_basis_info(double K, double h, int *R, double *err);
 

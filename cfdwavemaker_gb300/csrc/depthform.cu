@@ -26,6 +26,7 @@
 // table (quadrature).  The rank is the smallest R whose reconstruction error
 // over a test set of (k, z) is below 2e-8 of max F.
 #include "cfdwm.h"
+#include "ffmath.cuh"
 #include "sgrid_geom.cuh"
 
 #include <cuda_runtime.h>
@@ -313,6 +314,181 @@ __global__ void k_depth_coef(DfCoefArgs a) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// First-order sums of the columns for the tensor-core path, with float-float
+// phases (the plain path's FP64 phasor pass and its per-(component, column)
+// phasor table are not needed here):
+//   mode 0: eta1 and the Taylor gradients phi1_dxdz, phi1_dydz, phi1_dzdz,
+//           dp1_dz per column (Irregular.cpp:178-198, 1107-1192) into first[5][n];
+//   mode 1: u1, v1, w1 at the level heights z0 (Irregular.cpp:394-447) into
+//           sec[3][n nl].
+// Sums are FP32 with Kahan compensation.
+// ---------------------------------------------------------------------------
+struct DfFirstArgs {
+    long n;
+    const double *xy;          // [2][n]
+    double t, fx, fy;
+    const double *phase;       // [7][cstride]: kx, ky, omega, phase0, ramp parameters
+    const float *cf;           // [NCF][cstride]
+    int cstride, ncomp, trivial_ramp;
+    int nl;
+    const float *z0;           // [n nl] (mode 1)
+    float depth;
+    double *first;             // [5][n] (mode 0)
+    float *sec;                // [3][n nl] (mode 1)
+};
+
+constexpr int DFC = 128;       // components per shared-memory chunk
+constexpr float LOG2E_DF = 1.4426950408889634f;
+
+__device__ __forceinline__ float df_ex2(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ void df_kahan(float &s, float &c, float v) {
+    float y = v - c;
+    float t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+__device__ __forceinline__ double df_ramp(double t, double rt, double ts, double du) {
+    double rampdown = fmax(fmin(1. - ((t - ts - du + rt) / (rt + SMALL)), 1.), 0.);
+    double rampup = fmax(fmin(((t - ts) / (rt + SMALL)), 1.), 0.);
+    return rampup * rampdown;
+}
+
+// shared record of a component: phase coefficients as float pairs, ramp, 5 coefficients
+struct DfComp {
+    float kxh, kxl, kyh, kyl, wh, wl, ph, pl, r, c[5];
+};
+
+template <int MODE>
+__device__ __forceinline__ void df_stage(const DfFirstArgs &a, int i0, DfComp *sc) {
+    for (int e = threadIdx.x; e < DFC; e += blockDim.x) {
+        const int i = i0 + e;
+        DfComp d = {};
+        if (i < a.ncomp) {
+            const int cs = a.cstride;
+            ff_split(a.phase[i], d.kxh, d.kxl);
+            ff_split(a.phase[cs + i], d.kyh, d.kyl);
+            ff_split(-a.phase[2 * cs + i], d.wh, d.wl);
+            ff_split(a.phase[3 * cs + i], d.ph, d.pl);
+            const int ir = a.trivial_ramp ? 0 : i;
+            d.r = (float)df_ramp(a.t, a.phase[4 * cs + ir], a.phase[5 * cs + ir], a.phase[6 * cs + ir]);
+            if (MODE == 0) {
+                d.c[0] = a.cf[CF_A * cs + i];
+                d.c[1] = a.cf[CF_GX * cs + i];
+                d.c[2] = a.cf[CF_GY * cs + i];
+                d.c[3] = a.cf[CF_GZ * cs + i];
+                d.c[4] = a.cf[CF_GP * cs + i];
+            } else {
+                const float au = a.cf[CF_AU * cs + i] * a.cf[CF_Q * cs + i];
+                d.c[0] = a.cf[CF_K * cs + i];
+                d.c[1] = au * a.cf[CF_CT * cs + i];
+                d.c[2] = au * a.cf[CF_ST * cs + i];
+                d.c[3] = au;
+            }
+        }
+        sc[e] = d;
+    }
+}
+
+__device__ __forceinline__ void df_phasor(const DfComp &d, float dxh, float dxl, float dyh, float dyl, float th,
+                                          float tl, float &c, float &s) {
+    float2 ph = ff_add(ff_mul(d.kxh, d.kxl, dxh, dxl), ff_mul(d.kyh, d.kyl, dyh, dyl));
+    ph = ff_add(ph, ff_mul(d.wh, d.wl, th, tl));
+    ph = ff_add(ph, make_float2(d.ph, d.pl));
+    sincosf(ff_reduce_2pi(ph), &s, &c);
+}
+
+__global__ void __launch_bounds__(128) k_df_first_surface(DfFirstArgs a) {
+    __shared__ DfComp sc[DFC];
+    const long p = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    const bool valid = p < a.n;
+    const long pc = valid ? p : 0;
+    float dxh, dxl, dyh, dyl, th, tl;
+    ff_split(a.xy[pc] - a.fx, dxh, dxl);
+    ff_split(a.xy[a.n + pc] - a.fy, dyh, dyl);
+    ff_split(a.t, th, tl);
+    float s[5] = {0, 0, 0, 0, 0}, k[5] = {0, 0, 0, 0, 0};
+    for (int i0 = 0; i0 < a.ncomp; i0 += DFC) {
+        __syncthreads();
+        df_stage<0>(a, i0, sc);
+        __syncthreads();
+        const int iend = min(DFC, a.ncomp - i0);
+        for (int ii = 0; ii < iend; ii++) {
+            const DfComp &d = sc[ii];
+            float c, sn;
+            df_phasor(d, dxh, dxl, dyh, dyl, th, tl, c, sn);
+            const float rc = d.r * c, rs = d.r * sn;
+            df_kahan(s[0], k[0], rc * d.c[0]);
+            df_kahan(s[1], k[1], rc * d.c[1]);
+            df_kahan(s[2], k[2], rc * d.c[2]);
+            df_kahan(s[3], k[3], rs * d.c[3]);
+            df_kahan(s[4], k[4], rc * d.c[4]);
+        }
+    }
+    if (!valid) return;
+    for (int q = 0; q < 5; q++) a.first[q * a.n + p] = (double)s[q] - (double)k[q];
+}
+
+// blockDim = 32 columns x up to 8 level groups of 4 levels; blockIdx.y: further level groups
+__global__ void __launch_bounds__(256) k_df_first_levels(DfFirstArgs a) {
+    __shared__ DfComp sc[DFC];
+    const int cl = threadIdx.x & 31;
+    const int lg = blockIdx.y * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const long p = (long)blockIdx.x * 32 + cl;
+    const bool valid = p < a.n;
+    const long pc = valid ? p : 0;
+    float dxh, dxl, dyh, dyl, th, tl;
+    ff_split(a.xy[pc] - a.fx, dxh, dxl);
+    ff_split(a.xy[a.n + pc] - a.fy, dyh, dyl);
+    ff_split(a.t, th, tl);
+    float zk[4], yk[4];
+#pragma unroll
+    for (int l = 0; l < 4; l++) {
+        const int m = lg * 4 + l;
+        const float z = (valid && m < a.nl) ? a.z0[pc * a.nl + m] : 0.f;
+        zk[l] = z * LOG2E_DF;
+        yk[l] = -(z + 2.f * a.depth) * LOG2E_DF;
+    }
+    float su[4] = {0, 0, 0, 0}, sv[4] = {0, 0, 0, 0}, sw[4] = {0, 0, 0, 0};
+    float cu[4] = {0, 0, 0, 0}, cv[4] = {0, 0, 0, 0}, cw[4] = {0, 0, 0, 0};
+    for (int i0 = 0; i0 < a.ncomp; i0 += DFC) {
+        __syncthreads();
+        df_stage<1>(a, i0, sc);
+        __syncthreads();
+        const int iend = min(DFC, a.ncomp - i0);
+        for (int ii = 0; ii < iend; ii++) {
+            const DfComp &d = sc[ii];
+            float c, sn;
+            df_phasor(d, dxh, dxl, dyh, dyl, th, tl, c, sn);
+            const float rc = d.r * c, rs = d.r * sn;
+            const float au = d.c[1] * rc, av = d.c[2] * rc, aw = d.c[3] * rs, k = d.c[0];
+#pragma unroll
+            for (int l = 0; l < 4; l++) {
+                // cosh(k(z+h))/cosh(kh) = q (E + Y), sinh(k(z+h))/cosh(kh) = q (E - Y)
+                const float E = df_ex2(k * zk[l]), Y = df_ex2(k * yk[l]);
+                df_kahan(su[l], cu[l], au * (E + Y));
+                df_kahan(sv[l], cv[l], av * (E + Y));
+                df_kahan(sw[l], cw[l], aw * (E - Y));
+            }
+        }
+    }
+    if (!valid) return;
+    const long tot = a.n * a.nl;
+#pragma unroll
+    for (int l = 0; l < 4; l++) {
+        const int m = lg * 4 + l;
+        if (m >= a.nl) continue;
+        const long o = p * a.nl + m;
+        a.sec[o] = su[l];
+        a.sec[tot + o] = sv[l];
+        a.sec[2 * tot + o] = sw[l];
+    }
+}
+
 // eta2 of the columns from output column 0
 __global__ void k_df_take(long n, int nout, const float *out, float *eta2) {
     long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
@@ -472,6 +648,31 @@ int depthform_columns(DepthForm &df, const DevSea &sea, long nact, const double 
     k_df_take<<<(unsigned)((nact + 255) / 256), 256, 0, stream>>>(nact, df.nout, df.qout, eta2);
     note_launch();
     CK(cudaGetLastError());
+    return OK;
+}
+
+int depthform_first(const DevSea &sea, long nact, int nl, const double *xy, double t, const float *z0,
+                    double *first, float *sec, void *stream_) {
+    cudaStream_t stream = (cudaStream_t)stream_;
+    if (nact <= 0) return OK;
+    DfFirstArgs a;
+    a.n = nact; a.xy = xy; a.t = t; a.fx = sea.fx; a.fy = sea.fy;
+    a.phase = sea.d_phase; a.cf = sea.d_cf; a.cstride = sea.npad_g; a.ncomp = sea.n;
+    a.trivial_ramp = sea.trivial_ramp ? 1 : 0;
+    a.nl = nl; a.z0 = z0; a.depth = (float)sea.depth; a.first = first; a.sec = sec;
+    if (first) {
+        k_df_first_surface<<<(unsigned)((nact + 127) / 128), 128, 0, stream>>>(a);
+        note_launch();
+        CK(cudaGetLastError());
+    }
+    if (sec) {
+        const int ngrp = (nl + 3) / 4;
+        const int gpb = std::min(ngrp, 8);
+        dim3 grid((unsigned)((nact + 31) / 32), (unsigned)((ngrp + gpb - 1) / gpb));
+        k_df_first_levels<<<grid, 32 * gpb, 0, stream>>>(a);
+        note_launch();
+        CK(cudaGetLastError());
+    }
     return OK;
 }
 

@@ -33,6 +33,7 @@
 //    visited.  Every mbarrier wait is bounded; a timeout sets an error word.
 //  * k_qform_plain: the same sums on FP32 CUDA cores (the plain form).
 #include "cfdwm.h"
+#include "ffmath.cuh"
 
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -268,21 +269,6 @@ __global__ void k_qform_comps(int n, int npad, const double *phase, int cstride,
     out[i] = c;
 }
 
-// a*b as an unevaluated float pair (products of the lo parts dropped)
-__device__ __forceinline__ float2 ff_mul(float ah, float al, float bh, float bl) {
-    float p = ah * bh;
-    float e = fmaf(ah, bh, -p);
-    e = fmaf(ah, bl, fmaf(al, bh, e));
-    return make_float2(p, e);
-}
-// Knuth two-sum of the hi parts, error folded into the lo part
-__device__ __forceinline__ float2 ff_add(float2 a, float2 b) {
-    float s = a.x + b.x;
-    float bb = s - a.x;
-    float e = (a.x - (s - bb)) + (b.x - bb);
-    return make_float2(s, e + a.y + b.y);
-}
-
 struct QPrep {
     long rows;
     const QRow *row;
@@ -308,13 +294,7 @@ __global__ void __launch_bounds__(256) k_qform_prep(QPrep a) {
         float2 ph = ff_add(ff_mul(K.kxh, K.kxl, R.dxh, R.dxl), ff_mul(K.kyh, K.kyl, R.dyh, R.dyl));
         ph = ff_add(ph, ff_mul(K.wh, K.wl, R.th, R.tl));
         ph = ff_add(ph, make_float2(K.ph, K.pl));
-        // 2 pi = P1 + P2 + P3: P1 = 201/32 has 8 significant bits, so n P1 is exact for |n| < 2^16
-        const float P1 = 6.28125f, P2 = 1.9353071693331003e-3f, P3 = 1.0253376273028358e-11f;
-        float n = rintf(ph.x * 0.15915494309189535f);
-        float red = fmaf(-n, P1, ph.x);
-        red = fmaf(-n, P2, red);
-        red = fmaf(-n, P3, red);
-        red += ph.y;
+        float red = ff_reduce_2pi(ph);
         __sincosf(red, &s, &c);
         r = a.trivial_ramp ? R.ramp
                            : (float)q_freq_ramp(a.t[p * a.st], a.phase[4 * a.cstride + i], a.phase[5 * a.cstride + i],

@@ -393,9 +393,12 @@ static int fill_cols(DevGrid &g, const DevSea &sea, Workspace &ws, const int *ac
     if (nact == 0) return OK;
     GridGeom G = geom(g);
     const int npad = sea.npad_g;
-    // workspace: phasors [npad][nact], ramps [npad][nact], first-order sums [5][nact]
+    const bool tc = g.method == 1 && x->df.built;
     auto up = [](size_t b) { return (b + 255) / 256 * 256; };
-    size_t b_ph = up(sizeof(float2) * (size_t)npad * nact), b_rr = up(sizeof(float) * (size_t)npad * nact);
+    // workspace: plain: phasors [npad][nact], ramps [npad][nact], first-order
+    // sums [5][nact]; tensor-core: the first-order sums only
+    size_t b_ph = tc ? 0 : up(sizeof(float2) * (size_t)npad * nact);
+    size_t b_rr = tc ? 0 : up(sizeof(float) * (size_t)npad * nact);
     int rc = workspace_reserve(ws, b_ph + b_rr + sizeof(double) * 5 * nact);
     if (rc) return rc;
     char *b = (char *)ws.base;
@@ -406,28 +409,30 @@ static int fill_cols(DevGrid &g, const DevSea &sea, Workspace &ws, const int *ac
     note_launch();
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(x->tdev, &t, sizeof(double), cudaMemcpyHostToDevice, stream));
-    rc = launch_phasors_public(sea, nact, x->xy, x->xy + nact, x->tdev, 1, 1, 0, npad, ph, rr, first, stream);
-    if (rc) return rc;
-    const bool tc = g.method == 1 && x->df.built;
     if (tc) {
-        // eta2 and the 3R depth-separated quadratic forms of every column in one GEMM
-        rc = depthform_columns(x->df, sea, nact, x->xy, x->xy + nact, x->tdev, x->eta2, stream);
+        // eta1 and the Taylor gradients (float-float phases), then eta2 and the
+        // 3R depth-separated quadratic forms of every column in one GEMM
+        rc = depthform_first(sea, nact, g.nl, x->xy, t, nullptr, first, nullptr, stream);
+        if (!rc) rc = depthform_columns(x->df, sea, nact, x->xy, x->xy + nact, x->tdev, x->eta2, stream);
     } else {
-        rc = launch_eta_pairs(sea, nact, ph, rr, x->eta2, stream, x->split, x->split_cap);
+        rc = launch_phasors_public(sea, nact, x->xy, x->xy + nact, x->tdev, 1, 1, 0, npad, ph, rr, first, stream);
+        if (!rc) rc = launch_eta_pairs(sea, nact, ph, rr, x->eta2, stream, x->split, x->split_cap);
     }
     if (rc) return rc;
     k_levels<<<(unsigned)((nact + 127) / 128), 128, 0, stream>>>(G, nact, act, first, x->eta2, slot, ETA,
                                                                  x->zmin, x->zmax);
     note_launch();
     CK(cudaGetLastError());
-    // plain: first and second order per (pair, level); tc: first order here,
-    // the second order from the R basis functions of the level heights
-    rc = launch_column_pairs(sea, nact, g.nl, ph, rr, x->zmin, x->sec, tc ? 0 : 1, stream, x->split, x->split_cap);
-    if (rc) return rc;
     if (tc) {
-        rc = depthform_combine(x->df, nact, g.nl, x->zmin, x->sec, stream);
-        if (rc) return rc;
+        // first order at the level heights, then the second order from the R
+        // basis functions of the level heights
+        rc = depthform_first(sea, nact, g.nl, x->xy, t, x->zmin, nullptr, x->sec, stream);
+        if (!rc) rc = depthform_combine(x->df, nact, g.nl, x->zmin, x->sec, stream);
+    } else {
+        // first and second order per (pair, level)
+        rc = launch_column_pairs(sea, nact, g.nl, ph, rr, x->zmin, x->sec, 1, stream, x->split, x->split_cap);
     }
+    if (rc) return rc;
     long tot = nact * g.nl;
     k_scatter_levels<<<(unsigned)((tot + 255) / 256), 256, 0, stream>>>(G, nact, act, first, x->sec, x->zmax,
                                                                         slot, U[0], U[1], U[2]);

@@ -276,16 +276,19 @@ def run_regular(args):
         sampler = ClockSampler(local)
         sampler.start()
         l0 = lib.cfdwm_kernel_launches()
+        # a step is about 1 ms: the timed region repeats it so that it spans
+        # at least a few hundred ms of clock samples
+        reps = max(args.steps, 400)
         e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        for _ in range(args.steps):
+        for _ in range(reps):
             assert lib.wave_Kinematics_batch(*p, n, cw._ptr(dout)) == 0
         e1.record(stream)
         torch.cuda.synchronize()
-        launches += lib.cfdwm_kernel_launches() - l0
-        ms = e0.elapsed_time(e1) / args.steps
+        launches += (lib.cfdwm_kernel_launches() - l0) * args.steps // reps
+        ms = e0.elapsed_time(e1) / reps
         kt = C.c_double(0.0)
-        nk = lib.cfdwm_profile_read(9, C.byref(kt))
+        nk = lib.cfdwm_profile_read(9, C.byref(kt))     # per launch, over the reps
         lib.cfdwm_profile_enable(0)
         ck = sampler.stop()
         clocks = ck if clocks is None else clocks
@@ -581,6 +584,17 @@ class ClockSampler:
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
+            return
+        # return once nvidia-smi is running and has written a sample, so that
+        # short timed regions are sampled too
+        t0 = time.time()
+        while time.time() - t0 < 3.0:
+            try:
+                if os.path.getsize(self.path) > 0:
+                    break
+            except OSError:
+                pass
+            time.sleep(0.02)
 
     def stop(self):
         if self.proc is None:

@@ -284,6 +284,8 @@ struct TcForm {
     int *err = nullptr;
     void *scratch = nullptr;
     size_t scratch_bytes = 0;
+    void *aux = nullptr;        // stream of the operand preparation (several chunks)
+    void *ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
 };
 int tcform_split(TcForm &f, const double *coef64, const int *bmap_host, int nblk, int nout, int npad, bool fp16,
                  void *stream);

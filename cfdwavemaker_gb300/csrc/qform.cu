@@ -282,11 +282,7 @@ struct QPrep {
     float *Y;                  // [rows][2 npad]
 };
 
-__global__ void __launch_bounds__(256) k_qform_prep(QPrep a) {
-    // grid: x over rows, y over blocks of 256 components
-    const int i = blockIdx.y * blockDim.x + threadIdx.x;
-    const long p = blockIdx.x;
-    if (i >= a.npad || p >= a.rows) return;
+__device__ __forceinline__ void qform_prep_one(const QPrep &a, long p, int i) {
     float c = 0.f, s = 0.f, r = 0.f;
     if (i < a.ncomp) {
         const QRow R = a.row[p];
@@ -318,6 +314,17 @@ __global__ void __launch_bounds__(256) k_qform_prep(QPrep a) {
         H[o + a.npad] = hs;
         L[o] = __float2bfloat16_rn(xc - __bfloat162float(hc));
         L[o + a.npad] = __float2bfloat16_rn(xs - __bfloat162float(hs));
+    }
+}
+
+// Block-stride loop over (row, block of 256 components).
+__global__ void __launch_bounds__(256) k_qform_prep(QPrep a) {
+    const long nb = a.npad / 256;
+    const long tot = a.rows * nb;
+    for (long blk = blockIdx.x; blk < tot; blk += gridDim.x) {
+        const long p = blk / nb;
+        const int i = (int)(blk % nb) * 256 + threadIdx.x;
+        qform_prep_one(a, p, i);
     }
 }
 
@@ -733,6 +740,8 @@ int launch_phasors_public(const DevSea &sea, long n, const double *x, const doub
 void tcform_free(TcForm &f) {
     void *q[] = {f.Whi, f.Wlo, f.colscale, f.bmap, f.err, f.scratch};
     for (void *p : q) if (p) cudaFree(p);
+    for (void *e : f.ev) if (e) cudaEventDestroy((cudaEvent_t)e);
+    if (f.aux) cudaStreamDestroy((cudaStream_t)f.aux);
     f = TcForm();
 }
 
@@ -790,8 +799,27 @@ int tcform_eval(TcForm &f, const DevSea &sea, long n, const double *x, const dou
     long mpad = ((m + TBM - 1) / TBM) * TBM;
     size_t xb = (size_t)mpad * 2 * npad * 2;     // one 16-bit matrix
     size_t yb = (size_t)mpad * 2 * npad * 4;
-    int rc = tc_reserve(f, 2 * xb + yb + sizeof(QRow) * chunk + sizeof(QComp) * npad + 4096);
+    // several chunks: two operand buffers, the next chunk's operands prepared
+    // on a second stream, so that preparation and GEMM of neighbouring chunks
+    // overlap where the SMs have room (measured: 1277 against 1323 ms per step
+    // of 4e6 points)
+    const int nbuf = n > chunk ? 2 : 1;
+    const size_t bufb = ((2 * xb + yb + sizeof(QRow) * chunk + sizeof(QComp) * npad + 4095) / 4096) * 4096;
+    int rc = tc_reserve(f, nbuf * bufb);
     if (rc) return rc;
+    cudaStream_t pst = stream;
+    cudaEvent_t *ev = (cudaEvent_t *)f.ev;
+    if (nbuf == 2) {
+        if (!f.aux) {
+            cudaStream_t a2;
+            CK(cudaStreamCreateWithFlags(&a2, cudaStreamNonBlocking));
+            f.aux = a2;
+            for (int e = 0; e < 5; e++) CK(cudaEventCreateWithFlags(&ev[e], cudaEventDisableTiming));
+        }
+        pst = (cudaStream_t)f.aux;
+        CK(cudaEventRecord(ev[0], stream));          // inputs and the zeroed output are ordered before
+        CK(cudaStreamWaitEvent(pst, ev[0], 0));
+    }
     static bool attr = false;
     if (!attr) {
         CK(cudaFuncSetAttribute(k_qform_tc<128, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -801,28 +829,47 @@ int tcform_eval(TcForm &f, const DevSea &sea, long n, const double *x, const dou
         attr = true;
     }
     const int BN = f.fp16 ? 128 : 256;
-    for (long b = 0; b < n; b += chunk) {
+    int j = 0;
+    for (long b = 0; b < n; b += chunk, j++) {
         long mm = std::min(chunk, n - b);
-        char *base = (char *)f.scratch;
+        const int buf = j % nbuf;
+        char *base = (char *)f.scratch + buf * bufb;
+        // this buffer's previous GEMM has finished reading it
+        if (nbuf == 2 && j >= 2) CK(cudaStreamWaitEvent(pst, ev[3 + buf], 0));
         void *Xh = base, *Xl = base + xb;
         float *Y = (float *)(base + 2 * xb);
         QRow *rowrec = (QRow *)(base + 2 * xb + yb);
         QComp *comprec = (QComp *)(base + 2 * xb + yb + sizeof(QRow) * chunk);
-        k_qform_rows<<<(unsigned)((mm + 255) / 256), 256, 0, stream>>>(mm, x + b, y + b, t + b * st, st, sea.fx,
-                                                                       sea.fy, sea.d_phase, sea.npad_g, rowrec);
+        k_qform_rows<<<(unsigned)((mm + 255) / 256), 256, 0, pst>>>(mm, x + b, y + b, t + b * st, st, sea.fx,
+                                                                    sea.fy, sea.d_phase, sea.npad_g, rowrec);
         note_launch();
-        k_qform_comps<<<(unsigned)((npad + 255) / 256), 256, 0, stream>>>(sea.n, npad, sea.d_phase, sea.npad_g,
-                                                                          comprec);
+        k_qform_comps<<<(unsigned)((npad + 255) / 256), 256, 0, pst>>>(sea.n, npad, sea.d_phase, sea.npad_g,
+                                                                       comprec);
         note_launch();
         QPrep pp;
         pp.rows = mm; pp.row = rowrec; pp.comp = comprec; pp.phase = sea.d_phase; pp.t = t + b * st; pp.st = st;
         pp.cstride = sea.npad_g; pp.ncomp = sea.n; pp.npad = npad;
         pp.trivial_ramp = sea.trivial_ramp ? 1 : 0; pp.fp16 = f.fp16 ? 1 : 0;
         pp.Xhi = Xh; pp.Xlo = Xl; pp.Y = Y;
-        dim3 pg((unsigned)mm, (unsigned)(npad / 256));
-        k_qform_prep<<<pg, 256, 0, stream>>>(pp);
+        static int nsm_p = 0;
+        if (!nsm_p) {
+            int dev = 0;
+            CK(cudaGetDevice(&dev));
+            CK(cudaDeviceGetAttribute(&nsm_p, cudaDevAttrMultiProcessorCount, dev));
+        }
+        const long pblocks = mm * (long)(npad / 256);
+        // a full grid: with two blocks per SM beside the GEMM the preparation
+        // ran latency-bound at a tenth of its speed (24 ms against 2.3 ms per
+        // 65,536 x 4096 chunk) and became the bottleneck
+        const long pgrid = std::min<long>(pblocks, 1L << 20);
+        (void)nsm_p;
+        k_qform_prep<<<(unsigned)pgrid, 256, 0, pst>>>(pp);
         note_launch();
         CK(cudaGetLastError());
+        if (nbuf == 2) {
+            CK(cudaEventRecord(ev[1 + buf], pst));
+            CK(cudaStreamWaitEvent(stream, ev[1 + buf], 0));
+        }
         CUtensorMap mXh, mXl, mWh, mWl;
         if (make_map(&mXh, Xh, mm, 2L * npad, TBM, f.fp16) || make_map(&mXl, Xl, mm, 2L * npad, TBM, f.fp16) ||
             make_map(&mWh, f.Whi, (long)f.nblk * npad, npad, BN, f.fp16) ||
@@ -849,6 +896,7 @@ int tcform_eval(TcForm &f, const DevSea &sea, long n, const double *x, const dou
         note_launch();
         prof_end(PK_QFORM, stream);
         CK(cudaGetLastError());
+        if (nbuf == 2) CK(cudaEventRecord(ev[3 + buf], stream));
     }
     if (tc_error) {
         int h = 0;

@@ -111,3 +111,18 @@ def test_tensor_core_fp16_split_wide(wm, torch):
         err = norm_rel_err(got[:, f], ref[:, f])
         print("fp16x3 N=2048 field", f, "err", err)
         assert err <= TOL, (f, err)
+
+
+def test_tensor_core_several_chunks(wm, torch):
+    """More than one 65,536-row chunk: the operands of the next chunk are
+    prepared on a second stream while the GEMM of the previous one runs."""
+    txt = _sea(12, 4, 29)
+    n = 140000
+    x, y, t, got = _run(wm, torch, txt, n, 1, True, seed=8)
+    rng = np.random.default_rng(2)
+    rows = np.concatenate([rng.choice(65536, 60, replace=False), 65536 + rng.choice(65536, 60, replace=False),
+                           131072 + rng.choice(n - 131072, 60, replace=False)])
+    ref = _reference(txt, x[rows], y[rows], t[rows])
+    for f in range(4):
+        err = norm_rel_err(got[rows, f], ref[:, f])
+        assert err <= TOL, (f, err)

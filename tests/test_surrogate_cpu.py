@@ -64,3 +64,20 @@ def test_committed_weights_header():
     assert nl == 16 and n == sr.layout(16)[3]
     w = np.frombuffer(raw[24:], np.float32)
     assert w.size == n and np.all(np.isfinite(w))
+
+
+def test_oracle_features_per_column():
+    # each column's channels depend on that column alone
+    from cfdwavemaker_gb300 import surrogate as S
+    import oracle
+    p = {"hs": 4.0, "tp": 9.0, "gamma": 2.0, "s": 6.0, "mtheta": 30.0, "seed": 3, "nfreq": 8, "ndir": 3}
+    cfg = oracle.waveinput.read_text(S.sea_text(p, 6, 5, 3, 50.0, 20.0, 1.0, t0=2.0))
+    x = np.array([50.0, 61.5, 70.25])
+    y = np.array([20.0, 33.0, 24.5])
+    f_all, b_all, e_all = sr.features_columns(cfg, x, y, 4.2)
+    assert f_all.shape == (3, 8 * cfg["lsgrid"]["nl"])
+    for j in range(3):
+        f1, b1, e1 = sr.features_columns(cfg, x[j:j + 1], y[j:j + 1], 4.2)
+        np.testing.assert_array_equal(f1[0], f_all[j])
+        np.testing.assert_array_equal(b1[0], b_all[j])
+        assert e1[0] == e_all[j]

@@ -804,6 +804,22 @@ def run_ours(args):
     te = (time.perf_counter() - te0) / args.steps
     te = allmax(ws, te)
     clocks = sampler.stop()
+    if args.workload == "sgrid":
+        # the same step with the dynamic pressure on the ring (a fourth field
+        # of the update, its gradients and its query)
+        assert lib.cfdwm_sgrid_pressure(1) == 0, cw.last_error()
+        for _ in range(2):
+            step_device()
+        torch.cuda.synchronize()
+        ep0 = torch.cuda.Event(enable_timing=True)
+        ep1 = torch.cuda.Event(enable_timing=True)
+        ep0.record(stream)
+        for _ in range(args.steps):
+            step_device()
+        ep1.record(stream)
+        torch.cuda.synchronize()
+        res["pressure_ms"] = allmax(ws, ep0.elapsed_time(ep1) / args.steps)
+        assert lib.cfdwm_sgrid_pressure(0) == 0, cw.last_error()
     res.update(depth_rank=depth_rank)
     res.update(ms=ms, e2e_s=te, units=units, launches=launches, init_s=init_s, h2d=h2d, d2h=d2h,
                clocks=clocks, ws=ws, rank=rank, prof=prof, npairs=int(lib.cfdwm_npairs()),
@@ -1020,6 +1036,10 @@ def main():
         "kernels": r["prof"],
         "peaks_source": src,
     }
+    if "pressure_ms" in r:
+        line["with_pressure"] = {"ms_per_step": r["pressure_ms"],
+                                 "nodes_per_s": r["units"] * n / (r["pressure_ms"] / 1e3),
+                                 "note": "dynamic pressure on the ring (cfdwm_sgrid_pressure): a fourth field"}
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args)
     print(json.dumps(line))

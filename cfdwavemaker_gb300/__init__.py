@@ -164,6 +164,8 @@ def load(path: str | None = None):
     L.cfdwm_sgrid_method.argtypes = [C.c_int, ip]
     L.cfdwm_depth_basis.restype = C.c_int
     L.cfdwm_depth_basis.argtypes = [_d, _d, ip, _dp]
+    L.cfdwm_sgrid_pressure.restype = C.c_int
+    L.cfdwm_sgrid_pressure.argtypes = [C.c_int]
     L.cfdwm_surrogate_set_carry.restype = C.c_int
     L.cfdwm_surrogate_set_carry.argtypes = [_d]
     L.cfdwm_surrogate_stats.restype = C.c_int
@@ -347,6 +349,17 @@ class CFDwavemaker:
         ts = C.c_int()
         _check(self.lib.cfdwm_sgrid_state(C.byref(t0), C.byref(ts)))
         return t0.value, ts.value
+
+    def sgrid_method(self, method):
+        """Method of the s-grid column sums (0 plain, 1 tensor-core form); refills the ring.
+        Returns the rank of the depth basis (0 for the plain form)."""
+        r = C.c_int(0)
+        _check(self.lib.cfdwm_sgrid_method(int(method), C.byref(r)))
+        return r.value
+
+    def sgrid_pressure(self, on=True):
+        """Dynamic pressure on the s-grid ring (wave type 5); refills the ring."""
+        _check(self.lib.cfdwm_sgrid_pressure(1 if on else 0))
 
     def components(self):
         n = self.lib.cfdwm_components(None)

@@ -166,8 +166,9 @@ __device__ double d_ramp(const RampDev &r, double t, double x, double y) {
 }
 
 // Irregular wave types 1/5 and regular 21 finish here: out rows
-// 0 SurfElev, 1 VeloX, 2 VeloY, 3 VeloZ, 4 DynPres, 5 nhPres.
-__global__ void k_finish(long n, int wavetype, RampDev r, double rho, double g, const double *x,
+// 0 SurfElev, 1 VeloX, 2 VeloY, 3 VeloZ, 4 DynPres, 5 nhPres.  sgp: the
+// s-grid holds the dynamic pressure (row 4 of its query).
+__global__ void k_finish(long n, int wavetype, int sgp, RampDev r, double rho, double g, const double *x,
                          const double *y, const double *t, const double *f, const double *fe,
                          double *out) {
     long p = blockIdx.x * (long)blockDim.x + threadIdx.x;
@@ -182,13 +183,16 @@ __global__ void k_finish(long n, int wavetype, RampDev r, double rho, double g, 
         out[4 * n + p] = rr * f[4 * n + p];
         out[5 * n + p] = rr * (f[4 * n + p] - rho * g * f[0 * n + p]);
     } else if (wavetype == WT_IRR_SGRID) {
-        // f = [4][n] query at the clamped z, fe = [4][n] query at z = 0
+        // f = [4][n] query at the clamped z (sgp: [5][n] with the pressure),
+        // fe = [4][n] query at z = 0.  Without a pressure field the
+        // reference's 0.0 (CFDwavemaker.cpp:1808-1812, 1815-1891); with one,
+        // the irregular sea's forms (:1807-1808, 1826-1830) on the grid.
         out[0 * n + p] = fe[0 * n + p] * rr;
         out[1 * n + p] = f[1 * n + p] * rr;
         out[2 * n + p] = f[2 * n + p] * rr;
         out[3 * n + p] = f[3 * n + p] * rr;
-        out[4 * n + p] = 0.0;
-        out[5 * n + p] = 0.0;
+        out[4 * n + p] = sgp ? rr * f[4 * n + p] : 0.0;
+        out[5 * n + p] = sgp ? rr * (f[4 * n + p] - rho * g * f[0 * n + p]) : 0.0;
     } else {
         // f = [5][n] eta, u, v, w, p_nh of the regular theory
         out[0 * n + p] = rr * f[0 * n + p];
@@ -270,7 +274,8 @@ int eval_api(long n, const double *x, const double *y, const double *z, const do
     } else {
         return E_UNSUPPORTED;
     }
-    k_finish<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(n, wt, rd, M.cfg.rho, M.cfg.gravity, x, y, t,
+    const int sgp = (wt == WT_IRR_SGRID && M.grid.nf == 4) ? 1 : 0;
+    k_finish<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(n, wt, sgp, rd, M.cfg.rho, M.cfg.gravity, x, y, t,
                                                          f, fe, out);
     note_launch();
     CKR(cudaGetLastError());
@@ -511,7 +516,7 @@ void wave_force_update(double t) {
     if (!M.init || M.cfg.wavetype != WT_IRR_SGRID) return;
     cudaStream_t s = stream_of();
     while (grid_check_time(M.grid, t)) {
-        if (g_surr_use.on && surrogate_levels() == M.grid.nl) {
+        if (g_surr_use.on && surrogate_levels() == M.grid.nl && M.grid.nf == 3) {
             int mode = (g_surr_use.count++ % g_surr_use.plain_every == 0) ? 0 : 1;
             if (surrogate_step(M.cfg, M.sea, M.grid, M.grid_ws, mode, g_surr_use.tol, g_surr_use.nsample,
                                nullptr, nullptr, s) != OK)
@@ -864,6 +869,10 @@ int cfdwm_surrogate_compare(double *err4) {
 
 int cfdwm_surrogate_enable(int on, int plain_every, double tol, int nsample) {
     std::lock_guard<std::mutex> lk(g_model_mtx);
+    if (on && sgrid_loaded() && g_model.grid.nf != 3) {
+        set_error("surrogate: the learned update does not predict the pressure field");
+        return E_UNSUPPORTED;
+    }
     if (on && (surrogate_nparams() <= 0 || plain_every < 1 || nsample < 0 || nsample > 4096))
         return on && surrogate_nparams() <= 0 ? E_NOT_INITIALIZED : E_BAD_ARGUMENT;
     g_surr_use.on = on != 0;
@@ -893,6 +902,24 @@ int cfdwm_sgrid_method(int method, int *rank) {
 }
 
 int cfdwm_depth_basis(double K, double h, int *rank, double *err) { return depthform_basis_info(K, h, rank, err); }
+
+int cfdwm_sgrid_pressure(int on) {
+    std::lock_guard<std::mutex> lk(g_model_mtx);
+    Model &M = g_model;
+    if (!sgrid_loaded()) return E_UNSUPPORTED;
+    if (on && g_surr_use.on) {
+        set_error("s-grid: pressure and the learned update exclude each other");
+        return E_UNSUPPORTED;
+    }
+    cudaStream_t s = stream_of();
+    int rc = grid_set_pressure(M.grid, M.cfg, M.sea, on != 0, s);
+    if (rc) {
+        set_error(rc == E_UNSUPPORTED ? "s-grid: pressure needs a second-order sea" : "s-grid: pressure set-up failed");
+        return rc;
+    }
+    // the ring is refilled at the current t0 with (or without) the pressure
+    return grid_initialize(M.grid, M.sea, M.grid_ws, s);
+}
 
 int cfdwm_surrogate_set_carry(double wavelengths) {
     if (!(wavelengths >= 0.0)) return E_BAD_ARGUMENT;

@@ -145,6 +145,8 @@ struct DevSea {
     float *d_tab_eta = nullptr;  // grid-mask pair tiles of eta2 (A, B per pair)
     float *d_tab_grid = nullptr; // grid-mask pair tiles of uvw2
     float *d_tab_point = nullptr;// point-API pair tiles (built on demand)
+    float *d_tab_gp = nullptr;   // grid-mask pair tiles of the s-grid pressure: Pp, Mp (phase terms)
+    float *d_tab_gk = nullptr;   // grid-mask pair tiles of the phase-free pressure terms: X, Z
     int ntile_g = 0, ntile_p = 0;
 };
 
@@ -186,13 +188,15 @@ struct DevGrid {
     int nx = 0, ny = 0, nl = 0;
     double dx = 0, dy = 0, ds = 0, t0 = 0, dt = 0, depth = 0, swl = 0;
     int tstep = 0;
-    // FP32 fields, layouts of lsgrid_spline.cpp:35-61 ([slot][i][j][m])
+    // FP32 fields, layouts of lsgrid_spline.cpp:35-61 ([slot][i][j][m]);
+    // field 3 is the dynamic pressure, held only when nf = 4
+    int nf = 3;
     float *ETA = nullptr, *ETAdx = nullptr, *ETAdy = nullptr, *ETAdt = nullptr;
-    float *U[3] = {nullptr, nullptr, nullptr};
-    float *Ut[3] = {nullptr, nullptr, nullptr};
-    float *Ux[3] = {nullptr, nullptr, nullptr};
-    float *Uy[3] = {nullptr, nullptr, nullptr};
-    float *Us[3] = {nullptr, nullptr, nullptr};
+    float *U[4] = {nullptr, nullptr, nullptr, nullptr};
+    float *Ut[4] = {nullptr, nullptr, nullptr, nullptr};
+    float *Ux[4] = {nullptr, nullptr, nullptr, nullptr};
+    float *Uy[4] = {nullptr, nullptr, nullptr, nullptr};
+    float *Us[4] = {nullptr, nullptr, nullptr, nullptr};
     int *IGNORE = nullptr;
     float *zlev = nullptr;       // scratch: level heights of the slot being written
     double *colpts = nullptr;    // scratch: column x, y, t (FP64)
@@ -203,6 +207,10 @@ struct DevGrid {
 };
 // Selects the method of the column sums (builds the tensor-core form).
 int grid_set_method(DevGrid &g, const Config &cfg, const DevSea &sea, int method, void *stream);
+// Dynamic pressure on the ring (nf = 4) or not (nf = 3): allocates or frees
+// the pressure fields and rebuilds the tensor-core form for the field count.
+// The ring must be refilled afterwards (grid_initialize).
+int grid_set_pressure(DevGrid &g, const Config &cfg, const DevSea &sea, bool on, void *stream);
 // The error word of the tensor-core form (0: no bounded wait expired).
 int grid_tc_error(DevGrid &g, void *stream);
 int depthform_rank(DevGrid &g);
@@ -211,7 +219,7 @@ void grid_free(DevGrid &g);
 int grid_initialize(DevGrid &g, const DevSea &sea, Workspace &ws, void *stream);
 int grid_update(DevGrid &g, const DevSea &sea, Workspace &ws, void *stream);
 bool grid_check_time(const DevGrid &g, double t);
-// out [4][n] FP64: eta, u, v, w (no ramp)
+// out [1 + nf][n] FP64: eta, u, v, w (and p when nf = 4), no ramp
 int grid_query(const DevGrid &g, long n, const double *x, const double *y, const double *z,
                const double *t, double *out, void *stream);
 int grid_download(const DevGrid &g, int which, double *dst, long cap, void *stream);
@@ -298,21 +306,24 @@ constexpr int TC_NPAD = 256;    // the component count of a TcForm is a multiple
 struct DepthForm {
     bool built = false;
     int R = 0, nout = 0;
+    int nf = 3;                 // fields per basis function: u, v, w (and p)
     double K = 0, h = 0;
     TcForm tc;
     float *bz = nullptr;        // b_r(z) on a uniform table over [-h, 0]
-    float *qout = nullptr;      // [ncol][1 + 3R] GEMM outputs
+    float *qout = nullptr;      // [ncol][1 + nf R] GEMM outputs
     long qcap = 0;
 };
-int depthform_build(const Config &cfg, const DevSea &sea, DepthForm &df, void *stream);
+// nf = 3: u, v, w; nf = 4: and the phase terms of the pressure
+int depthform_build(const Config &cfg, const DevSea &sea, DepthForm &df, int nf, void *stream);
 void depthform_free(DepthForm &df);
 int depthform_columns(DepthForm &df, const DevSea &sea, long nact, const double *x, const double *y,
                       const double *tdev, float *eta2, void *stream);
 int depthform_combine(DepthForm &df, long nact, int nl, const float *z0, float *sec, void *stream);
 // First-order sums of the tensor-core path (float-float phases): first [5][n]
-// (eta1 and the Taylor gradients) and/or sec [3][n nl] (u1, v1, w1 at z0).
+// (eta1 and the Taylor gradients) and/or sec [nf][n nl] (u1, v1, w1, and dp1
+// when nf = 4, at z0).
 int depthform_first(const DevSea &sea, long nact, int nl, const double *xy, double t, const float *z0,
-                    double *first, float *sec, void *stream);
+                    double *first, float *sec, int nf, void *stream);
 int depthform_error(DepthForm &df, void *stream);
 int depthform_basis_info(double K, double h, int *R, double *err);
 

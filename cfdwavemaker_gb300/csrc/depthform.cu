@@ -266,11 +266,11 @@ __device__ __forceinline__ void cubic_w(double t, int n, int &i0, double wt[4]) 
 }
 
 struct DfCoefArgs {
-    int n, npad, ntile, R;
-    const float *tab_grid, *tab_eta;
+    int n, npad, ntile, R, nf;
+    const float *tab_grid, *tab_eta, *tab_gp;
     const double *fk, *gk;    // [R][DF_NK]
     double inv_dk;
-    double *coef;             // [2 + 6R][npad][npad]
+    double *coef;             // [2 + 2 nf R][npad][npad]
 };
 
 // One thread per (m, i): the coefficient of every block at W^T[m][i].
@@ -280,7 +280,7 @@ __global__ void k_depth_coef(DfCoefArgs a) {
     if (e >= tot) return;
     const int m = (int)(e / a.npad), i = (int)(e % a.npad);
     const long nn = tot;
-    const int nb = 2 + 6 * a.R;
+    const int nb = 2 + 2 * a.nf * a.R;
     if (i > m || i >= a.n || m >= a.n) {
         for (int b = 0; b < nb; b++) a.coef[(long)b * nn + e] = 0.0;
         return;
@@ -290,6 +290,7 @@ __global__ void k_depth_coef(DfCoefArgs a) {
     const float *g = a.tab_grid + rec * GRIDV_NC_DF;
     const double Pu = g[0], Mu = g[1], Pv = g[2], Mv = g[3], Pw = g[4], Mw = g[5];
     const double kp = g[6], km = g[7];
+    const double Pp = a.nf == 4 ? a.tab_gp[rec * 2] : 0.0, Mp = a.nf == 4 ? a.tab_gp[rec * 2 + 1] : 0.0;
     a.coef[e] = a.tab_eta[rec * EATA_NC_DF + 0];
     a.coef[nn + e] = a.tab_eta[rec * EATA_NC_DF + 1];
     int ip, im;
@@ -305,13 +306,17 @@ __global__ void k_depth_coef(DfCoefArgs a) {
             fm += wm[q] * fr[im + q];
             gm += wm[q] * gr[im + q];
         }
-        double *c = a.coef + (long)(2 + 6 * r) * nn + e;
+        double *c = a.coef + (long)(2 + 2 * a.nf * r) * nn + e;
         c[0] = Pu * fp + Mu * fm;          // u, c c
         c[nn] = Mu * fm - Pu * fp;         // u, s s
         c[2 * nn] = Pv * fp + Mv * fm;     // v, c c
         c[3 * nn] = Mv * fm - Pv * fp;     // v, s s
         c[4 * nn] = Pw * gp - Mw * gm;     // w, c s
         c[5 * nn] = Pw * gp + Mw * gm;     // w, s c
+        if (a.nf == 4) {
+            c[6 * nn] = Pp * fp + Mp * fm; // p, c c
+            c[7 * nn] = Mp * fm - Pp * fp; // p, s s
+        }
     }
 }
 
@@ -321,8 +326,8 @@ __global__ void k_depth_coef(DfCoefArgs a) {
 // phasor table are not needed here):
 //   mode 0: eta1 and the Taylor gradients phi1_dxdz, phi1_dydz, phi1_dzdz,
 //           dp1_dz per column (Irregular.cpp:178-198, 1107-1192) into first[5][n];
-//   mode 1: u1, v1, w1 at the level heights z0 (Irregular.cpp:394-447) into
-//           sec[3][n nl].
+//   mode 1: u1, v1, w1 (nf = 4: and dp1) at the level heights z0
+//           (Irregular.cpp:394-447, 1107-1120) into sec[nf][n nl].
 // Sums are FP32 with Kahan compensation.
 // ---------------------------------------------------------------------------
 struct DfFirstArgs {
@@ -332,11 +337,11 @@ struct DfFirstArgs {
     const double *phase;       // [7][cstride]: kx, ky, omega, phase0, ramp parameters
     const float *cf;           // [NCF][cstride]
     int cstride, ncomp, trivial_ramp;
-    int nl;
+    int nl, nf;
     const float *z0;           // [n nl] (mode 1)
     float depth;
     double *first;             // [5][n] (mode 0)
-    float *sec;                // [3][n nl] (mode 1)
+    float *sec;                // [nf][n nl] (mode 1)
 };
 
 constexpr int DFC = 128;       // components per shared-memory chunk
@@ -389,6 +394,7 @@ __device__ __forceinline__ void df_stage(const DfFirstArgs &a, int i0, DfComp *s
                 d.c[1] = au * a.cf[CF_CT * cs + i];
                 d.c[2] = au * a.cf[CF_ST * cs + i];
                 d.c[3] = au;
+                d.c[4] = a.cf[CF_AP * cs + i] * a.cf[CF_Q * cs + i];
             }
         }
         sc[e] = d;
@@ -454,8 +460,9 @@ __global__ void __launch_bounds__(256) k_df_first_levels(DfFirstArgs a) {
         zk[l] = z * LOG2E_DF;
         yk[l] = -(z + 2.f * a.depth) * LOG2E_DF;
     }
-    float su[4] = {0, 0, 0, 0}, sv[4] = {0, 0, 0, 0}, sw[4] = {0, 0, 0, 0};
-    float cu[4] = {0, 0, 0, 0}, cv[4] = {0, 0, 0, 0}, cw[4] = {0, 0, 0, 0};
+    float su[4] = {0, 0, 0, 0}, sv[4] = {0, 0, 0, 0}, sw[4] = {0, 0, 0, 0}, sp[4] = {0, 0, 0, 0};
+    float cu[4] = {0, 0, 0, 0}, cv[4] = {0, 0, 0, 0}, cw[4] = {0, 0, 0, 0}, cp[4] = {0, 0, 0, 0};
+    const bool pres = a.nf == 4;
     for (int i0 = 0; i0 < a.ncomp; i0 += DFC) {
         __syncthreads();
         df_stage<1>(a, i0, sc);
@@ -467,6 +474,7 @@ __global__ void __launch_bounds__(256) k_df_first_levels(DfFirstArgs a) {
             df_phasor(d, dxh, dxl, dyh, dyl, th, tl, c, sn);
             const float rc = d.r * c, rs = d.r * sn;
             const float au = d.c[1] * rc, av = d.c[2] * rc, aw = d.c[3] * rs, k = d.c[0];
+            const float ap = d.c[4] * rc;
 #pragma unroll
             for (int l = 0; l < 4; l++) {
                 // cosh(k(z+h))/cosh(kh) = q (E + Y), sinh(k(z+h))/cosh(kh) = q (E - Y)
@@ -474,6 +482,7 @@ __global__ void __launch_bounds__(256) k_df_first_levels(DfFirstArgs a) {
                 df_kahan(su[l], cu[l], au * (E + Y));
                 df_kahan(sv[l], cv[l], av * (E + Y));
                 df_kahan(sw[l], cw[l], aw * (E - Y));
+                if (pres) df_kahan(sp[l], cp[l], ap * (E + Y));
             }
         }
     }
@@ -487,6 +496,7 @@ __global__ void __launch_bounds__(256) k_df_first_levels(DfFirstArgs a) {
         a.sec[o] = su[l];
         a.sec[tot + o] = sv[l];
         a.sec[2 * tot + o] = sw[l];
+        if (pres) a.sec[3 * tot + o] = sp[l];
     }
 }
 
@@ -496,8 +506,8 @@ __global__ void k_df_take(long n, int nout, const float *out, float *eta2) {
     if (q < n) eta2[q] = out[q * nout];
 }
 
-// sec[f][e] += sum_r b_r(z0[e]) Q[q][1 + 3 r + f], e = q nl + m
-__global__ void k_df_combine(long nact, int nl, int R, int nout, const float *z0, const float *out,
+// sec[f][e] += sum_r b_r(z0[e]) Q[q][1 + nf r + f], e = q nl + m
+__global__ void k_df_combine(long nact, int nl, int R, int nf, int nout, const float *z0, const float *out,
                              const float *bz, float h, float inv_dz, float *sec) {
     long e = blockIdx.x * (long)blockDim.x + threadIdx.x;
     long tot = nact * nl;
@@ -512,26 +522,29 @@ __global__ void k_df_combine(long nact, int nl, int R, int nout, const float *z0
     float w2 = -(u + 1.f) * u * (u - 2.f) * 0.5f;
     float w3 = (u + 1.f) * u * (u - 1.f) * (1.f / 6.f);
     const float *Q = out + q * nout + 1;
-    float su = 0.f, sv = 0.f, sw = 0.f;
+    float su = 0.f, sv = 0.f, sw = 0.f, sp = 0.f;
     for (int r = 0; r < R; r++) {
         const float *b = bz + (long)r * DF_NZ + i - 1;
         float br = w0 * b[0] + w1 * b[1] + w2 * b[2] + w3 * b[3];
-        su = fmaf(br, Q[3 * r], su);
-        sv = fmaf(br, Q[3 * r + 1], sv);
-        sw = fmaf(br, Q[3 * r + 2], sw);
+        su = fmaf(br, Q[nf * r], su);
+        sv = fmaf(br, Q[nf * r + 1], sv);
+        sw = fmaf(br, Q[nf * r + 2], sw);
+        if (nf == 4) sp = fmaf(br, Q[nf * r + 3], sp);
     }
     sec[e] += su;
     sec[tot + e] += sv;
     sec[2 * tot + e] += sw;
+    if (nf == 4) sec[3 * tot + e] += sp;
 }
 
 // ---------------------------------------------------------------------------
 // Host
 // ---------------------------------------------------------------------------
-int depthform_build(const Config &cfg, const DevSea &sea, DepthForm &df, void *stream_) {
+int depthform_build(const Config &cfg, const DevSea &sea, DepthForm &df, int nf, void *stream_) {
     cudaStream_t stream = (cudaStream_t)stream_;
     depthform_free(df);
-    if (sea.n < 1 || !sea.d_tab_grid || !sea.d_tab_eta) return E_NOT_INITIALIZED;
+    if (nf != 3 && nf != 4) return E_BAD_ARGUMENT;
+    if (sea.n < 1 || !sea.d_tab_grid || !sea.d_tab_eta || (nf == 4 && !sea.d_tab_gp)) return E_NOT_INITIALIZED;
     double kmax = sea.kmax;
     for (double k : cfg.k) kmax = std::max(kmax, k);
     // the pair wavenumbers |k_i +- k_m| and the diagonal 2 k are <= 2 kmax
@@ -571,7 +584,8 @@ int depthform_build(const Config &cfg, const DevSea &sea, DepthForm &df, void *s
     df.R = R;
     df.K = K;
     df.h = h;
-    df.nout = 1 + 3 * R;
+    df.nf = nf;
+    df.nout = 1 + nf * R;
     CK(cudaMalloc(&df.bz, sizeof(float) * bz.size()));
     CK(cudaMemcpyAsync(df.bz, bz.data(), sizeof(float) * bz.size(), cudaMemcpyHostToDevice, stream));
     double *d_fk = nullptr, *d_gk = nullptr, *coef = nullptr;
@@ -580,29 +594,34 @@ int depthform_build(const Config &cfg, const DevSea &sea, DepthForm &df, void *s
     CK(cudaMemcpyAsync(d_fk, fk.data(), sizeof(double) * fk.size(), cudaMemcpyHostToDevice, stream));
     CK(cudaMemcpyAsync(d_gk, gk.data(), sizeof(double) * gk.size(), cudaMemcpyHostToDevice, stream));
     const int npad = ((sea.n + TC_NPAD - 1) / TC_NPAD) * TC_NPAD;
-    const int nblk = 2 + 6 * R;
+    const int nblk = 2 + 2 * nf * R;
     CK(cudaMalloc(&coef, sizeof(double) * (size_t)nblk * npad * npad));
     DfCoefArgs a;
-    a.n = sea.n; a.npad = npad; a.ntile = sea.ntile_g; a.R = R;
-    a.tab_grid = sea.d_tab_grid; a.tab_eta = sea.d_tab_eta; a.fk = d_fk; a.gk = d_gk;
+    a.n = sea.n; a.npad = npad; a.ntile = sea.ntile_g; a.R = R; a.nf = nf;
+    a.tab_grid = sea.d_tab_grid; a.tab_eta = sea.d_tab_eta; a.tab_gp = sea.d_tab_gp; a.fk = d_fk; a.gk = d_gk;
     a.inv_dk = 1.0 / dk; a.coef = coef;
     long tot = (long)npad * npad;
     k_depth_coef<<<(unsigned)((tot + 255) / 256), 256, 0, stream>>>(a);
     note_launch();
     CK(cudaGetLastError());
     // blocks: eta (c c, s s), then per r: u (c c, s s), v (c c, s s), w (c s, s c)
+    // and, nf = 4, p (c c, s s)
     std::vector<int> bmap(3 * nblk);
     auto setb = [&](int b, int kh, int yh, int col) { bmap[3 * b] = kh; bmap[3 * b + 1] = yh; bmap[3 * b + 2] = col; };
     setb(0, 0, 0, 0);
     setb(1, 1, 1, 0);
     for (int r = 0; r < R; r++) {
-        int b = 2 + 6 * r, o = 1 + 3 * r;
+        int b = 2 + 2 * nf * r, o = 1 + nf * r;
         setb(b + 0, 0, 0, o);
         setb(b + 1, 1, 1, o);
         setb(b + 2, 0, 0, o + 1);
         setb(b + 3, 1, 1, o + 1);
         setb(b + 4, 0, 1, o + 2);
         setb(b + 5, 1, 0, o + 2);
+        if (nf == 4) {
+            setb(b + 6, 0, 0, o + 3);
+            setb(b + 7, 1, 1, o + 3);
+        }
     }
     rc = tcform_split(df.tc, coef, bmap.data(), nblk, df.nout, npad, true, stream);
     cudaFree(coef);
@@ -631,8 +650,8 @@ void depthform_free(DepthForm &df) {
     df = DepthForm();
 }
 
-// second-order sums of the columns act[0..nact) at the level heights z0:
-// eta2 [nact] and sec [3][nact nl] (+=, after the first-order sums)
+// second-order sums of the columns act[0..nact): eta2 [nact] and the basis
+// coefficients of the level sums in qout (combined by depthform_combine)
 int depthform_columns(DepthForm &df, const DevSea &sea, long nact, const double *x, const double *y,
                       const double *tdev, float *eta2, void *stream_) {
     cudaStream_t stream = (cudaStream_t)stream_;
@@ -653,14 +672,14 @@ int depthform_columns(DepthForm &df, const DevSea &sea, long nact, const double 
 }
 
 int depthform_first(const DevSea &sea, long nact, int nl, const double *xy, double t, const float *z0,
-                    double *first, float *sec, void *stream_) {
+                    double *first, float *sec, int nf, void *stream_) {
     cudaStream_t stream = (cudaStream_t)stream_;
     if (nact <= 0) return OK;
     DfFirstArgs a;
     a.n = nact; a.xy = xy; a.t = t; a.fx = sea.fx; a.fy = sea.fy;
     a.phase = sea.d_phase; a.cf = sea.d_cf; a.cstride = sea.npad_g; a.ncomp = sea.n;
     a.trivial_ramp = sea.trivial_ramp ? 1 : 0;
-    a.nl = nl; a.z0 = z0; a.depth = (float)sea.depth; a.first = first; a.sec = sec;
+    a.nl = nl; a.nf = nf; a.z0 = z0; a.depth = (float)sea.depth; a.first = first; a.sec = sec;
     if (first) {
         k_df_first_surface<<<(unsigned)((nact + 127) / 128), 128, 0, stream>>>(a);
         note_launch();
@@ -680,7 +699,8 @@ int depthform_first(const DevSea &sea, long nact, int nl, const double *xy, doub
 int depthform_combine(DepthForm &df, long nact, int nl, const float *z0, float *sec, void *stream_) {
     cudaStream_t stream = (cudaStream_t)stream_;
     long tot = nact * nl;
-    k_df_combine<<<(unsigned)((tot + 255) / 256), 256, 0, stream>>>(nact, nl, df.R, df.nout, z0, df.qout, df.bz,
+    k_df_combine<<<(unsigned)((tot + 255) / 256), 256, 0, stream>>>(nact, nl, df.R, df.nf, df.nout, z0, df.qout,
+                                                                    df.bz,
                                                                     (float)df.h,
                                                                     (float)((DF_NZ - 1) / df.h), sec);
     note_launch();

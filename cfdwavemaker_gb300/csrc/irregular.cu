@@ -47,6 +47,10 @@ namespace cfdwm {
 
 constexpr int EATA_NC = 2;    // eta table: A (cc coefficient), B (ss coefficient)
 constexpr int GRIDV_NC = 8;   // uvw table: Pu, Mu, Pv, Mv, Pw, Mw, kp, km
+// s-grid pressure tables (grid mask, rho folded): Pp, Mp of the phase terms,
+// and X, Z of the phase-free terms (products of the first-order profiles for
+// a pair, the linear diagonal terms on the diagonal entry)
+constexpr int GRIDP_NC = 2;
 constexpr int POINTV_NC = 12; // point table: Pu, Mu, Pv, Mv, Pw, Mw, Pp, Mp, kp, km, Xpp, Xzz
 constexpr float LOG2E_F = 1.4426950408889634f;
 constexpr long SPLIT_TARGET_BLOCKS = 4 * 152;   // blocks a column-pair launch aims for
@@ -91,10 +95,11 @@ __device__ __forceinline__ double pair_k2(double ki, double km, double gam) {
     return __dadd_rn(__dadd_rn(__dmul_rn(ki, ki), __dmul_rn(km, km)), __dmul_rn(__dmul_rn(2.0 * ki, km), gam));
 }
 
-// One record per (tile, entry).  mode 0: grid mask (eta + uvw tables),
-// mode 1: point-API mask (u2/v2/w2/dp2 table).
+// One record per (tile, entry).  mode 0: grid mask (eta + uvw tables, and
+// the pressure tables tab_gp / tab_gk), mode 1: point-API mask
+// (u2/v2/w2/dp2 table).
 __global__ void k_build_tables(CompIn c, int TT, int nt, int mode, float *tab_eta,
-                               float *tab_v) {
+                               float *tab_v, float *tab_gp, float *tab_gk) {
     long t = blockIdx.x;
     int I = 0;
     while (tile_index(I, nt - 1, nt) < t) I++;
@@ -102,7 +107,7 @@ __global__ void k_build_tables(CompIn c, int TT, int nt, int mode, float *tab_et
     for (int e = threadIdx.x; e < TT * TT; e += blockDim.x) {
         int ii = e / TT, mm = e % TT;
         int i = I * TT + ii, m = M * TT + mm;
-        double out[12];
+        double out[12], pr[4] = {0.0, 0.0, 0.0, 0.0};   // pr: Pp, Mp, X, Z (mode 0)
         for (int q = 0; q < 12; q++) out[q] = 0.0;
         double eA = 0.0, eB = 0.0;
         const double h = c.depth, g = c.g, gg = c.g * c.g;
@@ -127,6 +132,11 @@ __global__ void k_build_tables(CompIn c, int TT, int nt, int mode, float *tab_et
                         out[8] = 2.0 * ki;
                     } else {
                         out[6] = 2.0 * ki;
+                        // uvw2 pressure, diagonal (Irregular.cpp:1034-1037): the
+                        // 2-phi term and the two terms linear in the profiles
+                        pr[0] = c.rho * AAd * (2.0 * oi) * q2;
+                        pr[2] = -c.rho * (gg * (2.0 * ki * cti + 2.0 * ki * sti) * 2.0) / (2.0 * oi);
+                        pr[3] = c.rho * (gg * (2.0 * ki) * 2.0) / (2.0 * oi);
                         if (2.0 * ki <= c.kmax) {
                             double ann = (Dnn - (ki * ki - Rn * Rn)) / Rn + 2.0 * Rn;
                             double pe = 0.25 * Ai * Ai * ann;
@@ -174,6 +184,11 @@ __global__ void k_build_tables(CompIn c, int TT, int nt, int mode, float *tab_et
                             out[8] = kp;
                         } else {
                             out[6] = kp;
+                            // uvw2 pressure, sum term and the phase-free
+                            // products of the profiles (Irregular.cpp:1074-1077)
+                            pr[0] = c.rho * AA * BB * (oi + om) * qp;
+                            pr[2] = -c.rho * (gg * (ki * cti * km * ctm + ki * sti * km * stm)) / (oi * om);
+                            pr[3] = c.rho * (gg * (ki * km)) / (oi * om);
                             double ap = (Dp - (ki * km * gam - Rn * Rm)) / sqrt(Rn * Rm) + (Rn + Rm);
                             double pe = 0.5 * Ai * Am * ap;
                             eA += pe;
@@ -194,6 +209,7 @@ __global__ void k_build_tables(CompIn c, int TT, int nt, int mode, float *tab_et
                             out[9] = kq;
                         } else {
                             out[7] = kq;
+                            pr[1] = c.rho * AA * CC * (oi - om) * qm;   // Irregular.cpp:1093
                             double am = (Dm - (ki * km * gam + Rn * Rm)) / sqrt(Rn * Rm) + (Rn + Rm);
                             double pe = 0.5 * Ai * Am * am;
                             eA += pe;
@@ -214,6 +230,10 @@ __global__ void k_build_tables(CompIn c, int TT, int nt, int mode, float *tab_et
             tab_eta[base * EATA_NC + 0] = (float)eA;
             tab_eta[base * EATA_NC + 1] = (float)eB;
             for (int q = 0; q < GRIDV_NC; q++) tab_v[base * GRIDV_NC + q] = (float)out[q];
+            tab_gp[base * GRIDP_NC + 0] = (float)pr[0];
+            tab_gp[base * GRIDP_NC + 1] = (float)pr[1];
+            tab_gk[base * GRIDP_NC + 0] = (float)pr[2];
+            tab_gk[base * GRIDP_NC + 1] = (float)pr[3];
         } else {
             for (int q = 0; q < POINTV_NC; q++) tab_v[base * POINTV_NC + q] = (float)out[q];
         }
@@ -324,8 +344,11 @@ int sea_build(const Config &cfg, DevSea &sea, bool point_table, void *stream_) {
         size_t ent = (size_t)ntiles * GRID_TILE * GRID_TILE;
         CK(cudaMalloc(&sea.d_tab_eta, sizeof(float) * ent * EATA_NC));
         CK(cudaMalloc(&sea.d_tab_grid, sizeof(float) * ent * GRIDV_NC));
+        CK(cudaMalloc(&sea.d_tab_gp, sizeof(float) * ent * GRIDP_NC));
+        CK(cudaMalloc(&sea.d_tab_gk, sizeof(float) * ent * GRIDP_NC));
         k_build_tables<<<(unsigned)ntiles, 256, 0, stream>>>(ci, GRID_TILE, sea.ntile_g, 0,
-                                                             sea.d_tab_eta, sea.d_tab_grid);
+                                                             sea.d_tab_eta, sea.d_tab_grid, sea.d_tab_gp,
+                                                             sea.d_tab_gk);
         note_launch();
         CK(cudaGetLastError());
         if (point_table) {
@@ -333,7 +356,7 @@ int sea_build(const Config &cfg, DevSea &sea, bool point_table, void *stream_) {
             size_t entp = (size_t)ntp * POINT_TILE * POINT_TILE;
             CK(cudaMalloc(&sea.d_tab_point, sizeof(float) * entp * POINTV_NC));
             k_build_tables<<<(unsigned)ntp, 256, 0, stream>>>(ci, POINT_TILE, sea.ntile_p, 1,
-                                                              nullptr, sea.d_tab_point);
+                                                              nullptr, sea.d_tab_point, nullptr, nullptr);
             note_launch();
             CK(cudaGetLastError());
         }
@@ -359,8 +382,10 @@ void sea_free(DevSea &sea) {
     if (sea.d_tab_eta) cudaFree(sea.d_tab_eta);
     if (sea.d_tab_grid) cudaFree(sea.d_tab_grid);
     if (sea.d_tab_point) cudaFree(sea.d_tab_point);
+    if (sea.d_tab_gp) cudaFree(sea.d_tab_gp);
+    if (sea.d_tab_gk) cudaFree(sea.d_tab_gk);
     sea.d_phase = nullptr; sea.d_cf = nullptr; sea.d_tab_eta = nullptr;
-    sea.d_tab_grid = nullptr; sea.d_tab_point = nullptr;
+    sea.d_tab_grid = nullptr; sea.d_tab_point = nullptr; sea.d_tab_gp = nullptr; sea.d_tab_gk = nullptr;
 }
 
 int workspace_reserve(Workspace &ws, size_t bytes) {
@@ -439,6 +464,7 @@ struct PairArgs {
     int nlg;             // level groups per column (power of two, <= 16)
     int ntile;           // component tiles of the table
     const float *tab;    // pair tiles
+    const float2 *tabp;  // pressure pair tiles (Pp, Mp), column kernel with pressure
     const float2 *ph;    // [npad][ncol]
     const float *rr;     // [npad][ncol]
     const float *cf;     // [NCF][cstride]
@@ -462,12 +488,15 @@ __device__ __forceinline__ void depth_fg(float k, float zk, float zetak, float &
     G = e1 - t;
 }
 
-// Column mode: u, v, w at LV levels per thread, grid (pair-cache) mask.
-template <int TT, int LV>
+// Column mode: u, v, w (PR: and the phase terms of the pressure, with the
+// first-order dp1) at LV levels per thread, grid (pair-cache) mask.
+template <int TT, int LV, bool PR>
 __global__ void __launch_bounds__(128) k_pairs_columns(PairArgs a) {
     extern __shared__ float4 smem4[];
+    constexpr int NF = PR ? 4 : 3;
     float *s_tab = reinterpret_cast<float *>(smem4);                       // TT*TT*8
-    float2 *s_ph = reinterpret_cast<float2 *>(s_tab + TT * TT * GRIDV_NC); // TT*cols
+    float2 *s_tp = reinterpret_cast<float2 *>(s_tab + TT * TT * GRIDV_NC); // TT*TT (PR)
+    float2 *s_ph = s_tp + (PR ? TT * TT : 0);                             // TT*cols
     const int cols = 128 / a.nlg;
     const int lg = threadIdx.x / cols, cl = threadIdx.x % cols;
     const long col = (long)blockIdx.x * cols + cl;
@@ -479,6 +508,7 @@ __global__ void __launch_bounds__(128) k_pairs_columns(PairArgs a) {
     float zk[LV], zetak[LV], yk[LV];   // z log2(e), -2(z + h) log2(e), -(z + 2h) log2(e)
     float2 zk2[LP], yk2[LP];
     float su[LV], cu[LV], sv[LV], cv[LV], sw[LV], cw[LV];
+    float sp[PR ? LV : 1], cq[PR ? LV : 1];     // pressure sum and carry
 #pragma unroll
     for (int l = 0; l < LV; l++) {
         int lev = lg * LV + l;
@@ -487,6 +517,7 @@ __global__ void __launch_bounds__(128) k_pairs_columns(PairArgs a) {
         zetak[l] = -2.f * (z + a.depth) * LOG2E_F;
         yk[l] = -(z + 2.f * a.depth) * LOG2E_F;
         su[l] = cu[l] = sv[l] = cv[l] = sw[l] = cw[l] = 0.f;
+        if (PR) sp[l] = cq[l] = 0.f;
     }
 #pragma unroll
     for (int j = 0; j < LP; j++) {
@@ -507,6 +538,10 @@ __global__ void __launch_bounds__(128) k_pairs_columns(PairArgs a) {
                     a.tab + tile_index(I, M, a.ntile) * (long)TT * TT * GRIDV_NC);
                 float4 *dst = reinterpret_cast<float4 *>(s_tab);
                 for (int e = threadIdx.x; e < TT * TT * GRIDV_NC / 4; e += blockDim.x) dst[e] = src[e];
+                if (PR) {
+                    const float2 *srp = a.tabp + tile_index(I, M, a.ntile) * (long)TT * TT;
+                    for (int e = threadIdx.x; e < TT * TT; e += blockDim.x) s_tp[e] = srp[e];
+                }
             }
             for (int e = threadIdx.x; e < TT * cols; e += blockDim.x) {
                 int mm = e / cols, c2 = e % cols;
@@ -523,9 +558,11 @@ __global__ void __launch_bounds__(128) k_pairs_columns(PairArgs a) {
                     // packed FP32x2 over level pairs: per pair and level,
                     // E = exp(k z), Y = exp(-k(z + 2h)) = E exp(-2k(z+h)),
                     // F = E + Y, G = E - Y (the normaliser is in the record)
-                    float2 au[LP], av[LP], aw[LP];
+                    float2 au[LP], av[LP], aw[LP], apr[PR ? LP : 1];
 #pragma unroll
                     for (int j = 0; j < LP; j++) au[j] = av[j] = aw[j] = make_float2(0.f, 0.f);
+#pragma unroll
+                    for (int j = 0; j < (PR ? LP : 1); j++) apr[j] = make_float2(0.f, 0.f);
                     const float2 neg1 = make_float2(-1.f, -1.f);
                     const int m0 = (M == I) ? ii : 0;
                     for (int mm = m0; mm < TT; mm++) {
@@ -541,6 +578,13 @@ __global__ void __launch_bounds__(128) k_pairs_columns(PairArgs a) {
                         const float2 vp2 = make_float2(vp, vp), vm2 = make_float2(vm, vm);
                         const float2 wp2 = make_float2(wp, wp), wm2 = make_float2(wm, wm);
                         const float2 kp2 = make_float2(c1.z, c1.z), km2 = make_float2(c1.w, c1.w);
+                        float2 pp2 = make_float2(0.f, 0.f), pm2 = pp2;
+                        if (PR) {
+                            const float2 tp = s_tp[ii * TT + mm];
+                            const float pp = tp.x * cp, pm_ = tp.y * cmn;
+                            pp2 = make_float2(pp, pp);
+                            pm2 = make_float2(pm_, pm_);
+                        }
 #pragma unroll
                         for (int j = 0; j < LP; j++) {
                             const float2 ap = __fmul2_rn(kp2, zk2[j]), bp = __fmul2_rn(kp2, yk2[j]);
@@ -554,6 +598,7 @@ __global__ void __launch_bounds__(128) k_pairs_columns(PairArgs a) {
                             au[j] = __ffma2_rn(up2, Fp, __ffma2_rn(um2, Fm, au[j]));
                             av[j] = __ffma2_rn(vp2, Fp, __ffma2_rn(vm2, Fm, av[j]));
                             aw[j] = __ffma2_rn(wp2, Gp, __ffma2_rn(wm2, Gm, aw[j]));
+                            if (PR) apr[j] = __ffma2_rn(pp2, Fp, __ffma2_rn(pm2, Fm, apr[j]));
                         }
                     }
 #pragma unroll
@@ -564,6 +609,10 @@ __global__ void __launch_bounds__(128) k_pairs_columns(PairArgs a) {
                         kahan(sv[2 * j + 1], cv[2 * j + 1], ri * av[j].y);
                         kahan(sw[2 * j], cw[2 * j], ri * aw[j].x);
                         kahan(sw[2 * j + 1], cw[2 * j + 1], ri * aw[j].y);
+                        if (PR) {
+                            kahan(sp[2 * j], cq[2 * j], ri * apr[j].x);
+                            kahan(sp[2 * j + 1], cq[2 * j + 1], ri * apr[j].y);
+                        }
                     }
                 }
             }
@@ -578,6 +627,8 @@ __global__ void __launch_bounds__(128) k_pairs_columns(PairArgs a) {
                     const float cu_ = au_ * a.cf[CF_CT * a.cstride + m] * pm.x;
                     const float cv_ = au_ * a.cf[CF_ST * a.cstride + m] * pm.x;
                     const float cw_ = au_ * pm.y;
+                    // dp1 (Irregular.cpp:1107-1120)
+                    const float cp_ = PR ? a.cf[CF_AP * a.cstride + m] * q * rm * pm.x : 0.f;
 #pragma unroll
                     for (int l = 0; l < LV; l++) {
                         float F, G;
@@ -585,13 +636,14 @@ __global__ void __launch_bounds__(128) k_pairs_columns(PairArgs a) {
                         kahan(su[l], cu[l], cu_ * F);
                         kahan(sv[l], cv[l], cv_ * F);
                         kahan(sw[l], cw[l], cw_ * G);
+                        if (PR) kahan(sp[l], cq[l], cp_ * F);
                     }
                 }
             }
         }
     }
     if (!valid) return;
-    float *out = a.out + (long)blockIdx.y * 3 * npts;
+    float *out = a.out + (long)blockIdx.y * NF * npts;
 #pragma unroll
     for (int l = 0; l < LV; l++) {
         int lev = lg * LV + l;
@@ -600,6 +652,7 @@ __global__ void __launch_bounds__(128) k_pairs_columns(PairArgs a) {
             out[0 * npts + o] = su[l];
             out[1 * npts + o] = sv[l];
             out[2 * npts + o] = sw[l];
+            if (PR) out[3 * npts + o] = sp[l];
         }
     }
 }
@@ -889,18 +942,43 @@ long column_pairs_split_floats(int nl) {
     int nlg = 1;
     while (nlg * LV < nl) nlg *= 2;
     long cols = 128 / nlg;
-    return 3L * nl * cols * 2 * SPLIT_TARGET_BLOCKS;
+    return 4L * nl * cols * 2 * SPLIT_TARGET_BLOCKS;
 }
 
+template <bool PR>
+static int column_pairs_t(const PairArgs &a, long nblk, int nslice, int cols, cudaStream_t stream) {
+    constexpr int LV = 8;
+    auto bytes = [](int c) {
+        return sizeof(float) * GRID_TILE * GRID_TILE * GRIDV_NC + (PR ? sizeof(float2) * GRID_TILE * GRID_TILE : 0) +
+               sizeof(float2) * GRID_TILE * c;
+    };
+    static bool attr = false;
+    if (!attr) {
+        CK(cudaFuncSetAttribute(k_pairs_columns<GRID_TILE, LV, PR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)bytes(128)));
+        attr = true;
+    }
+    prof_begin(PK_COLUMN_PAIRS, stream);
+    k_pairs_columns<GRID_TILE, LV, PR><<<dim3((unsigned)nblk, (unsigned)nslice), 128, bytes(cols), stream>>>(a);
+    note_launch();
+    prof_end(PK_COLUMN_PAIRS, stream);
+    CK(cudaGetLastError());
+    return OK;
+}
+
+// u, v, w (pressure: and p) sums of the columns at their levels, out [nf][ncol nl]
 int launch_column_pairs(const DevSea &sea, long ncol, int nl, const float2 *ph, const float *rr,
                         const float *z0, float *out, int pairs, cudaStream_t stream, float *split_buf,
-                        long split_cap) {
+                        long split_cap, bool pressure) {
     constexpr int LV = 8;
     int nlg = 1;
     while (nlg * LV < nl) nlg *= 2;
     if (nlg > 16) return E_TOO_LARGE;
+    if (pressure && !sea.d_tab_gp) return E_NOT_INITIALIZED;
+    const int nf = pressure ? 4 : 3;
     PairArgs a{};
     a.ncol = ncol; a.nl = nl; a.nlg = nlg; a.ntile = sea.ntile_g; a.tab = sea.d_tab_grid;
+    a.tabp = reinterpret_cast<const float2 *>(sea.d_tab_gp);
     a.ph = ph; a.rr = rr; a.cf = sea.d_cf; a.cstride = sea.npad_g; a.z0 = z0;
     a.depth = (float)sea.depth; a.out = out; a.pairs = pairs; a.first = 1;
     int cols = 128 / nlg;
@@ -915,32 +993,145 @@ int launch_column_pairs(const DevSea &sea, long ncol, int nl, const float2 *ph, 
         int want = (int)std::min<long>(ntp, (SPLIT_TARGET_BLOCKS + nblk - 1) / nblk);
         int per = (ntp + want - 1) / want;
         int ns = (ntp + per - 1) / per;
-        if ((long)ns * 3 * ncol * nl <= split_cap && ns > 1) {
+        if ((long)ns * nf * ncol * nl <= split_cap && ns > 1) {
             nslice = ns;
             a.tp_per = per;
             a.out = split_buf;
         }
     }
-    size_t smem = sizeof(float) * GRID_TILE * GRID_TILE * GRIDV_NC + sizeof(float2) * GRID_TILE * cols;
-    static bool attr = false;
-    if (!attr) {
-        CK(cudaFuncSetAttribute(k_pairs_columns<GRID_TILE, LV>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)(sizeof(float) * GRID_TILE * GRID_TILE * GRIDV_NC +
-                                      sizeof(float2) * GRID_TILE * 128)));
-        attr = true;
-    }
-    prof_begin(PK_COLUMN_PAIRS, stream);
-    k_pairs_columns<GRID_TILE, LV><<<dim3((unsigned)nblk, (unsigned)nslice), 128, smem, stream>>>(a);
-    note_launch();
-    prof_end(PK_COLUMN_PAIRS, stream);
-    CK(cudaGetLastError());
+    int rc = pressure ? column_pairs_t<true>(a, nblk, nslice, cols, stream)
+                      : column_pairs_t<false>(a, nblk, nslice, cols, stream);
+    if (rc) return rc;
     if (nslice > 1) {
-        long n = 3 * ncol * nl;
+        long n = (long)nf * ncol * nl;
         k_sum_slices<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(n, nslice, split_buf, out);
         note_launch();
         CK(cudaGetLastError());
     }
+    return OK;
+}
+
+// ---------------------------------------------------------------------------
+// Phase-free part of the s-grid pressure (uvw2, Irregular.cpp:1036-1037 and
+// 1076-1077): at the evaluation height z0 in [-h, 0] and time t
+//   K(z) = sum_pairs r_i [X px_i(z) px_m(z) + Z pz_i(z) pz_m(z)]
+//        + sum_diag  r_i [X px_i(z) + Z pz_i(z)],
+// px = cosh(k(z+h))/cosh(kh), pz = sinh(k(z+h))/cosh(kh), rho folded into X, Z.
+// K does not depend on the column, so one ring step needs one table of K and
+// dK/dz on nz uniform heights (read by cubic Hermite interpolation) instead
+// of a second pass over the pairs per node.
+// ---------------------------------------------------------------------------
+struct KinArgs {
+    const float2 *tabk;        // grid-mask pair tiles (X, Z)
+    int ntile, ncomp, npad, trivial_ramp, zb;
+    const double *phase;       // [7][npad]: ramp parameters in rows 4..6
+    const float *cf;           // [NCF][npad]
+    double t, depth, dz;
+    int nz;
+    double *kin;               // [nz][2]: K, dK/dz
+};
+
+constexpr int KIN_ZB = 4;      // heights per block (upper bound)
+
+__global__ void __launch_bounds__(256) k_pressure_kin(KinArgs a) {
+    extern __shared__ float smk[];
+    const int np = a.npad, zb = a.zb;
+    float *s_k = smk, *s_r = smk + np, *s_px = smk + 2 * np, *s_pz = s_px + (long)zb * np;
+    const int j0 = blockIdx.x * zb;
+    for (int i = threadIdx.x; i < np; i += blockDim.x) {
+        double k = 0.0, r = 0.0;
+        if (i < a.ncomp) {
+            k = a.cf[CF_K * np + i];
+            const int ir = a.trivial_ramp ? 0 : i;
+            r = d_freq_ramp(a.t, a.phase[4 * np + ir], a.phase[5 * np + ir], a.phase[6 * np + ir]);
+        }
+        s_k[i] = (float)k;
+        s_r[i] = (float)r;
+        for (int q = 0; q < zb; q++) {
+            const double z = fmin(0.0, -a.depth + a.dz * min(j0 + q, a.nz - 1));
+            // cosh(k(z+h))/cosh(kh) and sinh(k(z+h))/cosh(kh), both bounded by 1
+            const double qn = 1.0 / (1.0 + exp(-2.0 * k * a.depth));
+            const double E = exp(k * z), Y = exp(-k * (z + 2.0 * a.depth));
+            s_px[q * np + i] = (float)(qn * (E + Y));
+            s_pz[q * np + i] = (float)(qn * (E - Y));
+        }
+    }
+    __syncthreads();
+    float sK[KIN_ZB], cK[KIN_ZB], sD[KIN_ZB], cD[KIN_ZB];
+#pragma unroll
+    for (int q = 0; q < KIN_ZB; q++) sK[q] = cK[q] = sD[q] = cD[q] = 0.f;
+    constexpr int TT = GRID_TILE;
+    int I = 0, M = 0;
+    const long ntiles = tile_index(a.ntile - 1, a.ntile - 1, a.ntile) + 1;
+    for (long t = 0; t < ntiles; t++) {
+        const float2 *tk = a.tabk + t * (long)TT * TT;
+        for (int e = threadIdx.x; e < TT * TT; e += blockDim.x) {
+            const float2 c = tk[e];
+            if (c.x == 0.f && c.y == 0.f) continue;     // filtered pair or padding
+            const int i = I * TT + e / TT, m = M * TT + e % TT;
+            const float ri = s_r[i], ki = s_k[i], km = s_k[m];
+#pragma unroll
+            for (int q = 0; q < KIN_ZB; q++) {
+                if (q >= zb) break;
+                const float pxi = s_px[q * np + i], pzi = s_pz[q * np + i];
+                float v, dv;
+                if (i == m) {
+                    v = c.x * pxi + c.y * pzi;
+                    dv = ki * (c.x * pzi + c.y * pxi);
+                } else {
+                    const float pxm = s_px[q * np + m], pzm = s_pz[q * np + m];
+                    v = c.x * pxi * pxm + c.y * pzi * pzm;
+                    dv = c.x * (ki * pzi * pxm + km * pxi * pzm) + c.y * (ki * pxi * pzm + km * pzi * pxm);
+                }
+                kahan(sK[q], cK[q], ri * v);
+                kahan(sD[q], cD[q], ri * dv);
+            }
+        }
+        if (++M == a.ntile) { ++I; M = I; }
+    }
+    // block reduction in FP64, in a fixed order
+    __shared__ double red[2][256];
+    for (int q = 0; q < zb; q++) {
+        __syncthreads();
+        red[0][threadIdx.x] = (double)sK[q] - (double)cK[q];
+        red[1][threadIdx.x] = (double)sD[q] - (double)cD[q];
+        __syncthreads();
+        for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+            if ((int)threadIdx.x < w) {
+                red[0][threadIdx.x] += red[0][threadIdx.x + w];
+                red[1][threadIdx.x] += red[1][threadIdx.x + w];
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0 && j0 + q < a.nz) {
+            a.kin[2 * (j0 + q)] = red[0][0];
+            a.kin[2 * (j0 + q) + 1] = red[1][0];
+        }
+    }
+}
+
+int launch_pressure_kin(const DevSea &sea, double t, int nz, double *kin, cudaStream_t stream) {
+    if (!sea.d_tab_gk || nz < 2) return E_NOT_INITIALIZED;
+    const int np = sea.npad_g;
+    // shared memory: k, ramp and zb rows of px, pz per component
+    const size_t cap = 200 * 1024;
+    int zb = KIN_ZB;
+    while (zb > 1 && sizeof(float) * (size_t)np * (2 + 2 * zb) > cap) zb--;
+    const size_t smem = sizeof(float) * (size_t)np * (2 + 2 * zb);
+    if (smem > cap) return E_TOO_LARGE;
+    static bool attr = false;
+    if (!attr) {
+        CK(cudaFuncSetAttribute(k_pressure_kin, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap));
+        attr = true;
+    }
+    KinArgs a;
+    a.tabk = reinterpret_cast<const float2 *>(sea.d_tab_gk);
+    a.ntile = sea.ntile_g; a.ncomp = sea.n; a.npad = np; a.trivial_ramp = sea.trivial_ramp ? 1 : 0; a.zb = zb;
+    a.phase = sea.d_phase; a.cf = sea.d_cf;
+    a.t = t; a.depth = sea.depth; a.dz = sea.depth / (nz - 1); a.nz = nz; a.kin = kin;
+    k_pressure_kin<<<(unsigned)((nz + zb - 1) / zb), 256, smem, stream>>>(a);
+    note_launch();
+    CK(cudaGetLastError());
     return OK;
 }
 

@@ -42,8 +42,12 @@ int launch_eta_pairs(const DevSea &sea, long n, const float2 *ph, const float *r
                      cudaStream_t stream, float *split_buf, long split_cap);
 int launch_column_pairs(const DevSea &sea, long ncol, int nl, const float2 *ph, const float *rr,
                         const float *z0, float *out, int pairs, cudaStream_t stream, float *split_buf,
-                        long split_cap);
+                        long split_cap, bool pressure);
 long column_pairs_split_floats(int nl);
+int launch_pressure_kin(const DevSea &sea, double t, int nz, double *kin, cudaStream_t stream);
+
+// heights of the table of the phase-free pressure terms over [-h, 0]
+constexpr int KIN_NZ = 2049;
 int launch_phasors_public(const DevSea &sea, long n, const double *x, const double *y,
                           const double *t, long sx, long sy, long st, int npad, float2 *ph,
                           float *rr, double *first, cudaStream_t stream);
@@ -74,9 +78,13 @@ __global__ void k_levels(GridGeom g, long nact, const int *act, const double *fi
     }
 }
 
+// The level sums into the slot, with the Taylor terms above swl
+// (lsgrid_spline.cpp:892-897).  With UP: the dynamic pressure
+//   dp1(z0) + rho uvw2.p(z0) + dp1_dz max(0, z - swl),
+// the phase-free part of uvw2.p from the height table kin (cubic Hermite).
 __global__ void k_scatter_levels(GridGeom g, long nact, const int *act, const double *first,
-                                 const float *sec, const float *zmax, int slot, float *UX,
-                                 float *UY, float *UZ) {
+                                 const float *sec, const float *zmin, const float *zmax, int slot,
+                                 float *UX, float *UY, float *UZ, float *UP, const double *kin, int nkz) {
     long e = blockIdx.x * (long)blockDim.x + threadIdx.x;
     long tot = nact * g.nl;
     if (e >= tot) return;
@@ -88,6 +96,17 @@ __global__ void k_scatter_levels(GridGeom g, long nact, const int *act, const do
     UX[o] = sec[0 * tot + e] + (float)first[1 * nact + q] * za;
     UY[o] = sec[1 * tot + e] + (float)first[2 * nact + q] * za;
     UZ[o] = sec[2 * tot + e] + (float)first[3 * nact + q] * za;
+    if (UP) {
+        const double dz = g.depth / (nkz - 1);
+        double t = ((double)zmin[e] + g.depth) / dz;
+        t = fmin(fmax(t, 0.0), (double)(nkz - 1));
+        int i = min((int)t, nkz - 2);
+        double r = t - i;
+        double f0 = kin[2 * i], f1 = kin[2 * i + 2], d0 = kin[2 * i + 1], d1 = kin[2 * i + 3];
+        double a = dz * d0 - (f1 - f0), b = -dz * d1 + (f1 - f0);
+        double K = f0 * (1.0 - r) + f1 * r + r * (1.0 - r) * (a * (1.0 - r) + b * r);
+        UP[o] = (float)((double)sec[3 * tot + e] + K) + (float)first[4 * nact + q] * za;
+    }
 }
 
 // All finite differences of lsgrid_spline.cpp:124-366 in one pass over the
@@ -96,15 +115,15 @@ __global__ void k_scatter_levels(GridGeom g, long nact, const int *act, const do
 struct GradArgs {
     GridGeom g;
     int tstep;
-    const float *F[4];      // ETA, UX, UY, UZ
-    float *Fx[4], *Fy[4], *Fs[4], *Ft[4];
+    const float *F[5];      // ETA, UX, UY, UZ (and the pressure)
+    float *Fx[5], *Fy[5], *Fs[5], *Ft[5];
 };
 
 __global__ void k_gradients(GradArgs a) {
     const GridGeom &g = a.g;
     long nodes = (long)g.nx * g.ny * g.nl, cols = (long)g.nx * g.ny;
     long e = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    int field = blockIdx.y;                  // 0 ETA (column nodes), 1..3 U, V, W
+    int field = blockIdx.y;                  // 0 ETA (column nodes), 1..3 U, V, W, 4 P
     int nl = field == 0 ? 1 : g.nl;
     long S = field == 0 ? cols : nodes;
     if (e >= S) return;
@@ -154,10 +173,11 @@ struct QueryArgs {
     int tid1, tid2;
     double t0;
     const float *ETA, *ETAdt, *ETAdx, *ETAdy;
-    const float *U[3], *Ut[3], *Ux[3], *Uy[3], *Us[3];
+    const float *U[4], *Ut[4], *Ux[4], *Uy[4], *Us[4];
+    int nf;
     long n;
     const double *x, *y, *z, *t;
-    double *out;    // [4][n]
+    double *out;    // [1 + nf][n]
 };
 
 __device__ __forceinline__ float herm(float f0, float f1, float d0, float d1, float h, float r) {
@@ -266,7 +286,7 @@ __global__ void __launch_bounds__(128) k_query(QueryArgs a) {
     float sd0 = modff(n0, &s0i), sd1 = modff(n1, &s1i);
     int s0 = iclamp((int)s0i, 0, g.nl - 1), s1 = iclamp((int)s1i, 0, g.nl - 1);
     a.out[p] = eta;
-    for (int f = 0; f < 3; f++)
+    for (int f = 0; f < a.nf; f++)
         a.out[(long)(f + 1) * a.n + p] = spline_velo(a, f, xp, yp, s0, s1, xd, yd, sd0, sd1, td);
 }
 
@@ -292,6 +312,7 @@ struct GridExtra {
     double *tdev = nullptr;    // the slot time, read with stride 0 by the phasor pass
     float *split = nullptr;    // slices of a split column-pair launch
     long split_cap = 0;
+    double *kin = nullptr;     // [KIN_NZ][2] phase-free pressure terms of the slot being written
     DepthForm df;              // tensor-core form of the column sums (method 1)
 };
 static std::vector<std::pair<const DevGrid *, GridExtra>> g_extra;
@@ -354,7 +375,7 @@ int grid_create(const Config &cfg, DevGrid &g, void *stream_) {
     CK(cudaMalloc(&x->xy, sizeof(double) * 2 * c));
     CK(cudaMalloc(&x->zmin, sizeof(float) * v));
     CK(cudaMalloc(&x->zmax, sizeof(float) * v));
-    CK(cudaMalloc(&x->sec, sizeof(float) * 3 * v));
+    CK(cudaMalloc(&x->sec, sizeof(float) * 4 * v));
     CK(cudaMalloc(&x->eta2, sizeof(float) * c));
     CK(cudaMalloc(&x->tdev, sizeof(double)));
     x->split_cap = column_pairs_split_floats(g.nl);
@@ -366,18 +387,19 @@ int grid_create(const Config &cfg, DevGrid &g, void *stream_) {
 void grid_free(DevGrid &g) {
     float *ptrs[] = {g.ETA, g.ETAdx, g.ETAdy, g.ETAdt};
     for (float *p : ptrs) if (p) cudaFree(p);
-    for (int f = 0; f < 3; f++) {
+    for (int f = 0; f < 4; f++) {
         float *q[] = {g.U[f], g.Ut[f], g.Ux[f], g.Uy[f], g.Us[f]};
         for (float *p : q) if (p) cudaFree(p);
         g.U[f] = g.Ut[f] = g.Ux[f] = g.Uy[f] = g.Us[f] = nullptr;
     }
+    g.nf = 3;
     if (g.IGNORE) cudaFree(g.IGNORE);
     g.ETA = g.ETAdx = g.ETAdy = g.ETAdt = nullptr;
     g.IGNORE = nullptr;
     for (auto it = g_extra.begin(); it != g_extra.end(); ++it)
         if (it->first == &g) {
             GridExtra &x = it->second;
-            void *q[] = {x.act_all, x.act_live, x.xy, x.zmin, x.zmax, x.sec, x.eta2, x.tdev, x.split};
+            void *q[] = {x.act_all, x.act_live, x.xy, x.zmin, x.zmax, x.sec, x.eta2, x.tdev, x.split, x.kin};
             for (void *p : q) if (p) cudaFree(p);
             depthform_free(x.df);
             g_extra.erase(it);
@@ -386,11 +408,13 @@ void grid_free(DevGrid &g) {
 }
 
 // Plain second-order fill of the columns act[0..nact) at time t into ring
-// slot `slot` of the arrays ETA ([slot][nx*ny]) and U[f] ([slot][nx*ny*nl]).
+// slot `slot` of the arrays ETA ([slot][nx*ny]) and U[f] ([slot][nx*ny*nl]);
+// P (or null): the pressure field, when the grid holds one.
 static int fill_cols(DevGrid &g, const DevSea &sea, Workspace &ws, const int *act, long nact, double t,
-                     float *ETA, float *const U[3], int slot, cudaStream_t stream) {
+                     float *ETA, float *const U[3], float *P, int slot, cudaStream_t stream) {
     GridExtra *x = extra(g);
     if (nact == 0) return OK;
+    const bool pres = P != nullptr && g.nf == 4;
     GridGeom G = geom(g);
     const int npad = sea.npad_g;
     const bool tc = g.method == 1 && x->df.built;
@@ -412,7 +436,7 @@ static int fill_cols(DevGrid &g, const DevSea &sea, Workspace &ws, const int *ac
     if (tc) {
         // eta1 and the Taylor gradients (float-float phases), then eta2 and the
         // 3R depth-separated quadratic forms of every column in one GEMM
-        rc = depthform_first(sea, nact, g.nl, x->xy, t, nullptr, first, nullptr, stream);
+        rc = depthform_first(sea, nact, g.nl, x->xy, t, nullptr, first, nullptr, 3, stream);
         if (!rc) rc = depthform_columns(x->df, sea, nact, x->xy, x->xy + nact, x->tdev, x->eta2, stream);
     } else {
         rc = launch_phasors_public(sea, nact, x->xy, x->xy + nact, x->tdev, 1, 1, 0, npad, ph, rr, first, stream);
@@ -426,16 +450,24 @@ static int fill_cols(DevGrid &g, const DevSea &sea, Workspace &ws, const int *ac
     if (tc) {
         // first order at the level heights, then the second order from the R
         // basis functions of the level heights
-        rc = depthform_first(sea, nact, g.nl, x->xy, t, x->zmin, nullptr, x->sec, stream);
+        // (the form holds the pressure blocks when the grid holds pressure;
+        // a fill without P leaves them unused)
+        if (pres && x->df.nf != 4) return E_NOT_INITIALIZED;
+        rc = depthform_first(sea, nact, g.nl, x->xy, t, x->zmin, nullptr, x->sec, x->df.nf, stream);
         if (!rc) rc = depthform_combine(x->df, nact, g.nl, x->zmin, x->sec, stream);
     } else {
         // first and second order per (pair, level)
-        rc = launch_column_pairs(sea, nact, g.nl, ph, rr, x->zmin, x->sec, 1, stream, x->split, x->split_cap);
+        rc = launch_column_pairs(sea, nact, g.nl, ph, rr, x->zmin, x->sec, 1, stream, x->split, x->split_cap,
+                                 pres);
     }
     if (rc) return rc;
+    if (pres) {
+        rc = launch_pressure_kin(sea, t, KIN_NZ, x->kin, stream);
+        if (rc) return rc;
+    }
     long tot = nact * g.nl;
-    k_scatter_levels<<<(unsigned)((tot + 255) / 256), 256, 0, stream>>>(G, nact, act, first, x->sec, x->zmax,
-                                                                        slot, U[0], U[1], U[2]);
+    k_scatter_levels<<<(unsigned)((tot + 255) / 256), 256, 0, stream>>>(
+        G, nact, act, first, x->sec, x->zmin, x->zmax, slot, U[0], U[1], U[2], pres ? P : nullptr, x->kin, KIN_NZ);
     note_launch();
     CK(cudaGetLastError());
     return OK;
@@ -447,13 +479,13 @@ static int fill_slot(DevGrid &g, const DevSea &sea, Workspace &ws, int slot, dou
     GridExtra *x = extra(g);
     long nact = live_only ? x->n_live : x->n_all;
     const int *act = live_only ? x->act_live : x->act_all;
-    return fill_cols(g, sea, ws, act, nact, t, g.ETA, g.U, slot, stream);
+    return fill_cols(g, sea, ws, act, nact, t, g.ETA, g.U, g.nf == 4 ? g.U[3] : nullptr, slot, stream);
 }
 
 int grid_fill_columns(DevGrid &g, const DevSea &sea, Workspace &ws, const int *act, long nact, double t,
                       float *ETA, float *const U[3], int slot, void *stream) {
     if (nact < 0 || nact > (long)g.nx * g.ny) return E_BAD_ARGUMENT;
-    return fill_cols(g, sea, ws, act, nact, t, ETA, U, slot, (cudaStream_t)stream);
+    return fill_cols(g, sea, ws, act, nact, t, ETA, U, nullptr, slot, (cudaStream_t)stream);
 }
 
 int grid_fill_slot(DevGrid &g, const DevSea &sea, Workspace &ws, int slot, double t, void *stream) {
@@ -473,12 +505,12 @@ static int gradients(DevGrid &g, cudaStream_t stream) {
     a.g = geom(g);
     a.tstep = g.tstep;
     a.F[0] = g.ETA; a.Fx[0] = g.ETAdx; a.Fy[0] = g.ETAdy; a.Fs[0] = nullptr; a.Ft[0] = g.ETAdt;
-    for (int f = 0; f < 3; f++) {
+    for (int f = 0; f < 4; f++) {
         a.F[f + 1] = g.U[f]; a.Fx[f + 1] = g.Ux[f]; a.Fy[f + 1] = g.Uy[f];
         a.Fs[f + 1] = g.Us[f]; a.Ft[f + 1] = g.Ut[f];
     }
     long nodes = (long)g.nx * g.ny * g.nl;
-    dim3 grid((unsigned)((nodes + 255) / 256), 4);
+    dim3 grid((unsigned)((nodes + 255) / 256), (unsigned)(1 + g.nf));
     prof_begin(PK_GRADIENTS, stream);
     k_gradients<<<grid, 256, 0, stream>>>(a);
     note_launch();
@@ -508,11 +540,44 @@ int grid_gradients(DevGrid &g, void *stream) { return gradients(g, (cudaStream_t
 int grid_set_method(DevGrid &g, const Config &cfg, const DevSea &sea, int method, void *stream) {
     if (method != 0 && method != 1) return E_BAD_ARGUMENT;
     GridExtra *x = extra(g);
-    if (method == 1 && !x->df.built) {
-        int rc = depthform_build(cfg, sea, x->df, stream);
+    if (method == 1 && (!x->df.built || x->df.nf != g.nf)) {
+        int rc = depthform_build(cfg, sea, x->df, g.nf, stream);
         if (rc) return rc;
     }
     g.method = method;
+    return OK;
+}
+
+int grid_set_pressure(DevGrid &g, const Config &cfg, const DevSea &sea, bool on, void *stream_) {
+    cudaStream_t stream = (cudaStream_t)stream_;
+    GridExtra *x = extra(g);
+    const int nf = on ? 4 : 3;
+    if (on && (!sea.d_tab_gp || !sea.d_tab_gk)) return E_UNSUPPORTED;   // first-order sea
+    if (nf == g.nf) return OK;
+    long v = (long)g.nx * g.ny * g.nl;
+    if (on) {
+        CK(cudaMalloc(&g.U[3], sizeof(float) * 4 * v));
+        CK(cudaMalloc(&g.Ut[3], sizeof(float) * 4 * v));
+        CK(cudaMalloc(&g.Ux[3], sizeof(float) * 2 * v));
+        CK(cudaMalloc(&g.Uy[3], sizeof(float) * 2 * v));
+        CK(cudaMalloc(&g.Us[3], sizeof(float) * 2 * v));
+        CK(cudaMemsetAsync(g.U[3], 0, sizeof(float) * 4 * v, stream));
+        CK(cudaMemsetAsync(g.Ut[3], 0, sizeof(float) * 4 * v, stream));
+        if (!x->kin) CK(cudaMalloc(&x->kin, sizeof(double) * 2 * KIN_NZ));
+    } else {
+        float *q[] = {g.U[3], g.Ut[3], g.Ux[3], g.Uy[3], g.Us[3]};
+        for (float *p : q) if (p) cudaFree(p);
+        g.U[3] = g.Ut[3] = g.Ux[3] = g.Uy[3] = g.Us[3] = nullptr;
+    }
+    g.nf = nf;
+    // the tensor-core form carries the pressure blocks only when asked to
+    if (g.method == 1) {
+        int rc = depthform_build(cfg, sea, x->df, nf, stream);
+        if (rc) return rc;
+    } else if (x->df.built) {
+        depthform_free(x->df);
+    }
+    CK(cudaStreamSynchronize(stream));
     return OK;
 }
 
@@ -542,9 +607,10 @@ int grid_query(const DevGrid &g, long n, const double *x, const double *y, const
     a.g = geom(g);
     a.tid1 = (g.tstep + 1) % 4; a.tid2 = (g.tstep + 2) % 4; a.t0 = g.t0;
     a.ETA = g.ETA; a.ETAdt = g.ETAdt; a.ETAdx = g.ETAdx; a.ETAdy = g.ETAdy;
-    for (int f = 0; f < 3; f++) {
+    for (int f = 0; f < 4; f++) {
         a.U[f] = g.U[f]; a.Ut[f] = g.Ut[f]; a.Ux[f] = g.Ux[f]; a.Uy[f] = g.Uy[f]; a.Us[f] = g.Us[f];
     }
+    a.nf = g.nf;
     a.n = n; a.x = x; a.y = y; a.z = z; a.t = t; a.out = out;
     prof_begin(PK_QUERY, stream);
     k_query<<<(unsigned)((n + 127) / 128), 128, 0, stream>>>(a);
@@ -565,8 +631,12 @@ int grid_download(const DevGrid &g, int which, double *dst, long cap, void *stre
     case 4: src = g.ETAdx; n = 2 * c; break;
     case 5: src = g.ETAdy; n = 2 * c; break;
     case 6: src = g.ETAdt; n = 4 * c; break;
+    case 23:
+        if (g.nf != 4) return E_UNSUPPORTED;
+        src = g.U[3]; n = 4 * v; break;
     default:
-        if (which >= 7 && which <= 18) {
+        if (which >= 19 && which <= 22 && g.nf != 4) return E_UNSUPPORTED;
+        if (which >= 7 && which <= 22) {
             int f = (which - 7) / 4, k = (which - 7) % 4;
             const float *arr[4] = {g.Ut[f], g.Ux[f], g.Uy[f], g.Us[f]};
             src = arr[k];

@@ -1144,6 +1144,7 @@ int surrogate_step(const Config &cfg, const DevSea &sea, DevGrid &g, Workspace &
     mode &= 3;
     if (mode != 0 && !s.ready) return E_NOT_INITIALIZED;
     if (mode > 2 || nsample < 0 || nsample > 4096) return E_BAD_ARGUMENT;
+    if (mode != 0 && g.nf != 3) return E_UNSUPPORTED;   // the network predicts no pressure
     if (mode != 0) {
         int rc = attach_grid(s, g, st);
         if (rc) return rc;

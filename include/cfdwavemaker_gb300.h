@@ -152,7 +152,8 @@ CFDWM_EXPORT long cfdwm_npairs(void);
 CFDWM_EXPORT int cfdwm_components(double *dst);
 /* s-grid arrays (numbering of the reference's lsGridSpline members: 0 ETA,
  * 1-3 UX UY UZ, 4 ETAdx, 5 ETAdy, 6 ETAdt, 7+4f+q with q = dt, dx, dy, ds of
- * field f); returns the element count (dst may be NULL). */
+ * field f; with the pressure field (cfdwm_sgrid_pressure): 19-22 its dt, dx,
+ * dy, ds and 23 the field); returns the element count (dst may be NULL). */
 CFDWM_EXPORT long cfdwm_sgrid_array(int which, double *dst, long cap);
 CFDWM_EXPORT int cfdwm_sgrid_state(double *t0, int *tstep);
 /* Regular-wave solution: k, c, mean velocity, Bernoulli R, L, T, then B_j
@@ -212,6 +213,21 @@ CFDWM_EXPORT int cfdwm_sgrid_method(int method, int *rank);
 /* Host-only check of the depth basis for wavenumbers up to K and depth h:
  * R and the max reconstruction error over a test set of (k, z). */
 CFDWM_EXPORT int cfdwm_depth_basis(double K, double h, int *rank, double *err);
+/* Dynamic pressure on the s-grid ring (new; the reference's grid stores
+ * none: lsgrid_spline.cpp:892-897 computes uvw2's pressure and drops it, and
+ * wave_DynPres / wave_nhPres return 0.0 for wave type 5).  on = 1 adds a
+ * fourth field to the ring, at every node
+ *   dp1(z0) + rho uvw2.p(z0) + dp1_dz max(0, z - swl),  z0 = min(0, z)
+ * (Irregular.cpp:1107-1120, 975-1102, 1142-1155; the velocities' own
+ * convention, lsgrid_spline.cpp:889-897), with its finite-difference
+ * gradients, and wave_DynPres / wave_nhPres (and their batched forms) then
+ * return ramp * p and ramp * (p - rho g eta) from the spline query, as for
+ * the irregular sea (CFDwavemaker.cpp:1807-1808, 1826-1830).  on = 0 removes
+ * it (the default).  The ring is refilled at the current t0 (tstep restarts
+ * at 0).  Not combined with the learned update (Part 5): either call
+ * refuses while the other is on.  Returns 0, -2 (no s-grid model, a
+ * first-order sea, or the learned update on) or another status. */
+CFDWM_EXPORT int cfdwm_sgrid_pressure(int on);
 
 /* ===========================================================================
  * Part 5 -- learned s-grid update (new; no counterpart in the reference).

@@ -67,6 +67,8 @@ def lib():
         L.orc_sgrid_check_time.restype = C.c_int
         L.orc_sgrid_check_time.argtypes = [C.c_void_p, C.c_double]
         L.orc_sgrid_query.argtypes = [C.c_void_p, C.c_long, _dp, _dp, _dp, _dp, _dp, C.c_int]
+        L.orc_sgrid_query5.argtypes = [C.c_void_p, C.c_long, _dp, _dp, _dp, _dp, _dp, C.c_int]
+        L.orc_sgrid_set_pressure.argtypes = [C.c_void_p, C.c_int]
         L.orc_sgrid_array.restype = C.c_long
         L.orc_sgrid_array.argtypes = [C.c_void_p, C.c_int, _dp]
         L.orc_sgrid_state.argtypes = [C.c_void_p, _dp, C.POINTER(C.c_int)]
@@ -156,13 +158,16 @@ def ramp(cfg, x, y, t):
 class Sgrid:
     """lsGridSpline restatement (orc_sgrid) driven by a Sea."""
 
-    def __init__(self, cfg: dict, sea: Sea, nthreads=0, init=True):
+    def __init__(self, cfg: dict, sea: Sea, nthreads=0, init=True, pressure=False):
         g = cfg["lsgrid"]
         self.cfg, self.sea = cfg, sea
         d, dp = _arr(g["domain"])
         di, dip = _arr(g["domain_ignore"])
         self.h = lib().orc_sgrid_create(g["nx"], g["ny"], g["nl"], dp, dip, g["t0"], g["dt"],
                                         g["tan_a"], g["tan_b"], cfg["depth"], cfg["swl"])
+        self.pressure = bool(pressure)
+        if pressure:
+            lib().orc_sgrid_set_pressure(self.h, 1)
         if init:
             lib().orc_sgrid_init(self.h, sea.h, int(g["ignore_at_init"]), nthreads)
 
@@ -184,9 +189,11 @@ class Sgrid:
         lib().orc_sgrid_update_columns(self.h, self.sea.h, float(t), int(c0), int(c1), nthreads)
 
     def query(self, x, y, z, t, nthreads=0):
+        """[n][4] eta, u, v, w; with the pressure field [n][5] (and p)."""
         n, p, keep = _pts(x, y, z, t)
-        out = np.zeros((n, 4))
-        lib().orc_sgrid_query(self.h, n, p[0], p[1], p[2], p[3], out.ctypes.data_as(_dp), nthreads)
+        out = np.zeros((n, 5 if self.pressure else 4))
+        fn = lib().orc_sgrid_query5 if self.pressure else lib().orc_sgrid_query
+        fn(self.h, n, p[0], p[1], p[2], p[3], out.ctypes.data_as(_dp), nthreads)
         return out
 
     def array(self, which):

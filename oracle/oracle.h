@@ -88,13 +88,21 @@ int orc_sgrid_check_time(const orc_sgrid *g, double t);
 /* get_kinematics_at_point (lsgrid_spline.cpp:505-605): out [n][4]. */
 void orc_sgrid_query(const orc_sgrid *g, long n, const double *x, const double *y,
                      const double *z, const double *t, double *out, int nthreads);
+/* Dynamic pressure on the ring (extension of the reference's grid): before
+ * orc_sgrid_init, on = 1 adds the field dp1(z0) + rho uvw2.p(z0) +
+ * dp1_dz max(0, z - swl) at every node, with its gradients. */
+void orc_sgrid_set_pressure(orc_sgrid *g, int on);
+/* The query with the pressure: out [n][5] = eta, u, v, w, p. */
+void orc_sgrid_query5(const orc_sgrid *g, long n, const double *x, const double *y,
+                      const double *z, const double *t, double *out, int nthreads);
 /* Column-subset update for the CPU baseline: only columns [c0, c1) of the
  * flattened (i*ny+j) order are computed, into the next ring slot. */
 void orc_sgrid_update_columns(orc_sgrid *g, const orc_sea *s, double t, long c0, long c1,
                               int nthreads);
 /* Raw access to the grid arrays for tests.  which: 0 ETA, 1 UX, 2 UY, 3 UZ,
  * 4 ETAdx, 5 ETAdy, 6 ETAdt, 7 Udt, 8 Udx, 9 Udy, 10 Uds, 11 Vdt, 12 Vdx,
- * 13 Vdy, 14 Vds, 15 Wdt, 16 Wdx, 17 Wdy, 18 Wds, 19 IGNORE (as double). */
+ * 13 Vdy, 14 Vds, 15 Wdt, 16 Wdx, 17 Wdy, 18 Wds, 19 IGNORE (as double);
+ * with the pressure: 20 PP, 21 Pdt, 22 Pdx, 23 Pdy, 24 Pds. */
 long orc_sgrid_array(const orc_sgrid *g, int which, double *dst);
 void orc_sgrid_state(const orc_sgrid *g, double *t0, int *tstep);
 

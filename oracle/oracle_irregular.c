@@ -512,3 +512,6 @@ double orc__phi1_dxdz(const orc_sea *s, double t, double x, double y) { return p
 double orc__phi1_dydz(const orc_sea *s, double t, double x, double y) { return phi1_dydz(s, t, x, y); }
 double orc__phi1_dzdz(const orc_sea *s, double t, double x, double y) { return phi1_dzdz(s, t, x, y); }
 double orc__swl(const orc_sea *s) { return s->swl; }
+double orc__dp1(const orc_sea *s, double t, double x, double y, double z) { return dp1(s, t, x, y, z); }
+double orc__dp1_dz(const orc_sea *s, double t, double x, double y) { return dp1_dz(s, t, x, y); }
+double orc__rho(const orc_sea *s) { return s->rho; }

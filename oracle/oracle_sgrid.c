@@ -19,6 +19,9 @@ double orc__w1(const orc_sea *s, double t, double x, double y, double z);
 double orc__phi1_dxdz(const orc_sea *s, double t, double x, double y);
 double orc__phi1_dydz(const orc_sea *s, double t, double x, double y);
 double orc__phi1_dzdz(const orc_sea *s, double t, double x, double y);
+double orc__dp1(const orc_sea *s, double t, double x, double y, double z);
+double orc__dp1_dz(const orc_sea *s, double t, double x, double y);
+double orc__rho(const orc_sea *s);
 
 struct orc_sgrid {
     int nx, ny, nl;
@@ -29,6 +32,11 @@ struct orc_sgrid {
     double *ETA, *UX, *UY, *UZ, *ETAdx, *ETAdy, *ETAdt;
     double *Udt, *Udx, *Udy, *Uds, *Vdt, *Vdx, *Vdy, *Vds, *Wdt, *Wdx, *Wdy, *Wds;
     int *IGNORE;
+    /* dynamic pressure on the ring (an extension: the reference's grid keeps
+     * no pressure; its update computes uvw2.p, lsgrid_spline.cpp:892, and
+     * drops it) */
+    int pressure;
+    double *PP, *Pdt, *Pdx, *Pdy, *Pds;
 };
 
 static double dmin(double a, double b) { return a < b ? a : b; }
@@ -76,10 +84,21 @@ orc_sgrid *orc_sgrid_create(int nx, int ny, int nl, const double domain[4],
 void orc_sgrid_free(orc_sgrid *g) {
     if (!g) return;
     double *a[] = {g->ETA, g->UX, g->UY, g->UZ, g->ETAdx, g->ETAdy, g->ETAdt, g->Udt, g->Udx,
-                   g->Udy, g->Uds, g->Vdt, g->Vdx, g->Vdy, g->Vds, g->Wdt, g->Wdx, g->Wdy, g->Wds};
+                   g->Udy, g->Uds, g->Vdt, g->Vdx, g->Vdy, g->Vds, g->Wdt, g->Wdx, g->Wdy, g->Wds,
+                   g->PP, g->Pdt, g->Pdx, g->Pdy, g->Pds};
     for (size_t i = 0; i < sizeof(a) / sizeof(a[0]); i++) free(a[i]);
     free(g->IGNORE);
     free(g);
+}
+
+void orc_sgrid_set_pressure(orc_sgrid *g, int on) {
+    size_t v = (size_t)g->nx * g->ny * g->nl;
+    g->pressure = on ? 1 : 0;
+    if (on && !g->PP) {
+        g->PP = calloc(4 * v, sizeof(double)); g->Pdt = calloc(4 * v, sizeof(double));
+        g->Pdx = calloc(2 * v, sizeof(double)); g->Pdy = calloc(2 * v, sizeof(double));
+        g->Pds = calloc(2 * v, sizeof(double));
+    }
 }
 
 /* z2s/s2z/cart2sigmaS/sigmaS2cart, lsgrid_spline.cpp:91-122 */
@@ -112,6 +131,10 @@ static void fill_column(orc_sgrid *g, const orc_sea *s, int tt, int i, int j, do
         g->UX[id] = orc__u1(s, t, xp, yp, zmin) + o[0] + gx * zmax;
         g->UY[id] = orc__v1(s, t, xp, yp, zmin) + o[1] + gy * zmax;
         g->UZ[id] = orc__w1(s, t, xp, yp, zmin) + o[2] + gz * zmax;
+        /* the pressure with the velocities' convention: dp1 + rho uvw2.p at
+         * zmin, the Taylor term dp1_dz above swl (Irregular.cpp:1107-1155) */
+        if (g->pressure)
+            g->PP[id] = orc__dp1(s, t, xp, yp, zmin) + orc__rho(s) * o[3] + orc__dp1_dz(s, t, xp, yp) * zmax;
     }
 }
 
@@ -170,6 +193,10 @@ static void all_gradients(orc_sgrid *g) {
     grad_dt(g, g->UY, g->Vdt, v);
     grad_space(g, g->UZ, g->Wdx, g->Wdy, g->Wds, g->nl);
     grad_dt(g, g->UZ, g->Wdt, v);
+    if (g->pressure) {
+        grad_space(g, g->PP, g->Pdx, g->Pdy, g->Pds, g->nl);
+        grad_dt(g, g->PP, g->Pdt, v);
+    }
 }
 
 void orc_sgrid_init(orc_sgrid *g, const orc_sea *s, int with_ignore, int nthreads) {
@@ -328,6 +355,9 @@ static void query_one(const orc_sgrid *g, double tpt, double xpt, double ypt, do
     o[1] = spline_velo(g, g->UX, g->Udt, g->Udx, g->Udy, g->Uds, xp, yp, s0, s1, xd, yd, sd0, sd1, td, tid1, tid2);
     o[2] = spline_velo(g, g->UY, g->Vdt, g->Vdx, g->Vdy, g->Vds, xp, yp, s0, s1, xd, yd, sd0, sd1, td, tid1, tid2);
     o[3] = spline_velo(g, g->UZ, g->Wdt, g->Wdx, g->Wdy, g->Wds, xp, yp, s0, s1, xd, yd, sd0, sd1, td, tid1, tid2);
+    if (g->pressure)
+        o[4] = spline_velo(g, g->PP, g->Pdt, g->Pdx, g->Pdy, g->Pds, xp, yp, s0, s1, xd, yd, sd0, sd1, td, tid1,
+                           tid2);
 }
 
 void orc_sgrid_query(const orc_sgrid *g, long n, const double *x, const double *y,
@@ -336,7 +366,25 @@ void orc_sgrid_query(const orc_sgrid *g, long n, const double *x, const double *
     if (nthreads <= 0) nthreads = omp_get_max_threads();
 #pragma omp parallel for schedule(static) num_threads(nthreads)
 #endif
-    for (long p = 0; p < n; p++) query_one(g, t[p], x[p], y[p], z[p], out + 4 * p);
+    for (long p = 0; p < n; p++) {
+        double o[5];
+        query_one(g, t[p], x[p], y[p], z[p], o);
+        for (int q = 0; q < 4; q++) out[4 * p + q] = o[q];
+    }
+    (void)nthreads;
+}
+
+void orc_sgrid_query5(const orc_sgrid *g, long n, const double *x, const double *y,
+                      const double *z, const double *t, double *out, int nthreads) {
+#ifdef _OPENMP
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+#endif
+    for (long p = 0; p < n; p++) {
+        double o[5] = {0, 0, 0, 0, 0};
+        query_one(g, t[p], x[p], y[p], z[p], o);
+        for (int q = 0; q < 5; q++) out[5 * p + q] = o[q];
+    }
     (void)nthreads;
 }
 
@@ -367,6 +415,13 @@ long orc_sgrid_array(const orc_sgrid *g, int which, double *dst) {
     case 19:
         if (dst) for (size_t i = 0; i < c; i++) dst[i] = g->IGNORE[i];
         return (long)c;
+    case 20: case 21: case 22: case 23: case 24: {
+        if (!g->pressure) return -1;
+        const double *pa[5] = {g->PP, g->Pdt, g->Pdx, g->Pdy, g->Pds};
+        src = pa[which - 20];
+        n = (which <= 21 ? 4 : 2) * v;
+        break;
+    }
     default: return -1;
     }
     if (dst) memcpy(dst, src, n * sizeof(double));

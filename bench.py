@@ -820,6 +820,16 @@ def run_ours(args):
         torch.cuda.synchronize()
         res["pressure_ms"] = allmax(ws, ep0.elapsed_time(ep1) / args.steps)
         assert lib.cfdwm_sgrid_pressure(0) == 0, cw.last_error()
+        # .vtu export of the ring (lsGridSpline::export_vtu layout), host formatting
+        vpath = os.path.join(work, "ring.vtu")
+        tv = []
+        for _ in range(3):
+            tw0 = time.perf_counter()
+            assert lib.cfdwm_sgrid_write_vtu(vpath.encode(), 0) == 0, cw.last_error()
+            tv.append(time.perf_counter() - tw0)
+        res["vtu_s"] = float(np.median(tv))
+        res["vtu_bytes"] = os.path.getsize(vpath)
+        os.remove(vpath)
     res.update(depth_rank=depth_rank)
     res.update(ms=ms, e2e_s=te, units=units, launches=launches, init_s=init_s, h2d=h2d, d2h=d2h,
                clocks=clocks, ws=ws, rank=rank, prof=prof, npairs=int(lib.cfdwm_npairs()),
@@ -894,6 +904,25 @@ def traffic_from_profiles(kernel):
             return v.get("bytes_per_launch") if isinstance(v, dict) else v
     except (OSError, ValueError):
         return None
+
+
+def vtu_cpu_baseline(n):
+    """The oracle's single-threaded restatement of export_vtu (the reference's
+    fprintf loop) on an n x n x 16 grid of the same shape.  Its arrays are not
+    filled (zeros print shorter than the ring's values), so the time is a lower
+    bound of the reference's."""
+    from oracle import waveinput
+    import oracle
+    cfg = waveinput.read_text(sgrid_config(n, n))
+    og = oracle.Sgrid(cfg, oracle.Sea(cfg), init=False)
+    path = os.path.join(tempfile.mkdtemp(), "ring.vtu")
+    t0 = time.perf_counter()
+    og.export_vtu(path)
+    dt = time.perf_counter() - t0
+    size = os.path.getsize(path)
+    os.remove(path)
+    return {"s": dt, "MB": size / 1e6, "kind": "port", "cores": 1,
+            "sample": "the same grid shape with unfilled (zero) arrays: a lower bound"}
 
 
 def cpu_baseline(args, budget_s=15.0):
@@ -1036,6 +1065,11 @@ def main():
         "kernels": r["prof"],
         "peaks_source": src,
     }
+    if "vtu_s" in r:
+        line["vtu_export"] = {"s": r["vtu_s"], "MB": r["vtu_bytes"] / 1e6,
+                              "MB_per_s": r["vtu_bytes"] / 1e6 / r["vtu_s"], "threads": os.cpu_count()}
+        if not args.no_cpu_baseline:
+            line["vtu_export"]["cpu_baseline"] = vtu_cpu_baseline(args.grid)
     if "pressure_ms" in r:
         line["with_pressure"] = {"ms_per_step": r["pressure_ms"],
                                  "nodes_per_s": r["units"] * n / (r["pressure_ms"] / 1e3),

@@ -166,6 +166,8 @@ def load(path: str | None = None):
     L.cfdwm_depth_basis.argtypes = [_d, _d, ip, _dp]
     L.cfdwm_sgrid_pressure.restype = C.c_int
     L.cfdwm_sgrid_pressure.argtypes = [C.c_int]
+    L.cfdwm_sgrid_write_vtu.restype = C.c_int
+    L.cfdwm_sgrid_write_vtu.argtypes = [C.c_char_p, C.c_int]
     L.cfdwm_surrogate_set_carry.restype = C.c_int
     L.cfdwm_surrogate_set_carry.argtypes = [_d]
     L.cfdwm_surrogate_stats.restype = C.c_int

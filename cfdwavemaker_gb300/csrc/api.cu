@@ -413,6 +413,9 @@ int initialize_from_text(const std::string &text) {
             }
             if (!rc) rc = grid_initialize(M.grid, M.sea, M.grid_ws, s);
             if (rc) { free_model(); return rc; }
+            // [lsgrid2vtk]: the initial ring (lsgrid_spline.cpp:746-748, 837-839)
+            if (cfg.lsgrid.dump_vtk && grid_dump_vtu(M.grid, false, s) != OK)
+                std::fprintf(stderr, "cfdwavemaker_gb300: could not write the .vtu file\n");
         }
     } else {
         rc = regular_build(cfg, M.reg, s);
@@ -472,6 +475,11 @@ int cfdwm_initialize_text(const char *text) {
 
 int wave_Cleanup(void) {
     std::lock_guard<std::mutex> lk(g_model_mtx);
+    // the reference's grid writes the slot after the base slot when it is
+    // destroyed (lsgrid_spline.h:25-28)
+    Model &M = g_model;
+    if (M.init && M.cfg.wavetype == WT_IRR_SGRID && M.cfg.lsgrid.dump_vtk)
+        grid_dump_vtu(M.grid, true, stream_of());
     free_model();
     return 0;
 }
@@ -524,6 +532,8 @@ void wave_force_update(double t) {
         } else if (grid_update(M.grid, M.sea, M.grid_ws, s) != OK) {
             break;
         }
+        // [lsgrid2vtk]: every updated ring (lsgrid_spline.cpp:924-926)
+        if (M.cfg.lsgrid.dump_vtk) grid_dump_vtu(M.grid, false, s);
     }
     cudaStreamSynchronize(s);
 }
@@ -902,6 +912,16 @@ int cfdwm_sgrid_method(int method, int *rank) {
 }
 
 int cfdwm_depth_basis(double K, double h, int *rank, double *err) { return depthform_basis_info(K, h, rank, err); }
+
+int cfdwm_sgrid_write_vtu(const char *path, int last) {
+    std::lock_guard<std::mutex> lk(g_model_mtx);
+    if (!sgrid_loaded()) return E_UNSUPPORTED;
+    if (!path) return E_BAD_ARGUMENT;
+    const DevGrid &g = g_model.grid;
+    int rc = grid_write_vtu(g, path, g.cfg.vtk_timelabel, last != 0, stream_of());
+    if (rc) set_error(std::string("s-grid: cannot write ") + path);
+    return rc;
+}
 
 int cfdwm_sgrid_pressure(int on) {
     std::lock_guard<std::mutex> lk(g_model_mtx);

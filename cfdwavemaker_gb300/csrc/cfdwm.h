@@ -54,6 +54,9 @@ struct LsgridCfg {
     double t0 = 0.0, dt = 0.1, tan_a = 0.0, tan_b = 0.0;
     double domain_ignore[4] = {1.e12, -1.e12, 1.e12, -1.e12};
     bool ignore_domain = false, ignore_at_init = false, init_only = false;
+    // [lsgrid2vtk] (defaults of lsgrid_spline.h:58-61)
+    bool dump_vtk = false;
+    std::string vtk_path = "./", vtk_prefix = "kinematics", vtk_timelabel = "TimeValue";
 };
 
 struct Config {
@@ -223,6 +226,13 @@ bool grid_check_time(const DevGrid &g, double t);
 int grid_query(const DevGrid &g, long n, const double *x, const double *y, const double *z,
                const double *t, double *out, void *stream);
 int grid_download(const DevGrid &g, int which, double *dst, long cap, void *stream);
+// .vtu export of the ring's base slot (last: the slot after it), as
+// lsGridSpline::export_vtu (lsgrid_spline.cpp:1222-1403) writes it, to `path`.
+int grid_write_vtu(const DevGrid &g, const std::string &path, const std::string &timelabel, bool last,
+                   void *stream);
+// The reference's write_vtk (lsgrid_spline.cpp:1200-1219): the file
+// <vtk_path><vtk_prefix><tstep %05d>.vtu, creating the directory if needed.
+int grid_dump_vtu(const DevGrid &g, bool last, void *stream);
 // Plain fill of a column subset into ring slot `slot` of the given arrays
 // (the grid's own ETA/U or a scratch copy with the same layout).
 int grid_fill_columns(DevGrid &g, const DevSea &sea, Workspace &ws, const int *act, long nact, double t,

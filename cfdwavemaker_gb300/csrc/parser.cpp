@@ -229,8 +229,24 @@ int parse_waveinput_text(const std::string &raw, Config &cfg) {
             }
             cfg.property_read = true;
         }
+        if (line == "[lsgrid2vtk]") {
+            // .vtu output of the s-grid (CFDwavemaker.cpp:1205-1245); the
+            // [lsgrid] section must come first
+            if (cfg.wavetype != WT_IRR_SGRID)
+                return fail(cfg, "VTK output only works in combination with LSgrid");
+            LsgridCfg &g = cfg.lsgrid;
+            g.dump_vtk = true;
+            while (!f.eof) {
+                line = trim(f.get());
+                auto t = tokens(line);
+                if (starts(line, "storage_path") && t.size() > 1) g.vtk_path = t[1];
+                if (starts(line, "filename") && t.size() > 1) g.vtk_prefix = t[1];
+                if (starts(line, "vtk_timelabel") && t.size() > 1) g.vtk_timelabel = t[1];
+                if (starts(line, "[")) { skip = true; break; }
+            }
+        }
         if (line == "[wave input piston]" || line == "[sloping water]" ||
-            line == "[wave input swd]" || line == "[lsgrid2vtk]" || line == "[wave input vtk]") {
+            line == "[wave input swd]" || line == "[wave input vtk]") {
             // Recognised sections of paths this build does not serve; their
             // keywords are consumed so that parsing continues.
             while (!f.eof) {

@@ -132,6 +132,17 @@ def write_irregular(path, comps, depth, *, extrap=2, bandwidth=None, cutoff=None
         if lsgrid.get("ignore_at_init"):
             L.append("ignore_at_init 1")
         L.append("")
+        if lsgrid.get("vtk"):
+            # .vtu output of the grid: {"path": dir (with trailing /), "prefix": ..., "label": ...}
+            v = lsgrid["vtk"]
+            L.append("[lsgrid2vtk]")
+            if "path" in v:
+                L.append("storage_path %s" % v["path"])
+            if "prefix" in v:
+                L.append("filename %s" % v["prefix"])
+            if "label" in v:
+                L.append("vtk_timelabel %s" % v["label"])
+            L.append("")
     text = "\n".join(L) + "\n"
     if path is not None:
         d = os.path.dirname(os.path.abspath(path))

@@ -228,6 +228,16 @@ CFDWM_EXPORT int cfdwm_depth_basis(double K, double h, int *rank, double *err);
  * refuses while the other is on.  Returns 0, -2 (no s-grid model, a
  * first-order sea, or the learned update on) or another status. */
 CFDWM_EXPORT int cfdwm_sgrid_pressure(int on);
+/* .vtu file of the s-grid ring as lsGridSpline::export_vtu writes it
+ * (lsgrid_spline.cpp:1222-1403): the base slot at t0 (last = 0) or the slot
+ * after it at t0 + dt (last = 1), velocities as point data, node positions
+ * from that slot's elevation, hexahedral cells; the time label of the
+ * [lsgrid2vtk] section.  With a [lsgrid2vtk] section in waveinput.dat the
+ * library writes <storage_path><filename><tstep %05d>.vtu itself, as the
+ * reference does: after the initial fill, after every ring update and, with
+ * last = 1, at wave_Cleanup (the reference at its exit).  Returns 0, -2 (no
+ * s-grid model) or -5 (the file cannot be written). */
+CFDWM_EXPORT int cfdwm_sgrid_write_vtu(const char *path, int last);
 
 /* ===========================================================================
  * Part 5 -- learned s-grid update (new; no counterpart in the reference).

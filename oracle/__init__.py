@@ -69,6 +69,8 @@ def lib():
         L.orc_sgrid_query.argtypes = [C.c_void_p, C.c_long, _dp, _dp, _dp, _dp, _dp, C.c_int]
         L.orc_sgrid_query5.argtypes = [C.c_void_p, C.c_long, _dp, _dp, _dp, _dp, _dp, C.c_int]
         L.orc_sgrid_set_pressure.argtypes = [C.c_void_p, C.c_int]
+        L.orc_sgrid_export_vtu.restype = C.c_int
+        L.orc_sgrid_export_vtu.argtypes = [C.c_void_p, C.c_char_p, C.c_int, C.c_char_p]
         L.orc_sgrid_array.restype = C.c_long
         L.orc_sgrid_array.argtypes = [C.c_void_p, C.c_int, _dp]
         L.orc_sgrid_state.argtypes = [C.c_void_p, _dp, C.POINTER(C.c_int)]
@@ -195,6 +197,11 @@ class Sgrid:
         fn = lib().orc_sgrid_query5 if self.pressure else lib().orc_sgrid_query
         fn(self.h, n, p[0], p[1], p[2], p[3], out.ctypes.data_as(_dp), nthreads)
         return out
+
+    def export_vtu(self, path, last=False, label="TimeValue"):
+        """lsGridSpline::export_vtu into the file `path`."""
+        if lib().orc_sgrid_export_vtu(self.h, str(path).encode(), int(bool(last)), label.encode()) != 0:
+            raise OSError("cannot write " + str(path))
 
     def array(self, which):
         n = lib().orc_sgrid_array(self.h, which, None)

@@ -6,6 +6,7 @@
  */
 #include "oracle.h"
 #include <math.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
@@ -426,6 +427,91 @@ long orc_sgrid_array(const orc_sgrid *g, int which, double *dst) {
     }
     if (dst) memcpy(dst, src, n * sizeof(double));
     return (long)n;
+}
+
+/* export_vtu, lsgrid_spline.cpp:1222-1403: ASCII VTK UnstructuredGrid of the
+ * base slot (last = 0) or the slot after it (last = 1). */
+static void vtu_cells_tail(FILE *fp, long ncell, int per, const char *type) {
+    fputs("\t\t\t\t </DataArray>\n", fp);
+    fputs("\t\t\t\t <DataArray type=\"Int64\" Name=\"offsets\" format=\"ascii\">\n", fp);
+    for (long q = 1; q < ncell + 1; q++) fprintf(fp, "%d \n", (int)(q * per));
+    fputs("\t\t\t\t </DataArray>\n", fp);
+    fputs("\t\t\t\t <DataArray type=\"UInt8\" Name=\"types\" format=\"ascii\">\n", fp);
+    for (long q = 1; q < ncell + 1; q++) fprintf(fp, "%s \n", type);
+}
+
+int orc_sgrid_export_vtu(const orc_sgrid *g, const char *path, int last, const char *label) {
+    FILE *fp = fopen(path, "w");
+    if (!fp) return -1;
+    int nx = g->nx, ny = g->ny, nl = g->nl;
+    double tv = last ? g->t0 + g->dt : g->t0;
+    fputs("<?xml version=\"1.0\"?>\n"
+          "<VTKFile type=\"UnstructuredGrid\" version=\"1.0\" byte_order=\"LittleEndian\" header_type=\"UInt64\">\n", fp);
+    fputs("\t <UnstructuredGrid>\n", fp);
+    fprintf(fp, "\t\t <FieldData> \n");
+    fprintf(fp, "\t\t\t <DataArray type = \"Float64\" Name = \"%s\" NumberOfTuples = \"1\" format = \"ascii\" "
+                "RangeMin = \"%.3f\" RangeMax = \"%.3f\"> \n", label, tv, tv);
+    fprintf(fp, "\t\t\t %.3f \n", tv);
+    fprintf(fp, "\t\t\t </DataArray > \n");
+    fprintf(fp, "\t\t </FieldData> \n");
+    fprintf(fp, "\t\t <Piece NumberOfPoints=\"%d\" NumberOfCells=\"%d\">\n", nx * ny * nl,
+            (nx > 1 ? nx - 1 : 1) * (ny > 1 ? ny - 1 : 1) * (nl > 1 ? nl - 1 : 1));
+    fputs("\t\t\t <PointData Scalars=\"scalars\">\n", fp);
+    fprintf(fp, "\t\t\t\t <DataArray type=\"Float64\" NumberOfComponents=\"3\" Name=\"Velocity\" format=\"ascii\">\n");
+    int tt = last ? (g->tstep + 2) % 4 : (g->tstep + 1) % 4;
+    size_t b = (size_t)tt * nx * ny * nl;
+    for (size_t e = 0; e < (size_t)nx * ny * nl; e++)
+        fprintf(fp, "%g %g %g\n", g->UX[b + e], g->UY[b + e], g->UZ[b + e]);
+    fputs("\t\t\t\t </DataArray>\n", fp);
+    fputs("\t\t\t </PointData>\n", fp);
+    fputs("\t\t\t <Points>\n", fp);
+    fputs("\t\t\t\t <DataArray type=\"Float64\" NumberOfComponents=\"3\" format=\"ascii\">\n", fp);
+    for (int i = 0; i < nx; i++) {
+        double xpt = g->domain[0] + g->dx * i;
+        for (int j = 0; j < ny; j++) {
+            double ypt = g->domain[2] + g->dy * j;
+            double et = g->ETA[(size_t)tt * nx * ny + (size_t)i * ny + j];
+            for (int m = 0; m < nl; m++) {
+                double sp = -pow(tan(-(-1. + g->ds * m) * g->tan_a), g->tan_b) / pow(tan(g->tan_a), g->tan_b);
+                fprintf(fp, "%12.4f %12.4f %12.4f\n", xpt, ypt, s2z(g, sp, et, g->water_depth));
+            }
+        }
+    }
+    fputs("\t\t\t\t </DataArray>\n", fp);
+    fputs("\t\t\t </Points>\n", fp);
+    fputs("\t\t\t <Cells>\n", fp);
+    fputs("\t\t\t\t <DataArray type=\"Int64\" Name=\"connectivity\" format=\"ascii\">\n", fp);
+    if (nx > 1 && ny > 1 && nl > 1) {
+        for (int i = 0; i < nx - 1; i++)
+            for (int j = 0; j < ny - 1; j++)
+                for (int m = 0; m < nl - 1; m++) {
+                    unsigned a1 = nl * ny * i + nl * j + m, a2 = nl * ny * (i + 1) + nl * j + m;
+                    unsigned a3 = nl * ny * (i + 1) + nl * (j + 1) + m, a4 = nl * ny * i + nl * (j + 1) + m;
+                    fprintf(fp, "%u %u %u %u %u %u %u %u\n", a1, a2, a3, a4, a1 + 1, a2 + 1, a3 + 1, a4 + 1);
+                }
+        vtu_cells_tail(fp, (long)(nx - 1) * (ny - 1) * (nl - 1), 8, "12");
+    } else if (nx > 1 && ny == 1 && nl > 1) {
+        for (int i = 0; i < nx - 1; i++)
+            for (int m = 0; m < nl - 1; m++)
+                fprintf(fp, "%u %u %u %u\n", nl * i + m, nl * (i + 1) + m, nl * (i + 1) + m + 1, nl * i + m + 1);
+        vtu_cells_tail(fp, (long)(nx - 1) * (nl - 1), 4, "9");
+    } else if (nx == 1 && ny > 1 && nl > 1) {
+        for (int j = 0; j < ny - 1; j++)
+            for (int m = 0; m < nl - 1; m++)
+                fprintf(fp, "%u %u %u %u\n", nl * j + m, nl * (j + 1) + m, nl * (j + 1) + m + 1, nl * j + m + 1);
+        vtu_cells_tail(fp, (long)(ny - 1) * (nl - 1), 4, "9");
+    } else if (nx > 1 && ny > 1 && nl == 1) {
+        for (int i = 0; i < nx - 1; i++)
+            for (int j = 0; j < ny - 1; j++)
+                fprintf(fp, "%u %u %u %u\n", ny * i + j, ny * (i + 1) + j, ny * (i + 1) + j + 1, ny * i + j + 1);
+        vtu_cells_tail(fp, (long)(nx - 1) * (ny - 1), 4, "9");
+    }
+    fputs("\t\t\t\t </DataArray>\n", fp);
+    fputs("\t\t\t </Cells>\n", fp);
+    fputs("\t\t </Piece>\n", fp);
+    fputs("\t </UnstructuredGrid>\n", fp);
+    fputs("</VTKFile>\n", fp);
+    return fclose(fp) == 0 ? 0 : -1;
 }
 
 void orc_sgrid_state(const orc_sgrid *g, double *t0, int *tstep) {

@@ -123,6 +123,15 @@ void refp_force_update(double t) {
     quiet_end();
 }
 
+// lsGridSpline::export_vtu (lsgrid_spline.cpp:1222-1403) of the global grid into `path`.
+int refp_sgrid_export_vtu(const char *path, int last) {
+    FILE *fp = fopen(path, "w");
+    if (!fp) return -1;
+    sgrids.export_vtu(fp, last != 0);
+    fclose(fp);
+    return 0;
+}
+
 void refp_sgrid_dims(int *dims, double *vals) {
     dims[0] = sgrids.nx; dims[1] = sgrids.ny; dims[2] = sgrids.nl; dims[3] = sgrids.tstep;
     vals[0] = sgrids.t0; vals[1] = sgrids.dt; vals[2] = sgrids.dx; vals[3] = sgrids.dy;

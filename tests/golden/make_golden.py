@@ -59,6 +59,8 @@ def child(case_dir, spec_json, out_path):
     L.refp_sgrid_array.argtypes = [C.c_int, _dp]
     L.refp_fenton.restype = C.c_int
     L.refp_fenton.argtypes = [_dp]
+    L.refp_sgrid_export_vtu.restype = C.c_int
+    L.refp_sgrid_export_vtu.argtypes = [C.c_char_p, C.c_int]
     rc = L.refp_init(case_dir.encode())
     res = {"rc": np.array(rc)}
     with open(os.path.join(case_dir, "waveinput.dat")) as fh:
@@ -121,6 +123,17 @@ def child(case_dir, spec_json, out_path):
                 L.refp_api(which, qx.size, _p(qx), _p(qy), _p(qz), _p(qtt), _p(o))
                 snap["api_" + name] = o
             snap["query_t"] = qt
+            if spec.get("vtu"):
+                # the file the reference wrote itself for this ring ([lsgrid2vtk])
+                # and the export of the slot after the base slot
+                v = spec["vtu"]
+                auto = os.path.join(case_dir, v["path"], "%s%05d.vtu" % (v["prefix"], int(dims[3])))
+                with open(auto) as fh:
+                    snap["vtu"] = np.array(fh.read())
+                last = os.path.join(case_dir, "last.vtu")
+                assert L.refp_sgrid_export_vtu(last.encode(), 1) == 0
+                with open(last) as fh:
+                    snap["vtu_last"] = np.array(fh.read())
             snaps.append(snap)
         res["nsnap"] = np.array(len(snaps))
         for k, snap in enumerate(snaps):
@@ -143,7 +156,12 @@ def _grid_points(xs, ys, zs, ts):
             "t": T.ravel().tolist()}
 
 
+ONLY = set()     # case names given on the command line (none: every case)
+
+
 def _run_case(name, text, spec):
+    if ONLY and name not in ONLY:
+        return
     with tempfile.TemporaryDirectory() as d:
         with open(os.path.join(d, "waveinput.dat"), "w") as fh:
             fh.write(text)
@@ -263,6 +281,22 @@ def main():
             "query_x": qx.tolist(), "query_y": qy.tolist(), "query_z": qz.tolist()}
     _run_case("sgrid_ignore", txt, spec)
 
+    # (8b) .vtu output of the s-grid ([lsgrid2vtk], lsgrid_spline.cpp:1200-1403):
+    #      the files the reference writes at init and after an update, and the
+    #      export of the slot after the base slot; a 3-D grid and one that is
+    #      flat in y (quad cells).
+    for name, nx, ny, nl, bounds in (("sgrid_vtu", 6, 5, 4, (-30.0, 30.0, -20.0, 20.0)),
+                                     ("sgrid_vtu_flat", 7, 1, 5, (-30.0, 30.0, 0.0, 0.0))):
+        vtk = {"path": "vtk/", "prefix": "kin", "label": "TimeValue"}
+        grid = {"bounds": bounds, "nx": nx, "ny": ny, "nl": nl, "t0": 0.5, "dt": 0.5, "stretch": (0.7, 1.5),
+                "vtk": vtk}
+        comps = ss.irregular_components(3.0, 9.0, 2.0, 8, 0.45, 1.5, 40.0, 41, ndir=3, spreading_s=8.0)
+        txt = ss.write_irregular(None, comps, 40.0, extrap=2, lsgrid=grid)
+        spec = {"kind": "sgrid", "points": {"x": [0.0], "y": [0.0], "z": [0.0], "t": [0.0]},
+                "updates": [1.2], "query_t": [0.6, 1.1], "query_x": [0.0], "query_y": [0.0], "query_z": [-1.0],
+                "vtu": vtk}
+        _run_case(name, txt, spec)
+
     # (9) Stokes 5th (H=6 T=10 d=30) and Fenton (N=24 H=8 T=12 d=20), plus
     #     length-specified variants with direction, current and reference point.
     def reg_points(L_, d, H):
@@ -285,4 +319,5 @@ if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "--child":
         child(sys.argv[2], sys.argv[3], sys.argv[4])
     else:
+        ONLY.update(sys.argv[1:])
         main()

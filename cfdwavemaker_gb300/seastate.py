@@ -76,8 +76,10 @@ def irregular_components(hs, tp, gamma, nfreq, wmin, wmax, depth, seed, ndir=1,
 
 def write_irregular(path, comps, depth, *, extrap=2, bandwidth=None, cutoff=None,
                     gravity=None, rho=None, swl=None, mtheta=None, ref_point=None,
-                    ramps=None, lsgrid=None, normalize=None, amplify=None, ramp_columns=None):
-    """Write an irregular-sea ``waveinput.dat`` (ndir 0 format)."""
+                    ramps=None, lsgrid=None, normalize=None, amplify=None, ramp_columns=None,
+                    vertical_theory=None):
+    """Write an irregular-sea ``waveinput.dat`` (ndir 0 format).  vertical_theory:
+    None (the default Sharma-Dean theory) or "smit"."""
     L = ["@v310", "[wave type]", "irregular", "", "[general input data]", "depth %.17g" % depth]
     if mtheta is not None:
         L.append("mtheta %.17g" % mtheta)
@@ -108,6 +110,8 @@ def write_irregular(path, comps, depth, *, extrap=2, bandwidth=None, cutoff=None
         L.append("cutoff %.17g" % cutoff)
     if ramp_columns is not None:
         L.append("individual_ramp true")
+    if vertical_theory is not None:
+        L.append("vertical_theory %s" % vertical_theory)
     n = len(comps["omega"])
     L.append("nfreq %d" % n)
     L.append("ndir 0")

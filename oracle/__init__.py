@@ -67,6 +67,7 @@ def lib():
         L.orc_sgrid_check_time.restype = C.c_int
         L.orc_sgrid_check_time.argtypes = [C.c_void_p, C.c_double]
         L.orc_sgrid_query.argtypes = [C.c_void_p, C.c_long, _dp, _dp, _dp, _dp, _dp, C.c_int]
+        L.orc_smit_batch.argtypes = [C.c_void_p, C.c_long, _dp, _dp, _dp, _dp, _dp, C.c_int]
         L.orc_sgrid_query5.argtypes = [C.c_void_p, C.c_long, _dp, _dp, _dp, _dp, _dp, C.c_int]
         L.orc_sgrid_set_pressure.argtypes = [C.c_void_p, C.c_int]
         L.orc_sgrid_export_vtu.restype = C.c_int
@@ -142,6 +143,13 @@ class Sea:
         n, p, keep = _pts(x, y, z, t)
         out = np.zeros((n, 4))
         lib().orc_uvw2_batch(self.h, n, p[0], p[1], p[2], p[3], out.ctypes.data_as(_dp), nthreads)
+        return out
+
+    def smit(self, x, y, z, t, nthreads=0):
+        """u_smit, v_smit, w_smit, dp_smit (no ramp): [n, 4]."""
+        n, p, keep = _pts(x, y, z, t)
+        out = np.zeros((n, 4))
+        lib().orc_smit_batch(self.h, n, p[0], p[1], p[2], p[3], out.ctypes.data_as(_dp), nthreads)
         return out
 
     def eta2(self, x, y, t):
@@ -299,6 +307,9 @@ class Model:
         wt = cfg["wavetype"]
         if wt == 1:
             f = self.sea.fields(x, y, zc, t, 31, nthreads)
+            if cfg.get("vertical_theory") == 1:
+                # u, v, w, dp of the Smit s-coordinate theory (Irregular.cpp:25, 53, 77, 143)
+                f[:, 1:5] = self.sea.smit(x, y, zc, t, nthreads)
             out[:, 0:5] = r[:, None] * f
             out[:, 5] = r * (f[:, 4] - cfg["rho"] * cfg["gravity"] * f[:, 0])
         elif wt == 5:

@@ -60,6 +60,11 @@ void orc_uvw2(const orc_sea *s, double t, double x, double y, double z, double o
 void orc_irregular_batch(const orc_sea *s, long n, const double *x, const double *y,
                          const double *z, const double *t, int fields, double *out,
                          int nthreads);
+/* Smit et al. (2017) s-coordinate kinematics of vertical_theory smit
+ * (u_smit, v_smit, w_smit, dp_smit, Irregular.cpp:1622-2027): out [n][4] =
+ * u, v, w, dp without ramp; 0 above eta1 + eta2 + swl. */
+void orc_smit_batch(const orc_sea *s, long n, const double *x, const double *y, const double *z,
+                    const double *t, double *out, int nthreads);
 /* uvw2 batched: out [n][4]. */
 void orc_uvw2_batch(const orc_sea *s, long n, const double *x, const double *y,
                     const double *z, const double *t, double *out, int nthreads);

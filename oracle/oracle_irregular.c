@@ -425,6 +425,133 @@ void orc_uvw2(const orc_sea *s, double t, double xx, double yy, double zz, doubl
     out[0] = us; out[1] = vs; out[2] = ws; out[3] = ps;
 }
 
+/* --- Smit et al. (2017) s-coordinate second order, vertical_theory smit
+ *     (u_smit, v_smit, w_smit, dp_smit, Irregular.cpp:1622-2027) --- */
+
+/* Wheeler-stretched profiles, Irregular.cpp:121-138: the height is mapped to
+ * sf = h (h + z) / (h + eta) in [0, h]. */
+static double prof_s(double k, double depth, double z, double eta, int sinh_) {
+    double sf = depth * (depth + z) / (depth + eta);
+    return (sinh_ ? sinh(k * sf) : cosh(k * sf)) / cosh(k * depth);
+}
+
+/* H coefficient of the pair cache (Irregular.cpp:924-930, 951-958): the
+ * inversion of Smit's Eq. 10 with the Sharma-Dean alpha. */
+static double smit_h(double g, double om12, double oi, double om, double alpha, double k1dk2, double sgn) {
+    return -g / om12 * (alpha / 2.0 - (oi * oi + om * om + sgn * oi * om) / (2.0 * g) + g * k1dk2 / (2.0 * oi * om));
+}
+
+/* out = u, v, w, dp; 0 above the surface (eta1 + eta2 + swl). */
+void orc_smit(const orc_sea *s, double t, double xx, double yy, double zz, double out[4]) {
+    const int N = s->n;
+    const double h = s->depth, g = s->g, rho = s->rho;
+    double eta = orc_eta1(s, t, xx, yy);
+    if (s->order >= 1) eta += orc_eta2(s, t, xx, yy);
+    out[0] = out[1] = out[2] = out[3] = 0.0;
+    if (zz > eta + s->swl) return;
+    zz = dmax(-h, zz - s->swl);
+    double *buf = (double *)malloc(sizeof(double) * 4 * (size_t)(N > 0 ? N : 1));
+    double *ph = buf, *fr = buf + N, *Ch = buf + 2 * N, *Sh = buf + 3 * N;
+    for (int i = 0; i < N; i++) {
+        ph[i] = s->k[i] * (s->cth[i] * (xx - s->fx) + s->sth[i] * (yy - s->fy)) - s->omega[i] * t + s->phase0[i];
+        fr[i] = framp(s, i, t);
+        Ch[i] = prof_s(s->k[i], h, zz, eta, 0);
+        Sh[i] = prof_s(s->k[i], h, zz, eta, 1);
+    }
+    double u1 = 0, v1 = 0, w1 = 0, p1 = 0;
+    for (int i = 0; i < N; i++) {
+        double agk = s->A[i] * g * s->k[i] / s->omega[i];
+        u1 += agk * Ch[i] * s->cth[i] * cos(ph[i]) * fr[i];
+        v1 += agk * Ch[i] * s->sth[i] * cos(ph[i]) * fr[i];
+        w1 += agk * Sh[i] * sin(ph[i]) * fr[i];
+        p1 += s->A[i] * rho * g * Ch[i] * cos(ph[i]) * fr[i];
+    }
+    double u2 = 0, v2 = 0, w2 = 0, p2 = 0;
+    if (s->order >= 1) {
+        const double sp1 = (h + zz) / (h + eta), g1s = g * sp1;
+        double dphi2ds = 0.0;
+        for (int i = 0; i < N; i++) {          /* diagonal terms, no filter */
+            double ki = s->k[i], oi = s->omega[i];
+            double AA = s->A[i] * s->A[i] * fr[i] * fr[i];
+            double k2 = 2.0 * ki, om2 = 2.0 * oi;
+            double Rn = s->R[i], Rs = s->Rs[i];
+            double Dnn = (6.0 * Rs * Rs * (ki * ki - Rn * Rn)) / (2.0 * Rs * Rs - ki * tanh(2.0 * ki * h));
+            double ann = (Dnn - (ki * ki - Rn * Rn)) / Rn + 2.0 * Rn;
+            double H = -g / om2 * (ann / 2.0 - (3.0 * oi * oi) / (2.0 * g) + g * ki * ki / (2.0 * oi * oi));
+            double Ch2 = prof_s(k2, h, zz, eta, 0), Sh2 = prof_s(k2, h, zz, eta, 1);
+            double c2 = cos(2.0 * ph[i]), s2 = sin(2.0 * ph[i]);
+            double kx2 = 2.0 * ki * s->cth[i], ky2 = 2.0 * ki * s->sth[i];
+            u2 += 0.5 * AA * H * kx2 * (-c2) * Ch2;
+            u2 += 0.5 * AA * kx2 * g1s * (ki * Sh[i] / oi) * c2;
+            dphi2ds += -0.5 * AA * H * (k2 * h * Sh2) * s2;
+            dphi2ds += 0.5 * AA * g * (ki * Sh[i] / oi + sp1 * ki * (ki * h * Ch[i]) / oi) * s2;
+            v2 += 0.5 * AA * H * ky2 * (-c2) * Ch2;
+            w2 += 0.5 * AA * H * k2 * (-s2) * Sh2;
+            p2 += 0.5 * AA * rho * om2 * H * (-c2) * Ch2;
+            p2 -= 0.5 * AA * rho * g * g * ki * ki * (Ch[i] * Ch[i] - Sh[i] * Sh[i]) / (oi * oi) * c2;
+        }
+        for (long q = 0; q < s->np; q++) {     /* pair cache */
+            int i = s->pi[q], m = s->pm[q];
+            double ki = s->k[i], km = s->k[m], oi = s->omega[i], om = s->omega[m];
+            double AA = s->A[i] * s->A[m] * fr[i] * fr[m];
+            double gam = s->cth[i] * s->cth[m] + s->sth[i] * s->sth[m];
+            double k1dk2 = ki * km * gam;
+            double ai = ki * Sh[i] / oi, am_ = km * Sh[m] / om;
+            double bi = ki * (ki * h * Ch[i]) / oi, bm = km * (km * h * Ch[m]) / om;
+            if (s->hp[q]) {
+                double H = smit_h(g, oi + om, oi, om, s->ap[q], k1dk2, 1.0);
+                double pp = ph[i] + ph[m], c = cos(pp), sn = sin(pp);
+                double kx12 = ki * s->cth[i] + km * s->cth[m], ky12 = ki * s->sth[i] + km * s->sth[m];
+                double Ch12 = prof_s(s->kp[q], h, zz, eta, 0), Sh12 = prof_s(s->kp[q], h, zz, eta, 1);
+                u2 += AA * H * kx12 * (-c) * Ch12;
+                u2 += AA * kx12 * g1s * (ai + am_) * c;
+                dphi2ds += -AA * H * (s->kp[q] * h * Sh12) * sn;
+                dphi2ds += AA * g * ((ai + am_) + sp1 * (bi + bm)) * sn;
+                v2 += AA * H * ky12 * (-c) * Ch12;
+                w2 += AA * H * s->kp[q] * (-sn) * Sh12;
+                p2 += AA * rho * (oi + om) * H * (-c) * Ch12;
+                p2 -= AA * rho * g * g * k1dk2 * (Ch[i] * Ch[m] - Sh[i] * Sh[m]) / (oi * om) * c;
+            }
+            if (s->hm[q]) {
+                double om12 = oi - om;
+                double H = fabs(om12) > ORC_SMALL ? smit_h(g, om12, oi, om, s->am[q], k1dk2, -1.0) : 0.0;
+                double pm_ = ph[i] - ph[m], c = cos(pm_), sn = sin(pm_);
+                double kx12 = ki * s->cth[i] - km * s->cth[m], ky12 = ki * s->sth[i] - km * s->sth[m];
+                double Ch12 = prof_s(s->km[q], h, zz, eta, 0), Sh12 = prof_s(s->km[q], h, zz, eta, 1);
+                u2 += AA * H * kx12 * (-c) * Ch12;
+                u2 += AA * kx12 * g1s * (ai - am_) * c;
+                dphi2ds += -AA * H * (s->km[q] * h * Sh12) * sn;
+                dphi2ds += AA * g * ((ai - am_) + sp1 * (bi - bm)) * sn;
+                v2 += AA * H * ky12 * (-c) * Ch12;
+                w2 += AA * H * s->km[q] * (-sn) * Sh12;
+                p2 += AA * rho * om12 * H * (-c) * Ch12;
+                p2 -= AA * rho * g * g * k1dk2 * (Ch[i] * Ch[m] + Sh[i] * Sh[m]) / (oi * om) * c;
+            }
+        }
+        /* Lagrangian-to-Eulerian chain term of u (Irregular.cpp:1750-1768) */
+        double eta_x = 0.0, phi_s = 0.0;
+        for (int n = 0; n < N; n++) {
+            double sn = sin(ph[n]);
+            eta_x += -s->A[n] * s->k[n] * s->cth[n] * sn * fr[n];
+            phi_s += (g * s->A[n] / s->omega[n]) * s->k[n] * h * Sh[n] * sn * fr[n];
+        }
+        phi_s += dphi2ds;
+        u2 += -(h + zz) / ((h + eta) * (h + eta)) * eta_x * phi_s;
+    }
+    free(buf);
+    out[0] = u1 + u2; out[1] = v1 + v2; out[2] = w1 + w2; out[3] = p1 + p2;
+}
+
+void orc_smit_batch(const orc_sea *s, long n, const double *x, const double *y, const double *z,
+                    const double *t, double *out, int nthreads) {
+#ifdef _OPENMP
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads)
+#endif
+    for (long p = 0; p < n; p++) orc_smit(s, t[p], x[p], y[p], z[p], out + 4 * p);
+    (void)nthreads;
+}
+
 /* --- dispatch on order with the Taylor layer (Irregular.cpp:9-157) --- */
 double orc_eta(const orc_sea *s, double t, double x, double y) {
     if (s->order == 2) return s->swl + orc_eta1(s, t, x, y) + orc_eta2(s, t, x, y);

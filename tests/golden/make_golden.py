@@ -243,6 +243,23 @@ def main():
     pts = _grid_points([0.0, 60.0], [-20.0, 5.0], [-25.0, -6.0, 0.7, 1.9], [-0.5, 1.0, 3.3, 9.0])
     _run_case("ramps_swl", txt, {"kind": "irregular", "points": pts})
 
+    # (5b) vertical_theory smit (Smit et al. 2017 s-coordinate second order,
+    #      Irregular.cpp:1622-2027): a short-crested sea with pair filters and
+    #      swl, and one with individual ramps; points below, at and above the
+    #      surface.
+    comps = ss.irregular_components(2.5, 8.0, 2.5, 10, 0.45, 1.6, 30.0, 17, ndir=3, spreading_s=6.0)
+    txt = ss.write_irregular(None, comps, 30.0, extrap=2, swl=0.4, mtheta=25.0, rho=1025.0, bandwidth=0.6,
+                             cutoff=1.5, vertical_theory="smit")
+    pts = _grid_points([-12.0, 7.5, 31.0], [3.0, -9.0], [-30.0, -17.0, -4.0, -0.6, 0.2, 1.1, 3.5], [0.0, 4.2])
+    _run_case("smit_spread", txt, {"kind": "irregular", "points": pts})
+    comps = ss.irregular_components(3.0, 9.0, 2.0, 14, 0.4, 1.5, 50.0, 29, ndir=3, spreading_s=4.0)
+    n = comps["omega"].size
+    r5 = np.random.default_rng(505)    # own stream: the cases after this one keep theirs
+    rcols = [r5.uniform(1.0, 4.0, n), r5.uniform(-1.0, 1.0, n), r5.uniform(30.0, 80.0, n)]
+    txt = ss.write_irregular(None, comps, 50.0, extrap=2, ramp_columns=rcols, vertical_theory="smit")
+    pts = _grid_points([0.0, 22.0], [0.0, 5.0], [-50.0, -20.0, -5.0, -1.0, 0.0, 0.9], [0.5, 2.5, 6.0])
+    _run_case("smit_ramps", txt, {"kind": "irregular", "points": pts})
+
     # (6) linear theory (kinematics_surf_extrap 0, unclipped above swl).
     comps = ss.irregular_components(3.0, 8.0, 2.0, 30, 0.4, 1.9, 40.0, 5)
     txt = ss.write_irregular(None, comps, 40.0, extrap=0, swl=0.3)

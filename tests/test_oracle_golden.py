@@ -13,7 +13,8 @@ from conftest import golden_cfg, load_golden, norm_rel_err
 
 import oracle
 
-IRREGULAR = ["t005_focused", "t002_exact", "config1_point", "short_spread", "ramps_swl", "linear"]
+IRREGULAR = ["t005_focused", "t002_exact", "config1_point", "short_spread", "ramps_swl", "linear",
+             "smit_spread", "smit_ramps"]
 REGULAR = ["stokes5", "fenton24", "stokes5_len", "fenton_len"]
 API = ["SurfElev", "VeloX", "VeloY", "VeloZ", "DynPres", "nhPres"]
 

@@ -389,8 +389,11 @@ int initialize_from_text(const std::string &text) {
         std::fprintf(stderr, "cfdwavemaker_gb300: %s\n", t_ctx.err.c_str());
         return E_UNSUPPORTED;
     }
-    if ((wt == WT_IRREGULAR || wt == WT_IRR_SGRID) && cfg.vertical_theory == 1) {
-        set_error("vertical_theory smit (experimental upstream) is not served by this build");
+    // vertical_theory smit changes only Irregular::u/v/w/dp (Irregular.cpp:25, 53, 77,
+    // 143): the point API of wave type 1.  The s-grid update calls u1/uvw2 directly
+    // (lsgrid_spline.cpp:880-903), so wave type 5 is the same with either theory.
+    if (wt == WT_IRREGULAR && cfg.vertical_theory == 1 && cfg.order != 2) {
+        set_error("vertical_theory smit is served with second order (kinematics_surf_extrap 2) only");
         std::fprintf(stderr, "cfdwavemaker_gb300: %s\n", t_ctx.err.c_str());
         return E_UNSUPPORTED;
     }

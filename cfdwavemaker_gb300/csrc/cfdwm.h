@@ -132,6 +132,7 @@ enum CompCoef {
 // Record sizes are defined with the kernels (irregular.cu).
 constexpr int GRID_TILE = 32;
 constexpr int POINT_TILE = 16;
+constexpr int SMIT_TILE = 16;
 
 struct DevSea {
     int n = 0;              // components
@@ -151,7 +152,25 @@ struct DevSea {
     float *d_tab_gp = nullptr;   // grid-mask pair tiles of the s-grid pressure: Pp, Mp (phase terms)
     float *d_tab_gk = nullptr;   // grid-mask pair tiles of the phase-free pressure terms: X, Z
     int ntile_g = 0, ntile_p = 0;
+    // vertical_theory smit (Smit et al. 2017): its pair tiles (smit.cu)
+    bool smit = false;
+    float *d_tab_smit = nullptr;
+    int npad_s = 0, ntile_s = 0;
 };
+
+// FP64 component inputs (device pointers) of the Smit pair-table build.
+struct SmitIn {
+    int n;
+    const double *omega, *A, *k, *theta;
+    double depth, g, rho, mtheta_rad, cutoff, bandwidth, kmax;
+};
+// Builds sea.d_tab_smit (smit.cu).
+int smit_build(const SmitIn &c, DevSea &sea, void *stream);
+// u, v, w, dp of the Smit theory at n points into rows 1..4 of out (row
+// stride ldo), from the point phasors (float2 (cos, sin), [npad_g][n]) and
+// ramps, the first-order sums (first[0] = eta1) and eta2; scratch: 4 n floats.
+int smit_eval(const DevSea &sea, long n, const double *z, const void *ph, const float *rr, const double *first,
+              const float *eta2, float *scratch, long ldo, double *out, void *stream);
 
 // Builds the device tables (component coefficients and the FP64 transfer
 // functions of the pair tables, computed on the device).  point_table: also

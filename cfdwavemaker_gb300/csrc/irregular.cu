@@ -360,6 +360,15 @@ int sea_build(const Config &cfg, DevSea &sea, bool point_table, void *stream_) {
             note_launch();
             CK(cudaGetLastError());
         }
+        if (cfg.vertical_theory == 1) {
+            SmitIn si;
+            si.n = n; si.omega = ci.omega; si.A = ci.A; si.k = ci.k; si.theta = ci.theta;
+            si.depth = ci.depth; si.g = ci.g; si.rho = ci.rho; si.mtheta_rad = ci.mtheta_rad;
+            si.cutoff = ci.cutoff; si.bandwidth = ci.bandwidth; si.kmax = ci.kmax;
+            int rc = smit_build(si, sea, stream);
+            if (rc) return rc;
+            sea.smit = true;
+        }
         unsigned long long *d_cnt = nullptr, h_cnt = 0;
         CK(cudaMalloc(&d_cnt, sizeof(unsigned long long)));
         CK(cudaMemsetAsync(d_cnt, 0, sizeof(unsigned long long), stream));
@@ -384,6 +393,9 @@ void sea_free(DevSea &sea) {
     if (sea.d_tab_point) cudaFree(sea.d_tab_point);
     if (sea.d_tab_gp) cudaFree(sea.d_tab_gp);
     if (sea.d_tab_gk) cudaFree(sea.d_tab_gk);
+    if (sea.d_tab_smit) cudaFree(sea.d_tab_smit);
+    sea.d_tab_smit = nullptr;
+    sea.smit = false;
     sea.d_phase = nullptr; sea.d_cf = nullptr; sea.d_tab_eta = nullptr;
     sea.d_tab_grid = nullptr; sea.d_tab_point = nullptr; sea.d_tab_gp = nullptr; sea.d_tab_gk = nullptr;
 }
@@ -1173,13 +1185,18 @@ int irregular_eval(const DevSea &sea, long n, const double *x, const double *y, 
         WsLayout L = layout(m, npad, ws.base);
         rc = launch_phasors(sea, m, x + b, y + b, t + b, 1, 1, 1, npad, L.ph, L.rr, L.first, stream);
         if (rc) return rc;
+        // vertical_theory smit: u, v, w, dp need eta at the point first
+        const bool smit = sea.smit && (mask & 30);
         float *eta2 = nullptr;
-        if ((mask & 1) && sea.order == 2) {
+        if (((mask & 1) || smit) && sea.order == 2) {
             eta2 = L.sec + 4 * m;
             rc = launch_eta_pairs(sea, m, L.ph, L.rr, eta2, stream);
             if (rc) return rc;
         }
-        if (mask & 30) {
+        if (smit) {
+            rc = smit_eval(sea, m, z + b, L.ph, L.rr, L.first, eta2, L.sec, n, out + b, stream);
+            if (rc) return rc;
+        } else if (mask & 30) {
             k_prep_z<<<(unsigned)((m + 255) / 256), 256, 0, stream>>>(m, z + b, sea.swl, sea.order, L.z0);
             note_launch();
             CK(cudaGetLastError());
@@ -1189,7 +1206,8 @@ int irregular_eval(const DevSea &sea, long n, const double *x, const double *y, 
             if (rc) return rc;
         }
         k_combine<<<(unsigned)((m + 255) / 256), 256, 0, stream>>>(m, n, sea.order, sea.swl, z + b,
-                                                                   L.first, L.sec, eta2, mask, out + b);
+                                                                   L.first, L.sec, eta2, smit ? (mask & 1) : mask,
+                                                                   out + b);
         note_launch();
         CK(cudaGetLastError());
     }

@@ -25,7 +25,8 @@ pytestmark = pytest.mark.gpu
 TOL = 1e-5
 TOL_GRAD = 1e-4
 API = ["SurfElev", "VeloX", "VeloY", "VeloZ", "DynPres", "nhPres"]
-IRREGULAR = ["t005_focused", "t002_exact", "config1_point", "short_spread", "ramps_swl", "linear"]
+IRREGULAR = ["t005_focused", "t002_exact", "config1_point", "short_spread", "ramps_swl", "linear",
+             "smit_spread", "smit_ramps"]
 REGULAR = ["stokes5", "fenton24", "stokes5_len", "fenton_len"]
 
 

@@ -558,9 +558,10 @@ def qform_cpu_baseline(budget_s=12.0):
             "sample": "%d points, uvw2 at z=0 (4096 components, FP64 oracle; eta2 adds ~10%%)" % n}
 
 
-def point_config():
+def point_config(vertical_theory=None):
     from cfdwavemaker_gb300 import seastate as ss
-    return ss.write_irregular(None, ss.config1_sea(), 50.0, extrap=2)
+    return ss.write_irregular(None, ss.config1_sea(), 50.0, extrap=2,
+                              vertical_theory=None if vertical_theory in (None, "sharma") else vertical_theory)
 
 
 class ClockSampler:
@@ -675,7 +676,7 @@ def run_ours(args):
     if args.workload == "sgrid":
         txt = sgrid_config(args.grid, args.grid)
     else:
-        txt = point_config()
+        txt = point_config(args.vertical_theory)
     t_init = time.time()
     rc = wm.initialize_text(txt)
     if rc != 0:
@@ -949,16 +950,22 @@ def cpu_baseline(args, budget_s=15.0):
         return {"value": rate, "unit": "grid nodes/s", "cores": nthr, "kind": "port",
                 "sample": "%d columns x 16 levels of one ring update (1024 components, 521k pairs), "
                           "FP64 oracle restatement of lsGridSpline::update, extrapolates linearly" % ncols}
-    cfg = waveinput.read_text(point_config())
+    smit = getattr(args, "vertical_theory", "sharma") == "smit"
+    cfg = waveinput.read_text(point_config(args.vertical_theory if smit else None))
     m = oracle.Model(cfg)
     rng = np.random.default_rng(5)
     n = max(nthr * 8, 64)
     x = rng.uniform(0, 500, n); z = rng.uniform(-50, 0, n); t = rng.uniform(0, 7, n)
     t0 = time.perf_counter()
-    m.sea.fields(x, 0 * x, z, t, 1 | 2 | 8 | 16, nthr)
+    if smit:
+        m.sea.fields(x, 0 * x, z, t, 1, nthr)
+        m.sea.smit(x, 0 * x, z, t, nthr)
+    else:
+        m.sea.fields(x, 0 * x, z, t, 1 | 2 | 8 | 16, nthr)
     el = time.perf_counter() - t0
     return {"value": n / el, "unit": "points/s", "cores": nthr, "kind": "port",
-            "sample": "%d random points of the 256x32x8 set, eta+u+w+dp, FP64 oracle" % n}
+            "sample": "%d random points of the 256x32x8 set, eta+u+w+dp%s, FP64 oracle"
+                      % (n, " (Smit theory: u, v, w, dp)" if smit else "")}
 
 
 def main():
@@ -969,6 +976,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="qform", choices=["qform", "sgrid", "point", "surrogate", "regular"])
     ap.add_argument("--surr-steps", type=int, default=600, help="ring steps of the learned-update loop")
+    ap.add_argument("--vertical-theory", default="sharma", choices=["sharma", "smit"],
+                    help="point workload: the Sharma-Dean theory or the Smit s-coordinate theory")
     ap.add_argument("--plain-every", type=int, default=20)
     ap.add_argument("--plain-steps", type=int, default=20, help="steps on which the plain loop is timed")
     ap.add_argument("--surr-tol", type=float, default=5e-2,
@@ -995,6 +1004,8 @@ def main():
         "surrogate": SURR_WORKLOAD % (args.surr_steps, args.plain_every, args.nsample, args.surr_tol),
         "regular": REG_WORKLOAD,
     }[args.workload]
+    if args.workload == "point" and args.vertical_theory == "smit":
+        workload += "; vertical_theory smit (Smit et al. 2017 s-coordinate second order)"
     if args.impl == "reference":
         rank = int(os.environ.get("RANK", "0"))
         if rank != 0:

@@ -885,12 +885,17 @@ def roofline(args, r, pk, src):
     if "point_pairs" in prof:
         kp = prof["point_pairs"]
         n = r["units"]
-        P = r["ncomp"] * (r["ncomp"] + 1) / 2
+        smit = getattr(args, "vertical_theory", "sharma") == "smit"
+        # Sharma-Dean point sums: every pair of the triangle (no filter);
+        # Smit: the pair-cache pairs and every diagonal term
+        P = (r["npairs"] + r["ncomp"]) if smit else r["ncomp"] * (r["ncomp"] + 1) / 2
         t = kp["avg_ms"] / 1e3
         ex2 = 4.0 * n * P / t
         peak = 152 * 32 * f_mhz * 1e6
-        return {"kernel": "k_pairs_points", "bound": "sfu", "achieved": ex2 / 1e9, "peak": peak / 1e9,
-                "unit": "Gex2/s", "frac": ex2 / peak, "traffic": traffic_from_profiles("k_pairs_points"),
+        name = "k_smit_points" if smit else "k_pairs_points"
+        return {"kernel": name, "bound": "sfu", "achieved": ex2 / 1e9, "peak": peak / 1e9,
+                "unit": "Gex2/s", "frac": ex2 / peak, "traffic": traffic_from_profiles(name),
+                "algorithmic": "4 ex2 per (pair, point); %d pairs x %d points per launch" % (P, n),
                 "avg_launch_ms": kp["avg_ms"],
                 "peak_source": "derived: 152 SM x 32 XU lanes/clk x median SM clock %.0f MHz" % f_mhz}
     return None

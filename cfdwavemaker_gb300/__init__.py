@@ -11,6 +11,7 @@ library has not been built: there is no CPU fallback.
 from __future__ import annotations
 
 import ctypes as C
+import math
 import os
 
 import numpy as np
@@ -168,6 +169,8 @@ def load(path: str | None = None):
     L.cfdwm_sgrid_pressure.argtypes = [C.c_int]
     L.cfdwm_sgrid_write_vtu.restype = C.c_int
     L.cfdwm_sgrid_write_vtu.argtypes = [C.c_char_p, C.c_int]
+    L.cfdwm_spectrum_components.restype = C.c_int
+    L.cfdwm_spectrum_components.argtypes = [_dp, C.c_int, C.c_int, C.c_ulonglong, vp]
     L.cfdwm_surrogate_set_carry.restype = C.c_int
     L.cfdwm_surrogate_set_carry.argtypes = [_d]
     L.cfdwm_surrogate_stats.restype = C.c_int
@@ -376,6 +379,17 @@ class CFDwavemaker:
         out = np.zeros(256)
         n = self.lib.cfdwm_regular_solution(_ptr(out), 256)
         return out[:max(n, 0)]
+
+
+def spectrum_components(hs, tp, gamma, nfreq, wmin, wmax, depth, seed, ndir=1, spreading_s=10.0,
+                        theta_span=math.pi / 2, g=9.81):
+    """Seeded JONSWAP / cos-2s components generated on the GPU
+    (cfdwm_spectrum_components): dict of omega, A, k, phase, theta."""
+    L = load()
+    p = np.array([hs, tp, gamma, wmin, wmax, depth, spreading_s, theta_span, g], dtype=np.float64)
+    out = np.zeros((5, nfreq * ndir))
+    _check(L.cfdwm_spectrum_components(p.ctypes.data_as(_dp), int(nfreq), int(ndir), int(seed), _ptr(out)))
+    return dict(zip(("omega", "A", "k", "phase", "theta"), out))
 
 
 def parse_text(text: str):

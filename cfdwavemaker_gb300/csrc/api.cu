@@ -916,6 +916,23 @@ int cfdwm_sgrid_method(int method, int *rank) {
 
 int cfdwm_depth_basis(double K, double h, int *rank, double *err) { return depthform_basis_info(K, h, rank, err); }
 
+int cfdwm_spectrum_components(const double *params, int nfreq, int ndir, unsigned long long seed, double *comps) {
+    if (!params || !comps || nfreq < 1 || ndir < 1) return E_BAD_ARGUMENT;
+    cudaStream_t s = stream_of();
+    const size_t bytes = sizeof(double) * 5 * (size_t)nfreq * ndir;
+    double *d = nullptr;
+    CKR(cudaMalloc(&d, bytes));
+    int rc = spectrum_components(params, nfreq, ndir, seed, d, s);
+    if (rc == OK) {
+        if (cudaMemcpyAsync(comps, d, bytes, cudaMemcpyDefault, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            rc = E_CUDA;
+    }
+    cudaFree(d);
+    if (rc == E_BAD_ARGUMENT) set_error("spectrum: bad parameters");
+    return rc;
+}
+
 int cfdwm_sgrid_write_vtu(const char *path, int last) {
     std::lock_guard<std::mutex> lk(g_model_mtx);
     if (!sgrid_loaded()) return E_UNSUPPORTED;

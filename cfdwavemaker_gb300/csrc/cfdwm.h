@@ -158,6 +158,12 @@ struct DevSea {
     int npad_s = 0, ntile_s = 0;
 };
 
+// Seeded JONSWAP / cos-2s component columns [5][nfreq ndir] (omega, A, k,
+// phase, theta) into device memory (spectrum.cu).  p: hs, tp, gamma, wmin,
+// wmax, depth, spreading s, direction span, gravity.
+int spectrum_components(const double *p, int nfreq, int ndir, unsigned long long seed, double *out_dev,
+                        void *stream);
+
 // FP64 component inputs (device pointers) of the Smit pair-table build.
 struct SmitIn {
     int n;

@@ -47,14 +47,33 @@ def cos2s_weights(theta, s, theta0=0.0):
     return d / np.sum(d)
 
 
+def splitmix64(seed, n):
+    """The first n outputs of SplitMix64 (Steele, Lea & Flood 2014) from state
+    ``seed``: the mix of seed + c 0x9E3779B97F4A7C15, c = 1..n (uint64)."""
+    with np.errstate(over="ignore"):
+        c = np.arange(1, n + 1, dtype=np.uint64)
+        z = np.uint64(seed % (1 << 64)) + c * np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        return z ^ (z >> np.uint64(31))
+
+
+def splitmix_phases(seed, n):
+    """Phases 2 pi u_c, u_c = the top 53 bits of the c-th SplitMix64 output / 2^53:
+    the phases the library's device generator gives (cfdwm_spectrum_components)."""
+    z = splitmix64(seed, n)
+    return 2.0 * math.pi * ((z >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0))
+
+
 def irregular_components(hs, tp, gamma, nfreq, wmin, wmax, depth, seed, ndir=1,
-                         spreading_s=None, theta_span=math.pi / 2, g=9.81):
+                         spreading_s=None, theta_span=math.pi / 2, g=9.81, phase_rng="numpy"):
     """Component arrays (omega, A, k, phase, theta) for a seeded sea state.
 
     Frequencies are equally spaced in [wmin, wmax]; amplitudes are
     sqrt(2 S(w) dw D(theta) dtheta); phases are uniform in [0, 2 pi) from
-    ``seed``.  With ndir > 1 the directions are equally spaced over
-    +-theta_span around 0 and weighted with cos-2s spreading.
+    ``seed`` (numpy's generator, or with phase_rng="splitmix" the library's
+    own, see splitmix_phases).  With ndir > 1 the directions are equally
+    spaced over +-theta_span around 0 and weighted with cos-2s spreading.
     """
     rng = np.random.default_rng(seed)
     om = np.linspace(wmin, wmax, nfreq)
@@ -70,7 +89,10 @@ def irregular_components(hs, tp, gamma, nfreq, wmin, wmax, depth, seed, ndir=1,
     theta = np.tile(th, om.size)
     A = np.sqrt(2.0 * np.repeat(S, th.size) * dw * np.tile(D, om.size))
     k = dispersion_k(omega, depth, g)
-    phase = rng.uniform(0.0, 2.0 * math.pi, omega.size)
+    if phase_rng == "splitmix":
+        phase = splitmix_phases(seed, omega.size)
+    else:
+        phase = rng.uniform(0.0, 2.0 * math.pi, omega.size)
     return {"omega": omega, "A": A, "k": k, "phase": phase, "theta": theta}
 
 

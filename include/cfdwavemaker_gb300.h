@@ -238,6 +238,21 @@ CFDWM_EXPORT int cfdwm_sgrid_pressure(int on);
  * last = 1, at wave_Cleanup (the reference at its exit).  Returns 0, -2 (no
  * s-grid model) or -5 (the file cannot be written). */
 CFDWM_EXPORT int cfdwm_sgrid_write_vtu(const char *path, int last);
+/* Sea-state components generated on the device (new; the reference reads
+ * them from waveinput.dat, CFDwavemaker.cpp:677-800, and leaves generating
+ * them to external tools).  params[9] = Hs, Tp, gamma, wmin, wmax, depth,
+ * spreading s, direction span (rad), gravity.  comps (host or device) receives
+ * [5][nfreq ndir] = omega, A, k, phase, theta: the five columns of the
+ * "ndir 0" format, component f ndir + d with
+ *   omega_f = linspace(wmin, wmax, nfreq), theta_d = linspace(-span, span, ndir)
+ *   (theta = 0 when ndir = 1),
+ *   A = sqrt(2 S(omega_f) dw D_d), S the JONSWAP density (sigma 0.07 / 0.09)
+ *   scaled to 4 sqrt(sum S dw) = Hs, D_d = cos(theta_d / 2)^(2 s) normalised
+ *   to sum 1, k from w^2 = g k tanh(k h) (FP64 Newton), phase = 2 pi u with
+ *   u the top 53 bits of SplitMix64(seed + (c + 1) 0x9E3779B97F4A7C15) / 2^53.
+ * Returns 0, -3 (bad parameters) or -4. */
+CFDWM_EXPORT int cfdwm_spectrum_components(const double *params, int nfreq, int ndir, unsigned long long seed,
+                                           double *comps);
 
 /* ===========================================================================
  * Part 5 -- learned s-grid update (new; no counterpart in the reference).

@@ -158,3 +158,30 @@ def test_sgrid_pressure_off_and_exclusions(wm):
     # and the velocities after switching back are the golden ones again
     for which in range(4):
         assert norm_rel_err(wm.sgrid_array(which), g["s0_arr%d" % which]) <= TOL
+
+
+def test_sgrid_pressure_with_component_ramps(wm):
+    """Individual (per-component) ramps still rising during the ring steps:
+    the ramps enter the pressure's phase-free height table per time step."""
+    from cfdwavemaker_gb300 import seastate as ss
+    comps = ss.irregular_components(3.0, 8.0, 2.0, 10, 0.45, 1.6, 30.0, 77, ndir=3, spreading_s=5.0)
+    n = comps["omega"].size
+    rng = np.random.default_rng(12)
+    rcols = [rng.uniform(1.0, 3.0, n), rng.uniform(-0.5, 0.5, n), rng.uniform(30.0, 60.0, n)]
+    grid = {"bounds": (0.0, 60.0, -20.0, 20.0), "nx": 9, "ny": 7, "nl": 6, "t0": 0.2, "dt": 0.4,
+            "stretch": (0.7, 1.5)}
+    txt = ss.write_irregular(None, comps, 30.0, extrap=2, lsgrid=grid, ramp_columns=rcols)
+    cfg = oracle.waveinput.read_text(txt)
+    og = oracle.Sgrid(cfg, oracle.Sea(cfg), pressure=True)
+    for method in (0, 1):
+        assert wm.initialize_text(txt) == 0, cw.last_error()
+        wm.sgrid_method(method)
+        wm.sgrid_pressure(True)
+        if method == 1:
+            og = oracle.Sgrid(cfg, oracle.Sea(cfg), pressure=True)
+        for k, tt in enumerate([None, 1.3, 2.2]):
+            if tt is not None:
+                wm.force_update(tt)
+                og.force_update(tt)
+            _, ts = wm.sgrid_state()
+            _compare_pressure(wm, og, ts, ("ramps", method, k))

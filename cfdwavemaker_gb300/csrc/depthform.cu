@@ -440,11 +440,17 @@ __global__ void __launch_bounds__(128) k_df_first_surface(DfFirstArgs a) {
     for (int q = 0; q < 5; q++) a.first[q * a.n + p] = (double)s[q] - (double)k[q];
 }
 
-// blockDim = 32 columns x up to 8 level groups of 4 levels; blockIdx.y: further level groups
+// blockDim = 32 columns x up to 8 level groups of 4 levels; blockIdx.y: further level groups.
+// The warps of a block hold the same 32 columns: each computes the phasors of
+// every nw-th component of a chunk into shared memory, and all of them read
+// the whole chunk, so a (column, component) phasor is formed once per block.
+// A chunk's terms are summed in FP32 and the chunk sum is added to a Kahan
+// (sum, carry) pair per output.
 __global__ void __launch_bounds__(256) k_df_first_levels(DfFirstArgs a) {
     __shared__ DfComp sc[DFC];
-    const int cl = threadIdx.x & 31;
-    const int lg = blockIdx.y * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    __shared__ float2 s_ph[DFC][32];     // (r cos, r sin) of (component, column)
+    const int cl = threadIdx.x & 31, wg = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int lg = blockIdx.y * nw + wg;
     const long p = (long)blockIdx.x * 32 + cl;
     const bool valid = p < a.n;
     const long pc = valid ? p : 0;
@@ -468,22 +474,35 @@ __global__ void __launch_bounds__(256) k_df_first_levels(DfFirstArgs a) {
         df_stage<1>(a, i0, sc);
         __syncthreads();
         const int iend = min(DFC, a.ncomp - i0);
+        for (int ii = wg; ii < iend; ii += nw) {
+            float c, sn;
+            df_phasor(sc[ii], dxh, dxl, dyh, dyl, th, tl, c, sn);
+            s_ph[ii][cl] = make_float2(sc[ii].r * c, sc[ii].r * sn);
+        }
+        __syncthreads();
+        float tu[4] = {0, 0, 0, 0}, tv[4] = {0, 0, 0, 0}, tw[4] = {0, 0, 0, 0}, tp[4] = {0, 0, 0, 0};
         for (int ii = 0; ii < iend; ii++) {
             const DfComp &d = sc[ii];
-            float c, sn;
-            df_phasor(d, dxh, dxl, dyh, dyl, th, tl, c, sn);
-            const float rc = d.r * c, rs = d.r * sn;
-            const float au = d.c[1] * rc, av = d.c[2] * rc, aw = d.c[3] * rs, k = d.c[0];
-            const float ap = d.c[4] * rc;
+            const float2 ph = s_ph[ii][cl];
+            const float au = d.c[1] * ph.x, av = d.c[2] * ph.x, aw = d.c[3] * ph.y, k = d.c[0];
+            const float ap = d.c[4] * ph.x;
 #pragma unroll
             for (int l = 0; l < 4; l++) {
                 // cosh(k(z+h))/cosh(kh) = q (E + Y), sinh(k(z+h))/cosh(kh) = q (E - Y)
                 const float E = df_ex2(k * zk[l]), Y = df_ex2(k * yk[l]);
-                df_kahan(su[l], cu[l], au * (E + Y));
-                df_kahan(sv[l], cv[l], av * (E + Y));
-                df_kahan(sw[l], cw[l], aw * (E - Y));
-                if (pres) df_kahan(sp[l], cp[l], ap * (E + Y));
+                const float F = E + Y, G = E - Y;
+                tu[l] = fmaf(au, F, tu[l]);
+                tv[l] = fmaf(av, F, tv[l]);
+                tw[l] = fmaf(aw, G, tw[l]);
+                if (pres) tp[l] = fmaf(ap, F, tp[l]);
             }
+        }
+#pragma unroll
+        for (int l = 0; l < 4; l++) {
+            df_kahan(su[l], cu[l], tu[l]);
+            df_kahan(sv[l], cv[l], tv[l]);
+            df_kahan(sw[l], cw[l], tw[l]);
+            if (pres) df_kahan(sp[l], cp[l], tp[l]);
         }
     }
     if (!valid) return;

@@ -313,6 +313,10 @@ struct GridExtra {
     float *split = nullptr;    // slices of a split column-pair launch
     long split_cap = 0;
     double *kin = nullptr;     // [KIN_NZ][2] phase-free pressure terms of the slot being written
+    // the table depends on t only through the component ramps: the ramps it
+    // was built with, and the ramp parameters (ramptime, starttime, duration)
+    std::vector<double> kin_r, ramp_par;
+    bool kin_valid = false;
     DepthForm df;              // tensor-core form of the column sums (method 1)
 };
 static std::vector<std::pair<const DevGrid *, GridExtra>> g_extra;
@@ -462,8 +466,22 @@ static int fill_cols(DevGrid &g, const DevSea &sea, Workspace &ws, const int *ac
     }
     if (rc) return rc;
     if (pres) {
-        rc = launch_pressure_kin(sea, t, KIN_NZ, x->kin, stream);
-        if (rc) return rc;
+        // rebuild the height table only when a component ramp changed (once
+        // every ramp has reached 1, the table stays valid)
+        const size_t nc = x->ramp_par.size() / 3;
+        std::vector<double> r(nc);
+        for (size_t i = 0; i < nc; i++) {
+            const double rt = x->ramp_par[3 * i], ts = x->ramp_par[3 * i + 1], du = x->ramp_par[3 * i + 2];
+            const double down = std::max(std::min(1. - ((t - ts - du + rt) / (rt + SMALL)), 1.), 0.);
+            const double up = std::max(std::min((t - ts) / (rt + SMALL), 1.), 0.);
+            r[i] = up * down;
+        }
+        if (!x->kin_valid || r != x->kin_r) {
+            rc = launch_pressure_kin(sea, t, KIN_NZ, x->kin, stream);
+            if (rc) return rc;
+            x->kin_r = r;
+            x->kin_valid = true;
+        }
     }
     long tot = nact * g.nl;
     k_scatter_levels<<<(unsigned)((tot + 255) / 256), 256, 0, stream>>>(
@@ -564,6 +582,13 @@ int grid_set_pressure(DevGrid &g, const Config &cfg, const DevSea &sea, bool on,
         CK(cudaMemsetAsync(g.U[3], 0, sizeof(float) * 4 * v, stream));
         CK(cudaMemsetAsync(g.Ut[3], 0, sizeof(float) * 4 * v, stream));
         if (!x->kin) CK(cudaMalloc(&x->kin, sizeof(double) * 2 * KIN_NZ));
+        x->ramp_par.resize(3 * cfg.omega.size());
+        for (size_t i = 0; i < cfg.omega.size(); i++) {
+            x->ramp_par[3 * i] = cfg.ramptime[i];
+            x->ramp_par[3 * i + 1] = cfg.starttime[i];
+            x->ramp_par[3 * i + 2] = cfg.duration[i];
+        }
+        x->kin_valid = false;
     } else {
         float *q[] = {g.U[3], g.Ut[3], g.Ux[3], g.Uy[3], g.Us[3]};
         for (float *p : q) if (p) cudaFree(p);

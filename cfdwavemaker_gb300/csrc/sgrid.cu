@@ -61,8 +61,13 @@ __global__ void k_column_coords(GridGeom g, long nact, const int *act, double *x
 }
 
 // ETA of the slot, the level heights and the level offsets above swl.
+// blockDim 128; the stretched coordinate of each level (which depends on the
+// level only) is formed once per block
 __global__ void k_levels(GridGeom g, long nact, const int *act, const double *first,
                          const float *eta2, int slot, float *ETA, float *zmin, float *zmax) {
+    __shared__ double s_sig[128];
+    for (int m = threadIdx.x; m < g.nl; m += blockDim.x) s_sig[m] = d_sigma_level(g, m);
+    __syncthreads();
     long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
     if (q >= nact) return;
     int c = act[q];
@@ -72,7 +77,7 @@ __global__ void k_levels(GridGeom g, long nact, const int *act, const double *fi
     for (int m = 0; m < g.nl; m++) {
         // the reference evaluates the levels from the stored value; the FP32
         // store is the value the query sees, so use it here too
-        double z = d_sigmaS2cart(g, m, (double)ef);
+        double z = d_s2z(g, s_sig[m], (double)ef);
         zmin[q * g.nl + m] = (float)fmin(0.0, z);
         zmax[q * g.nl + m] = (float)fmax(0.0, z - g.swl);
     }
@@ -117,6 +122,7 @@ struct GradArgs {
     int tstep;
     const float *F[5];      // ETA, UX, UY, UZ (and the pressure)
     float *Fx[5], *Fy[5], *Fs[5], *Ft[5];
+    float rdx, rdy, rds, rdt;   // reciprocal spacings
 };
 
 __global__ void k_gradients(GradArgs a) {
@@ -133,35 +139,38 @@ __global__ void k_gradients(GradArgs a) {
     const float *D = a.F[field];
     int tids[2] = {(a.tstep + 1) % 4, (a.tstep + 2) % 4};
     long sx = (long)g.ny * nl, sy = nl;
+    // FP32 differences of the FP32 node values times the reciprocal spacings
+    // (one-sided at the boundaries, central inside)
+    const float rdx = a.rdx, rdy = a.rdy, rds = a.rds, rdt = a.rdt;
     for (int q = 0; q < 2; q++) {
         const float *d = D + tids[q] * S;
         float gx, gy;
         if (g.nx == 1) gx = 0.f;
-        else if (i == 0) gx = (float)((d[e + sx] - d[e]) / g.dx);
-        else if (i == g.nx - 1) gx = (float)((d[e] - d[e - sx]) / g.dx);
-        else gx = (float)((d[e + sx] - d[e - sx]) / (2 * g.dx));
+        else if (i == 0) gx = (d[e + sx] - d[e]) * rdx;
+        else if (i == g.nx - 1) gx = (d[e] - d[e - sx]) * rdx;
+        else gx = (d[e + sx] - d[e - sx]) * (0.5f * rdx);
         if (g.ny == 1) gy = 0.f;
-        else if (j == 0) gy = (float)((d[e + sy] - d[e]) / g.dy);
-        else if (j == g.ny - 1) gy = (float)((d[e] - d[e - sy]) / g.dy);
-        else gy = (float)((d[e + sy] - d[e - sy]) / (2 * g.dy));
+        else if (j == 0) gy = (d[e + sy] - d[e]) * rdy;
+        else if (j == g.ny - 1) gy = (d[e] - d[e - sy]) * rdy;
+        else gy = (d[e + sy] - d[e - sy]) * (0.5f * rdy);
         a.Fx[field][q * S + e] = gx;
         a.Fy[field][q * S + e] = gy;
         if (field > 0) {
             float gs;
             if (nl == 1) gs = 0.f;
-            else if (m == 0) gs = (float)((d[e + 1] - d[e]) / g.ds);
-            else if (m == nl - 1) gs = (float)((d[e] - d[e - 1]) / g.ds);
-            else gs = (float)((d[e + 1] - d[e - 1]) / (2 * g.ds));
+            else if (m == 0) gs = (d[e + 1] - d[e]) * rds;
+            else if (m == nl - 1) gs = (d[e] - d[e - 1]) * rds;
+            else gs = (d[e + 1] - d[e - 1]) * (0.5f * rds);
             a.Fs[field][q * S + e] = gs;
         }
     }
     float *T = a.Ft[field];
     if (a.tstep > 0) {
         int tid = (a.tstep + 2) % 4, tid1 = (a.tstep + 3) % 4, tid0 = (a.tstep + 1) % 4;
-        T[tid * S + e] = (float)(((double)D[tid1 * S + e] - D[tid0 * S + e]) / (2 * g.dt));
+        T[tid * S + e] = (D[tid1 * S + e] - D[tid0 * S + e]) * (0.5f * rdt);
     } else {
-        T[1 * S + e] = (float)(((double)D[2 * S + e] - D[1 * S + e]) / g.dt);
-        T[2 * S + e] = (float)(((double)D[3 * S + e] - D[1 * S + e]) / (2 * g.dt));
+        T[1 * S + e] = (D[2 * S + e] - D[1 * S + e]) * rdt;
+        T[2 * S + e] = (D[3 * S + e] - D[1 * S + e]) * (0.5f * rdt);
     }
 }
 
@@ -522,6 +531,7 @@ static int gradients(DevGrid &g, cudaStream_t stream) {
     GradArgs a;
     a.g = geom(g);
     a.tstep = g.tstep;
+    a.rdx = (float)(1.0 / g.dx); a.rdy = (float)(1.0 / g.dy); a.rds = (float)(1.0 / g.ds); a.rdt = (float)(1.0 / g.dt);
     a.F[0] = g.ETA; a.Fx[0] = g.ETAdx; a.Fy[0] = g.ETAdy; a.Fs[0] = nullptr; a.Ft[0] = g.ETAdt;
     for (int f = 0; f < 4; f++) {
         a.F[f + 1] = g.U[f]; a.Fx[f + 1] = g.Ux[f]; a.Fy[f + 1] = g.Uy[f];

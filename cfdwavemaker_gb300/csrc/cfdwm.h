@@ -174,9 +174,12 @@ struct SmitIn {
 int smit_build(const SmitIn &c, DevSea &sea, void *stream);
 // u, v, w, dp of the Smit theory at n points into rows 1..4 of out (row
 // stride ldo), from the point phasors (float2 (cos, sin), [npad_g][n]) and
-// ramps, the first-order sums (first[0] = eta1) and eta2; scratch: 4 n floats.
+// ramps, the first-order sums (first[0] = eta1) and eta2; scratch: 4 n floats;
+// split_buf (split_cap floats, or null): partial sums when the pair loop is
+// split over blocks for few points.
 int smit_eval(const DevSea &sea, long n, const double *z, const void *ph, const float *rr, const double *first,
-              const float *eta2, float *scratch, long ldo, double *out, void *stream);
+              const float *eta2, float *scratch, float *split_buf, long split_cap, long ldo, double *out,
+              void *stream);
 
 // Builds the device tables (component coefficients and the FP64 transfer
 // functions of the pair tables, computed on the device).  point_table: also

@@ -692,9 +692,14 @@ __global__ void __launch_bounds__(128) k_pairs_points(PairArgs a) {
     const float z = valid ? a.z0[pc] : 0.f;
     const float zk = z * LOG2E_F, zetak = -2.f * (z + a.depth) * LOG2E_F;
     float su = 0, cu = 0, sv = 0, cv = 0, sw = 0, cw = 0, sq = 0, cq = 0;
+    // slice of the tile-pair loop owned by this blockIdx.y (block-uniform)
+    const int tp_lo = blockIdx.y * a.tp_per, tp_hi = tp_lo + a.tp_per;
+    int tp = -1;
     for (int I = 0; I < a.ntile; I++) {
         for (int M = I; M < a.ntile; M++) {
             if (!a.pairs && M != I) continue;
+            tp++;
+            if (tp < tp_lo || tp >= tp_hi) continue;
             __syncthreads();
             if (a.pairs) {
                 const float4 *src = reinterpret_cast<const float4 *>(
@@ -775,10 +780,11 @@ __global__ void __launch_bounds__(128) k_pairs_points(PairArgs a) {
         }
     }
     if (!valid) return;
-    a.out[0 * a.ncol + p] = su;
-    a.out[1 * a.ncol + p] = sv;
-    a.out[2 * a.ncol + p] = sw;
-    a.out[3 * a.ncol + p] = sq;
+    float *out = a.out + (long)blockIdx.y * 4 * a.ncol;
+    out[0 * a.ncol + p] = su;
+    out[1 * a.ncol + p] = sv;
+    out[2 * a.ncol + p] = sw;
+    out[3 * a.ncol + p] = sq;
 }
 
 // Elevation mode: eta2 from the pair cache (Irregular.cpp:223-293).  The
@@ -838,8 +844,27 @@ struct WsLayout {
     double *first;
     float *z0;
     float *sec;
+    float *split;         // partial sums of a split point-pair launch
+    long split_cap;       // its floats
     size_t bytes;
 };
+
+// Slices of the tile-pair loop for a point launch of n points: enough blocks
+// to fill the GPU (SPLIT_TARGET_BLOCKS) when the points alone give fewer.
+static int point_slices(long n, int ntp) {
+    const long nblk = (n + 127) / 128;
+    if (nblk >= SPLIT_TARGET_BLOCKS || ntp <= 1) return 1;
+    return (int)std::min<long>(ntp, (SPLIT_TARGET_BLOCKS + nblk - 1) / nblk);
+}
+// floats of the split region: up to 7 partial rows per slice and point.  A
+// split launch has fewer than SPLIT_TARGET_BLOCKS blocks of 128 points and
+// at most ceil(SPLIT_TARGET_BLOCKS / blocks) slices, so slices x points stay
+// below 128 (2 SPLIT_TARGET_BLOCKS); the region has that fixed size, whatever
+// the batch (a batch's last, short chunk may split while its first does not).
+static long point_split_floats(long n) {
+    (void)n;
+    return 7L * 128 * 2 * SPLIT_TARGET_BLOCKS;
+}
 
 WsLayout layout(long n, int npad, void *base) {
     WsLayout L;
@@ -850,12 +875,16 @@ WsLayout layout(long n, int npad, void *base) {
     size_t o_first = take(sizeof(double) * 5 * (size_t)n);
     size_t o_z = take(sizeof(float) * (size_t)n);
     size_t o_sec = take(sizeof(float) * 5 * (size_t)n);
+    const long scap = point_split_floats(n);
+    size_t o_split = take(sizeof(float) * (size_t)std::max<long>(scap, 1));
     char *b = (char *)base;
     L.ph = (float2 *)(b + o_ph);
     L.rr = (float *)(b + o_rr);
     L.first = (double *)(b + o_first);
     L.z0 = (float *)(b + o_z);
     L.sec = (float *)(b + o_sec);
+    L.split = (float *)(b + o_split);
+    L.split_cap = scap;
     L.bytes = off;
     return L;
 }
@@ -1148,11 +1177,22 @@ int launch_pressure_kin(const DevSea &sea, double t, int nz, double *kin, cudaSt
 }
 
 static int launch_point_pairs(const DevSea &sea, long n, const float2 *ph, const float *rr,
-                              const float *z0, float *out, int pairs, cudaStream_t stream) {
+                              const float *z0, float *out, int pairs, cudaStream_t stream, float *split_buf,
+                              long split_cap) {
     PairArgs a{};
     a.ncol = n; a.nl = 1; a.nlg = 1; a.ntile = sea.ntile_p; a.tab = sea.d_tab_point;
     a.ph = ph; a.rr = rr; a.cf = sea.d_cf; a.cstride = sea.npad_g; a.z0 = z0;
     a.depth = (float)sea.depth; a.out = out; a.pairs = pairs; a.first = 1;
+    // few points: the tile-pair loop split over blockIdx.y, slices summed in order
+    const int ntp = pairs ? sea.ntile_p * (sea.ntile_p + 1) / 2 : sea.ntile_p;
+    int nslice = point_slices(n, ntp);
+    a.tp_per = (ntp + nslice - 1) / nslice;
+    nslice = (ntp + a.tp_per - 1) / a.tp_per;
+    if (nslice > 1 && (!split_buf || 4L * n * nslice > split_cap)) {
+        nslice = 1;
+        a.tp_per = ntp;
+    }
+    if (nslice > 1) a.out = split_buf;
     size_t smem = sizeof(float) * POINT_TILE * POINT_TILE * POINTV_NC + 2 * sizeof(float2) * POINT_TILE * 128;
     static bool attr = false;
     if (!attr) {
@@ -1161,10 +1201,15 @@ static int launch_point_pairs(const DevSea &sea, long n, const float2 *ph, const
         attr = true;
     }
     prof_begin(PK_POINT_PAIRS, stream);
-    k_pairs_points<POINT_TILE><<<(unsigned)((n + 127) / 128), 128, smem, stream>>>(a);
+    k_pairs_points<POINT_TILE><<<dim3((unsigned)((n + 127) / 128), (unsigned)nslice), 128, smem, stream>>>(a);
     note_launch();
     prof_end(PK_POINT_PAIRS, stream);
     CK(cudaGetLastError());
+    if (nslice > 1) {
+        k_sum_slices<<<(unsigned)((4 * n + 255) / 256), 256, 0, stream>>>(4 * n, nslice, split_buf, out);
+        note_launch();
+        CK(cudaGetLastError());
+    }
     return OK;
 }
 
@@ -1194,7 +1239,8 @@ int irregular_eval(const DevSea &sea, long n, const double *x, const double *y, 
             if (rc) return rc;
         }
         if (smit) {
-            rc = smit_eval(sea, m, z + b, L.ph, L.rr, L.first, eta2, L.sec, n, out + b, stream);
+            rc = smit_eval(sea, m, z + b, L.ph, L.rr, L.first, eta2, L.sec, L.split, L.split_cap, n, out + b,
+                           stream);
             if (rc) return rc;
         } else if (mask & 30) {
             k_prep_z<<<(unsigned)((m + 255) / 256), 256, 0, stream>>>(m, z + b, sea.swl, sea.order, L.z0);
@@ -1202,7 +1248,8 @@ int irregular_eval(const DevSea &sea, long n, const double *x, const double *y, 
             CK(cudaGetLastError());
             // the point table is padded to POINT_TILE; the phasor rows beyond
             // npad_p are never read by the point kernel
-            rc = launch_point_pairs(sea, m, L.ph, L.rr, L.z0, L.sec, sea.order != 0 ? 1 : 0, stream);
+            rc = launch_point_pairs(sea, m, L.ph, L.rr, L.z0, L.sec, sea.order != 0 ? 1 : 0, stream, L.split,
+                                    L.split_cap);
             if (rc) return rc;
         }
         k_combine<<<(unsigned)((m + 255) / 256), 256, 0, stream>>>(m, n, sea.order, sea.swl, z + b,

@@ -183,9 +183,13 @@ struct SmitArgs {
     const double *phase;       // [7][cstride]: omega in row 2
     const float *zs, *sp1, *chain, *above;
     float depth;
+    int tp_per;                // tile pairs per blockIdx.y
+    float *part;               // [slices][7][n] partial sums (split launches), or null
     long ldo;
     double *out;               // rows 1..4: u, v, w, dp
 };
+
+constexpr int SMIT_PARTS = 7;  // u, v, w, dp, d phi2/ds, eta_x, d phi1/ds
 
 template <int TT>
 __global__ void __launch_bounds__(128) k_smit_points(SmitArgs a) {
@@ -203,8 +207,12 @@ __global__ void __launch_bounds__(128) k_smit_points(SmitArgs a) {
     const float zk = zs * L2E, zetak = -2.f * (zs + h) * L2E;
     float su = 0, cu = 0, sv = 0, cv = 0, sw = 0, cw = 0, sq = 0, cq = 0, sd = 0, cd = 0;
     float ex = 0, cex = 0, ps = 0, cps = 0;   // first-order eta_x and d phi1 / ds of the chain term
+    const int tp_lo = blockIdx.y * a.tp_per, tp_hi = tp_lo + a.tp_per;   // this block's tile pairs
+    int tp = -1;
     for (int I = 0; I < a.ntile; I++) {
         for (int M = I; M < a.ntile; M++) {
+            tp++;
+            if (tp < tp_lo || tp >= tp_hi) continue;      // block-uniform
             __syncthreads();
             {
                 const float4 *src = reinterpret_cast<const float4 *>(a.tab + stile(I, M, a.ntile) * (long)TT * TT * SNC);
@@ -305,12 +313,36 @@ __global__ void __launch_bounds__(128) k_smit_points(SmitArgs a) {
         }
     }
     if (!valid) return;
+    if (a.part) {
+        float *o = a.part + (long)blockIdx.y * SMIT_PARTS * a.n + p;
+        const float v[SMIT_PARTS] = {su - cu, sv - cv, sw - cw, sq - cq, sd - cd, ex - cex, ps - cps};
+        for (int q = 0; q < SMIT_PARTS; q++) o[(long)q * a.n] = v[q];
+        return;
+    }
     const bool up = a.above[p] != 0.f;
     const double chain = (double)a.chain[p] * ((double)ex - cex) * (((double)ps - cps) + ((double)sd - cd));
     a.out[1 * a.ldo + p] = up ? 0.0 : ((double)su - cu) + chain;
     a.out[2 * a.ldo + p] = up ? 0.0 : (double)sv - cv;
     a.out[3 * a.ldo + p] = up ? 0.0 : (double)sw - cw;
     a.out[4 * a.ldo + p] = up ? 0.0 : (double)sq - cq;
+}
+
+// The slices of a split launch summed in order, then the chain term.
+__global__ void k_smit_finish(long n, int nslice, const float *part, const float *chain, const float *above,
+                              long ldo, double *out) {
+    long p = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    double v[SMIT_PARTS];
+    for (int q = 0; q < SMIT_PARTS; q++) {
+        float s = 0.f, c = 0.f;
+        for (int k = 0; k < nslice; k++) skahan(s, c, part[((long)k * SMIT_PARTS + q) * n + p]);
+        v[q] = (double)s - c;
+    }
+    const bool up = above[p] != 0.f;
+    out[1 * ldo + p] = up ? 0.0 : v[0] + (double)chain[p] * v[5] * (v[6] + v[4]);
+    out[2 * ldo + p] = up ? 0.0 : v[1];
+    out[3 * ldo + p] = up ? 0.0 : v[2];
+    out[4 * ldo + p] = up ? 0.0 : v[3];
 }
 
 }  // namespace
@@ -332,7 +364,8 @@ int smit_build(const SmitIn &c, DevSea &sea, void *stream_) {
 }
 
 int smit_eval(const DevSea &sea, long n, const double *z, const void *ph, const float *rr, const double *first,
-              const float *eta2, float *scratch, long ldo, double *out, void *stream_) {
+              const float *eta2, float *scratch, float *split_buf, long split_cap, long ldo, double *out,
+              void *stream_) {
     cudaStream_t stream = (cudaStream_t)stream_;
     if (!sea.d_tab_smit) return E_NOT_INITIALIZED;
     if (n <= 0) return OK;
@@ -346,6 +379,19 @@ int smit_eval(const DevSea &sea, long n, const double *z, const void *ph, const 
     a.ph = static_cast<const float2 *>(ph); a.rr = rr; a.cf = sea.d_cf; a.phase = sea.d_phase;
     a.zs = zs; a.sp1 = sp1; a.chain = chain; a.above = above;
     a.depth = (float)sea.depth; a.ldo = ldo; a.out = out;
+    // few points: the tile-pair loop split over blockIdx.y (as many blocks as
+    // fill the GPU), the slices summed in order by k_smit_finish
+    const long nblk = (n + 127) / 128;
+    const int ntp = sea.ntile_s * (sea.ntile_s + 1) / 2;
+    const long target = 4L * 152;
+    int nslice = nblk >= target ? 1 : (int)std::min<long>(ntp, (target + nblk - 1) / nblk);
+    a.tp_per = (ntp + nslice - 1) / nslice;
+    nslice = (ntp + a.tp_per - 1) / a.tp_per;
+    if (nslice > 1 && (!split_buf || (long)SMIT_PARTS * n * nslice > split_cap)) {
+        nslice = 1;
+        a.tp_per = ntp;
+    }
+    a.part = nslice > 1 ? split_buf : nullptr;
     const size_t smem = sizeof(float) * ST * ST * SNC + 2 * sizeof(float2) * ST * 128 + sizeof(float) * ST * 128;
     static bool attr = false;
     if (!attr) {
@@ -353,10 +399,15 @@ int smit_eval(const DevSea &sea, long n, const double *z, const void *ph, const 
         attr = true;
     }
     prof_begin(PK_POINT_PAIRS, stream);
-    k_smit_points<ST><<<(unsigned)((n + 127) / 128), 128, smem, stream>>>(a);
+    k_smit_points<ST><<<dim3((unsigned)nblk, (unsigned)nslice), 128, smem, stream>>>(a);
     note_launch();
     prof_end(PK_POINT_PAIRS, stream);
     CK(cudaGetLastError());
+    if (nslice > 1) {
+        k_smit_finish<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(n, nslice, split_buf, chain, above, ldo, out);
+        note_launch();
+        CK(cudaGetLastError());
+    }
     return OK;
 }
 

@@ -358,15 +358,11 @@ __device__ __forceinline__ void df_kahan(float &s, float &c, float v) {
     c = (t - s) - y;
     s = t;
 }
-__device__ __forceinline__ double df_ramp(double t, double rt, double ts, double du) {
-    double rampdown = fmax(fmin(1. - ((t - ts - du + rt) / (rt + SMALL)), 1.), 0.);
-    double rampup = fmax(fmin(((t - ts) / (rt + SMALL)), 1.), 0.);
-    return rampup * rampdown;
-}
 
 // shared record of a component: phase coefficients as float pairs, ramp, 5 coefficients
 struct DfComp {
-    float kxh, kxl, kyh, kyl, wh, wl, ph, pl, r, c[5];
+    FfComp f;
+    float c[5];
 };
 
 template <int MODE>
@@ -376,12 +372,7 @@ __device__ __forceinline__ void df_stage(const DfFirstArgs &a, int i0, DfComp *s
         DfComp d = {};
         if (i < a.ncomp) {
             const int cs = a.cstride;
-            ff_split(a.phase[i], d.kxh, d.kxl);
-            ff_split(a.phase[cs + i], d.kyh, d.kyl);
-            ff_split(-a.phase[2 * cs + i], d.wh, d.wl);
-            ff_split(a.phase[3 * cs + i], d.ph, d.pl);
-            const int ir = a.trivial_ramp ? 0 : i;
-            d.r = (float)df_ramp(a.t, a.phase[4 * cs + ir], a.phase[5 * cs + ir], a.phase[6 * cs + ir]);
+            d.f = ff_component(a.phase, cs, i, a.trivial_ramp, a.t);
             if (MODE == 0) {
                 d.c[0] = a.cf[CF_A * cs + i];
                 d.c[1] = a.cf[CF_GX * cs + i];
@@ -401,13 +392,6 @@ __device__ __forceinline__ void df_stage(const DfFirstArgs &a, int i0, DfComp *s
     }
 }
 
-__device__ __forceinline__ void df_phasor(const DfComp &d, float dxh, float dxl, float dyh, float dyl, float th,
-                                          float tl, float &c, float &s) {
-    float2 ph = ff_add(ff_mul(d.kxh, d.kxl, dxh, dxl), ff_mul(d.kyh, d.kyl, dyh, dyl));
-    ph = ff_add(ph, ff_mul(d.wh, d.wl, th, tl));
-    ph = ff_add(ph, make_float2(d.ph, d.pl));
-    sincosf(ff_reduce_2pi(ph), &s, &c);
-}
 
 __global__ void __launch_bounds__(128) k_df_first_surface(DfFirstArgs a) {
     __shared__ DfComp sc[DFC];
@@ -427,8 +411,8 @@ __global__ void __launch_bounds__(128) k_df_first_surface(DfFirstArgs a) {
         for (int ii = 0; ii < iend; ii++) {
             const DfComp &d = sc[ii];
             float c, sn;
-            df_phasor(d, dxh, dxl, dyh, dyl, th, tl, c, sn);
-            const float rc = d.r * c, rs = d.r * sn;
+            ff_phasor(d.f, dxh, dxl, dyh, dyl, th, tl, c, sn);
+            const float rc = d.f.r * c, rs = d.f.r * sn;
             df_kahan(s[0], k[0], rc * d.c[0]);
             df_kahan(s[1], k[1], rc * d.c[1]);
             df_kahan(s[2], k[2], rc * d.c[2]);
@@ -476,8 +460,8 @@ __global__ void __launch_bounds__(256) k_df_first_levels(DfFirstArgs a) {
         const int iend = min(DFC, a.ncomp - i0);
         for (int ii = wg; ii < iend; ii += nw) {
             float c, sn;
-            df_phasor(sc[ii], dxh, dxl, dyh, dyl, th, tl, c, sn);
-            s_ph[ii][cl] = make_float2(sc[ii].r * c, sc[ii].r * sn);
+            ff_phasor(sc[ii].f, dxh, dxl, dyh, dyl, th, tl, c, sn);
+            s_ph[ii][cl] = make_float2(sc[ii].f.r * c, sc[ii].f.r * sn);
         }
         __syncthreads();
         float tu[4] = {0, 0, 0, 0}, tv[4] = {0, 0, 0, 0}, tw[4] = {0, 0, 0, 0}, tp[4] = {0, 0, 0, 0};

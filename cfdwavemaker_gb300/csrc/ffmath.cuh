@@ -37,4 +37,38 @@ __host__ __device__ __forceinline__ void ff_split(double v, float &hi, float &lo
     lo = (float)(v - (double)hi);
 }
 
+// Irregular::freq_ramp (Irregular.cpp:200-204), FP64
+__device__ __forceinline__ double ff_freq_ramp(double t, double rt, double ts, double du) {
+    const double small = 1.e-12;   // Irregular.h:8
+    double rampdown = fmax(fmin(1. - ((t - ts - du + rt) / (rt + small)), 1.), 0.);
+    double rampup = fmax(fmin(((t - ts) / (rt + small)), 1.), 0.);
+    return rampup * rampdown;
+}
+
+// One component's phase coefficients as float pairs and its ramp at time t.
+struct FfComp {
+    float kxh, kxl, kyh, kyl, wh, wl, ph, pl, r;
+};
+// Component i of the FP64 phase rows [7][cs] (kx, ky, omega, phase0, ramptime,
+// starttime, duration); with trivial_ramp every component has component 0's ramp.
+__device__ __forceinline__ FfComp ff_component(const double *phase, int cs, int i, int trivial_ramp, double t) {
+    FfComp d;
+    ff_split(phase[i], d.kxh, d.kxl);
+    ff_split(phase[cs + i], d.kyh, d.kyl);
+    ff_split(-phase[2 * cs + i], d.wh, d.wl);
+    ff_split(phase[3 * cs + i], d.ph, d.pl);
+    const int ir = trivial_ramp ? 0 : i;
+    d.r = (float)ff_freq_ramp(t, phase[4 * cs + ir], phase[5 * cs + ir], phase[6 * cs + ir]);
+    return d;
+}
+// cos and sin of kx (x - fx) + ky (y - fy) - omega t + phase0, the offsets and
+// t given as float pairs
+__device__ __forceinline__ void ff_phasor(const FfComp &d, float dxh, float dxl, float dyh, float dyl, float th,
+                                          float tl, float &c, float &s) {
+    float2 ph = ff_add(ff_mul(d.kxh, d.kxl, dxh, dxl), ff_mul(d.kyh, d.kyl, dyh, dyl));
+    ph = ff_add(ph, ff_mul(d.wh, d.wl, th, tl));
+    ph = ff_add(ph, make_float2(d.ph, d.pl));
+    sincosf(ff_reduce_2pi(ph), &s, &c);
+}
+
 }  // namespace cfdwm

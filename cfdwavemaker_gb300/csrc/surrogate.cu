@@ -31,8 +31,10 @@
 // step) next to the plain pair sum (about 4e13 operations), so the
 // convolutions are direct FP32 CUDA-core kernels with shared-memory tiles:
 // input tile + halo and a 16-output-channel weight slice per block, weight
-// reads as warp broadcasts.
+// reads as warp broadcasts.  The features form their phases in float-float
+// arithmetic in the kernel (no FP64 phasor table of the halo grid).
 #include "cfdwm.h"
+#include "ffmath.cuh"
 #include "sgrid_geom.cuh"
 
 #include <cuda_bf16.h>
@@ -56,9 +58,6 @@ namespace cfdwm {
         }                                                      \
     } while (0)
 
-int launch_phasors_public(const DevSea &sea, long n, const double *x, const double *y, const double *t,
-                          long sx, long sy, long st, int npad, float2 *ph, float *rr, double *first,
-                          cudaStream_t stream);
 GridGeom grid_geom(const DevGrid &g);
 
 namespace {
@@ -91,8 +90,10 @@ struct FeatArgs {
     GridGeom g;
     int nxh, nyh;
     long ncolh;
-    const float2 *ph;      // [npad][ncolh] phasors (cos, sin)
-    const float *rr;       // [npad][ncolh] ramps
+    const double *xy;      // [2][ncolh] coordinates of the halo columns
+    double t, fx, fy;
+    const double *phase;   // [7][cstride]: kx, ky, omega, phase0, ramp parameters
+    int trivial_ramp;
     const double *first;   // [5][ncolh]: eta1, phi1_dxdz, phi1_dydz, phi1_dzdz, dp1_dz
     const float *cf;
     int cstride, ncomp;
@@ -102,14 +103,25 @@ struct FeatArgs {
     float *eta1;           // [nx ny] (interior), or null
 };
 
-// blockDim = 32 columns x ceil(nl / 4) level groups of 4 levels
+constexpr int FC = 128;      // components per shared-memory chunk
+
+// blockDim = 32 columns x ceil(nl / 4) level groups of 4 levels.  The warps
+// hold the same 32 columns: each forms the float-float phasors of every
+// nw-th component of a chunk into shared memory, and all of them read the
+// whole chunk, so a (column, component) phasor is formed once per block.
 __global__ void __launch_bounds__(256) k_surr_features(FeatArgs a) {
-    __shared__ float s_c[5][256];    // k, cu, cv, cw, cp of a chunk of components
-    const int cl = threadIdx.x & 31, lg = threadIdx.x >> 5;
+    __shared__ FfComp s_f[FC];
+    __shared__ float s_c[5][FC];         // k, cu, cv, cw, cp of the chunk's components
+    __shared__ float2 s_ph[FC][32];      // (r cos, r sin) of (component, column)
+    const int cl = threadIdx.x & 31, lg = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const long p = (long)blockIdx.x * 32 + cl;
     const bool valid = p < a.ncolh;
     const long pc = valid ? p : 0;
     const GridGeom &g = a.g;
+    float dxh, dxl, dyh, dyl, th, tl;
+    ff_split(a.xy[pc] - a.fx, dxh, dxl);
+    ff_split(a.xy[a.ncolh + pc] - a.fy, dyh, dyl);
+    ff_split(a.t, th, tl);
     const double e1 = a.first[pc];
     float zk[4], yk[4], za[4];
 #pragma unroll
@@ -126,12 +138,14 @@ __global__ void __launch_bounds__(256) k_surr_features(FeatArgs a) {
     for (int l = 0; l < 4; l++)
 #pragma unroll
         for (int q = 0; q < NQ; q++) acc[l][q] = 0.f;
-    for (int i0 = 0; i0 < a.ncomp; i0 += 256) {
+    for (int i0 = 0; i0 < a.ncomp; i0 += FC) {
         __syncthreads();
-        for (int e = threadIdx.x; e < 256; e += blockDim.x) {
+        for (int e = threadIdx.x; e < FC; e += blockDim.x) {
             int i = i0 + e;
             float k = 0.f, cu = 0.f, cv = 0.f, cw = 0.f, cp = 0.f;
+            FfComp f = {};
             if (i < a.ncomp) {
+                f = ff_component(a.phase, a.cstride, i, a.trivial_ramp, a.t);
                 float q = a.cf[CF_Q * a.cstride + i];
                 float au = a.cf[CF_AU * a.cstride + i] * q;
                 k = a.cf[CF_K * a.cstride + i];
@@ -140,15 +154,20 @@ __global__ void __launch_bounds__(256) k_surr_features(FeatArgs a) {
                 cw = au;
                 cp = a.cf[CF_A * a.cstride + i] * q;
             }
+            s_f[e] = f;
             s_c[0][e] = k; s_c[1][e] = cu; s_c[2][e] = cv; s_c[3][e] = cw; s_c[4][e] = cp;
         }
         __syncthreads();
-        const int iend = min(256, a.ncomp - i0);
+        const int iend = min(FC, a.ncomp - i0);
+        for (int ii = lg; ii < iend; ii += nw) {
+            float c, sn;
+            ff_phasor(s_f[ii], dxh, dxl, dyh, dyl, th, tl, c, sn);
+            s_ph[ii][cl] = make_float2(s_f[ii].r * c, s_f[ii].r * sn);
+        }
+        __syncthreads();
         for (int ii = 0; ii < iend; ii++) {
-            const long i = i0 + ii;
-            const float2 pv = a.ph[i * a.ncolh + pc];
-            const float r = a.rr[i * a.ncolh + pc];
-            const float rc = r * pv.x, rs = r * pv.y;
+            const float2 pv = s_ph[ii][cl];
+            const float rc = pv.x, rs = pv.y;
             const float k = s_c[0][ii];
             const float q0 = s_c[1][ii] * rc, q1 = s_c[1][ii] * rs;
             const float q2 = s_c[2][ii] * rc, q3 = s_c[2][ii] * rs;
@@ -588,7 +607,6 @@ struct Surrogate {
     const float *g_eta = nullptr;      // identity of the attached grid
     double g_dx = 0, g_dy = 0, g_dom[4] = {0, 0, 0, 0}, g_ign[4] = {0, 0, 0, 0};
     double *xyh = nullptr;
-    double *tdev = nullptr;
     float *feat = nullptr, *base = nullptr, *eta1 = nullptr, *pred = nullptr, *hbuf = nullptr;
     float *R = nullptr;        // residual (plain - network) of the last plain slot, [cout][nx ny]
     float *Rtmp = nullptr;
@@ -606,10 +624,10 @@ struct Surrogate {
 static Surrogate g_s;
 
 static void free_grid_side(Surrogate &s) {
-    void *q[] = {s.xyh, s.tdev, s.feat, s.base, s.eta1, s.pred, s.hbuf, s.rETA, s.rU[0], s.rU[1], s.rU[2],
+    void *q[] = {s.xyh, s.feat, s.base, s.eta1, s.pred, s.hbuf, s.rETA, s.rU[0], s.rU[1], s.rU[2],
                  s.d_sample, s.d_err, s.R, s.Rtmp};
     for (void *p : q) if (p) cudaFree(p);
-    s.xyh = nullptr; s.tdev = nullptr; s.feat = s.base = s.eta1 = s.pred = s.hbuf = s.rETA = s.R = nullptr;
+    s.xyh = nullptr; s.feat = s.base = s.eta1 = s.pred = s.hbuf = s.rETA = s.R = nullptr;
     s.Rtmp = nullptr;
     s.have_res = false;
     s.rU[0] = s.rU[1] = s.rU[2] = nullptr;
@@ -926,7 +944,6 @@ static int attach_grid(Surrogate &s, DevGrid &g, cudaStream_t st) {
     const int nxh = g.nx + 2 * SH, nyh = g.ny + 2 * SH;
     const long nh = (long)nxh * nyh, nxy = (long)g.nx * g.ny, n = nxy * g.nl;
     CK(cudaMalloc(&s.xyh, sizeof(double) * 2 * nh));
-    CK(cudaMalloc(&s.tdev, sizeof(double)));
     CK(cudaMalloc(&s.feat, sizeof(float) * s.cin * nh));
     CK(cudaMalloc(&s.base, sizeof(float) * 3 * n));
     CK(cudaMalloc(&s.eta1, sizeof(float) * nxy));
@@ -961,24 +978,20 @@ static int features(Surrogate &s, const Config &cfg, const DevSea &sea, DevGrid 
                     float *feat, float *base, float *eta1, cudaStream_t st) {
     const int nxh = g.nx + 2 * SH, nyh = g.ny + 2 * SH;
     const long nh = (long)nxh * nyh;
-    const int npad = sea.npad_g;
-    auto up = [](size_t b) { return (b + 255) / 256 * 256; };
-    size_t b_ph = up(sizeof(float2) * (size_t)npad * nh), b_rr = up(sizeof(float) * (size_t)npad * nh);
-    int rc = workspace_reserve(ws, b_ph + b_rr + sizeof(double) * 5 * nh);
+    int rc = workspace_reserve(ws, sizeof(double) * 5 * nh);
     if (rc) return rc;
-    char *b = (char *)ws.base;
-    float2 *ph = (float2 *)b;
-    float *rr = (float *)(b + b_ph);
-    double *first = (double *)(b + b_ph + b_rr);
-    CK(cudaMemcpyAsync(s.tdev, &t, sizeof(double), cudaMemcpyHostToDevice, st));
-    rc = launch_phasors_public(sea, nh, s.xyh, s.xyh + nh, s.tdev, 1, 1, 0, npad, ph, rr, first, st);
+    double *first = (double *)ws.base;
+    // eta1 and the Taylor gradients of the halo columns (float-float phases)
+    rc = depthform_first(sea, nh, g.nl, s.xyh, t, nullptr, first, nullptr, 3, st);
     if (rc) return rc;
     double sigma, om, km;
     sea_scales(cfg, sigma, om, km);
     FeatArgs a;
     a.g = grid_geom(g);
     a.nxh = nxh; a.nyh = nyh; a.ncolh = nh;
-    a.ph = ph; a.rr = rr; a.first = first; a.cf = sea.d_cf; a.cstride = sea.npad_g; a.ncomp = sea.n;
+    a.xy = s.xyh; a.t = t; a.fx = sea.fx; a.fy = sea.fy; a.phase = sea.d_phase;
+    a.trivial_ramp = sea.trivial_ramp ? 1 : 0;
+    a.first = first; a.cf = sea.d_cf; a.cstride = sea.npad_g; a.ncomp = sea.n;
     a.inv_su = (float)(1.0 / (sigma * om));
     a.inv_sp = (float)(1.0 / sigma);
     a.feat = feat; a.base = base; a.eta1 = eta1;

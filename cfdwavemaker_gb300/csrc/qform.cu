@@ -282,49 +282,62 @@ struct QPrep {
     float *Y;                  // [rows][2 npad]
 };
 
-__device__ __forceinline__ void qform_prep_one(const QPrep &a, long p, int i) {
-    float c = 0.f, s = 0.f, r = 0.f;
-    if (i < a.ncomp) {
-        const QRow R = a.row[p];
-        const QComp K = a.comp[i];
-        float2 ph = ff_add(ff_mul(K.kxh, K.kxl, R.dxh, R.dxl), ff_mul(K.kyh, K.kyl, R.dyh, R.dyl));
-        ph = ff_add(ph, ff_mul(K.wh, K.wl, R.th, R.tl));
-        ph = ff_add(ph, make_float2(K.ph, K.pl));
-        float red = ff_reduce_2pi(ph);
-        __sincosf(red, &s, &c);
-        r = a.trivial_ramp ? R.ramp
-                           : (float)q_freq_ramp(a.t[p * a.st], a.phase[4 * a.cstride + i], a.phase[5 * a.cstride + i],
-                                                a.phase[6 * a.cstride + i]);
-    }
-    long o = p * 2 * a.npad + i;
-    a.Y[o] = c;
-    a.Y[o + a.npad] = s;
-    float xc = r * c, xs = r * s;
-    if (a.fp16) {
-        __half *H = (__half *)a.Xhi, *L = (__half *)a.Xlo;
-        __half hc = __float2half_rn(xc), hs = __float2half_rn(xs);
-        H[o] = hc;
-        H[o + a.npad] = hs;
-        L[o] = __float2half_rn((xc - __half2float(hc)) * 2048.0f);
-        L[o + a.npad] = __float2half_rn((xs - __half2float(hs)) * 2048.0f);
-    } else {
-        __nv_bfloat16 *H = (__nv_bfloat16 *)a.Xhi, *L = (__nv_bfloat16 *)a.Xlo;
-        __nv_bfloat16 hc = __float2bfloat16_rn(xc), hs = __float2bfloat16_rn(xs);
-        H[o] = hc;
-        H[o + a.npad] = hs;
-        L[o] = __float2bfloat16_rn(xc - __bfloat162float(hc));
-        L[o + a.npad] = __float2bfloat16_rn(xs - __bfloat162float(hs));
-    }
-}
+constexpr int PREP_ROWS = 8;       // rows per block of the operand preparation
 
-// Block-stride loop over (row, block of 256 components).
-__global__ void __launch_bounds__(256) k_qform_prep(QPrep a) {
-    const long nb = a.npad / 256;
-    const long tot = a.rows * nb;
-    for (long blk = blockIdx.x; blk < tot; blk += gridDim.x) {
-        const long p = blk / nb;
-        const int i = (int)(blk % nb) * 256 + threadIdx.x;
-        qform_prep_one(a, p, i);
+// blockDim 128: thread t owns components i = 256 blockIdx.x + 2t and i + 1
+// (their float-float coefficients stay in registers); blockIdx.y: a group of
+// PREP_ROWS rows.  Per (row, component): the float-float phase, its cos and
+// sin (Y), and r cos, r sin split into hi and lo 16-bit parts (X); the pairs
+// of components are written as float2 / 16-bit pairs.
+__global__ void __launch_bounds__(128) k_qform_prep(QPrep a) {
+    const int i = blockIdx.x * 256 + 2 * threadIdx.x;
+    QComp K[2];
+    bool on[2];
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+        on[q] = i + q < a.ncomp;
+        K[q] = on[q] ? a.comp[i + q] : QComp{0, 0, 0, 0, 0, 0, 0, 0};
+    }
+    const long p0 = (long)blockIdx.y * PREP_ROWS;
+    for (int rr = 0; rr < PREP_ROWS; rr++) {
+        const long p = p0 + rr;
+        if (p >= a.rows) break;
+        const QRow R = a.row[p];
+        float c[2] = {0.f, 0.f}, s[2] = {0.f, 0.f}, r[2] = {0.f, 0.f};
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+            if (!on[q]) continue;
+            float2 ph = ff_add(ff_mul(K[q].kxh, K[q].kxl, R.dxh, R.dxl), ff_mul(K[q].kyh, K[q].kyl, R.dyh, R.dyl));
+            ph = ff_add(ph, ff_mul(K[q].wh, K[q].wl, R.th, R.tl));
+            ph = ff_add(ph, make_float2(K[q].ph, K[q].pl));
+            __sincosf(ff_reduce_2pi(ph), &s[q], &c[q]);
+            r[q] = a.trivial_ramp ? R.ramp
+                                  : (float)q_freq_ramp(a.t[p * a.st], a.phase[4 * a.cstride + i + q],
+                                                       a.phase[5 * a.cstride + i + q], a.phase[6 * a.cstride + i + q]);
+        }
+        const long o = p * 2 * a.npad + i;
+        *reinterpret_cast<float2 *>(a.Y + o) = make_float2(c[0], c[1]);
+        *reinterpret_cast<float2 *>(a.Y + o + a.npad) = make_float2(s[0], s[1]);
+        const float xc0 = r[0] * c[0], xc1 = r[1] * c[1], xs0 = r[0] * s[0], xs1 = r[1] * s[1];
+        if (a.fp16) {
+            const __half2 hc = __floats2half2_rn(xc0, xc1), hs = __floats2half2_rn(xs0, xs1);
+            const float2 fc = __half22float2(hc), fs = __half22float2(hs);
+            __half2 *H = reinterpret_cast<__half2 *>((__half *)a.Xhi + o);
+            __half2 *L = reinterpret_cast<__half2 *>((__half *)a.Xlo + o);
+            H[0] = hc;
+            H[a.npad / 2] = hs;
+            L[0] = __floats2half2_rn((xc0 - fc.x) * 2048.0f, (xc1 - fc.y) * 2048.0f);
+            L[a.npad / 2] = __floats2half2_rn((xs0 - fs.x) * 2048.0f, (xs1 - fs.y) * 2048.0f);
+        } else {
+            const __nv_bfloat162 hc = __floats2bfloat162_rn(xc0, xc1), hs = __floats2bfloat162_rn(xs0, xs1);
+            const float2 fc = __bfloat1622float2(hc), fs = __bfloat1622float2(hs);
+            __nv_bfloat162 *H = reinterpret_cast<__nv_bfloat162 *>((__nv_bfloat16 *)a.Xhi + o);
+            __nv_bfloat162 *L = reinterpret_cast<__nv_bfloat162 *>((__nv_bfloat16 *)a.Xlo + o);
+            H[0] = hc;
+            H[a.npad / 2] = hs;
+            L[0] = __floats2bfloat162_rn(xc0 - fc.x, xc1 - fc.y);
+            L[a.npad / 2] = __floats2bfloat162_rn(xs0 - fs.x, xs1 - fs.y);
+        }
     }
 }
 
@@ -851,19 +864,9 @@ int tcform_eval(TcForm &f, const DevSea &sea, long n, const double *x, const dou
         pp.cstride = sea.npad_g; pp.ncomp = sea.n; pp.npad = npad;
         pp.trivial_ramp = sea.trivial_ramp ? 1 : 0; pp.fp16 = f.fp16 ? 1 : 0;
         pp.Xhi = Xh; pp.Xlo = Xl; pp.Y = Y;
-        static int nsm_p = 0;
-        if (!nsm_p) {
-            int dev = 0;
-            CK(cudaGetDevice(&dev));
-            CK(cudaDeviceGetAttribute(&nsm_p, cudaDevAttrMultiProcessorCount, dev));
-        }
-        const long pblocks = mm * (long)(npad / 256);
         // a full grid: with two blocks per SM beside the GEMM the preparation
-        // ran latency-bound at a tenth of its speed (24 ms against 2.3 ms per
-        // 65,536 x 4096 chunk) and became the bottleneck
-        const long pgrid = std::min<long>(pblocks, 1L << 20);
-        (void)nsm_p;
-        k_qform_prep<<<(unsigned)pgrid, 256, 0, pst>>>(pp);
+        // ran latency-bound at a tenth of its speed and became the bottleneck
+        k_qform_prep<<<dim3((unsigned)(npad / 256), (unsigned)((mm + PREP_ROWS - 1) / PREP_ROWS)), 128, 0, pst>>>(pp);
         note_launch();
         CK(cudaGetLastError());
         if (nbuf == 2) {

@@ -234,8 +234,9 @@ def regular_cases():
 
 
 def run_regular(args):
-    """configs[1]: both regular theories at 1e7 points each per step, through
-    wave_Kinematics_batch (device arrays for value; host arrays for e2e)."""
+    """The regular-wave workload: Stokes 5th and Fenton stream function at 1e7
+    points each per step, through wave_Kinematics_batch (device arrays for
+    value; host arrays for e2e)."""
     import torch
     import cfdwavemaker_gb300 as cw
     ws, rank, local = dist_init()

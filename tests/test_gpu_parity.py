@@ -233,6 +233,29 @@ def test_sgrid_tensor_core_method_vs_plain(wm):
         assert err <= tol, (w, err)
 
 
+def test_sgrid_full_size_tensor_core_vs_plain(wm):
+    """The benchmark's grid at full size: 256 x 256 columns x 16 levels of the
+    1024-component sea; the tensor-core form against the plain form (itself
+    pinned to the reference) on every node of the ring after the initial fill
+    and one update."""
+    import ctypes as C
+    from cfdwavemaker_gb300 import seastate as ss
+    comps = ss.config3_sea()
+    grid = {"bounds": (0.0, 1000.0, 0.0, 1000.0), "nx": 256, "ny": 256, "nl": 16, "t0": 0.0, "dt": 0.5,
+            "stretch": (0.7, 1.5)}
+    txt = ss.write_irregular(None, comps, 100.0, extrap=2, lsgrid=grid)
+    arrs = {}
+    for method in (0, 1):
+        assert wm.initialize_text(txt) == 0, cw.last_error()
+        R = C.c_int(0)
+        assert wm.lib.cfdwm_sgrid_method(method, C.byref(R)) == 0, cw.last_error()
+        wm.force_update(0.7)
+        arrs[method] = [wm.sgrid_array(w) for w in range(4)]
+    for w in range(4):
+        err = norm_rel_err(arrs[1][w], arrs[0][w])
+        assert err <= TOL, (w, err)
+
+
 def test_sgrid_opposite_directions_vs_oracle(wm):
     """Directions exactly opposite at equal frequency (theta = -90 and +90 deg
     of a spread rotated by mtheta = 228.70473821303267 deg): the radicand of

@@ -126,3 +126,19 @@ def test_tensor_core_several_chunks(wm, torch):
     for f in range(4):
         err = norm_rel_err(got[rows, f], ref[:, f])
         assert err <= TOL, (f, err)
+
+
+def test_full_size_sea_fp16_split(wm, torch):
+    """The benchmark's sea at full size: 256 frequencies x 16 directions = 4096
+    components (8.4e6 pair-cache pairs), 131,072 rows in two chunks; a sample of
+    rows in both chunks against the FP64 oracle."""
+    txt = _sea(256, 16, 2024)
+    n = 131072
+    x, y, t, got = _run(wm, torch, txt, n, 1, True, seed=13)
+    rng = np.random.default_rng(4)
+    rows = np.concatenate([rng.choice(65536, 12, replace=False), 65536 + rng.choice(65536, 12, replace=False)])
+    ref = _reference(txt, x[rows], y[rows], t[rows])
+    for f in range(4):
+        err = norm_rel_err(got[rows, f], ref[:, f])
+        print("fp16x3 N=4096 field", f, "err", err)
+        assert err <= TOL, (f, err)

@@ -229,6 +229,7 @@ struct DevGrid {
     float *Uy[4] = {nullptr, nullptr, nullptr, nullptr};
     float *Us[4] = {nullptr, nullptr, nullptr, nullptr};
     int *IGNORE = nullptr;
+    float *QIMG = nullptr;       // query image of the two slots a query reads ([2][nodes][5][4] floats)
     float *zlev = nullptr;       // scratch: level heights of the slot being written
     double *colpts = nullptr;    // scratch: column x, y, t (FP64)
     double *first = nullptr;     // scratch: eta1, gx, gy, gz per column

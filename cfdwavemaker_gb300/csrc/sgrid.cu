@@ -182,7 +182,7 @@ struct QueryArgs {
     int tid1, tid2;
     double t0;
     const float *ETA, *ETAdt, *ETAdx, *ETAdy;
-    const float *U[4], *Ut[4], *Ux[4], *Uy[4], *Us[4];
+    const float4 *img;      // query image: [2][nodes][5] (U, U_t, U_x, U_y, U_s over the fields)
     int nf;
     long n;
     const double *x, *y, *z, *t;
@@ -209,47 +209,51 @@ __device__ __forceinline__ float cart2sigmaS(const GridGeom &g, float tanab, flo
 
 __device__ __forceinline__ int iclamp(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
-__device__ float spline_velo(const QueryArgs &a, int f, int xp, int yp, int s0, int s1, float xd,
-                             float yd, float sd0, float sd1, float td) {
+__device__ __forceinline__ float4 herm4(float4 f0, float4 f1, float4 d0, float4 d1, float h, float r) {
+    return make_float4(herm(f0.x, f1.x, d0.x, d1.x, h, r), herm(f0.y, f1.y, d0.y, d1.y, h, r),
+                       herm(f0.z, f1.z, d0.z, d1.z, h, r), herm(f0.w, f1.w, d0.w, d1.w, h, r));
+}
+__device__ __forceinline__ float4 lin4(float4 f0, float4 f1, float r) {
+    return make_float4(lin(f0.x, f1.x, r), lin(f0.y, f1.y, r), lin(f0.z, f1.z, r), lin(f0.w, f1.w, r));
+}
+
+// spline_interp_velo (lsgrid_spline.cpp:386-502) of every velocity field at
+// once: the eight corners of each of the two bracketing slots are read as
+// records of the query image, and the reductions x -> y -> s -> t run on the
+// fields as float4 lanes (the reference's order, per field).
+__device__ float4 spline_velo4(const QueryArgs &a, int xp, int yp, int s0, int s1, float xd, float yd, float sd0,
+                               float sd1, float td) {
     const GridGeom &g = a.g;
     const long nn = (long)g.nx * g.ny * g.nl;
     const int x1 = iclamp(xp + 1, 0, g.nx - 1), y1 = iclamp(yp + 1, 0, g.ny - 1);
     const int ls[2] = {s0, s1};
-    const int tsl[2] = {a.tid1, a.tid2};
-    float red[2], redt[2];
-    for (int q = 0; q < 2; q++) {            // q = 0: slot tid1 at s0; q = 1: slot tid2 at s1
-        int l0 = ls[q], l1 = iclamp(ls[q] + 1, 0, g.nl - 1);
-        long bv = (long)tsl[q] * nn, bg = (long)q * nn;
-        long idx[8];
-        int xs[8] = {xp, xp, x1, x1, xp, xp, x1, x1};
-        int ys[8] = {yp, y1, yp, y1, yp, y1, yp, y1};
-        int zs[8] = {l0, l0, l0, l0, l1, l1, l1, l1};
-        for (int k = 0; k < 8; k++) idx[k] = ((long)xs[k] * g.ny + ys[k]) * g.nl + zs[k];
-        float C[8], Cx[8], Cy[8], Cs[8], Ct[8];
-        for (int k = 0; k < 8; k++) {
-            C[k] = __ldg(a.U[f] + bv + idx[k]);
-            Ct[k] = __ldg(a.Ut[f] + bv + idx[k]);
-            Cx[k] = __ldg(a.Ux[f] + bg + idx[k]);
-            Cy[k] = __ldg(a.Uy[f] + bg + idx[k]);
-            Cs[k] = __ldg(a.Us[f] + bg + idx[k]);
+    const float dx = (float)g.dx, dy = (float)g.dy, ds = (float)g.ds;
+    float4 red[2], redt[2];
+    for (int q = 0; q < 2; q++) {            // q = 0: slot (tstep+1)%4 at s0; q = 1: slot (tstep+2)%4 at s1
+        const int l0 = ls[q], l1 = iclamp(ls[q] + 1, 0, g.nl - 1);
+        const float4 *base = a.img + (long)q * nn * 5;
+        // corners: x-pairs (xp, x1) at (yp, l0), (y1, l0), (yp, l1), (y1, l1)
+        const int ys[4] = {yp, y1, yp, y1}, zs[4] = {l0, l0, l1, l1};
+        float4 v[4], yv[4], tv[4], sv[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const float4 *ra = base + (((long)xp * g.ny + ys[k]) * g.nl + zs[k]) * 5;
+            const float4 *rb = base + (((long)x1 * g.ny + ys[k]) * g.nl + zs[k]) * 5;
+            const float4 aU = __ldg(ra), aT = __ldg(ra + 1), aX = __ldg(ra + 2), aY = __ldg(ra + 3), aS = __ldg(ra + 4);
+            const float4 bU = __ldg(rb), bT = __ldg(rb + 1), bX = __ldg(rb + 2), bY = __ldg(rb + 3), bS = __ldg(rb + 4);
+            v[k] = herm4(aU, bU, aX, bX, dx, xd);
+            yv[k] = lin4(aY, bY, xd);
+            tv[k] = lin4(aT, bT, xd);
+            sv[k] = lin4(aS, bS, xd);
         }
-        const float dx = (float)g.dx, dy = (float)g.dy, ds = (float)g.ds;
-        float v00 = herm(C[0], C[2], Cx[0], Cx[2], dx, xd), v10 = herm(C[1], C[3], Cx[1], Cx[3], dx, xd);
-        float v01 = herm(C[4], C[6], Cx[4], Cx[6], dx, xd), v11 = herm(C[5], C[7], Cx[5], Cx[7], dx, xd);
-        float y00 = lin(Cy[0], Cy[2], xd), y10 = lin(Cy[1], Cy[3], xd);
-        float y01 = lin(Cy[4], Cy[6], xd), y11 = lin(Cy[5], Cy[7], xd);
-        float t00 = lin(Ct[0], Ct[2], xd), t10 = lin(Ct[1], Ct[3], xd);
-        float t01 = lin(Ct[4], Ct[6], xd), t11 = lin(Ct[5], Ct[7], xd);
-        float s00 = lin(Cs[0], Cs[2], xd), s10 = lin(Cs[1], Cs[3], xd);
-        float s01 = lin(Cs[4], Cs[6], xd), s11 = lin(Cs[5], Cs[7], xd);
-        float c0 = herm(v00, v10, y00, y10, dy, yd), c1 = herm(v01, v11, y01, y11, dy, yd);
-        float c0s = lin(s00, s10, yd), c1s = lin(s01, s11, yd);
-        float c0t = lin(t00, t10, yd), c1t = lin(t01, t11, yd);
-        float sd = q == 0 ? sd0 : sd1;
-        red[q] = herm(c0, c1, c0s, c1s, ds, sd);
-        redt[q] = lin(c0t, c1t, sd);
+        const float4 c0 = herm4(v[0], v[1], yv[0], yv[1], dy, yd), c1 = herm4(v[2], v[3], yv[2], yv[3], dy, yd);
+        const float4 c0s = lin4(sv[0], sv[1], yd), c1s = lin4(sv[2], sv[3], yd);
+        const float4 c0t = lin4(tv[0], tv[1], yd), c1t = lin4(tv[2], tv[3], yd);
+        const float sd = q == 0 ? sd0 : sd1;
+        red[q] = herm4(c0, c1, c0s, c1s, ds, sd);
+        redt[q] = lin4(c0t, c1t, sd);
     }
-    return herm(red[0], red[1], redt[0], redt[1], (float)g.dt, td);
+    return herm4(red[0], red[1], redt[0], redt[1], (float)g.dt, td);
 }
 
 __global__ void __launch_bounds__(128) k_query(QueryArgs a) {
@@ -295,8 +299,42 @@ __global__ void __launch_bounds__(128) k_query(QueryArgs a) {
     float sd0 = modff(n0, &s0i), sd1 = modff(n1, &s1i);
     int s0 = iclamp((int)s0i, 0, g.nl - 1), s1 = iclamp((int)s1i, 0, g.nl - 1);
     a.out[p] = eta;
-    for (int f = 0; f < a.nf; f++)
-        a.out[(long)(f + 1) * a.n + p] = spline_velo(a, f, xp, yp, s0, s1, xd, yd, sd0, sd1, td);
+    const float4 u = spline_velo4(a, xp, yp, s0, s1, xd, yd, sd0, sd1, td);
+    a.out[1 * a.n + p] = u.x;
+    a.out[2 * a.n + p] = u.y;
+    a.out[3 * a.n + p] = u.z;
+    if (a.nf == 4) a.out[4 * a.n + p] = u.w;
+}
+
+// The query image of the two slots the queries read, (tstep+1)%4 and
+// (tstep+2)%4: per node one record of five float4, U, U_t, U_x, U_y, U_s, each
+// over the velocity fields (and the pressure; lane 3 is 0 without it).  A
+// query corner is then one 80-byte record instead of 5 nf separate loads.
+struct QImgArgs {
+    const float *U[4], *Ut[4], *Ux[4], *Uy[4], *Us[4];
+    int nf, tstep;
+    long nodes;
+    float4 *img;
+};
+__global__ void k_query_image(QImgArgs a) {
+    const long e = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (e >= a.nodes) return;
+    const int q = blockIdx.y;
+    const long S = a.nodes;
+    const long ts = (long)((a.tstep + 1 + q) % 4) * S + e, gs = (long)q * S + e;
+    float r[5][4];
+#pragma unroll
+    for (int f = 0; f < 4; f++) {
+        const bool on = f < a.nf;
+        r[0][f] = on ? a.U[f][ts] : 0.f;
+        r[1][f] = on ? a.Ut[f][ts] : 0.f;
+        r[2][f] = on ? a.Ux[f][gs] : 0.f;
+        r[3][f] = on ? a.Uy[f][gs] : 0.f;
+        r[4][f] = on ? a.Us[f][gs] : 0.f;
+    }
+    float4 *o = a.img + ((long)q * S + e) * 5;
+#pragma unroll
+    for (int k = 0; k < 5; k++) o[k] = make_float4(r[k][0], r[k][1], r[k][2], r[k][3]);
 }
 
 // ---------------------------------------------------------------------------
@@ -393,6 +431,7 @@ int grid_create(const Config &cfg, DevGrid &g, void *stream_) {
     CK(cudaMalloc(&x->tdev, sizeof(double)));
     x->split_cap = column_pairs_split_floats(g.nl);
     CK(cudaMalloc(&x->split, sizeof(float) * x->split_cap));
+    CK(cudaMalloc(&g.QIMG, sizeof(float4) * 10 * v));
     CK(cudaStreamSynchronize(stream));
     return OK;
 }
@@ -407,8 +446,10 @@ void grid_free(DevGrid &g) {
     }
     g.nf = 3;
     if (g.IGNORE) cudaFree(g.IGNORE);
+    if (g.QIMG) cudaFree(g.QIMG);
     g.ETA = g.ETAdx = g.ETAdy = g.ETAdt = nullptr;
     g.IGNORE = nullptr;
+    g.QIMG = nullptr;
     for (auto it = g_extra.begin(); it != g_extra.end(); ++it)
         if (it->first == &g) {
             GridExtra &x = it->second;
@@ -542,6 +583,14 @@ static int gradients(DevGrid &g, cudaStream_t stream) {
     prof_begin(PK_GRADIENTS, stream);
     k_gradients<<<grid, 256, 0, stream>>>(a);
     note_launch();
+    CK(cudaGetLastError());
+    QImgArgs qa;
+    for (int f = 0; f < 4; f++) {
+        qa.U[f] = g.U[f]; qa.Ut[f] = g.Ut[f]; qa.Ux[f] = g.Ux[f]; qa.Uy[f] = g.Uy[f]; qa.Us[f] = g.Us[f];
+    }
+    qa.nf = g.nf; qa.tstep = g.tstep; qa.nodes = nodes; qa.img = reinterpret_cast<float4 *>(g.QIMG);
+    k_query_image<<<dim3((unsigned)((nodes + 255) / 256), 2), 256, 0, stream>>>(qa);
+    note_launch();
     prof_end(PK_GRADIENTS, stream);
     CK(cudaGetLastError());
     return OK;
@@ -642,9 +691,7 @@ int grid_query(const DevGrid &g, long n, const double *x, const double *y, const
     a.g = geom(g);
     a.tid1 = (g.tstep + 1) % 4; a.tid2 = (g.tstep + 2) % 4; a.t0 = g.t0;
     a.ETA = g.ETA; a.ETAdt = g.ETAdt; a.ETAdx = g.ETAdx; a.ETAdy = g.ETAdy;
-    for (int f = 0; f < 4; f++) {
-        a.U[f] = g.U[f]; a.Ut[f] = g.Ut[f]; a.Ux[f] = g.Ux[f]; a.Uy[f] = g.Uy[f]; a.Us[f] = g.Us[f];
-    }
+    a.img = reinterpret_cast<const float4 *>(g.QIMG);
     a.nf = g.nf;
     a.n = n; a.x = x; a.y = y; a.z = z; a.t = t; a.out = out;
     prof_begin(PK_QUERY, stream);

@@ -230,6 +230,7 @@ def test_sgrid_tensor_core_method_vs_plain(wm):
     for w in range(19):
         tol = TOL if w <= 3 else TOL_GRAD
         err = norm_rel_err(arrs[1][w], arrs[0][w])
+        print("tensor-core vs plain, array", w, "err", err)
         assert err <= tol, (w, err)
 
 
@@ -253,6 +254,7 @@ def test_sgrid_full_size_tensor_core_vs_plain(wm):
         arrs[method] = [wm.sgrid_array(w) for w in range(4)]
     for w in range(4):
         err = norm_rel_err(arrs[1][w], arrs[0][w])
+        print("full size, tensor-core vs plain, array", w, "err", err)
         assert err <= TOL, (w, err)
 
 

@@ -24,8 +24,10 @@
 // matrix, its eigenvectors by cyclic Jacobi rotations, b_r on a fine z table
 // (barycentric interpolation through the nodes), f_r and g_r on a fine k
 // table (quadrature).  The rank is the smallest R whose reconstruction error
-// over a test set of (k, z) is below 3e-7 of max F: the profile error then
-// enters the second-order sums at or below FP32 rounding of the result.
+// over a test set of (k, z) is below 4e-6 of max F: the profile error then
+// stays at the level of the fp16x3 split's own error on the second-order sums
+// (about 5e-6 of their maximum), and the whole field (first order included)
+// differs from the plain form by a few 1e-7.
 #include "cfdwm.h"
 #include "ffmath.cuh"
 #include "sgrid_geom.cuh"
@@ -200,7 +202,7 @@ static int build_basis(double K, double h, DfBasis &B) {
     std::vector<double> bb((size_t)DF_RMAX * nz);
     for (int r = 0; r < DF_RMAX && r < nz; r++)
         for (int j = 0; j < nz; j++) bb[(size_t)r * nz + j] = V[(size_t)ord[r] * nz + j] / std::sqrt(w[j]);
-    // smallest R with max |F - sum_r f_r b_r| <= 3e-7 * 2 over a test set
+    // smallest R with max |F - sum_r f_r b_r| <= 4e-6 * 2 over a test set
     std::vector<double> lw = bary_weights(z, w, -h, 0.0);
     const int nkt = 48, nzt = 160;
     const int rmax = std::min(DF_RMAX, nz);
@@ -228,7 +230,7 @@ static int build_basis(double K, double h, DfBasis &B) {
                 for (int r = 0; r < Rt; r++) Fa += ft[(size_t)a * rmax + r] * bt[(size_t)r * nzt + c];
                 emax = std::max(emax, std::fabs(Ft[(size_t)a * nzt + c] - Fa));
             }
-        if (emax <= 6e-7) {
+        if (emax <= 8e-6) {
             R = Rt;
             e_at_R = emax;
             break;

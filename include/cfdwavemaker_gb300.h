@@ -204,7 +204,7 @@ CFDWM_EXPORT int cfdwm_irregular_fields_noalloc(const double *x, const double *y
  * 1: (default; environment CFDWM_SGRID_METHOD=0 at wave_Initialize selects
  *    the plain form) the depth-separable tensor-core form: the depth profiles
  *    e^{kz} +- e^{-k(z+2h)} are expanded in R orthonormal functions of z
- *    (R chosen so that the expansion error is <= 3e-7 of max F), each
+ *    (R chosen so that the expansion error is <= 4e-6 of max F), each
  *    coefficient sum is a quadratic form over the column's phasors, and all
  *    of them with eta2 run as one split-fp16 tcgen05 GEMM over the columns.
  * rank (may be NULL) receives R.  The ring is refilled at the current t0

@@ -959,12 +959,10 @@ int launch_eta_pairs(const DevSea &sea, long n, const float2 *ph, const float *r
         }
     }
     size_t smem = sizeof(float2) * (GRID_TILE * GRID_TILE + GRID_TILE * 128);
-    static bool attr = false;
-    if (!attr) {
-        CK(cudaFuncSetAttribute(k_pairs_eta<GRID_TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)smem));
-        attr = true;
-    }
+    // set once per process (thread-safe static initialisation)
+    static const cudaError_t attr = cudaFuncSetAttribute(k_pairs_eta<GRID_TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem);
+    CK(attr);
     prof_begin(PK_ETA_PAIRS, stream);
     k_pairs_eta<GRID_TILE><<<dim3((unsigned)nblk, (unsigned)nslice), 128, smem, stream>>>(a);
     note_launch();
@@ -993,12 +991,10 @@ static int column_pairs_t(const PairArgs &a, long nblk, int nslice, int cols, cu
         return sizeof(float) * GRID_TILE * GRID_TILE * GRIDV_NC + (PR ? sizeof(float2) * GRID_TILE * GRID_TILE : 0) +
                sizeof(float2) * GRID_TILE * c;
     };
-    static bool attr = false;
-    if (!attr) {
-        CK(cudaFuncSetAttribute(k_pairs_columns<GRID_TILE, LV, PR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)bytes(128)));
-        attr = true;
-    }
+    // set once per process (thread-safe static initialisation)
+    static const cudaError_t attr = cudaFuncSetAttribute(k_pairs_columns<GRID_TILE, LV, PR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)bytes(128));
+    CK(attr);
     prof_begin(PK_COLUMN_PAIRS, stream);
     k_pairs_columns<GRID_TILE, LV, PR><<<dim3((unsigned)nblk, (unsigned)nslice), 128, bytes(cols), stream>>>(a);
     note_launch();
@@ -1160,11 +1156,9 @@ int launch_pressure_kin(const DevSea &sea, double t, int nz, double *kin, cudaSt
     while (zb > 1 && sizeof(float) * (size_t)np * (2 + 2 * zb) > cap) zb--;
     const size_t smem = sizeof(float) * (size_t)np * (2 + 2 * zb);
     if (smem > cap) return E_TOO_LARGE;
-    static bool attr = false;
-    if (!attr) {
-        CK(cudaFuncSetAttribute(k_pressure_kin, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap));
-        attr = true;
-    }
+    // set once per process (thread-safe static initialisation)
+    static const cudaError_t attr = cudaFuncSetAttribute(k_pressure_kin, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap);
+    CK(attr);
     KinArgs a;
     a.tabk = reinterpret_cast<const float2 *>(sea.d_tab_gk);
     a.ntile = sea.ntile_g; a.ncomp = sea.n; a.npad = np; a.trivial_ramp = sea.trivial_ramp ? 1 : 0; a.zb = zb;
@@ -1194,12 +1188,10 @@ static int launch_point_pairs(const DevSea &sea, long n, const float2 *ph, const
     }
     if (nslice > 1) a.out = split_buf;
     size_t smem = sizeof(float) * POINT_TILE * POINT_TILE * POINTV_NC + 2 * sizeof(float2) * POINT_TILE * 128;
-    static bool attr = false;
-    if (!attr) {
-        CK(cudaFuncSetAttribute(k_pairs_points<POINT_TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)smem));
-        attr = true;
-    }
+    // set once per process (thread-safe static initialisation)
+    static const cudaError_t attr = cudaFuncSetAttribute(k_pairs_points<POINT_TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem);
+    CK(attr);
     prof_begin(PK_POINT_PAIRS, stream);
     k_pairs_points<POINT_TILE><<<dim3((unsigned)((n + 127) / 128), (unsigned)nslice), 128, smem, stream>>>(a);
     note_launch();

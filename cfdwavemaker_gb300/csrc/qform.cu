@@ -833,14 +833,15 @@ int tcform_eval(TcForm &f, const DevSea &sea, long n, const double *x, const dou
         CK(cudaEventRecord(ev[0], stream));          // inputs and the zeroed output are ordered before
         CK(cudaStreamWaitEvent(pst, ev[0], 0));
     }
-    static bool attr = false;
-    if (!attr) {
-        CK(cudaFuncSetAttribute(k_qform_tc<128, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                TcCfg<128, true>::SMEM));
-        CK(cudaFuncSetAttribute(k_qform_tc<256, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                TcCfg<256, false>::SMEM));
-        attr = true;
-    }
+    // set once per process (thread-safe static initialisation)
+    static const cudaError_t attr = [] {
+        cudaError_t e = cudaFuncSetAttribute(k_qform_tc<128, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             TcCfg<128, true>::SMEM);
+        if (e != cudaSuccess) return e;
+        return cudaFuncSetAttribute(k_qform_tc<256, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    TcCfg<256, false>::SMEM);
+    }();
+    CK(attr);
     const int BN = f.fp16 ? 128 : 256;
     int j = 0;
     for (long b = 0; b < n; b += chunk, j++) {

@@ -393,11 +393,9 @@ int smit_eval(const DevSea &sea, long n, const double *z, const void *ph, const 
     }
     a.part = nslice > 1 ? split_buf : nullptr;
     const size_t smem = sizeof(float) * ST * ST * SNC + 2 * sizeof(float2) * ST * 128 + sizeof(float) * ST * 128;
-    static bool attr = false;
-    if (!attr) {
-        CK(cudaFuncSetAttribute(k_smit_points<ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        attr = true;
-    }
+    // set once per process (thread-safe static initialisation)
+    static const cudaError_t attr = cudaFuncSetAttribute(k_smit_points<ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    CK(attr);
     prof_begin(PK_POINT_PAIRS, stream);
     k_smit_points<ST><<<dim3((unsigned)nblk, (unsigned)nslice), 128, smem, stream>>>(a);
     note_launch();

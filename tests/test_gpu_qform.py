@@ -142,3 +142,19 @@ def test_full_size_sea_fp16_split(wm, torch):
         err = norm_rel_err(got[rows, f], ref[:, f])
         print("fp16x3 N=4096 field", f, "err", err)
         assert err <= TOL, (f, err)
+
+
+def test_tensor_core_fp16_split_component_ramps(wm, torch):
+    """Individual component ramps still rising at the evaluation times: the
+    ramp enters the operands per (row, component)."""
+    from cfdwavemaker_gb300 import seastate as ss
+    comps = ss.irregular_components(6.0, 12.0, 2.0, 24, 0.25, 1.6, 100.0, 31, ndir=4, spreading_s=10.0)
+    n = comps["omega"].size
+    rng = np.random.default_rng(6)
+    rcols = [rng.uniform(20.0, 120.0, n), rng.uniform(-5.0, 10.0, n), rng.uniform(300.0, 600.0, n)]
+    txt = ss.write_irregular(None, comps, 100.0, extrap=2, ramp_columns=rcols)
+    x, y, t, got = _run(wm, torch, txt, 3000, 1, True, seed=9)
+    ref = _reference(txt, x, y, t)
+    for f in range(4):
+        err = norm_rel_err(got[:, f], ref[:, f])
+        assert err <= TOL, (f, err)

@@ -185,3 +185,6 @@ def test_sgrid_pressure_with_component_ramps(wm):
                 og.force_update(tt)
             _, ts = wm.sgrid_state()
             _compare_pressure(wm, og, ts, ("ramps", method, k))
+            for which in range(4):      # elevation and velocities of the ring too
+                err = norm_rel_err(wm.sgrid_array(which), og.array(which))
+                assert err <= TOL, ("ramps", method, k, which, err)

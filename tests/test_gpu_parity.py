@@ -315,3 +315,26 @@ def test_empty_and_ragged_batches(wm):
         eta = wm.surface_elevation_batch(x, np.zeros(n), np.full(n, 2.0))
         ref = np.array([wm.lib.wave_SurfElev(float(a), 0.0, 2.0) for a in x[:3]])
         np.testing.assert_allclose(eta[:3], ref, rtol=0, atol=1e-12)
+
+
+def test_batches_across_chunk_boundaries(wm):
+    """A host batch of 1,100,000 points crosses the host staging chunk
+    (2^20 points) and the device evaluation chunk (2^18 points); points on
+    both sides of every boundary against the FP64 oracle."""
+    g = load_golden("config1_point")
+    init(wm, g)
+    cfg = golden_cfg(g)
+    n = 1_100_000
+    rng = np.random.default_rng(21)
+    x = rng.uniform(0, 500, n)
+    z = rng.uniform(-50, 0, n)
+    t = rng.uniform(0, 7, n)
+    y = np.zeros(n)
+    u, v, w = wm.velocity_batch(x, y, z, t)
+    p = wm.dynamic_pressure_batch(x, y, z, t)
+    idx = np.unique(np.concatenate([np.arange(0, 3), np.arange((1 << 18) - 3, (1 << 18) + 3),
+                                    np.arange((1 << 19) - 2, (1 << 19) + 2), np.arange((1 << 20) - 3, (1 << 20) + 3),
+                                    np.arange(n - 3, n), rng.choice(n, 20, replace=False)]))
+    ref = oracle.Model(cfg).api(x[idx], y[idx], z[idx], t[idx])
+    for arr, q in ((u, 1), (w, 3), (p, 4)):
+        assert norm_rel_err(arr[idx], ref[:, q]) <= TOL, q

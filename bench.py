@@ -515,6 +515,7 @@ def qform_line(args, r):
     value = f["pts_per_s"] * n
     gemm_ms = f["gemm_ms_per_step"]
     achieved = flop_pt * f["rows"] / (gemm_ms / 1e3) / 1e12 if gemm_ms > 0 else None
+    peak_s = pk.get("bf16_tflops_sustained", pk["bf16_tflops"])
     plain = forms.get("plain_fp32", {})
     line = {
         "metric": METRIC, "value": value, "unit": "points/s", "n_gpus": n, "steps": args.steps,
@@ -527,12 +528,13 @@ def qform_line(args, r):
                 "d2h_bytes_per_step": r["d2h"]},
         "gpu_launches": f["launches"],
         "clocks": f["clocks"],
-        "roofline": {"kernel": "k_qform_tc", "bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops"],
-                     "unit": "TFLOP/s", "frac": (achieved / pk["bf16_tflops"]) if achieved else None,
+        "roofline": {"kernel": "k_qform_tc", "bound": "tensor", "achieved": achieved, "peak": peak_s,
+                     "unit": "TFLOP/s", "frac": (achieved / peak_s) if achieved else None,
                      "traffic": traffic_from_profiles("k_qform_tc"),
-                     "issued_frac": (3 * achieved / pk["bf16_tflops"]) if achieved else None,
+                     "issued_frac": (3 * achieved / peak_s) if achieved else None,
                      "algorithmic": "2 flop x 4 N (N+1) coefficients per point, N = %d" % N,
-                     "peak_source": src + " bf16 burst (dense), MEASURED_PEAKS.json"},
+                     "peak_source": src + " bf16 sustained (dense; the GEMM runs inside steps of about a "
+                                          "second), MEASURED_PEAKS.json"},
         "forms": {k: {kk: vv for kk, vv in v.items() if kk != "clocks"} for k, v in forms.items()},
         "speedup_vs_plain": (f["pts_per_s"] / plain["pts_per_s"]) if plain else None,
         "init_s": r["init_s"],
@@ -659,7 +661,8 @@ def peaks():
         with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as fh:
             return json.load(fh), "measured"
     except OSError:
-        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0,
+                "sm_max_mhz": 2070.0}, "fallback"
 
 
 # ---------------------------------------------------------------------------

@@ -21,15 +21,17 @@
 //  * X is split into hi + lo 16-bit parts (bf16 or fp16) by a prep kernel
 //    that writes one chunk of rows to a scratch buffer; W is split once at
 //    set-up (stored transposed, K-major, as the B operand).
-//  * k_qform_tc: warp-specialised tcgen05 GEMM, one 128 x 256 output tile
-//    per CTA: warp 0 issues TMA loads (128B swizzle) into a two-stage ring,
-//    one thread of warp 1 issues tcgen05.mma (M=128, N=256, K=16) for the
-//    three split products Xh Wh + Xh Wl + Xl Wh into an FP32 TMEM
-//    accumulator (fp16: the cross products go to a second accumulator with
-//    the lo parts scaled by 2^11), warps 2-5 read TMEM with tcgen05.ld,
-//    multiply by the right-hand phasors and reduce the row, one atomic add
-//    per (row, tile).  Tiles are ordered in groups so that the X and W tiles
-//    in flight stay L2-resident.  Only the K blocks of the upper triangle are
+//  * k_qform_tc: warp-specialised persistent tcgen05 GEMM on CTA pairs
+//    (cta_group::2), one 256 x 256 output tile per pair: warp 0 of each CTA
+//    issues TMA loads (128B swizzle) of its 128 rows of X and its half of
+//    the W tile into a stage ring, one thread of CTA 0 issues tcgen05.mma
+//    (M=256, N=256, K=16) for the three split products Xh Wh + Xh Wl + Xl Wh
+//    into FP32 TMEM accumulators (fp16: the cross products go to a second
+//    accumulator with the lo parts scaled by 2^11), warps 2-9 read TMEM with
+//    tcgen05.ld, multiply by the right-hand phasors (column-major, loaded
+//    before the accumulator is ready) and reduce the row, one atomic add per
+//    (row, tile).  Tiles are ordered in groups so that the X and W tiles in
+//    flight stay L2-resident.  Only the K blocks of the upper triangle are
 //    visited.  Every mbarrier wait is bounded; a timeout sets an error word.
 //  * k_qform_plain: the same sums on FP32 CUDA cores (the plain form).
 #include "cfdwm.h"
@@ -41,6 +43,7 @@
 #include <cuda_runtime.h>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <vector>
 
 namespace cfdwm {
@@ -279,17 +282,21 @@ struct QPrep {
     int cstride, ncomp, npad;
     int trivial_ramp, fp16;
     void *Xhi, *Xlo;           // [rows][2 npad]
-    float *Y;                  // [rows][2 npad]
+    float *Y;                  // [2 npad][ldy], column-major: rows adjacent
+    long ldy;                  // >= rows rounded up to PREP_ROWS
 };
 
-constexpr int PREP_ROWS = 8;       // rows per block of the operand preparation
+constexpr int PREP_ROWS = 16;      // rows per block of the operand preparation
 
 // blockDim 128: thread t owns components i = 256 blockIdx.x + 2t and i + 1
 // (their float-float coefficients stay in registers); blockIdx.y: a group of
 // PREP_ROWS rows.  Per (row, component): the float-float phase, its cos and
-// sin (Y), and r cos, r sin split into hi and lo 16-bit parts (X); the pairs
-// of components are written as float2 / 16-bit pairs.
+// sin (Y), and r cos, r sin split into hi and lo 16-bit parts (X).  X rows are
+// written as 16-bit pairs; Y is staged in shared memory and written
+// column-major, each column's 16 rows (64 B) by 16 adjacent threads (rows
+// past the last are zero).
 __global__ void __launch_bounds__(128) k_qform_prep(QPrep a) {
+    __shared__ float s_y[512][PREP_ROWS + 1];     // [cos 256 | sin 256][row]
     const int i = blockIdx.x * 256 + 2 * threadIdx.x;
     QComp K[2];
     bool on[2];
@@ -301,23 +308,29 @@ __global__ void __launch_bounds__(128) k_qform_prep(QPrep a) {
     const long p0 = (long)blockIdx.y * PREP_ROWS;
     for (int rr = 0; rr < PREP_ROWS; rr++) {
         const long p = p0 + rr;
-        if (p >= a.rows) break;
-        const QRow R = a.row[p];
         float c[2] = {0.f, 0.f}, s[2] = {0.f, 0.f}, r[2] = {0.f, 0.f};
+        if (p < a.rows) {
+            const QRow R = a.row[p];
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+                if (!on[q]) continue;
+                float2 ph = ff_add(ff_mul(K[q].kxh, K[q].kxl, R.dxh, R.dxl), ff_mul(K[q].kyh, K[q].kyl, R.dyh, R.dyl));
+                ph = ff_add(ph, ff_mul(K[q].wh, K[q].wl, R.th, R.tl));
+                ph = ff_add(ph, make_float2(K[q].ph, K[q].pl));
+                __sincosf(ff_reduce_2pi(ph), &s[q], &c[q]);
+                r[q] = a.trivial_ramp ? R.ramp
+                                      : (float)q_freq_ramp(a.t[p * a.st], a.phase[4 * a.cstride + i + q],
+                                                           a.phase[5 * a.cstride + i + q],
+                                                           a.phase[6 * a.cstride + i + q]);
+            }
+        }
 #pragma unroll
         for (int q = 0; q < 2; q++) {
-            if (!on[q]) continue;
-            float2 ph = ff_add(ff_mul(K[q].kxh, K[q].kxl, R.dxh, R.dxl), ff_mul(K[q].kyh, K[q].kyl, R.dyh, R.dyl));
-            ph = ff_add(ph, ff_mul(K[q].wh, K[q].wl, R.th, R.tl));
-            ph = ff_add(ph, make_float2(K[q].ph, K[q].pl));
-            __sincosf(ff_reduce_2pi(ph), &s[q], &c[q]);
-            r[q] = a.trivial_ramp ? R.ramp
-                                  : (float)q_freq_ramp(a.t[p * a.st], a.phase[4 * a.cstride + i + q],
-                                                       a.phase[5 * a.cstride + i + q], a.phase[6 * a.cstride + i + q]);
+            s_y[2 * threadIdx.x + q][rr] = c[q];
+            s_y[256 + 2 * threadIdx.x + q][rr] = s[q];
         }
+        if (p >= a.rows) continue;
         const long o = p * 2 * a.npad + i;
-        *reinterpret_cast<float2 *>(a.Y + o) = make_float2(c[0], c[1]);
-        *reinterpret_cast<float2 *>(a.Y + o + a.npad) = make_float2(s[0], s[1]);
         const float xc0 = r[0] * c[0], xc1 = r[1] * c[1], xs0 = r[0] * s[0], xs1 = r[1] * s[1];
         if (a.fp16) {
             const __half2 hc = __floats2half2_rn(xc0, xc1), hs = __floats2half2_rn(xs0, xs1);
@@ -338,6 +351,15 @@ __global__ void __launch_bounds__(128) k_qform_prep(QPrep a) {
             L[0] = __floats2bfloat162_rn(xc0 - fc.x, xc1 - fc.y);
             L[a.npad / 2] = __floats2bfloat162_rn(xs0 - fs.x, xs1 - fs.y);
         }
+    }
+    __syncthreads();
+    // Y: warp w writes columns 2 k + (lane >> 4), k = w, w + 4, ..., rows lane & 15
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int rr = lane & (PREP_ROWS - 1);
+    const int i0 = blockIdx.x * 256;
+    for (int col = 2 * warp + (lane >> 4); col < 512; col += 8) {
+        const long gcol = col < 256 ? (long)i0 + col : (long)a.npad + i0 + (col - 256);
+        a.Y[gcol * a.ldy + p0 + rr] = s_y[col][rr];
     }
 }
 
@@ -405,18 +427,21 @@ __global__ void __launch_bounds__(128) k_qform_plain(QPlain a) {
 // tcgen05 tensor-core form
 // ---------------------------------------------------------------------------
 constexpr int TBM = 128, TBK = 64;
-// two variants (TMEM holds 512 FP32 columns), each with two accumulator
-// buffers so that the epilogue of one tile hides behind the next tile's MMAs:
-//   bf16, one accumulator, N = 256, 2 stages;
-//   fp16, hi and cross accumulators, N = 128, 3 stages.
-// (An fp16 variant with N = 256 and a single buffer measured no faster at
-// N = 4096: 1207 ms against 1161 ms per 4e6 points.)
+// variants (TMEM holds 512 FP32 columns), all with N = 256 MMAs (measured:
+// M = 128, N = 128 MMAs kept the tensor pipe about 60% busy, N = 256 about 80%):
+//   bf16, one accumulator, two accumulator buffers, so that the epilogue of
+//   one tile hides behind the next tile's MMAs;
+//   fp16, hi and cross accumulators filling TMEM, one buffer;
+// each on one SM (M = 128) or on a CTA pair (M = 256, cta_group::2: each CTA
+// holds its 128 rows of X and half of the W tile, so each SM stages and reads
+// half the W bytes; measured 3-10% faster than the one-SM form).
 constexpr int TBN = 256;                  // component padding unit
 constexpr int A_TILE = TBM * TBK * 2;     // 16 KiB
-template <int BN, bool TWO> struct TcCfg {
-    static constexpr int B_TILE = BN * TBK * 2;
-    static constexpr int STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;
-    static constexpr int STAGES = BN == 128 ? 3 : 2;
+template <int BN, bool TWO, bool PAIR> struct TcCfg {
+    static constexpr int BROWS = PAIR ? BN / 2 : BN;     // W rows held by one CTA
+    static constexpr int B_TILE = BROWS * TBK * 2;
+    static constexpr int STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;   // one CTA's share of a stage
+    static constexpr int STAGES = 196608 / STAGE_BYTES < 4 ? 196608 / STAGE_BYTES : 4;
     static constexpr int SMEM = STAGES * STAGE_BYTES + 1024 + 256;
     static constexpr int ACOLS = TWO ? 2 * BN : BN;     // TMEM columns of one tile
     static constexpr int NBUF = 512 / ACOLS;             // accumulator buffers
@@ -468,6 +493,61 @@ __device__ __forceinline__ void umma(uint32_t dt, uint64_t a, uint64_t b, uint32
 __device__ __forceinline__ void umma_commit(uint64_t *bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(bar)) : "memory");
 }
+// CTA-pair forms (cta_group::2).  The load lands in this CTA's shared memory
+// and signals the mbarrier at cluster address `bar`, which may be the peer's.
+__device__ __forceinline__ void tma_2d_pair(void *dst, const CUtensorMap *m, uint32_t bar, int x, int y) {
+    asm volatile("cp.async.bulk.tensor.2d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes"
+                 " [%0], [%1, {%3, %4}], [%2];"
+                 ::"r"(su32(dst)), "l"(m), "r"(bar), "r"(x), "r"(y) : "memory");
+}
+// one MMA of the pair: M = 256 (128 rows from each CTA's shared memory at the
+// same offsets), N columns (the first half of B from this CTA, the second from
+// the peer); each CTA's TMEM receives its own 128 rows
+__device__ __forceinline__ void umma_pair(uint32_t dt, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+    asm volatile("{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n}"
+                 ::"r"(dt), "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+// arrives once on the mbarrier at this offset in both CTAs of the pair when the
+// pair's MMAs issued so far have completed
+__device__ __forceinline__ void umma_pair_commit(uint64_t *bar) {
+    asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;"
+                 ::"r"(su32(bar)), "h"((uint16_t)3) : "memory");
+}
+// cluster address of the same shared-memory location in CTA `rank`
+__device__ __forceinline__ uint32_t mapa_rank(const void *p, uint32_t rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(su32(p)), "r"(rank));
+    return r;
+}
+__device__ __forceinline__ void mbar_arrive_remote(uint32_t bar) {
+    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_cluster(uint64_t *b, uint32_t parity) {
+    uint32_t ok;
+    asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+                 "selp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(ok) : "r"(su32(b)), "r"(parity) : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ uint32_t cluster_ctarank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ uint32_t cluster_id_x() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ uint32_t ncluster_x() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%nclusterid.x;" : "=r"(r));
+    return r;
+}
+// every thread of every CTA of the cluster
+__device__ __forceinline__ void cluster_sync_all() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
@@ -483,12 +563,13 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
 struct QTC {
     long rows;               // rows of this chunk
     int npad;                // components (multiple of 256)
-    int ntn;                 // column tiles per block (npad / 256)
+    int ntn;                 // column tiles per block (npad / N)
     int group_m;             // row blocks per tile group
     int nblk;                // coefficient blocks of W
     int nout;                // outputs per row
     const int *bmap;         // per block: X half, Y half, output column
-    const float *Y;          // [rows][2 npad]
+    const float *Y;          // [2 npad][ldy], column-major
+    long ldy;
     const float *colscale;   // [nblk][npad] (1 for bf16)
     float *out;              // [rows][nout] accumulated with atomics
     int fp16;
@@ -509,68 +590,123 @@ __device__ __forceinline__ bool mbar_wait_e(uint64_t *b, uint32_t parity, int *e
     return true;
 }
 
+// the same with cluster-scope acquire: the arrivals come from both CTAs of a pair
+__device__ __forceinline__ bool mbar_wait_ec(uint64_t *b, uint32_t parity, int *err, int code) {
+    long long t0 = clock64();
+    int n = 0;
+    while (!mbar_try_cluster(b, parity)) {
+        if ((++n & 255) == 0 && *(volatile int *)err != 0) return false;
+        if (clock64() - t0 > WAIT_LIMIT) {
+            atomicExch(err, code);
+            return false;
+        }
+    }
+    return true;
+}
+
 struct TileInfo {
     long rb;
     int blk, tn, nkb;
 };
 
-// grouped tile order: a group of group_m row blocks sweeps all column tiles
-template <int BN>
-__device__ __forceinline__ bool tile_of(const QTC &a, long nrb, long t, TileInfo &ti) {
+// grouped tile order: a group of group_m row units sweeps all column tiles.
+// A row unit is CS consecutive row blocks, one per CTA of a cluster (CTA rank
+// r takes block CS u + r; a block past the last row reads zeros through TMA
+// and stores nothing), so that the CTAs of a cluster share every W tile.
+// Validity depends on the unit only: the CTAs of a cluster walk the same
+// tile sequence.
+template <int BN, int CS>
+__device__ __forceinline__ bool tile_of(const QTC &a, long nru, long t, int crank, TileInfo &ti) {
     const int ncol = a.nblk * a.ntn;
-    const long per_group = (long)a.group_m * ncol;
+    const long gm = a.group_m / CS > 0 ? a.group_m / CS : 1;
+    const long per_group = gm * ncol;
     long grp = t / per_group, in = t % per_group;
-    long gm0 = grp * a.group_m;
-    long gsz = nrb - gm0 < a.group_m ? nrb - gm0 : a.group_m;
+    long gm0 = grp * gm;
+    long gsz = nru - gm0 < gm ? nru - gm0 : gm;
     if (gsz <= 0) return false;
-    ti.rb = gm0 + in % gsz;
+    long ru = gm0 + in % gsz;
     int ct = (int)(in / gsz);
-    if (ti.rb >= nrb || ct >= ncol) return false;
+    if (ru >= nru || ct >= ncol) return false;
+    ti.rb = ru * CS + crank;
     ti.blk = ct / a.ntn;
     ti.tn = ct % a.ntn;
     ti.nkb = (ti.tn * BN + BN) / TBK;          // upper triangle: i < m0 + BN
     return true;
 }
 
-// Persistent: CTA c takes tiles c, c + gridDim.x, ...  Warp 0 streams the
-// operand tiles through the stage ring (continuously across tiles), one
-// thread of warp 1 issues the MMAs into TMEM accumulator buffer (j & 1) of
-// its j-th tile, warps 2-5 drain the other buffer meanwhile: the epilogue of
-// tile j overlaps the MMAs of tile j + 1.
-template <int BN, bool TWO>
-__global__ void __launch_bounds__(192, 1) k_qform_tc(const __grid_constant__ CUtensorMap mXh,
+// Persistent: CTA (or CTA pair) c takes tile units c, c + (number of units
+// in flight), ...  Warp 0 streams the operand tiles through the stage ring
+// (continuously across tiles), one thread of warp 1 issues the MMAs into TMEM
+// accumulator buffer j % NBUF of its j-th tile, warps 2-9 drain it when its
+// MMAs complete: with two buffers (bf16) the epilogue of tile j overlaps the
+// MMAs of tile j + 1.
+// Epilogue warp w reads TMEM lane quarter w % 4 (its 32 rows) and column half
+// (w - 2) / 4; it loads its rows' right-hand phasors Y, scaled by the column
+// scales, before it waits for the accumulator, so those loads (coalesced: Y is
+// column-major) overlap the tile's MMAs.
+//
+// PAIR: a cluster of two CTAs computes a 256-row tile with cta_group::2 MMAs.
+// Both CTAs load their own 128 rows of X and their half of the W tile into
+// their own shared memory; every load signals the full barrier of CTA 0,
+// whose one thread issues the pair's MMAs.  Its commits arrive on the empty,
+// accumulator-full and done barriers of both CTAs; the epilogue warps of both
+// CTAs arrive on CTA 0's drained barrier (count 8).  Before it exits, each
+// producer waits for the last release of its stages, so no commit is still
+// on its way to a CTA that has left.
+constexpr int TC_THREADS = 320;            // producer, MMA and 8 epilogue warps
+constexpr int TC_EPI_WARPS = 8;
+
+template <int BN, bool TWO, bool PAIR>
+__global__ void __launch_bounds__(TC_THREADS, 1) k_qform_tc(const __grid_constant__ CUtensorMap mXh,
                                                      const __grid_constant__ CUtensorMap mXl,
                                                      const __grid_constant__ CUtensorMap mWh,
                                                      const __grid_constant__ CUtensorMap mWl, QTC a) {
-    using CF = TcCfg<BN, TWO>;
+    using CF = TcCfg<BN, TWO, PAIR>;
+    constexpr int CS = PAIR ? 2 : 1;
     constexpr int TSTAGES = CF::STAGES, STAGE_BYTES = CF::STAGE_BYTES, B_TILE = CF::B_TILE;
-    constexpr int ACOLS = CF::ACOLS, NBUF = CF::NBUF;
+    constexpr int BROWS = CF::BROWS, ACOLS = CF::ACOLS, NBUF = CF::NBUF;
+    static_assert((BROWS * 128) % 1024 == 0, "W halves keep the 1024 B swizzle atom");
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *full = (uint64_t *)(smem + TSTAGES * STAGE_BYTES);
     uint64_t *empty = full + TSTAGES;
     uint64_t *accf = empty + TSTAGES;         // [2] accumulator buffer full
     uint64_t *acce = accf + 2;                // [2] accumulator buffer drained
-    uint64_t *mdone = acce + 2;               // all MMAs of this CTA complete
+    uint64_t *mdone = acce + 2;               // all MMAs into this CTA's TMEM complete
     uint32_t *tmem_slot = (uint32_t *)(mdone + 1);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int crank = PAIR ? (int)cluster_ctarank() : 0;
+    const bool leader = crank == 0;
+    const long cid = PAIR ? (long)cluster_id_x() : (long)blockIdx.x;
+    const long ncl = PAIR ? (long)ncluster_x() : (long)gridDim.x;
     const long nrb = (a.rows + TBM - 1) / TBM;
-    const long ntiles = nrb * (long)a.nblk * a.ntn;
-    if (*(volatile int *)a.err != 0) return;
+    const long nru = (nrb + CS - 1) / CS;
+    const long ntiles = nru * (long)a.nblk * a.ntn;
+    // (a pair does not return early: its CTAs address each other until the end)
+    if (!PAIR && *(volatile int *)a.err != 0) return;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < TSTAGES; s++) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
-        for (int b = 0; b < 2; b++) { mbar_init(&accf[b], 1); mbar_init(&acce[b], 4); }
+        for (int b = 0; b < 2; b++) { mbar_init(&accf[b], 1); mbar_init(&acce[b], TC_EPI_WARPS * CS); }
         mbar_init(mdone, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     const uint32_t ncols_tmem = 512;          // two buffers of 256 FP32 columns (one or two accumulators)
     if (warp == 1) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(tmem_slot)),
-                     "r"(ncols_tmem));
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+        if (PAIR) {
+            asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(tmem_slot)),
+                         "r"(ncols_tmem));
+            asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;");
+        } else {
+            asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(tmem_slot)),
+                         "r"(ncols_tmem));
+            asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+        }
     }
     __syncthreads();
+    // the peer's barriers are initialised (and its TMEM allocated) before any
+    // load or MMA of the pair addresses them
+    if (PAIR) cluster_sync_all();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
 
@@ -579,11 +715,13 @@ __global__ void __launch_bounds__(192, 1) k_qform_tc(const __grid_constant__ CUt
     __syncthreads();
     if (warp == 0) {
         if (lane == 0) {
+            // the full barriers every load of the pair signals: CTA 0's
+            const uint32_t full0 = PAIR ? mapa_rank(full, 0) : 0u;
             long g = 0;
             bool ok = true;
-            for (long t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+            for (long t = cid; t < ntiles && ok; t += ncl) {
                 TileInfo ti;
-                if (!tile_of<BN>(a, nrb, t, ti)) continue;
+                if (!tile_of<BN, CS>(a, nru, t, crank, ti)) continue;
                 const int khalf = a.bmap[3 * ti.blk];
                 const int m0 = ti.tn * BN;
                 for (int kb = 0; kb < ti.nkb; kb++, g++) {
@@ -591,34 +729,50 @@ __global__ void __launch_bounds__(192, 1) k_qform_tc(const __grid_constant__ CUt
                     uint32_t ph = (uint32_t)((g / TSTAGES) & 1);
                     if (!mbar_wait_e(&empty[s], ph ^ 1, a.err, 1)) { ok = false; break; }
                     uint8_t *st = smem + s * STAGE_BYTES;
-                    mbar_expect_tx(&full[s], STAGE_BYTES);
+                    // CTA 0 expects the bytes of both CTAs' shares
+                    if (leader) mbar_expect_tx(&full[s], CS * STAGE_BYTES);
                     int kx = khalf * a.npad + kb * TBK;
                     int ky = (int)(ti.rb * TBM);
-                    tma_2d(st, &mXh, &full[s], kx, ky);
-                    tma_2d(st + A_TILE, &mXl, &full[s], kx, ky);
-                    int wy = ti.blk * a.npad + m0;
-                    tma_2d(st + 2 * A_TILE, &mWh, &full[s], kb * TBK, wy);
-                    tma_2d(st + 2 * A_TILE + B_TILE, &mWl, &full[s], kb * TBK, wy);
+                    int wy = ti.blk * a.npad + m0 + crank * BROWS;
+                    if (PAIR) {
+                        const uint32_t fb = full0 + (uint32_t)(s * 8);
+                        tma_2d_pair(st, &mXh, fb, kx, ky);
+                        tma_2d_pair(st + A_TILE, &mXl, fb, kx, ky);
+                        tma_2d_pair(st + 2 * A_TILE, &mWh, fb, kb * TBK, wy);
+                        tma_2d_pair(st + 2 * A_TILE + B_TILE, &mWl, fb, kb * TBK, wy);
+                    } else {
+                        tma_2d(st, &mXh, &full[s], kx, ky);
+                        tma_2d(st + A_TILE, &mXl, &full[s], kx, ky);
+                        tma_2d(st + 2 * A_TILE, &mWh, &full[s], kb * TBK, wy);
+                        tma_2d(st + 2 * A_TILE + B_TILE, &mWl, &full[s], kb * TBK, wy);
+                    }
                     issued_s = g + 1;
                 }
             }
+            // the last release of each stage (pair: CTA 0's commit, which also
+            // arrives here), so nothing is on its way to this CTA after it exits
+            if (ok && PAIR)
+                for (long h = g - TSTAGES > 0 ? g - TSTAGES : 0; h < g; h++)
+                    if (!mbar_wait_e(&empty[h % TSTAGES], (uint32_t)((h / TSTAGES) & 1), a.err, 7)) break;
         }
     } else if (warp == 1) {
-        if (lane == 0) {
-            // kind::f16, D = F32, A/B = bf16 (1) or f16 (0), both K-major, N = 256, M = 128
+        if (lane == 0 && leader) {
+            // kind::f16, D = F32, A/B = bf16 (1) or f16 (0), both K-major, N = BN, M = 128 CS
             const uint32_t fmt = a.fp16 ? 0u : 1u;
             const uint32_t idesc = (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(BN >> 3) << 17) |
-                                   ((uint32_t)(TBM >> 4) << 24);
+                                   ((uint32_t)((CS * TBM) >> 4) << 24);
             long g = 0;
             int j = 0;
             bool ok = true;
-            for (long t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+            for (long t = cid; t < ntiles && ok; t += ncl) {
                 TileInfo ti;
-                if (!tile_of<BN>(a, nrb, t, ti)) continue;
+                if (!tile_of<BN, CS>(a, nru, t, crank, ti)) continue;
                 const int buf = j % NBUF;
                 const uint32_t use = (uint32_t)(j / NBUF);
-                // the epilogue has drained this buffer's previous tile
-                if (!mbar_wait_e(&acce[buf], (use & 1) ^ 1, a.err, 5)) break;
+                // the epilogues (of both CTAs) have drained this buffer's previous tile
+                const bool drained = PAIR ? mbar_wait_ec(&acce[buf], (use & 1) ^ 1, a.err, 5)
+                                          : mbar_wait_e(&acce[buf], (use & 1) ^ 1, a.err, 5);
+                if (!drained) break;
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 const uint32_t acc = tmem + (uint32_t)(buf * ACOLS);
                 const uint32_t acc2 = TWO ? acc + BN : acc;     // fp16: cross products
@@ -633,78 +787,132 @@ __global__ void __launch_bounds__(192, 1) k_qform_tc(const __grid_constant__ CUt
                     for (int k = 0; k < TBK / 16; k++) {
                         uint64_t o = (uint64_t)(k * 32) >> 4;     // 16 elements = 32 bytes per step
                         uint32_t first = (kb == 0 && k == 0) ? 0u : 1u;
-                        umma(acc, dXh + o, dWh + o, idesc, first);
-                        umma(acc2, dXh + o, dWl + o, idesc, TWO ? first : 1u);
-                        umma(acc2, dXl + o, dWh + o, idesc, 1u);
+                        if (PAIR) {
+                            umma_pair(acc, dXh + o, dWh + o, idesc, first);
+                            umma_pair(acc2, dXh + o, dWl + o, idesc, TWO ? first : 1u);
+                            umma_pair(acc2, dXl + o, dWh + o, idesc, 1u);
+                        } else {
+                            umma(acc, dXh + o, dWh + o, idesc, first);
+                            umma(acc2, dXh + o, dWl + o, idesc, TWO ? first : 1u);
+                            umma(acc2, dXl + o, dWh + o, idesc, 1u);
+                        }
                     }
-                    umma_commit(&empty[s]);
+                    if (PAIR) umma_pair_commit(&empty[s]);
+                    else umma_commit(&empty[s]);
                     consumed_s = g + 1;
                 }
                 if (!ok) break;
-                umma_commit(&accf[buf]);
+                if (PAIR) umma_pair_commit(&accf[buf]);
+                else umma_commit(&accf[buf]);
                 j++;
             }
-            umma_commit(mdone);
+            if (PAIR) umma_pair_commit(mdone);
+            else umma_commit(mdone);
         }
     } else {
-        // epilogue: warps 2..5 own TMEM lane quarters (warp % 4)
-        const int q = warp & 3;
+        // epilogue: warps 2..9, lane quarter q, column half hc
+        constexpr int HC = BN / 2, NCH = HC / 32;
+        const int q = warp & 3, hc = (warp - 2) >> 2;
+        const uint32_t acce0 = PAIR ? mapa_rank(acce, 0) : 0u;
         int j = 0;
-        for (long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        for (long t = cid; t < ntiles; t += ncl) {
             TileInfo ti;
-            if (!tile_of<BN>(a, nrb, t, ti)) continue;
+            if (!tile_of<BN, CS>(a, nru, t, crank, ti)) continue;
             const int buf = j % NBUF;
             const uint32_t use = (uint32_t)(j / NBUF);
+            const int yhalf = a.bmap[3 * ti.blk + 1], outcol = a.bmap[3 * ti.blk + 2];
+            const int c0 = ti.tn * BN + hc * HC;       // first column of this warp
+            const long row = ti.rb * TBM + q * 32 + lane;
+            const bool live = row < a.rows;
+            // Y (column-major: the warp's 32 rows of a column are adjacent)
+            // times the column scales; the first NSL chunks of 32 columns are
+            // loaded before the accumulator is ready, the others one chunk ahead
+            const float *Yc = a.Y + ((long)yhalf * a.npad + c0) * a.ldy + (live ? row : 0);
+            const float *cs = a.colscale + (long)ti.blk * a.npad + c0;
+            constexpr int NSL = NCH < 2 ? NCH : 2;
+            float ys[NSL][32];
+#pragma unroll
+            for (int c = 0; c < NSL; c++)
+#pragma unroll
+                for (int jj = 0; jj < 32; jj++) ys[c][jj] = live ? __ldg(Yc + (long)(c * 32 + jj) * a.ldy) : 0.f;
+#pragma unroll
+            for (int c = 0; c < NSL; c++)
+#pragma unroll
+                for (int jj = 0; jj < 32; jj += 4) {
+                    const float4 s4 = __ldg(reinterpret_cast<const float4 *>(cs + c * 32 + jj));
+                    ys[c][jj] *= s4.x;
+                    ys[c][jj + 1] *= s4.y;
+                    ys[c][jj + 2] *= s4.z;
+                    ys[c][jj + 3] *= s4.w;
+                }
             bool ok = mbar_wait_e(&accf[buf], use & 1, a.err, 3);
             // tcgen05.ld is warp-collective (.sync.aligned): decide per warp
             ok = __all_sync(0xffffffffu, ok);
             if (!ok) break;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const int yhalf = a.bmap[3 * ti.blk + 1], outcol = a.bmap[3 * ti.blk + 2];
-            const int m0 = ti.tn * BN;
-            const long row = ti.rb * TBM + q * 32 + lane;
-            const float *Yr = a.Y + (row < a.rows ? row : 0) * 2L * a.npad + (long)yhalf * a.npad + m0;
-            const float *cs = a.colscale + (long)ti.blk * a.npad + m0;
-            const uint32_t acc = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * ACOLS);
+            const uint32_t acc = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * ACOLS) + (uint32_t)(hc * HC);
             float part = 0.f;
-            for (int c = 0; c < BN / 32; c++) {
+#pragma unroll
+            for (int c = 0; c < NCH; c++) {
+                const int sl = c % NSL;
+                if (c >= NSL) {
+                    // loaded while chunk c - NSL was reduced
+#pragma unroll
+                    for (int jj = 0; jj < 32; jj += 4) {
+                        const float4 s4 = __ldg(reinterpret_cast<const float4 *>(cs + c * 32 + jj));
+                        ys[sl][jj] *= s4.x;
+                        ys[sl][jj + 1] *= s4.y;
+                        ys[sl][jj + 2] *= s4.z;
+                        ys[sl][jj + 3] *= s4.w;
+                    }
+                }
                 float v[32];
                 tmem_ld32(acc + c * 32, v);
+#pragma unroll
+                for (int jj = 0; jj < 32; jj++) part = fmaf(v[jj], ys[sl][jj], part);
                 if (TWO) {
+                    // cross products: lo parts carry a factor 2^11
                     float w[32];
                     tmem_ld32(acc + BN + c * 32, w);
-                    for (int jj = 0; jj < 32; jj++) v[jj] = fmaf(w[jj], 1.0f / 2048.0f, v[jj]);
+                    float pw = 0.f;
+#pragma unroll
+                    for (int jj = 0; jj < 32; jj++) pw = fmaf(w[jj], ys[sl][jj], pw);
+                    part = fmaf(pw, 1.0f / 2048.0f, part);
                 }
-                if (row < a.rows) {
-                    for (int jj = 0; jj < 32; jj += 4) {
-                        float4 y4 = *reinterpret_cast<const float4 *>(Yr + c * 32 + jj);
-                        float4 s4 = *reinterpret_cast<const float4 *>(cs + c * 32 + jj);
-                        part = fmaf(v[jj] * s4.x, y4.x, part);
-                        part = fmaf(v[jj + 1] * s4.y, y4.y, part);
-                        part = fmaf(v[jj + 2] * s4.z, y4.z, part);
-                        part = fmaf(v[jj + 3] * s4.w, y4.w, part);
-                    }
+                if (c + NSL < NCH) {
+#pragma unroll
+                    for (int jj = 0; jj < 32; jj++)
+                        ys[sl][jj] = live ? __ldg(Yc + (long)((c + NSL) * 32 + jj) * a.ldy) : 0.f;
                 }
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             __syncwarp();
-            if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(&acce[buf])) : "memory");
-            if (row < a.rows) atomicAdd(a.out + row * a.nout + outcol, part);
+            if (lane == 0) {
+                if (PAIR) mbar_arrive_remote(acce0 + (uint32_t)(buf * 8));
+                else asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(&acce[buf])) : "memory");
+            }
+            if (live) atomicAdd(a.out + row * a.nout + outcol, part);
             j++;
         }
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        // every MMA issued has completed before the accumulators are freed
+        // every MMA into this CTA's TMEM has completed before it is freed
         mbar_wait(mdone, 0, a.err, 6);
         // error path only: wait (bounded) for the copies still in flight
-        for (long g = consumed_s; g < issued_s; g++)
-            mbar_wait(&full[g % TSTAGES], (uint32_t)((g / TSTAGES) & 1), a.err, 4);
+        if (leader)
+            for (long g = consumed_s; g < issued_s; g++)
+                mbar_wait(&full[g % TSTAGES], (uint32_t)((g / TSTAGES) & 1), a.err, 4);
     }
     __syncthreads();
+    // neither CTA of a pair leaves while the other may still address it
+    if (PAIR) cluster_sync_all();
     if (warp == 1) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols_tmem));
+        if (PAIR)
+            asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols_tmem));
+        else
+            asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols_tmem));
     }
 }
 
@@ -787,6 +995,73 @@ int tcform_split(TcForm &f, const double *coef64, const int *bmap_host, int nblk
     return OK;
 }
 
+// Launches the GEMM of one chunk: as many CTAs (or CTA pairs) as fit on the
+// device at once (one CTA per SM), at most one per tile unit.
+template <int BN, bool TWO, bool PAIR>
+static int launch_tc(const CUtensorMap &mXh, const CUtensorMap &mXl, const CUtensorMap &mWh, const CUtensorMap &mWl,
+                     const QTC &q, long nunits, cudaStream_t stream) {
+    using CF = TcCfg<BN, TWO, PAIR>;
+    // set and queried once per process (thread-safe static initialisation)
+    static const int maxunits = [] {
+        if (cudaFuncSetAttribute(k_qform_tc<BN, TWO, PAIR>, cudaFuncAttributeMaxDynamicSharedMemorySize, CF::SMEM) !=
+            cudaSuccess)
+            return -1;
+        int dev = 0, nsm = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            return -1;
+        if (!PAIR) return nsm;
+        cudaLaunchConfig_t c = {};
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = 2;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        c.gridDim = dim3((unsigned)(2 * (nsm / 2)));
+        c.blockDim = dim3(TC_THREADS);
+        c.dynamicSmemBytes = CF::SMEM;
+        c.attrs = at;
+        c.numAttrs = 1;
+        int n = 0;
+        if (cudaOccupancyMaxActiveClusters(&n, k_qform_tc<BN, TWO, PAIR>, &c) != cudaSuccess) return -1;
+        return n;
+    }();
+    if (maxunits <= 0) {
+        std::fprintf(stderr, "cfdwm: the tensor-core form (pair %d) does not fit on this device\n", (int)PAIR);
+        return E_CUDA;
+    }
+    const long nu = std::min<long>(nunits, maxunits);
+    if (!PAIR) {
+        k_qform_tc<BN, TWO, false><<<(unsigned)nu, TC_THREADS, CF::SMEM, stream>>>(mXh, mXl, mWh, mWl, q);
+    } else {
+        cudaLaunchConfig_t c = {};
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = 2;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        c.gridDim = dim3((unsigned)(nu * 2));
+        c.blockDim = dim3(TC_THREADS);
+        c.dynamicSmemBytes = CF::SMEM;
+        c.stream = stream;
+        c.attrs = at;
+        c.numAttrs = 1;
+        CK(cudaLaunchKernelEx(&c, k_qform_tc<BN, TWO, true>, mXh, mXl, mWh, mWl, q));
+    }
+    note_launch();
+    CK(cudaGetLastError());
+    return OK;
+}
+
+// The GEMM on CTA pairs (cta_group::2) or on single CTAs; CFDWM_TC_PAIR=0 or 1
+// overrides the default.  The results do not depend on it beyond the order of
+// the epilogue's atomic adds.
+static bool tc_pair() {
+    const char *e = std::getenv("CFDWM_TC_PAIR");
+    if (e && (e[0] == '0' || e[0] == '1') && e[1] == 0) return e[0] == '1';
+    return true;
+}
+
 static int tc_reserve(TcForm &f, size_t bytes) {
     if (f.scratch_bytes >= bytes) return OK;
     if (f.scratch) cudaFree(f.scratch);
@@ -833,16 +1108,9 @@ int tcform_eval(TcForm &f, const DevSea &sea, long n, const double *x, const dou
         CK(cudaEventRecord(ev[0], stream));          // inputs and the zeroed output are ordered before
         CK(cudaStreamWaitEvent(pst, ev[0], 0));
     }
-    // set once per process (thread-safe static initialisation)
-    static const cudaError_t attr = [] {
-        cudaError_t e = cudaFuncSetAttribute(k_qform_tc<128, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             TcCfg<128, true>::SMEM);
-        if (e != cudaSuccess) return e;
-        return cudaFuncSetAttribute(k_qform_tc<256, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    TcCfg<256, false>::SMEM);
-    }();
-    CK(attr);
-    const int BN = f.fp16 ? 128 : 256;
+    const int BN = 256;
+    const bool pair = tc_pair();
+    const int CSZ = pair ? 2 : 1;
     int j = 0;
     for (long b = 0; b < n; b += chunk, j++) {
         long mm = std::min(chunk, n - b);
@@ -864,7 +1132,7 @@ int tcform_eval(TcForm &f, const DevSea &sea, long n, const double *x, const dou
         pp.rows = mm; pp.row = rowrec; pp.comp = comprec; pp.phase = sea.d_phase; pp.t = t + b * st; pp.st = st;
         pp.cstride = sea.npad_g; pp.ncomp = sea.n; pp.npad = npad;
         pp.trivial_ramp = sea.trivial_ramp ? 1 : 0; pp.fp16 = f.fp16 ? 1 : 0;
-        pp.Xhi = Xh; pp.Xlo = Xl; pp.Y = Y;
+        pp.Xhi = Xh; pp.Xlo = Xl; pp.Y = Y; pp.ldy = mpad;
         // a full grid: with two blocks per SM beside the GEMM the preparation
         // ran latency-bound at a tenth of its speed and became the bottleneck
         k_qform_prep<<<dim3((unsigned)(npad / 256), (unsigned)((mm + PREP_ROWS - 1) / PREP_ROWS)), 128, 0, pst>>>(pp);
@@ -876,30 +1144,24 @@ int tcform_eval(TcForm &f, const DevSea &sea, long n, const double *x, const dou
         }
         CUtensorMap mXh, mXl, mWh, mWl;
         if (make_map(&mXh, Xh, mm, 2L * npad, TBM, f.fp16) || make_map(&mXl, Xl, mm, 2L * npad, TBM, f.fp16) ||
-            make_map(&mWh, f.Whi, (long)f.nblk * npad, npad, BN, f.fp16) ||
-            make_map(&mWl, f.Wlo, (long)f.nblk * npad, npad, BN, f.fp16))
+            make_map(&mWh, f.Whi, (long)f.nblk * npad, npad, BN / CSZ, f.fp16) ||
+            make_map(&mWl, f.Wlo, (long)f.nblk * npad, npad, BN / CSZ, f.fp16))
             return E_CUDA;
         QTC q;
         q.rows = mm; q.npad = npad; q.ntn = npad / BN; q.group_m = 8; q.nblk = f.nblk; q.nout = f.nout;
-        q.bmap = f.bmap; q.Y = Y; q.colscale = f.colscale;
+        q.bmap = f.bmap; q.Y = Y; q.ldy = mpad; q.colscale = f.colscale;
         q.out = out + (long)f.nout * b; q.fp16 = f.fp16 ? 1 : 0; q.err = f.err;
         long nrb = (mm + TBM - 1) / TBM;
-        long ntiles = nrb * (long)f.nblk * q.ntn;
-        static int nsm = 0;
-        if (!nsm) {
-            int dev = 0;
-            CK(cudaGetDevice(&dev));
-            CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-        }
-        long nctas = std::min<long>(ntiles, nsm);
+        long nunits = (nrb + CSZ - 1) / CSZ * (long)f.nblk * q.ntn;
         prof_begin(PK_QFORM, stream);
         if (!f.fp16)
-            k_qform_tc<256, false><<<(unsigned)nctas, 192, TcCfg<256, false>::SMEM, stream>>>(mXh, mXl, mWh, mWl, q);
+            rc = pair ? launch_tc<256, false, true>(mXh, mXl, mWh, mWl, q, nunits, stream)
+                      : launch_tc<256, false, false>(mXh, mXl, mWh, mWl, q, nunits, stream);
         else
-            k_qform_tc<128, true><<<(unsigned)nctas, 192, TcCfg<128, true>::SMEM, stream>>>(mXh, mXl, mWh, mWl, q);
-        note_launch();
+            rc = pair ? launch_tc<256, true, true>(mXh, mXl, mWh, mWl, q, nunits, stream)
+                      : launch_tc<256, true, false>(mXh, mXl, mWh, mWl, q, nunits, stream);
         prof_end(PK_QFORM, stream);
-        CK(cudaGetLastError());
+        if (rc) return rc;
         if (nbuf == 2) CK(cudaEventRecord(ev[3 + buf], stream));
     }
     if (tc_error) {

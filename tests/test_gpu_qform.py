@@ -158,3 +158,36 @@ def test_tensor_core_fp16_split_component_ramps(wm, torch):
     for f in range(4):
         err = norm_rel_err(got[:, f], ref[:, f])
         assert err <= TOL, (f, err)
+
+
+@pytest.mark.parametrize("fp16", [True, False])
+@pytest.mark.parametrize("n", [333, 1000, 70001])
+def test_tensor_core_pair_and_single_forms_agree(wm, torch, fp16, n):
+    """The GEMM on CTA pairs (cta_group::2, M = 256) and on single CTAs
+    (M = 128) gives the same sums: every 128-row block runs the same K
+    sequence, and only the order of the per-tile atomic adds into each output
+    (not fixed even between two runs) differs, so the bar is a few FP32
+    roundings, 1e-6 normwise.  Row counts of 3, 8 and 547 row blocks (two
+    chunks) leave a row block past the last row in the last pair."""
+    txt = _sea(40, 8, 37)
+    outs = {}
+    old = os.environ.get("CFDWM_TC_PAIR")
+    try:
+        for pr in ("0", "1"):
+            os.environ["CFDWM_TC_PAIR"] = pr
+            outs[pr] = _run(wm, torch, txt, n, 1, fp16, seed=41)
+    finally:
+        if old is None:
+            os.environ.pop("CFDWM_TC_PAIR", None)
+        else:
+            os.environ["CFDWM_TC_PAIR"] = old
+    single, pair = outs["0"][3], outs["1"][3]
+    assert np.all(np.isfinite(pair))
+    for f in range(4):
+        err = norm_rel_err(pair[:, f], single[:, f])
+        assert err <= 1e-6, (f, err)
+    if n == 1000:
+        x, y, t, _ = outs["1"]
+        ref = _reference(txt, x, y, t)
+        for f in range(4):
+            assert norm_rel_err(pair[:, f], ref[:, f]) <= (TOL if fp16 else TOL_BF16)

@@ -560,6 +560,15 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7]),
+          "=f"(v[8]), "=f"(v[9]), "=f"(v[10]), "=f"(v[11]), "=f"(v[12]), "=f"(v[13]), "=f"(v[14]), "=f"(v[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
 struct QTC {
     long rows;               // rows of this chunk
     int npad;                // components (multiple of 256)
@@ -824,11 +833,62 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_qform_tc(const __grid_constan
             const int c0 = ti.tn * BN + hc * HC;       // first column of this warp
             const long row = ti.rb * TBM + q * 32 + lane;
             const bool live = row < a.rows;
-            // Y (column-major: the warp's 32 rows of a column are adjacent)
-            // times the column scales; the first NSL chunks of 32 columns are
-            // loaded before the accumulator is ready, the others one chunk ahead
             const float *Yc = a.Y + ((long)yhalf * a.npad + c0) * a.ldy + (live ? row : 0);
             const float *cs = a.colscale + (long)ti.blk * a.npad + c0;
+            if (TWO) {
+                // fp16, one accumulator buffer: read this warp's TMEM rows first
+                // (hi + cross / 2^11, HC values a thread), release the buffer to
+                // the next tile's MMAs, then load Y (column-major: the warp's 32
+                // rows of a column are adjacent) and reduce meanwhile
+                bool ok = mbar_wait_e(&accf[buf], use & 1, a.err, 3);
+                ok = __all_sync(0xffffffffu, ok);
+                if (!ok) break;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t acc =
+                    tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * ACOLS) + (uint32_t)(hc * HC);
+                float tv[NCH][32];
+#pragma unroll
+                for (int c = 0; c < NCH; c++) {
+                    tmem_ld32(acc + c * 32, tv[c]);
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        float w[16];
+                        tmem_ld16(acc + BN + c * 32 + h * 16, w);
+#pragma unroll
+                        for (int jj = 0; jj < 16; jj++)
+                            tv[c][h * 16 + jj] = fmaf(w[jj], 1.0f / 2048.0f, tv[c][h * 16 + jj]);
+                    }
+                }
+                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                __syncwarp();
+                if (lane == 0) {
+                    if (PAIR) mbar_arrive_remote(acce0 + (uint32_t)(buf * 8));
+                    else asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(&acce[buf])) : "memory");
+                }
+                float part = 0.f;
+                if (live) {
+#pragma unroll
+                    for (int c = 0; c < NCH; c++)
+#pragma unroll
+                        for (int jj = 0; jj < 32; jj += 4) {
+                            const float4 s4 = __ldg(reinterpret_cast<const float4 *>(cs + c * 32 + jj));
+                            const float y0 = __ldg(Yc + (long)(c * 32 + jj) * a.ldy);
+                            const float y1 = __ldg(Yc + (long)(c * 32 + jj + 1) * a.ldy);
+                            const float y2 = __ldg(Yc + (long)(c * 32 + jj + 2) * a.ldy);
+                            const float y3 = __ldg(Yc + (long)(c * 32 + jj + 3) * a.ldy);
+                            part = fmaf(tv[c][jj] * s4.x, y0, part);
+                            part = fmaf(tv[c][jj + 1] * s4.y, y1, part);
+                            part = fmaf(tv[c][jj + 2] * s4.z, y2, part);
+                            part = fmaf(tv[c][jj + 3] * s4.w, y3, part);
+                        }
+                    atomicAdd(a.out + row * a.nout + outcol, part);
+                }
+                j++;
+                continue;
+            }
+            // bf16, two accumulator buffers: Y times the column scales; the
+            // first NSL chunks of 32 columns are loaded before the accumulator
+            // is ready, the others one chunk ahead
             constexpr int NSL = NCH < 2 ? NCH : 2;
             float ys[NSL][32];
 #pragma unroll

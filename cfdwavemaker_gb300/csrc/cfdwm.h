@@ -304,9 +304,12 @@ struct DevRegular {
     int theory = 0;         // 0 Stokes5, 1 Fenton
     int N = 0;
     double *d_sol = nullptr;  // FP64 solution block (coefficients), see regular.cu
+    float *d_cf = nullptr;    // its harmonic coefficients in FP32, [4][64] (U, W, E, Q)
     int status = 0;           // Fenton: 0 converged, 3 not fully converged
     // host copies of the scalars
     double k = 0, c = 0, wave_length = 0, wave_period = 0;
+    double head[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};   // solution words 0-9
+    double soff[4] = {0, 0, 0, 0};                       // offsets: eta, u, R - g (d - z0), ubar
 };
 int regular_build(const Config &cfg, DevRegular &r, void *stream);
 void regular_free(DevRegular &r);

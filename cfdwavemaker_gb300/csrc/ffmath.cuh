@@ -37,6 +37,56 @@ __host__ __device__ __forceinline__ void ff_split(double v, float &hi, float &lo
     lo = (float)(v - (double)hi);
 }
 
+// v as an unevaluated float pair by integer operations on its bits only: FP64
+// instructions, conversions included, run at a small fraction of the FP32
+// rate on this GPU, and even a predicated-off FP64 fallback takes their issue
+// slots.  For 2^-74 <= |v| < 2^127, hi keeps the leading 24 significant bits
+// (truncated) and lo the next 29 rounded to 24, so hi + lo carries 48 bits;
+// 2^-126 <= |v| < 2^-74 gives (hi, 0); smaller magnitudes give 0; larger,
+// infinite and NaN inputs give an infinity or a NaN of v's sign.
+__device__ __forceinline__ float2 ff_from_double(double v) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const unsigned hw = (unsigned)(b >> 32), lw = (unsigned)b;
+    const unsigned sign = hw & 0x80000000u;
+    const int e = (int)((hw >> 20) & 0x7FFu);          // biased exponent
+    if (e < 897) return make_float2(__uint_as_float(sign), 0.f);
+    if (e > 1150) {
+        const bool nan = e == 2047 && ((hw & 0xFFFFFu) | lw) != 0u;
+        return make_float2(__uint_as_float(sign | (nan ? 0x7FC00000u : 0x7F800000u)), 0.f);
+    }
+    const float hi = __uint_as_float(sign | ((unsigned)(e - 896) << 23) | ((hw & 0xFFFFFu) << 3) | (lw >> 29));
+    if (e < 949) return make_float2(hi, 0.f);
+    // the low 29 mantissa bits have weight 2^(e - 1075): float exponent field e - 948
+    const float scale = __uint_as_float((unsigned)(e - 948) << 23);
+    const float lo = __uint_as_float(__float_as_uint(__uint2float_rn(lw & 0x1FFFFFFFu) * scale) | sign);
+    return make_float2(hi, lo);
+}
+
+// f as a double, exactly, by integer operations only (all float classes)
+__device__ __forceinline__ double d_from_float(float f) {
+    const unsigned b = __float_as_uint(f);
+    const unsigned sign = b & 0x80000000u, e = (b >> 23) & 0xFFu, m = b & 0x7FFFFFu;
+    unsigned hw, lw;
+    if (e == 255u) {                                  // infinity, NaN (payload kept)
+        hw = sign | 0x7FF00000u | (m >> 3);
+        lw = (m & 7u) << 29;
+    } else if (e == 0u) {
+        if (m == 0u) {                                // signed zero
+            hw = sign;
+            lw = 0u;
+        } else {                                      // subnormal: m 2^-149, normalised
+            const int lz = __clz(m);                  // 9..31
+            const unsigned mm = (m << (lz - 8)) & 0x7FFFFFu;
+            hw = sign | ((unsigned)(905 - lz) << 20) | (mm >> 3);
+            lw = (mm & 7u) << 29;
+        }
+    } else {
+        hw = sign | ((e + 896u) << 20) | (m >> 3);
+        lw = (m & 7u) << 29;
+    }
+    return __hiloint2double((int)hw, (int)lw);
+}
+
 // Irregular::freq_ramp (Irregular.cpp:200-204), FP64
 __device__ __forceinline__ double ff_freq_ramp(double t, double rt, double ts, double du) {
     const double small = 1.e-12;   // Irregular.h:8

@@ -15,6 +15,7 @@
 // generated by complex recurrence from one sincos, the depth ratios
 // cosh(j k y)/cosh(j k d) from two exponentials raised to the j-th power.
 #include "cfdwm.h"
+#include "ffmath.cuh"
 
 #include <cuda_runtime.h>
 #include <cmath>
@@ -35,7 +36,6 @@ namespace cfdwm {
 
 constexpr int MAXN = 64;                 // largest Fourier order accepted
 constexpr int MAXNUM = 2 * MAXN + 10;    // unknowns of the Newton system
-constexpr double TWO_PI_D = 6.283185307179586476925286766559;
 
 // Solution block layout (FP64, device):
 //   [0] k  [1] c  [2] ubar  [3] R  [4] L  [5] T  [6] status  [7] N
@@ -347,32 +347,39 @@ struct EvalArgs {
     long n;
     const double *x, *y, *z, *t;
     double *out;        // [5][n]
-    const double *sol;
-    int N, theory, finite;
-    double x0, y0, t0, z0, d, g, rho;
+    const float *cf;    // [4][MAXN]: U, W, E, Q harmonic coefficients in FP32
+    int N, finite;
+    float2 P[6];        // k cos th, k sin th, -k c, -x0, -y0, -t0 as float pairs
+    float F[12];        // k, cos th, sin th, k d, d - z0, -z0, eta offset, u offset,
+                        // R - g (d - z0), ubar, g, rho
 };
 
+// One thread per point.  FP64 runs at a small fraction of the FP32 rate on
+// this GPU, and a kernel with an FP64 phase, FP64 outputs and per-block FP64
+// to FP32 conversions of the coefficients kept the FP64 pipe 85-88% busy
+// (14% of DRAM).  So the coefficients and constants arrive in FP32 (converted
+// once on the host), the coordinates are split into float pairs by integer
+// operations, the phase is formed in float-float and reduced, the sums are
+// FP32, and the outputs are widened to double exactly by integer operations.
 __global__ void __launch_bounds__(128) k_regular_eval(EvalArgs a) {
     __shared__ float cU[MAXN], cW[MAXN], cE[MAXN], cQ[MAXN];
-    __shared__ double S[16];
     for (int j = threadIdx.x; j < MAXN; j += blockDim.x) {
-        cU[j] = (float)a.sol[OFF_U + j];
-        cW[j] = (float)a.sol[OFF_W + j];
-        cE[j] = (float)a.sol[OFF_E + j];
-        cQ[j] = (float)a.sol[OFF_Q + j];
+        cU[j] = a.cf[j];
+        cW[j] = a.cf[MAXN + j];
+        cE[j] = a.cf[2 * MAXN + j];
+        cQ[j] = a.cf[3 * MAXN + j];
     }
-    if (threadIdx.x < 10) S[threadIdx.x] = a.sol[threadIdx.x];
-    if (threadIdx.x >= 10 && threadIdx.x < 14) S[threadIdx.x] = a.sol[OFF_S + threadIdx.x - 10];
     __syncthreads();
     long p = blockIdx.x * (long)blockDim.x + threadIdx.x;
     if (p >= a.n) return;
-    const double k = S[0], c = S[1], cth = S[8], sth = S[9];
-    // kx = k (cos th (X - x0) + sin th (Y - y0) - c (t - t0)), FP64 then reduced
-    double kx = k * (cth * (a.x[p] - a.x0) + sth * (a.y[p] - a.y0) - c * (a.t[p] - a.t0));
-    double nn = rint(kx * (1.0 / TWO_PI_D));
-    float r = (float)fma(-nn, TWO_PI_D, kx);
+    // kx = k (cos th (X - x0) + sin th (Y - y0) - c (t - t0)) in float-float
+    const float2 dx = ff_add(ff_from_double(a.x[p]), a.P[3]);
+    const float2 dy = ff_add(ff_from_double(a.y[p]), a.P[4]);
+    const float2 dt = ff_add(ff_from_double(a.t[p]), a.P[5]);
+    float2 kx = ff_add(ff_mul(a.P[0].x, a.P[0].y, dx.x, dx.y), ff_mul(a.P[1].x, a.P[1].y, dy.x, dy.y));
+    kx = ff_add(kx, ff_mul(a.P[2].x, a.P[2].y, dt.x, dt.y));
     float s1, c1;
-    sincosf(r, &s1, &c1);
+    sincosf(ff_reduce_2pi(kx), &s1, &c1);
     const int N = a.N;
     // elevation: sum_j E_j cos(j kx)
     float cj = c1, sj = s1, eta = 0.f;
@@ -381,12 +388,13 @@ __global__ void __launch_bounds__(128) k_regular_eval(EvalArgs a) {
         float cn = cj * c1 - sj * s1, sn = sj * c1 + cj * s1;
         cj = cn; sj = sn;
     }
-    double etad = (double)eta + S[10];
+    const float etao = eta + a.F[6];
     // velocity sums with depth ratios
+    const float2 zf = ff_from_double(a.z[p]);
     float su = 0.f, sw = 0.f;
     if (a.finite) {
-        const float kd = (float)(k * a.d);
-        const float ky = (float)(k * (a.z[p] + a.d - a.z0));
+        const float kd = a.F[3];
+        const float ky = a.F[0] * ((zf.x + a.F[4]) + zf.y);
         const float e1 = expf(ky - kd), e2 = expf(-2.f * ky), e3 = expf(-2.f * kd);
         float p1 = 1.f, p2 = 1.f, p3 = 1.f;
         cj = c1; sj = s1;
@@ -401,7 +409,7 @@ __global__ void __launch_bounds__(128) k_regular_eval(EvalArgs a) {
             cj = cn; sj = sn;
         }
     } else {
-        const float ky = (float)(k * (a.z[p] - a.z0));
+        const float ky = a.F[0] * ((zf.x + a.F[5]) + zf.y);
         const float e1 = expf(ky);
         float p1 = 1.f;
         cj = c1; sj = s1;
@@ -413,17 +421,16 @@ __global__ void __launch_bounds__(128) k_regular_eval(EvalArgs a) {
             cj = cn; sj = sn;
         }
     }
-    const double uoff = S[11];
-    const double U = uoff + (double)su;
-    a.out[0 * a.n + p] = etad;
-    a.out[1 * a.n + p] = cth * U;
-    a.out[2 * a.n + p] = sth * U;
-    a.out[3 * a.n + p] = (double)sw;
-    // p_nh = rho (R - g (eta + d - z0) - q'^2 / 2), q'^2 = (U_osc - ubar)^2 + w^2
-    double up = (double)su - S[13];
-    double q2 = up * up + (double)sw * (double)sw;
-    // S[12] = R - g (d - z0) and etad includes z0: R - g (eta + d - z0)
-    a.out[4 * a.n + p] = a.rho * (S[12] - a.g * etad - 0.5 * q2);
+    const float U = a.F[7] + su;
+    a.out[0 * a.n + p] = d_from_float(etao);
+    a.out[1 * a.n + p] = d_from_float(a.F[1] * U);
+    a.out[2 * a.n + p] = d_from_float(a.F[2] * U);
+    a.out[3 * a.n + p] = d_from_float(sw);
+    // p_nh = rho (R - g (eta + d - z0) - q'^2 / 2), q'^2 = (U_osc - ubar)^2 + w^2;
+    // F[8] = R - g (d - z0), and the elevation includes z0
+    const float up = su - a.F[9];
+    const float q2 = fmaf(up, up, sw * sw);
+    a.out[4 * a.n + p] = d_from_float(a.F[11] * (fmaf(-a.F[10], etao, a.F[8]) - 0.5f * q2));
 }
 
 // ----------------------------- host side ---------------------------------
@@ -465,25 +472,45 @@ int regular_build(const Config &cfg, DevRegular &r, void *stream_) {
     CK(cudaStreamSynchronize(stream));
     r.status = (int)h[6];
     r.k = h[0]; r.c = h[1]; r.wave_length = h[4]; r.wave_period = h[5];
+    for (int q = 0; q < 10; q++) r.head[q] = h[q];
+    for (int q = 0; q < 4; q++) r.soff[q] = h[OFF_S + q];
+    // the harmonic coefficients in FP32 for the evaluation kernel
+    float cf[4 * MAXN];
+    for (int j = 0; j < MAXN; j++) {
+        cf[j] = (float)h[OFF_U + j];
+        cf[MAXN + j] = (float)h[OFF_W + j];
+        cf[2 * MAXN + j] = (float)h[OFF_E + j];
+        cf[3 * MAXN + j] = (float)h[OFF_Q + j];
+    }
+    CK(cudaMalloc(&r.d_cf, sizeof cf));
+    CK(cudaMemcpyAsync(r.d_cf, cf, sizeof cf, cudaMemcpyHostToDevice, stream));
+    CK(cudaStreamSynchronize(stream));
     if (r.status == 2) return E_SOLVER;
     return OK;
 }
 
 void regular_free(DevRegular &r) {
     if (r.d_sol) cudaFree(r.d_sol);
+    if (r.d_cf) cudaFree(r.d_cf);
     r.d_sol = nullptr;
+    r.d_cf = nullptr;
 }
 
 int regular_eval(const DevRegular &r, const Config &cfg, long n, const double *x, const double *y,
                  const double *z, const double *t, double *out, void *stream_) {
     cudaStream_t stream = (cudaStream_t)stream_;
     if (n <= 0) return OK;
+    if (!r.d_cf) return E_NOT_INITIALIZED;
     EvalArgs a;
-    a.n = n; a.x = x; a.y = y; a.z = z; a.t = t; a.out = out; a.sol = r.d_sol;
-    a.N = r.N; a.theory = r.theory;
+    a.n = n; a.x = x; a.y = y; a.z = z; a.t = t; a.out = out; a.cf = r.d_cf;
+    a.N = r.N;
     a.finite = (cfg.depth > 0.0 && cfg.depth < 1e8) ? 1 : 0;
-    a.x0 = cfg.x_pos; a.y0 = cfg.y_pos; a.t0 = cfg.tofmax; a.z0 = cfg.swl; a.d = cfg.depth;
-    a.g = cfg.gravity; a.rho = cfg.rho;
+    const double k = r.head[0], c = r.head[1], cth = r.head[8], sth = r.head[9];
+    const double pv[6] = {k * cth, k * sth, -k * c, -cfg.x_pos, -cfg.y_pos, -cfg.tofmax};
+    for (int q = 0; q < 6; q++) ff_split(pv[q], a.P[q].x, a.P[q].y);
+    const double fv[12] = {k, cth, sth, k * cfg.depth, cfg.depth - cfg.swl, -cfg.swl,
+                           r.soff[0], r.soff[1], r.soff[2], r.soff[3], cfg.gravity, cfg.rho};
+    for (int q = 0; q < 12; q++) a.F[q] = (float)fv[q];
     prof_begin(PK_REGULAR, stream);
     k_regular_eval<<<(unsigned)((n + 127) / 128), 128, 0, stream>>>(a);
     note_launch();

@@ -133,6 +133,7 @@ enum CompCoef {
 constexpr int GRID_TILE = 32;
 constexpr int POINT_TILE = 16;
 constexpr int SMIT_TILE = 16;
+constexpr int DF_COMP_FLOATS = 14;   // floats of one depthform.cu component record
 
 struct DevSea {
     int n = 0;              // components
@@ -156,6 +157,10 @@ struct DevSea {
     bool smit = false;
     float *d_tab_smit = nullptr;
     int npad_s = 0, ntile_s = 0;
+    // per-launch component records of the tensor-core path's first-order
+    // kernels (depthform.cu): float-pair phase coefficients, ramp, 5
+    // coefficients; two regions (surface, levels) of npad_g records
+    float *d_dfcomp = nullptr;
 };
 
 // Seeded JONSWAP / cos-2s component columns [5][nfreq ndir] (omega, A, k,

@@ -344,6 +344,7 @@ struct DfFirstArgs {
     float depth;
     double *first;             // [5][n] (mode 0)
     float *sec;                // [nf][n nl] (mode 1)
+    const void *comps;         // this launch's component records (DfComp, ncomp of them)
 };
 
 constexpr int DFC = 128;       // components per shared-memory chunk
@@ -367,33 +368,44 @@ struct DfComp {
     float c[5];
 };
 
+static_assert(sizeof(DfComp) == DF_COMP_FLOATS * sizeof(float), "component record size");
+
+// The records of all components at this launch's time, one thread each:
+// converting the FP64 phase rows and evaluating the FP64 ramp once here, not
+// in every block (FP64 runs at a small fraction of the FP32 rate on this GPU;
+// done per block it kept the FP64 pipe 71% busy in the level kernel).
 template <int MODE>
-__device__ __forceinline__ void df_stage(const DfFirstArgs &a, int i0, DfComp *sc) {
-    for (int e = threadIdx.x; e < DFC; e += blockDim.x) {
-        const int i = i0 + e;
-        DfComp d = {};
-        if (i < a.ncomp) {
-            const int cs = a.cstride;
-            d.f = ff_component(a.phase, cs, i, a.trivial_ramp, a.t);
-            if (MODE == 0) {
-                d.c[0] = a.cf[CF_A * cs + i];
-                d.c[1] = a.cf[CF_GX * cs + i];
-                d.c[2] = a.cf[CF_GY * cs + i];
-                d.c[3] = a.cf[CF_GZ * cs + i];
-                d.c[4] = a.cf[CF_GP * cs + i];
-            } else {
-                const float au = a.cf[CF_AU * cs + i] * a.cf[CF_Q * cs + i];
-                d.c[0] = a.cf[CF_K * cs + i];
-                d.c[1] = au * a.cf[CF_CT * cs + i];
-                d.c[2] = au * a.cf[CF_ST * cs + i];
-                d.c[3] = au;
-                d.c[4] = a.cf[CF_AP * cs + i] * a.cf[CF_Q * cs + i];
-            }
-        }
-        sc[e] = d;
+__global__ void k_df_comps(DfFirstArgs a, DfComp *out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.ncomp) return;
+    const int cs = a.cstride;
+    DfComp d;
+    d.f = ff_component(a.phase, cs, i, a.trivial_ramp, a.t);
+    if (MODE == 0) {
+        d.c[0] = a.cf[CF_A * cs + i];
+        d.c[1] = a.cf[CF_GX * cs + i];
+        d.c[2] = a.cf[CF_GY * cs + i];
+        d.c[3] = a.cf[CF_GZ * cs + i];
+        d.c[4] = a.cf[CF_GP * cs + i];
+    } else {
+        const float au = a.cf[CF_AU * cs + i] * a.cf[CF_Q * cs + i];
+        d.c[0] = a.cf[CF_K * cs + i];
+        d.c[1] = au * a.cf[CF_CT * cs + i];
+        d.c[2] = au * a.cf[CF_ST * cs + i];
+        d.c[3] = au;
+        d.c[4] = a.cf[CF_AP * cs + i] * a.cf[CF_Q * cs + i];
     }
+    out[i] = d;
 }
 
+// a chunk of DFC records into shared memory (zero past the last component)
+__device__ __forceinline__ void df_stage(const DfFirstArgs &a, int i0, DfComp *sc) {
+    const float *src = reinterpret_cast<const float *>(a.comps) + (long)i0 * DF_COMP_FLOATS;
+    float *dst = reinterpret_cast<float *>(sc);
+    const int nrec = min(DFC, a.ncomp - i0);
+    for (int e = threadIdx.x; e < DFC * DF_COMP_FLOATS; e += blockDim.x)
+        dst[e] = e < nrec * DF_COMP_FLOATS ? src[e] : 0.f;
+}
 
 __global__ void __launch_bounds__(128) k_df_first_surface(DfFirstArgs a) {
     __shared__ DfComp sc[DFC];
@@ -407,7 +419,7 @@ __global__ void __launch_bounds__(128) k_df_first_surface(DfFirstArgs a) {
     float s[5] = {0, 0, 0, 0, 0}, k[5] = {0, 0, 0, 0, 0};
     for (int i0 = 0; i0 < a.ncomp; i0 += DFC) {
         __syncthreads();
-        df_stage<0>(a, i0, sc);
+        df_stage(a, i0, sc);
         __syncthreads();
         const int iend = min(DFC, a.ncomp - i0);
         for (int ii = 0; ii < iend; ii++) {
@@ -457,7 +469,7 @@ __global__ void __launch_bounds__(256) k_df_first_levels(DfFirstArgs a) {
     const bool pres = a.nf == 4;
     for (int i0 = 0; i0 < a.ncomp; i0 += DFC) {
         __syncthreads();
-        df_stage<1>(a, i0, sc);
+        df_stage(a, i0, sc);
         __syncthreads();
         const int iend = min(DFC, a.ncomp - i0);
         for (int ii = wg; ii < iend; ii += nw) {
@@ -685,7 +697,13 @@ int depthform_first(const DevSea &sea, long nact, int nl, const double *xy, doub
     a.phase = sea.d_phase; a.cf = sea.d_cf; a.cstride = sea.npad_g; a.ncomp = sea.n;
     a.trivial_ramp = sea.trivial_ramp ? 1 : 0;
     a.nl = nl; a.nf = nf; a.z0 = z0; a.depth = (float)sea.depth; a.first = first; a.sec = sec;
+    if (!sea.d_dfcomp) return E_NOT_INITIALIZED;
+    DfComp *recs = reinterpret_cast<DfComp *>(sea.d_dfcomp);
+    const unsigned cb = (unsigned)((sea.n + 127) / 128);
     if (first) {
+        k_df_comps<0><<<cb, 128, 0, stream>>>(a, recs);
+        note_launch();
+        a.comps = recs;
         k_df_first_surface<<<(unsigned)((nact + 127) / 128), 128, 0, stream>>>(a);
         note_launch();
         CK(cudaGetLastError());
@@ -694,6 +712,9 @@ int depthform_first(const DevSea &sea, long nact, int nl, const double *xy, doub
         const int ngrp = (nl + 3) / 4;
         const int gpb = std::min(ngrp, 8);
         dim3 grid((unsigned)((nact + 31) / 32), (unsigned)((ngrp + gpb - 1) / gpb));
+        k_df_comps<1><<<cb, 128, 0, stream>>>(a, recs + sea.npad_g);
+        note_launch();
+        a.comps = recs + sea.npad_g;
         k_df_first_levels<<<grid, 32 * gpb, 0, stream>>>(a);
         note_launch();
         CK(cudaGetLastError());

@@ -112,13 +112,15 @@ __device__ __forceinline__ FfComp ff_component(const double *phase, int cs, int 
     return d;
 }
 // cos and sin of kx (x - fx) + ky (y - fy) - omega t + phase0, the offsets and
-// t given as float pairs
+// t given as float pairs.  The reduced argument lies in about [-pi, pi], where
+// the SFU's sine and cosine are within a few 1e-7; the general sincosf kept
+// the FP64 pipe busy in the per-(column, component) loops.
 __device__ __forceinline__ void ff_phasor(const FfComp &d, float dxh, float dxl, float dyh, float dyl, float th,
                                           float tl, float &c, float &s) {
     float2 ph = ff_add(ff_mul(d.kxh, d.kxl, dxh, dxl), ff_mul(d.kyh, d.kyl, dyh, dyl));
     ph = ff_add(ph, ff_mul(d.wh, d.wl, th, tl));
     ph = ff_add(ph, make_float2(d.ph, d.pl));
-    sincosf(ff_reduce_2pi(ph), &s, &c);
+    __sincosf(ff_reduce_2pi(ph), &s, &c);
 }
 
 }  // namespace cfdwm

@@ -333,6 +333,7 @@ int sea_build(const Config &cfg, DevSea &sea, bool point_table, void *stream_) {
 
     CK(cudaMalloc(&sea.d_phase, sizeof(double) * 7 * sea.npad_g));
     CK(cudaMalloc(&sea.d_cf, sizeof(float) * NCF * sea.npad_g));
+    CK(cudaMalloc(&sea.d_dfcomp, sizeof(float) * DF_COMP_FLOATS * 2 * sea.npad_g));
     k_component_coefs<<<(sea.npad_g + 127) / 128, 128, 0, stream>>>(
         ci, sea.npad_g, cfg.x_pos, cfg.y_pos, cfg.tofmax, d_in + 4 * nn, d_in + 5 * nn,
         d_in + 6 * nn, d_in + 7 * nn, sea.d_phase, sea.d_cf);
@@ -394,7 +395,9 @@ void sea_free(DevSea &sea) {
     if (sea.d_tab_gp) cudaFree(sea.d_tab_gp);
     if (sea.d_tab_gk) cudaFree(sea.d_tab_gk);
     if (sea.d_tab_smit) cudaFree(sea.d_tab_smit);
+    if (sea.d_dfcomp) cudaFree(sea.d_dfcomp);
     sea.d_tab_smit = nullptr;
+    sea.d_dfcomp = nullptr;
     sea.smit = false;
     sea.d_phase = nullptr; sea.d_cf = nullptr; sea.d_tab_eta = nullptr;
     sea.d_tab_grid = nullptr; sea.d_tab_point = nullptr; sea.d_tab_gp = nullptr; sea.d_tab_gk = nullptr;

@@ -123,6 +123,7 @@ enum CompCoef {
     CF_GP,        // A rho g k                 dp1_dz
     CF_X1,        // rho * -g^2 (2k ct + 2k st) 2 / (2 omega)   dp2 diagonal, times px
     CF_Z1,        // rho *  g^2 (2k) 2 / (2 omega)              dp2 diagonal, times pz
+    CF_KW,        // k / omega (0 for omega <= 0)               Smit theory
     NCF
 };
 
@@ -161,6 +162,9 @@ struct DevSea {
     // kernels (depthform.cu): float-pair phase coefficients, ramp, 5
     // coefficients; two regions (surface, levels) of npad_g records
     float *d_dfcomp = nullptr;
+    // per-component records of the point phasor kernel (irregular.cu):
+    // kx, ky, -omega, phase0 as float pairs, then A, GX, GY, GZ, GP
+    float *d_phrec = nullptr;
 };
 
 // Seeded JONSWAP / cos-2s component columns [5][nfreq ndir] (omega, A, k,

@@ -26,6 +26,7 @@
 //  * Accumulation is compensated: a tile row is summed in FP32, then added to
 //    a Kahan (sum, carry) pair per output.
 #include "cfdwm.h"
+#include "ffmath.cuh"
 
 #include <cuda_runtime.h>
 #include <algorithm>
@@ -282,6 +283,7 @@ __global__ void k_component_coefs(CompIn c, int npad, double fx, double fy, doub
         v[CF_GP] = A * c.rho * g * k;
         v[CF_X1] = -c.rho * (gg * (2 * k * ct + 2 * k * st_) * 2) / (2 * w);
         v[CF_Z1] = c.rho * (gg * (2 * k) * 2) / (2 * w);
+        v[CF_KW] = w > 0.0 ? k / w : 0.0;
     }
     ph_out[0 * npad + i] = kx;
     ph_out[1 * npad + i] = ky;
@@ -291,6 +293,29 @@ __global__ void k_component_coefs(CompIn c, int npad, double fx, double fy, doub
     ph_out[5 * npad + i] = r1;
     ph_out[6 * npad + i] = r2;
     for (int q = 0; q < NCF; q++) cf[q * npad + i] = (float)v[q];
+}
+
+constexpr int PH_REC = 13;       // floats of a phasor record
+constexpr int PH_CHUNK = 128;    // records per shared-memory chunk
+
+// The phasor records of all components (time-independent, built once with the sea).
+__global__ void k_phasor_records(int n, int npad, const double *phase, const float *cf, int cs, float *rec) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npad) return;
+    float *o = rec + (long)i * PH_REC;
+    if (i >= n) {
+        for (int q = 0; q < PH_REC; q++) o[q] = 0.f;
+        return;
+    }
+    ff_split(phase[i], o[0], o[1]);
+    ff_split(phase[cs + i], o[2], o[3]);
+    ff_split(-phase[2 * cs + i], o[4], o[5]);
+    ff_split(phase[3 * cs + i], o[6], o[7]);
+    o[8] = cf[CF_A * cs + i];
+    o[9] = cf[CF_GX * cs + i];
+    o[10] = cf[CF_GY * cs + i];
+    o[11] = cf[CF_GZ * cs + i];
+    o[12] = cf[CF_GP * cs + i];
 }
 
 int sea_build(const Config &cfg, DevSea &sea, bool point_table, void *stream_) {
@@ -334,9 +359,17 @@ int sea_build(const Config &cfg, DevSea &sea, bool point_table, void *stream_) {
     CK(cudaMalloc(&sea.d_phase, sizeof(double) * 7 * sea.npad_g));
     CK(cudaMalloc(&sea.d_cf, sizeof(float) * NCF * sea.npad_g));
     CK(cudaMalloc(&sea.d_dfcomp, sizeof(float) * DF_COMP_FLOATS * 2 * sea.npad_g));
+    // records for up to the next multiple of 256 components (the plain
+    // precision form pads to 256), zero past the last component
+    const int nrec_cap = ((sea.npad_g + 255) / 256) * 256;
+    CK(cudaMalloc(&sea.d_phrec, sizeof(float) * PH_REC * nrec_cap));
     k_component_coefs<<<(sea.npad_g + 127) / 128, 128, 0, stream>>>(
         ci, sea.npad_g, cfg.x_pos, cfg.y_pos, cfg.tofmax, d_in + 4 * nn, d_in + 5 * nn,
         d_in + 6 * nn, d_in + 7 * nn, sea.d_phase, sea.d_cf);
+    note_launch();
+    CK(cudaGetLastError());
+    k_phasor_records<<<(nrec_cap + 127) / 128, 128, 0, stream>>>(n, nrec_cap, sea.d_phase, sea.d_cf,
+                                                                 sea.npad_g, sea.d_phrec);
     note_launch();
     CK(cudaGetLastError());
 
@@ -396,8 +429,10 @@ void sea_free(DevSea &sea) {
     if (sea.d_tab_gk) cudaFree(sea.d_tab_gk);
     if (sea.d_tab_smit) cudaFree(sea.d_tab_smit);
     if (sea.d_dfcomp) cudaFree(sea.d_dfcomp);
+    if (sea.d_phrec) cudaFree(sea.d_phrec);
     sea.d_tab_smit = nullptr;
     sea.d_dfcomp = nullptr;
+    sea.d_phrec = nullptr;
     sea.smit = false;
     sea.d_phase = nullptr; sea.d_cf = nullptr; sea.d_tab_eta = nullptr;
     sea.d_tab_grid = nullptr; sea.d_tab_point = nullptr; sea.d_tab_gp = nullptr; sea.d_tab_gk = nullptr;
@@ -431,43 +466,76 @@ struct PhArgs {
     int cstride;            // npad_g
     double fx, fy;
     int trivial_ramp;
+    const float *rec;       // [npad_g][PH_REC] phasor records
     float2 *ph;             // [npad][n]
     float *rr;              // [npad][n]
     double *first;          // [5][n]: eta1, gx, gy, gz, gp
 };
 
+__device__ __forceinline__ void ph_kahan(float &s, float &c, float v) {
+    const float y = v - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
+// One thread per point: the phasors (cos, sin) and ramps of every component
+// and the first-order sums eta1 and the Taylor gradients.  The phase
+// kx (x - fx) + ky (y - fy) - omega t + phase0 is formed in float-float from
+// the records (the point's coordinates split by integer operations) and
+// reduced, then the SFU sine and cosine; the sums are FP32 with Kahan
+// compensation.  FP64 per (point, component) -- phase, reduction and FP64
+// sums -- kept the FP64 pipe the bound on this GPU.  Only non-trivial
+// component ramps are evaluated in FP64 (Irregular.cpp:200-204).
 __global__ void __launch_bounds__(128) k_phasors(PhArgs a) {
-    long p = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (p >= a.n) return;
-    const double dx = a.x[p * a.sx] - a.fx, dy = a.y[p * a.sy] - a.fy, t = a.t[p * a.st];
+    __shared__ float s_rec[PH_CHUNK * PH_REC];
+    __shared__ float2 s_off[2];
+    const long p = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    const bool valid = p < a.n;
+    const long pc = valid ? p : 0;
+    if (threadIdx.x == 0) {
+        ff_split(-a.fx, s_off[0].x, s_off[0].y);
+        ff_split(-a.fy, s_off[1].x, s_off[1].y);
+    }
+    __syncthreads();
+    const double tp = a.t[pc * a.st];
+    const float2 dx = ff_add(ff_from_double(a.x[pc * a.sx]), s_off[0]);
+    const float2 dy = ff_add(ff_from_double(a.y[pc * a.sy]), s_off[1]);
+    const float2 tt = ff_from_double(tp);
     const double *P = a.phase;
     const int cs = a.cstride;
-    double rconst = d_freq_ramp(t, P[4 * cs], P[5 * cs], P[6 * cs]);
-    double e1 = 0, gx = 0, gy = 0, gz = 0, gp = 0;
-    for (int i = 0; i < a.npad; i++) {
-        float c = 0.f, s = 0.f, r = 0.f;
-        if (i < a.ncomp) {
-            double ph = fma(P[i], dx, fma(P[cs + i], dy, fma(-P[2 * cs + i], t, P[3 * cs + i])));
-            double nn = rint(ph * INV_TWO_PI);
-            float red = (float)fma(-nn, TWO_PI, ph);
-            sincosf(red, &s, &c);
-            r = a.trivial_ramp ? (float)rconst
-                               : (float)d_freq_ramp(t, P[4 * cs + i], P[5 * cs + i], P[6 * cs + i]);
-            float rc = r * c, rs = r * s;
-            e1 += (double)(rc * a.cf[CF_A * cs + i]);
-            gx += (double)(rc * a.cf[CF_GX * cs + i]);
-            gy += (double)(rc * a.cf[CF_GY * cs + i]);
-            gz += (double)(rs * a.cf[CF_GZ * cs + i]);
-            gp += (double)(rc * a.cf[CF_GP * cs + i]);
+    const float rconst = a.trivial_ramp ? (float)d_freq_ramp(tp, P[4 * cs], P[5 * cs], P[6 * cs]) : 0.f;
+    float sm[5] = {0, 0, 0, 0, 0}, cm[5] = {0, 0, 0, 0, 0};
+    for (int i0 = 0; i0 < a.npad; i0 += PH_CHUNK) {
+        const int nrec = min(PH_CHUNK, a.npad - i0);
+        __syncthreads();
+        for (int e = threadIdx.x; e < nrec * PH_REC; e += blockDim.x) s_rec[e] = a.rec[(long)i0 * PH_REC + e];
+        __syncthreads();
+        if (!valid) continue;
+        for (int ii = 0; ii < nrec; ii++) {
+            const int i = i0 + ii;
+            const float *R = s_rec + ii * PH_REC;
+            float c = 0.f, s = 0.f, r = 0.f;
+            if (i < a.ncomp) {
+                float2 ph = ff_add(ff_mul(R[0], R[1], dx.x, dx.y), ff_mul(R[2], R[3], dy.x, dy.y));
+                ph = ff_add(ph, ff_mul(R[4], R[5], tt.x, tt.y));
+                ph = ff_add(ph, make_float2(R[6], R[7]));
+                __sincosf(ff_reduce_2pi(ph), &s, &c);
+                r = a.trivial_ramp ? rconst
+                                   : (float)d_freq_ramp(tp, P[4 * cs + i], P[5 * cs + i], P[6 * cs + i]);
+                const float rc = r * c, rs = r * s;
+                ph_kahan(sm[0], cm[0], rc * R[8]);
+                ph_kahan(sm[1], cm[1], rc * R[9]);
+                ph_kahan(sm[2], cm[2], rc * R[10]);
+                ph_kahan(sm[3], cm[3], rs * R[11]);
+                ph_kahan(sm[4], cm[4], rc * R[12]);
+            }
+            a.ph[(long)i * a.n + p] = make_float2(c, s);
+            a.rr[(long)i * a.n + p] = r;
         }
-        a.ph[(long)i * a.n + p] = make_float2(c, s);
-        a.rr[(long)i * a.n + p] = r;
     }
-    a.first[0 * a.n + p] = e1;
-    a.first[1 * a.n + p] = gx;
-    a.first[2 * a.n + p] = gy;
-    a.first[3 * a.n + p] = gz;
-    a.first[4 * a.n + p] = gp;
+    if (!valid) return;
+    for (int q = 0; q < 5; q++) a.first[q * a.n + p] = (double)sm[q] - (double)cm[q];
 }
 
 // ---------------------------------------------------------------------------
@@ -925,7 +993,8 @@ static int launch_phasors(const DevSea &sea, long n, const double *x, const doub
     a.ncomp = sea.n; a.npad = npad; a.phase = sea.d_phase; a.cf = sea.d_cf;
     a.cstride = sea.npad_g; a.fx = sea.fx; a.fy = sea.fy;
     a.trivial_ramp = sea.trivial_ramp ? 1 : 0;
-    a.ph = ph; a.rr = rr; a.first = first;
+    a.ph = ph; a.rr = rr; a.first = first; a.rec = sea.d_phrec;
+    if (!sea.d_phrec || npad > ((sea.npad_g + 255) / 256) * 256) return E_BAD_ARGUMENT;
     prof_begin(PK_PHASORS, stream);
     k_phasors<<<(unsigned)((n + 127) / 128), 128, 0, stream>>>(a);
     note_launch();

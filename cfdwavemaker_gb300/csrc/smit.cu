@@ -221,10 +221,8 @@ __global__ void __launch_bounds__(128) k_smit_points(SmitArgs a) {
             }
             if (threadIdx.x < TT) {
                 const int m = M * TT + threadIdx.x;
-                const float km = a.cf[CF_K * a.cstride + m];
-                const double om = a.phase[2 * a.cstride + m];
-                s_k[threadIdx.x] = km;
-                s_a[threadIdx.x] = om > 0.0 ? (float)(km / om) : 0.f;
+                s_k[threadIdx.x] = a.cf[CF_K * a.cstride + m];
+                s_a[threadIdx.x] = a.cf[CF_KW * a.cstride + m];
             }
             for (int mm = 0; mm < TT; mm++) {
                 const int m = M * TT + mm;
@@ -250,9 +248,10 @@ __global__ void __launch_bounds__(128) k_smit_points(SmitArgs a) {
                     const float q = a.cf[CF_Q * a.cstride + i];
                     pfi = make_float2(q * F, q * G);
                 }
+                // k_i / omega_i from the coefficient rows: an FP64 division here,
+                // per (point, component, tile pair), kept the FP64 pipe 31% busy
                 const float ki = a.cf[CF_K * a.cstride + i];
-                const double oid = a.phase[2 * a.cstride + i];
-                const float ai = oid > 0.0 ? (float)(ki / oid) : 0.f;
+                const float ai = a.cf[CF_KW * a.cstride + i];
                 const float A1 = ai * pfi.y, B1 = ai * ki * h * pfi.x;
                 float au = 0, av = 0, aw = 0, ap = 0, ad = 0;
                 const int m0 = (M == I) ? ii : 0;

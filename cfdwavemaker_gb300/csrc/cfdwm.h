@@ -158,9 +158,9 @@ struct DevSea {
     bool smit = false;
     float *d_tab_smit = nullptr;
     int npad_s = 0, ntile_s = 0;
-    // per-launch component records of the tensor-core path's first-order
-    // kernels (depthform.cu): float-pair phase coefficients, ramp, 5
-    // coefficients; two regions (surface, levels) of npad_g records
+    // per-launch component records of the first-order kernels: float-pair
+    // phase coefficients, ramp, 5 coefficients; three regions of npad_g
+    // records (depthform.cu surface and levels, surrogate.cu features)
     float *d_dfcomp = nullptr;
     // per-component records of the point phasor kernel (irregular.cu):
     // kx, ky, -omega, phase0 as float pairs, then A, GX, GY, GZ, GP

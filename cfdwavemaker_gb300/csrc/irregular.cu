@@ -358,7 +358,7 @@ int sea_build(const Config &cfg, DevSea &sea, bool point_table, void *stream_) {
 
     CK(cudaMalloc(&sea.d_phase, sizeof(double) * 7 * sea.npad_g));
     CK(cudaMalloc(&sea.d_cf, sizeof(float) * NCF * sea.npad_g));
-    CK(cudaMalloc(&sea.d_dfcomp, sizeof(float) * DF_COMP_FLOATS * 2 * sea.npad_g));
+    CK(cudaMalloc(&sea.d_dfcomp, sizeof(float) * DF_COMP_FLOATS * 3 * sea.npad_g));
     // records for up to the next multiple of 256 components (the plain
     // precision form pads to 256), zero past the last component
     const int nrec_cap = ((sea.npad_g + 255) / 256) * 256;

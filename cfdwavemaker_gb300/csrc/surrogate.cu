@@ -101,9 +101,37 @@ struct FeatArgs {
     float *feat;           // [NQ nl][ncolh]
     float *base;           // [3][nx ny nl] first order with the Taylor term (interior), or null
     float *eta1;           // [nx ny] (interior), or null
+    const void *recs;      // this launch's component records (SurrRec, ncomp of them)
 };
 
 constexpr int FC = 128;      // components per shared-memory chunk
+
+// a component's record: float-pair phase coefficients and ramp at the
+// launch's time, then k, cu, cv, cw, cp
+struct SurrRec {
+    FfComp f;
+    float c[5];
+};
+static_assert(sizeof(SurrRec) == DF_COMP_FLOATS * sizeof(float), "component record size");
+
+// The records of all components, one thread each: the FP64 phase rows and
+// ramps converted once per launch instead of in every block (FP64 runs at a
+// small fraction of the FP32 rate on this GPU).
+__global__ void k_surr_recs(FeatArgs a, SurrRec *out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.ncomp) return;
+    const int cs = a.cstride;
+    SurrRec d;
+    d.f = ff_component(a.phase, cs, i, a.trivial_ramp, a.t);
+    const float q = a.cf[CF_Q * cs + i];
+    const float au = a.cf[CF_AU * cs + i] * q;
+    d.c[0] = a.cf[CF_K * cs + i];
+    d.c[1] = au * a.cf[CF_CT * cs + i];
+    d.c[2] = au * a.cf[CF_ST * cs + i];
+    d.c[3] = au;
+    d.c[4] = a.cf[CF_A * cs + i] * q;
+    out[i] = d;
+}
 
 // blockDim = 32 columns x ceil(nl / 4) level groups of 4 levels.  The warps
 // hold the same 32 columns: each forms the float-float phasors of every
@@ -141,21 +169,11 @@ __global__ void __launch_bounds__(256) k_surr_features(FeatArgs a) {
     for (int i0 = 0; i0 < a.ncomp; i0 += FC) {
         __syncthreads();
         for (int e = threadIdx.x; e < FC; e += blockDim.x) {
-            int i = i0 + e;
-            float k = 0.f, cu = 0.f, cv = 0.f, cw = 0.f, cp = 0.f;
-            FfComp f = {};
-            if (i < a.ncomp) {
-                f = ff_component(a.phase, a.cstride, i, a.trivial_ramp, a.t);
-                float q = a.cf[CF_Q * a.cstride + i];
-                float au = a.cf[CF_AU * a.cstride + i] * q;
-                k = a.cf[CF_K * a.cstride + i];
-                cu = au * a.cf[CF_CT * a.cstride + i];
-                cv = au * a.cf[CF_ST * a.cstride + i];
-                cw = au;
-                cp = a.cf[CF_A * a.cstride + i] * q;
-            }
-            s_f[e] = f;
-            s_c[0][e] = k; s_c[1][e] = cu; s_c[2][e] = cv; s_c[3][e] = cw; s_c[4][e] = cp;
+            const int i = i0 + e;
+            SurrRec d = {};
+            if (i < a.ncomp) d = reinterpret_cast<const SurrRec *>(a.recs)[i];
+            s_f[e] = d.f;
+            s_c[0][e] = d.c[0]; s_c[1][e] = d.c[1]; s_c[2][e] = d.c[2]; s_c[3][e] = d.c[3]; s_c[4][e] = d.c[4];
         }
         __syncthreads();
         const int iend = min(FC, a.ncomp - i0);
@@ -995,6 +1013,11 @@ static int features(Surrogate &s, const Config &cfg, const DevSea &sea, DevGrid 
     a.inv_su = (float)(1.0 / (sigma * om));
     a.inv_sp = (float)(1.0 / sigma);
     a.feat = feat; a.base = base; a.eta1 = eta1;
+    if (!sea.d_dfcomp) return E_NOT_INITIALIZED;
+    SurrRec *recs = reinterpret_cast<SurrRec *>(sea.d_dfcomp) + 2L * sea.npad_g;
+    k_surr_recs<<<(unsigned)((sea.n + 127) / 128), 128, 0, st>>>(a, recs);
+    note_launch();
+    a.recs = recs;
     int ngrp = (g.nl + 3) / 4;
     prof_begin(PK_SURR_FEATURES, st);
     k_surr_features<<<(unsigned)((nh + 31) / 32), 32 * ngrp, 0, st>>>(a);

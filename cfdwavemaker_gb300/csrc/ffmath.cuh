@@ -87,6 +87,27 @@ __device__ __forceinline__ double d_from_float(float f) {
     return __hiloint2double((int)hw, (int)lw);
 }
 
+// sin and cos of a reduced argument (|x| <= about 3.3) in FP32 FMAs only:
+// quarter-period Cody-Waite reduction (pi/2 = A + B + C, A and B short enough
+// that q A and q B are exact for |q| <= 2), then the Taylor series of sin to
+// r^9 and of cos to r^10 on |r| <= pi/4 (truncation below 2e-9); measured
+// against sin/cos at FP64 on a fine grid of [-3.3, 3.3]: below 1e-7 absolute.
+__device__ __forceinline__ void ff_sincos_poly(float x, float &s, float &c) {
+    const float q = rintf(x * 0.636619772f);
+    float r = fmaf(-q, 1.5703125f, x);
+    r = fmaf(-q, 4.837512969970703125e-4f, r);
+    r = fmaf(-q, 7.549789948768648e-8f, r);
+    const float r2 = r * r;
+    const float ps = fmaf(r2, fmaf(r2, fmaf(r2, 2.7557319e-6f, -1.98412698e-4f), 8.33333333e-3f), -0.166666667f);
+    const float pc =
+        fmaf(r2, fmaf(r2, fmaf(r2, fmaf(r2, -2.75573192e-7f, 2.48015873e-5f), -1.38888889e-3f), 4.16666667e-2f),
+             -0.5f);
+    const float sr = fmaf(r * r2, ps, r), cr = fmaf(r2, pc, 1.0f);
+    const int qi = ((int)q) & 3;
+    s = qi == 0 ? sr : qi == 1 ? cr : qi == 2 ? -sr : -cr;
+    c = qi == 0 ? cr : qi == 1 ? -sr : qi == 2 ? -cr : sr;
+}
+
 // Irregular::freq_ramp (Irregular.cpp:200-204), FP64
 __device__ __forceinline__ double ff_freq_ramp(double t, double rt, double ts, double du) {
     const double small = 1.e-12;   // Irregular.h:8

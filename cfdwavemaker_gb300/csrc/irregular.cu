@@ -483,8 +483,9 @@ __device__ __forceinline__ void ph_kahan(float &s, float &c, float v) {
 // and the first-order sums eta1 and the Taylor gradients.  The phase
 // kx (x - fx) + ky (y - fy) - omega t + phase0 is formed in float-float from
 // the records (the point's coordinates split by integer operations) and
-// reduced, then the SFU sine and cosine; the sums are FP32 with Kahan
-// compensation.  FP64 per (point, component) -- phase, reduction and FP64
+// reduced, then sine and cosine by polynomial (within 1e-7; the SFU's few
+// 1e-7 raised the plain form's error against FP64 tenfold); the sums are FP32
+// with Kahan compensation.  FP64 per (point, component) -- phase, reduction and FP64
 // sums -- kept the FP64 pipe the bound on this GPU.  Only non-trivial
 // component ramps are evaluated in FP64 (Irregular.cpp:200-204).
 __global__ void __launch_bounds__(128) k_phasors(PhArgs a) {
@@ -520,7 +521,7 @@ __global__ void __launch_bounds__(128) k_phasors(PhArgs a) {
                 float2 ph = ff_add(ff_mul(R[0], R[1], dx.x, dx.y), ff_mul(R[2], R[3], dy.x, dy.y));
                 ph = ff_add(ph, ff_mul(R[4], R[5], tt.x, tt.y));
                 ph = ff_add(ph, make_float2(R[6], R[7]));
-                __sincosf(ff_reduce_2pi(ph), &s, &c);
+                ff_sincos_poly(ff_reduce_2pi(ph), s, c);
                 r = a.trivial_ramp ? rconst
                                    : (float)d_freq_ramp(tp, P[4 * cs + i], P[5 * cs + i], P[6 * cs + i]);
                 const float rc = r * c, rs = r * s;

@@ -21,6 +21,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include <atomic>
@@ -282,6 +283,27 @@ int eval_api(long n, const double *x, const double *y, const double *z, const do
     return OK;
 }
 
+// Copies n doubles between pageable and pinned host memory on up to 16 host
+// threads (a single core moves about 10 GB/s; the copies were most of the
+// host-buffer calls' time beside the GPU work).
+static void host_copy(double *dst, const double *src, long n) {
+    const long per = 1L << 18;                       // 2 MB a thread at least
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const long nt = std::min<long>(std::min<long>(hw, 16), std::max<long>(1, n / per));
+    if (nt <= 1) {
+        std::memcpy(dst, src, sizeof(double) * n);
+        return;
+    }
+    std::vector<std::thread> th;
+    th.reserve(nt - 1);
+    for (long k = 1; k < nt; k++) {
+        const long lo = n * k / nt, hi = n * (k + 1) / nt;
+        th.emplace_back([=] { std::memcpy(dst + lo, src + lo, sizeof(double) * (hi - lo)); });
+    }
+    std::memcpy(dst, src, sizeof(double) * (n / nt));
+    for (auto &t : th) t.join();
+}
+
 // Runs eval_api on user arrays, staging host memory as needed.  outs[q]
 // receives row q of the pipeline output (NULL: not wanted).  For VFrac the
 // caller post-processes row 0.
@@ -337,7 +359,7 @@ int run_batch(const double *x, const double *y, const double *z, const double *t
                 CKR(cudaMemcpyAsync(din + (long)q * m, src[q] + b, sizeof(double) * m,
                                     cudaMemcpyDeviceToDevice, s));
             } else {
-                std::memcpy(hp + (long)q * m, src[q] + b, sizeof(double) * m);
+                host_copy(hp + (long)q * m, src[q] + b, m);
                 CKR(cudaMemcpyAsync(din + (long)q * m, hp + (long)q * m, sizeof(double) * m,
                                     cudaMemcpyHostToDevice, s));
             }
@@ -349,14 +371,26 @@ int run_batch(const double *x, const double *y, const double *z, const double *t
             note_launch();
             CKR(cudaGetLastError());
         }
-        CKR(cudaMemcpyAsync(hp + 4 * m, dout, sizeof(double) * 6 * m, cudaMemcpyDeviceToHost, s));
+        // only the rows asked for come back: row q of dout to hp + (4 + q) m;
+        // the Kinematics records are interleaved on the device (into din,
+        // whose inputs are consumed) and come back as one block
+        for (int q = 0; q < 6; q++)
+            if (outs[q])
+                CKR(cudaMemcpyAsync(hp + (4 + q) * m, dout + (long)q * m, sizeof(double) * m,
+                                    cudaMemcpyDeviceToHost, s));
+        if (vf_out)
+            CKR(cudaMemcpyAsync(hp + 9 * m, dout + 5 * m, sizeof(double) * m, cudaMemcpyDeviceToHost, s));
+        if (kin_out) {
+            k_interleave4<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(m, dout, din);
+            note_launch();
+            CKR(cudaGetLastError());
+            CKR(cudaMemcpyAsync(hp, din, sizeof(double) * 4 * m, cudaMemcpyDeviceToHost, s));
+        }
         CKR(cudaStreamSynchronize(s));
         for (int q = 0; q < 6; q++)
-            if (outs[q]) std::memcpy(outs[q] + b, hp + (4 + q) * m, sizeof(double) * m);
-        if (vf_out) std::memcpy(vf_out + b, hp + 9 * m, sizeof(double) * m);
-        if (kin_out)
-            for (long p = 0; p < m; p++)
-                for (int q = 0; q < 4; q++) kin_out[4 * (b + p) + q] = hp[(4 + q) * m + p];
+            if (outs[q]) host_copy(outs[q] + b, hp + (4 + q) * m, m);
+        if (vf_out) host_copy(vf_out + b, hp + 9 * m, m);
+        if (kin_out) host_copy(kin_out + 4 * b, hp, 4 * m);
     }
     return OK;
 }

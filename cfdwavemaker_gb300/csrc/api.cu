@@ -190,40 +190,45 @@ __device__ double d_ramp(const RampDev &r, double t, double x, double y) {
 // Irregular wave types 1/5 and regular 21 finish here: out rows
 // 0 SurfElev, 1 VeloX, 2 VeloY, 3 VeloZ, 4 DynPres, 5 nhPres.  sgp: the
 // s-grid holds the dynamic pressure (row 4 of its query).
+// The API rows of the model outputs: out[6][n] (eta, u, v, w, dp, nhpres;
+// or null) and/or the wave_Kinematics records kin[n][4] (eta, u, v, w; or
+// null), written in one pass.  Without a ramp the factor is not applied: FP64
+// multiplies run at a small fraction of the FP32 rate on this GPU.
 __global__ void k_finish(long n, int wavetype, int sgp, RampDev r, double rho, double g, const double *x,
                          const double *y, const double *t, const double *f, const double *fe,
-                         double *out) {
+                         double *out, double *kin) {
     long p = blockIdx.x * (long)blockDim.x + threadIdx.x;
     if (p >= n) return;
-    double rr = d_ramp(r, t[p], x[p], y[p]);
+    const bool ramped = r.init;
+    const double rr = ramped ? d_ramp(r, t[p], x[p], y[p]) : 1.0;
+    double v[6];
     if (wavetype == WT_IRREGULAR) {
         // f = [5][n] eta, u, v, w, dp of Irregular::*
-        out[0 * n + p] = rr * f[0 * n + p];
-        out[1 * n + p] = rr * f[1 * n + p];
-        out[2 * n + p] = rr * f[2 * n + p];
-        out[3 * n + p] = rr * f[3 * n + p];
-        out[4 * n + p] = rr * f[4 * n + p];
-        out[5 * n + p] = rr * (f[4 * n + p] - rho * g * f[0 * n + p]);
+        for (int q = 0; q < 5; q++) v[q] = f[q * n + p];
+        v[5] = f[4 * n + p] - rho * g * f[0 * n + p];
     } else if (wavetype == WT_IRR_SGRID) {
         // f = [4][n] query at the clamped z (sgp: [5][n] with the pressure),
         // fe = [4][n] query at z = 0.  Without a pressure field the
         // reference's 0.0 (CFDwavemaker.cpp:1808-1812, 1815-1891); with one,
         // the irregular sea's forms (:1807-1808, 1826-1830) on the grid.
-        out[0 * n + p] = fe[0 * n + p] * rr;
-        out[1 * n + p] = f[1 * n + p] * rr;
-        out[2 * n + p] = f[2 * n + p] * rr;
-        out[3 * n + p] = f[3 * n + p] * rr;
-        out[4 * n + p] = sgp ? rr * f[4 * n + p] : 0.0;
-        out[5 * n + p] = sgp ? rr * (f[4 * n + p] - rho * g * f[0 * n + p]) : 0.0;
+        v[0] = fe[0 * n + p];
+        v[1] = f[1 * n + p];
+        v[2] = f[2 * n + p];
+        v[3] = f[3 * n + p];
+        v[4] = sgp ? f[4 * n + p] : 0.0;
+        v[5] = sgp ? f[4 * n + p] - rho * g * f[0 * n + p] : 0.0;
     } else {
         // f = [5][n] eta, u, v, w, p_nh of the regular theory
-        out[0 * n + p] = rr * f[0 * n + p];
-        out[1 * n + p] = rr * f[1 * n + p];
-        out[2 * n + p] = rr * f[2 * n + p];
-        out[3 * n + p] = rr * f[3 * n + p];
-        out[4 * n + p] = 0.0;
-        out[5 * n + p] = rr * f[4 * n + p];
+        for (int q = 0; q < 4; q++) v[q] = f[q * n + p];
+        v[4] = 0.0;
+        v[5] = f[4 * n + p];
     }
+    if (ramped)
+        for (int q = 0; q < 6; q++) v[q] *= rr;
+    if (out)
+        for (int q = 0; q < 6; q++) out[q * n + p] = v[q];
+    if (kin)
+        for (int q = 0; q < 4; q++) kin[4 * p + q] = v[q];
 }
 
 // wave_VFrac (CFDwavemaker.cpp:1990-2009) from the ramped elevation.
@@ -256,7 +261,7 @@ RampDev ramp_dev(const RampCfg &r) {
 // The device pipeline: out[6][n] of the reference's wave_* functions for
 // the points (x, y, z, t), all device pointers.  want: bit q = output q.
 int eval_api(long n, const double *x, const double *y, const double *z, const double *t, int want,
-             double *out, cudaStream_t s) {
+             double *out, cudaStream_t s, double *kin = nullptr) {
     Model &M = g_model;
     if (!M.init) return E_NOT_INITIALIZED;
     if (n <= 0) return OK;
@@ -298,7 +303,7 @@ int eval_api(long n, const double *x, const double *y, const double *z, const do
     }
     const int sgp = (wt == WT_IRR_SGRID && M.grid.nf == 4) ? 1 : 0;
     k_finish<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(n, wt, sgp, rd, M.cfg.rho, M.cfg.gravity, x, y, t,
-                                                         f, fe, out);
+                                                         f, fe, out, kin);
     note_launch();
     CKR(cudaGetLastError());
     return OK;
@@ -356,7 +361,10 @@ int run_batch(const double *x, const double *y, const double *z, const double *t
         if (rc) return rc;
         out = (double *)dev_out.base;
         const double *zz = z ? z : t;   // z unused for SurfElev only
-        rc = eval_api(n, x, y, zz, t, want, out, s);
+        bool rows = vf_out != nullptr;
+        for (int q = 0; q < 6; q++) rows = rows || outs[q] != nullptr;
+        // the Kinematics records come straight from the finishing pass
+        rc = eval_api(n, x, y, zz, t, want, rows ? out : nullptr, s, kin_out);
         if (rc) return rc;
         for (int q = 0; q < 6; q++) {
             if (!outs[q]) continue;
@@ -370,11 +378,6 @@ int run_batch(const double *x, const double *y, const double *z, const double *t
         }
         if (vf_out) {
             k_vfrac<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, z, out, vf_dcell, vf_out);
-            note_launch();
-            CKR(cudaGetLastError());
-        }
-        if (kin_out) {
-            k_interleave4<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, out, kin_out);
             note_launch();
             CKR(cudaGetLastError());
         }

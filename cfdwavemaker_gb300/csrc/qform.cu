@@ -1057,11 +1057,11 @@ int tcform_split(TcForm &f, const double *coef64, const int *bmap_host, int nblk
 
 // Launches the GEMM of one chunk: as many CTAs (or CTA pairs) as fit on the
 // device at once (one CTA per SM), at most one per tile unit.
+// CTAs (or CTA pairs) of this form that fit on the device at once; set and
+// queried once per process (thread-safe static initialisation); <= 0: none.
 template <int BN, bool TWO, bool PAIR>
-static int launch_tc(const CUtensorMap &mXh, const CUtensorMap &mXl, const CUtensorMap &mWh, const CUtensorMap &mWl,
-                     const QTC &q, long nunits, cudaStream_t stream) {
+static int tc_max_units() {
     using CF = TcCfg<BN, TWO, PAIR>;
-    // set and queried once per process (thread-safe static initialisation)
     static const int maxunits = [] {
         if (cudaFuncSetAttribute(k_qform_tc<BN, TWO, PAIR>, cudaFuncAttributeMaxDynamicSharedMemorySize, CF::SMEM) !=
             cudaSuccess)
@@ -1083,9 +1083,20 @@ static int launch_tc(const CUtensorMap &mXh, const CUtensorMap &mXl, const CUten
         c.attrs = at;
         c.numAttrs = 1;
         int n = 0;
-        if (cudaOccupancyMaxActiveClusters(&n, k_qform_tc<BN, TWO, PAIR>, &c) != cudaSuccess) return -1;
+        if (cudaOccupancyMaxActiveClusters(&n, k_qform_tc<BN, TWO, PAIR>, &c) != cudaSuccess) {
+            cudaGetLastError();
+            return -1;
+        }
         return n;
     }();
+    return maxunits;
+}
+
+template <int BN, bool TWO, bool PAIR>
+static int launch_tc(const CUtensorMap &mXh, const CUtensorMap &mXl, const CUtensorMap &mWh, const CUtensorMap &mWl,
+                     const QTC &q, long nunits, cudaStream_t stream) {
+    using CF = TcCfg<BN, TWO, PAIR>;
+    const int maxunits = tc_max_units<BN, TWO, PAIR>();
     if (maxunits <= 0) {
         std::fprintf(stderr, "cfdwm: the tensor-core form (pair %d) does not fit on this device\n", (int)PAIR);
         return E_CUDA;
@@ -1169,7 +1180,8 @@ int tcform_eval(TcForm &f, const DevSea &sea, long n, const double *x, const dou
         CK(cudaStreamWaitEvent(pst, ev[0], 0));
     }
     const int BN = 256;
-    const bool pair = tc_pair();
+    // CTA pairs where two-CTA clusters fit on the device, else single CTAs
+    const bool pair = tc_pair() && (f.fp16 ? tc_max_units<256, true, true>() : tc_max_units<256, false, true>()) > 0;
     const int CSZ = pair ? 2 : 1;
     int j = 0;
     for (long b = 0; b < n; b += chunk, j++) {

@@ -426,18 +426,27 @@ def run_qform(args):
     lib.cfdwm_set_stream(C.c_void_p(stream.cuda_stream))
     ptr = [cw._ptr(a) for a in d]
     res = {"init_s": init_s, "forms": {}}
-    # FP64 oracle on a sample of rows
+    # Accuracy, outside the timed regions, on two references:
+    #  * the FP64 oracle on NS rows spread evenly over every 65,536-row chunk;
+    #  * the GPU plain FP32 form (itself within a few 1e-7 of FP64) on every
+    #    row of the first chunk, normalised by that chunk's max |plain|.
     import oracle
     cfg = oracle.waveinput.read_text(txt)
     sea = oracle.Sea(cfg)
-    ns = 24
-    refE = sea.eta2(x[:ns], y[:ns], t[:ns])
-    refU = sea.uvw2(x[:ns], y[:ns], np.zeros(ns), t[:ns])
+    ns = min(R, args.oracle_rows)
+    orows = np.unique(np.linspace(0, R - 1, ns).round().astype(np.int64))
+    refE = oracle_eta2_parallel(sea, x[orows], y[orows], t[orows])
+    refU = sea.uvw2(x[orows], y[orows], np.zeros(orows.size), t[orows])
     ref = np.stack([refE, refU[:, 0], refU[:, 1], refU[:, 2]], axis=1)
+    names = ("eta", "u", "v", "w")
 
-    def errs(o):
-        g = o[:ns].astype(np.float64)
-        return [float(np.max(np.abs(g[:, f] - ref[:, f])) / np.max(np.abs(ref[:, f]))) for f in range(4)]
+    def stats(got, want):
+        g = got.astype(np.float64)
+        d = g - want
+        den = np.max(np.abs(want), axis=0)
+        return {"max": [float(v) for v in np.max(np.abs(d), axis=0) / den],
+                "rms": [float(v) for v in np.sqrt(np.mean(d * d, axis=0)) / den],
+                "rms_rel": [float(v) for v in np.sqrt(np.mean(d * d, axis=0) / np.mean(want * want, axis=0))]}
 
     def timed(method, rows, steps, warm):
         for _ in range(warm):
@@ -454,16 +463,29 @@ def run_qform(args):
         timed.launches = lib.cfdwm_kernel_launches() - l0
         return e0.elapsed_time(e1) / steps
 
+    chunk = min(R, 65536)
+    plain_chunk = None
     for fp16 in (0, 1):
         name = "tc_fp16x3" if fp16 else "tc_bf16x3"
         tb = time.time()
         assert lib.cfdwm_qform_build(fp16) == 0, cw.last_error()
         build_s = time.time() - tb
         if fp16 == 0:
+            # the plain FP32 form on the first chunk, and on the oracle rows
             sub = min(R, args.plain_rows)
+            lib.cfdwm_profile_enable(1)
             ms = timed(0, sub, 1, 1)
+            kt = C.c_double(0.0)
+            nk = lib.cfdwm_profile_read(6, C.byref(kt))
+            lib.cfdwm_profile_enable(0)
+            plain_chunk = out[:chunk].cpu().numpy().astype(np.float64)
+            orow_t = torch.tensor(orows, device="cuda")
+            od = [a[orow_t].contiguous() for a in d]
+            oo = torch.zeros((orows.size, 4), device="cuda", dtype=torch.float32)
+            assert lib.cfdwm_qform_eval(*[cw._ptr(a) for a in od], orows.size, 0, cw._ptr(oo)) == 0
             res["forms"]["plain_fp32"] = {"ms_rows": ms, "rows": sub, "pts_per_s": sub / (ms / 1e3),
-                                          "err": errs(out.cpu().numpy())}
+                                          "kernel_ms": kt.value / max(1, nk),
+                                          "err_vs_fp64": stats(oo.cpu().numpy(), ref)}
         lib.cfdwm_profile_enable(1)
         lib.cfdwm_profile_read(6, None)
         sampler = ClockSampler(local)
@@ -473,9 +495,19 @@ def run_qform(args):
         tot = C.c_double(0.0)
         nk = lib.cfdwm_profile_read(6, C.byref(tot))
         lib.cfdwm_profile_enable(0)
-        res["forms"][name] = {"ms": ms, "rows": R, "pts_per_s": R / (ms / 1e3), "err": errs(out.cpu().numpy()),
+        o = out.cpu().numpy()
+        ev64 = stats(o[orows], ref)
+        evp = stats(o[:chunk], plain_chunk)
+        res["forms"][name] = {"ms": ms, "rows": R, "pts_per_s": R / (ms / 1e3),
+                              "err_vs_fp64": ev64, "err_vs_plain_chunk": evp,
+                              # the bar: the worse of the two references, per field
+                              "err": [max(a, b) for a, b in zip(ev64["max"], evp["max"])],
                               "build_s": build_s, "gemm_launches": int(nk), "launches": int(timed.launches),
                               "gemm_ms_per_step": tot.value / max(1, args.steps), "clocks": clocks}
+    res["accuracy_rows"] = {"fp64_oracle_rows": int(orows.size), "fields": names,
+                            "plain_chunk_rows": int(chunk),
+                            "norm": "max and rms of |form - ref| over the rows / max |ref| over the same rows; "
+                                    "rms_rel = rms(form - ref) / rms(ref)"}
     # end to end: host arrays in pinned memory, copies inside the timed region
     hx = [torch.from_numpy(a).pin_memory() for a in (x, y, t)]
     hout = torch.empty((R, 4), dtype=torch.float32).pin_memory()
@@ -537,16 +569,44 @@ def qform_line(args, r):
                                           "second), MEASURED_PEAKS.json"},
         "forms": {k: {kk: vv for kk, vv in v.items() if kk != "clocks"} for k, v in forms.items()},
         "speedup_vs_plain": (f["pts_per_s"] / plain["pts_per_s"]) if plain else None,
+        "accuracy": dict(r["accuracy_rows"], head_form=head,
+                         err_max=f["err_vs_plain_chunk"]["max"], err_rms=f["err_vs_plain_chunk"]["rms"],
+                         err_max_fp64=f["err_vs_fp64"]["max"], err_rms_fp64=f["err_vs_fp64"]["rms"],
+                         bar=1e-5),
         "init_s": r["init_s"],
         "peaks_source": src,
     }
+    if plain and plain.get("kernel_ms"):
+        # the plain form's kernel against the FP32 CUDA-core peak: 8 FMA per
+        # (pair, row), pairs counted over the visited tiles (diagonal tiles in
+        # full: their lower triangle holds zeros); peak = 152 SMs x 128 lanes
+        # x 2 flop x the maximum SM clock (no measured FP32 figure exists)
+        nt = N // 32
+        pairs = nt * (nt + 1) // 2 * 1024
+        ach = 16.0 * pairs * plain["rows"] / (plain["kernel_ms"] / 1e3) / 1e12
+        fp32_peak = 152 * 128 * 2 * pk.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
+        line["plain_roofline"] = {"kernel": "k_qform_plain", "bound": "fp32 FMA", "achieved": ach,
+                                  "peak": fp32_peak, "unit": "TFLOP/s", "frac": ach / fp32_peak,
+                                  "peak_source": "derived: 152 SMs x 128 FP32 lanes x 2 flop x sm_max_mhz"}
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = qform_cpu_baseline()
     return line
 
 
+def oracle_eta2_parallel(sea, x, y, t):
+    """Irregular::eta2 of the FP64 oracle at many points on all host cores
+    (one point per call; the ctypes calls release the GIL)."""
+    import concurrent.futures as cf
+    nthr = os.cpu_count() or 1
+    parts = np.array_split(np.arange(len(x)), nthr)
+    with cf.ThreadPoolExecutor(nthr) as ex:
+        outs = list(ex.map(lambda ix: sea.eta2(x[ix], y[ix], t[ix]), parts))
+    return np.concatenate(outs) if outs else np.zeros(0)
+
+
 def qform_cpu_baseline(budget_s=12.0):
-    """FP64 oracle (eta2 from the pair cache and uvw2 at z = 0) on a few rows."""
+    """FP64 oracle on a few rows: eta2 from the pair cache and uvw2 at z = 0,
+    the same four outputs per point as the GPU forms."""
     import oracle
     cfg = oracle.waveinput.read_text(qform_config())
     sea = oracle.Sea(cfg)
@@ -556,9 +616,10 @@ def qform_cpu_baseline(budget_s=12.0):
     x = rng.uniform(0, 1000, n); y = rng.uniform(0, 1000, n); t = rng.uniform(0, 100, n)
     t0 = time.perf_counter()
     sea.uvw2(x, y, np.zeros(n), t, nthr)
+    oracle_eta2_parallel(sea, x, y, t)
     el = time.perf_counter() - t0
     return {"value": n / el, "unit": "points/s", "cores": nthr, "kind": "port",
-            "sample": "%d points, uvw2 at z=0 (4096 components, FP64 oracle; eta2 adds ~10%%)" % n}
+            "sample": "%d points, eta2 and uvw2 at z=0 (4096 components, FP64 oracle)" % n}
 
 
 def point_config(vertical_theory=None):
@@ -997,6 +1058,8 @@ def main():
     ap.add_argument("--rows", type=int, default=4_000_000, help="points of the precision-form workload")
     ap.add_argument("--plain-rows", type=int, default=65536,
                     help="row subset on which the plain FP32 form of the precision workload is timed")
+    ap.add_argument("--oracle-rows", type=int, default=256,
+                    help="rows of the precision workload checked against the FP64 oracle (spread over every chunk)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--grid", type=int, default=256,
                     help="columns per side of the s-grid (256 is the named workload; smaller sizes "

@@ -118,6 +118,25 @@ def load(path: str | None = None):
     L.cfdwm_sgrid_state.argtypes = [_dp, C.POINTER(C.c_int)]
     L.cfdwm_regular_solution.restype = C.c_int
     L.cfdwm_regular_solution.argtypes = [vp, C.c_int]
+    L.cfdwm_regular_status.restype = C.c_int
+    L.cfdwm_regular_status.argtypes = []
+    # column shard of the s-grid ring (cfdwavemaker_gb300.shard)
+    L.cfdwm_partition_columns.restype = C.c_int
+    L.cfdwm_partition_columns.argtypes = [C.POINTER(C.c_long), C.c_int, C.c_int, C.POINTER(C.c_int)]
+    L.cfdwm_sgrid_partition.restype = C.c_int
+    L.cfdwm_sgrid_partition.argtypes = [C.c_int, C.POINTER(C.c_int)]
+    L.cfdwm_sgrid_due.restype = C.c_int
+    L.cfdwm_sgrid_due.argtypes = [_d]
+    L.cfdwm_sgrid_step_block.restype = C.c_int
+    L.cfdwm_sgrid_step_block.argtypes = [C.c_int, C.c_int]
+    L.cfdwm_sgrid_block_count.restype = C.c_long
+    L.cfdwm_sgrid_block_count.argtypes = [C.c_int, C.c_int, C.c_int]
+    L.cfdwm_sgrid_block_export.restype = C.c_int
+    L.cfdwm_sgrid_block_export.argtypes = [C.c_int, C.c_int, C.c_int, vp]
+    L.cfdwm_sgrid_block_import.restype = C.c_int
+    L.cfdwm_sgrid_block_import.argtypes = [C.c_int, C.c_int, C.c_int, vp]
+    L.cfdwm_sgrid_step_finish.restype = C.c_int
+    L.cfdwm_sgrid_step_finish.argtypes = []
     L.cfdwm_parse_text.restype = C.c_int
     L.cfdwm_parse_text.argtypes = [C.c_char_p, vp, vp, C.c_int]
     L.cfdwm_irregular_fields_noalloc.restype = C.c_int

@@ -22,7 +22,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden",
          "-I" + os.path.join(os.path.dirname(HERE), "include")]
 SOURCES = ["parser.cpp", "irregular.cu", "sgrid.cu", "regular.cu", "api.cu", "noalloc.cu", "qform.cu",
-           "surrogate.cu", "depthform.cu", "vtu.cpp", "smit.cu", "spectrum.cu"]
+           "surrogate.cu", "depthform.cu", "vtu.cpp", "smit.cu", "spectrum.cu", "shard.cpp"]
 
 
 def _compile(src):

@@ -63,6 +63,7 @@ namespace {
 
 struct Model {
     bool init = false;
+    int device = -1;          // the device current at initialisation: tables live there
     Config cfg;
     DevSea sea;
     DevGrid grid;
@@ -71,6 +72,12 @@ struct Model {
 };
 Model g_model;
 std::mutex g_model_mtx;
+// status word of the last regular-wave set-up (cfdwm_regular_status)
+int g_last_reg_status = -1;
+
+}  // namespace
+int noalloc_prepare();     // noalloc.cu
+namespace {
 
 // Ring updates through the learned update (cfdwm_surrogate_enable): every
 // plain_every-th update is plain, the others are predicted and checked.
@@ -471,10 +478,14 @@ int initialize_from_text(const std::string &text) {
     }
     cudaStream_t s = stream_of();
     M.cfg = cfg;
+    if (cudaGetDevice(&M.device) != cudaSuccess) M.device = -1;
     if (wt == WT_IRREGULAR || wt == WT_IRR_SGRID) {
         dump_spectral_components(cfg);
         rc = sea_build(cfg, M.sea, wt == WT_IRREGULAR, s);
         if (rc) { free_model(); return rc; }
+        // the fixed workspace of the allocation-free entry point is committed
+        // here, while the caller may still allocate (its module loads lazily)
+        noalloc_prepare();
         if (wt == WT_IRR_SGRID) {
             rc = grid_create(cfg, M.grid, s);
             // column sums: the depth-separable tensor-core form unless
@@ -494,8 +505,15 @@ int initialize_from_text(const std::string &text) {
         }
     } else {
         rc = regular_build(cfg, M.reg, s);
+        g_last_reg_status = (rc == OK || rc == E_SOLVER) ? M.reg.status : -1;
         if (rc) {
-            set_error("regular-wave setup failed");
+            if (rc == E_SOLVER && M.reg.status == 2)
+                set_error("FentonStream: singular Jacobian in the Newton solve");
+            else if (rc == E_SOLVER)
+                set_error("FentonStream: the Newton iteration left the finite numbers (no solution for this "
+                          "wave height)");
+            else
+                set_error("regular-wave setup failed");
             free_model();
             return rc;
         }
@@ -522,6 +540,7 @@ const DevSea *api_loaded_sea(int *wavetype) {
     if (wavetype) *wavetype = g_model.init ? g_model.cfg.wavetype : 0;
     return g_model.init ? &g_model.sea : nullptr;
 }
+int api_model_device() { return g_model.init ? g_model.device : -1; }
 void api_set_error(const char *msg) { set_error(msg); }
 void *api_user_stream() { return t_ctx.user_set ? (void *)t_ctx.user : nullptr; }
 
@@ -817,6 +836,65 @@ int cfdwm_parse_text(const char *text, double *scalars, double *comps, int cap) 
             for (int i = 0; i < n; i++) comps[(long)q * n + i] = (*src[q])[i];
     }
     return n;
+}
+
+int cfdwm_regular_status(void) { return g_last_reg_status; }
+
+// ---- column shard of the s-grid ring ---------------------------------------
+int cfdwm_sgrid_partition(int nranks, int *bounds) {
+    if (!g_model.init || g_model.cfg.wavetype != WT_IRR_SGRID) return E_UNSUPPORTED;
+    if (nranks < 1 || !bounds) return E_BAD_ARGUMENT;
+    std::vector<long> w;
+    grid_row_weights(g_model.grid, w);
+    partition_columns(w.data(), g_model.grid.nx, nranks, bounds);
+    return OK;
+}
+
+int cfdwm_sgrid_due(double t) {
+    if (!g_model.init || g_model.cfg.wavetype != WT_IRR_SGRID) return 0;
+    return grid_check_time(g_model.grid, t) ? 1 : 0;
+}
+
+int cfdwm_sgrid_step_block(int i0, int i1) {
+    std::lock_guard<std::mutex> lk(g_model_mtx);
+    Model &M = g_model;
+    if (!M.init || M.cfg.wavetype != WT_IRR_SGRID) return E_UNSUPPORTED;
+    return grid_step_block(M.grid, M.sea, M.grid_ws, i0, i1, stream_of());
+}
+
+long cfdwm_sgrid_block_count(int field, int i0, int i1) {
+    const DevGrid &g = g_model.grid;
+    if (!g_model.init || g_model.cfg.wavetype != WT_IRR_SGRID) return E_UNSUPPORTED;
+    if (i0 < 0 || i1 > g.nx || i0 > i1 || field < 0 || field > g.nf) return E_BAD_ARGUMENT;
+    return grid_block_elems(g, field, i0, i1);
+}
+
+static int block_copy(int field, int i0, int i1, float *buf, bool into) {
+    std::lock_guard<std::mutex> lk(g_model_mtx);
+    Model &M = g_model;
+    if (!M.init || M.cfg.wavetype != WT_IRR_SGRID) return E_UNSUPPORTED;
+    cudaStream_t s = stream_of();
+    int rc = grid_block_copy(M.grid, field, i0, i1, buf, into, s);
+    if (rc) return rc;
+    return cudaStreamSynchronize(s) == cudaSuccess ? OK : E_CUDA;
+}
+
+int cfdwm_sgrid_block_export(int field, int i0, int i1, float *dst) { return block_copy(field, i0, i1, dst, false); }
+
+int cfdwm_sgrid_block_import(int field, int i0, int i1, const float *src) {
+    return block_copy(field, i0, i1, const_cast<float *>(src), true);
+}
+
+int cfdwm_sgrid_step_finish(void) {
+    std::lock_guard<std::mutex> lk(g_model_mtx);
+    Model &M = g_model;
+    if (!M.init || M.cfg.wavetype != WT_IRR_SGRID) return E_UNSUPPORTED;
+    cudaStream_t s = stream_of();
+    int rc = grid_gradients(M.grid, s);
+    if (rc) return rc;
+    // [lsgrid2vtk]: every updated ring (lsgrid_spline.cpp:924-926)
+    if (M.cfg.lsgrid.dump_vtk) grid_dump_vtu(M.grid, false, s);
+    return cudaStreamSynchronize(s) == cudaSuccess ? OK : E_CUDA;
 }
 
 int cfdwm_regular_solution(double *dst, int cap) {

@@ -214,11 +214,6 @@ int irregular_eval(const DevSea &sea, long n, const double *x, const double *y,
 // Workspace bytes irregular_eval needs for a batch of n points.
 size_t irregular_eval_scratch_bytes(const DevSea &sea, long n);
 
-// Point-batched second-order sums only (for tests of the pair kernels):
-// which = 0 -> u2,v2,w2,dp2 of the point API at z, 1 -> uvw2 (grid mask).
-int irregular_second_order(const DevSea &sea, long n, const double *x, const double *y,
-                           const double *z, const double *t, int which, double *out,
-                           Workspace &ws, void *stream);
 
 // ---------------------------------------------------------------------------
 // Device-resident s-grid (sgrid.cu)
@@ -279,6 +274,14 @@ int grid_fill_columns(DevGrid &g, const DevSea &sea, Workspace &ws, const int *a
 int grid_fill_slot(DevGrid &g, const DevSea &sea, Workspace &ws, int slot, double t, void *stream);
 int grid_gradients(DevGrid &g, void *stream);
 void grid_live_columns(DevGrid &g, const int **act, long *n);
+// Column shard (sgrid.cu): live columns per row i; one ring step that fills
+// only the rows [i0, i1) of the new slot (no gradients); copies of a block of
+// rows of the newest slot; the host partition (shard.cpp).
+void grid_row_weights(const DevGrid &g, std::vector<long> &w);
+int grid_step_block(DevGrid &g, const DevSea &sea, Workspace &ws, int i0, int i1, void *stream);
+long grid_block_elems(const DevGrid &g, int f, int i0, int i1);
+int grid_block_copy(DevGrid &g, int f, int i0, int i1, float *buf, bool into_grid, void *stream);
+void partition_columns(const long *w, int n, int nranks, int *bounds);
 
 // ---------------------------------------------------------------------------
 // Learned s-grid update (surrogate.cu)

@@ -1331,11 +1331,4 @@ size_t irregular_eval_scratch_bytes(const DevSea &sea, long n) {
     return layout(std::min(n, chunk), sea.npad_g, nullptr).bytes;
 }
 
-int irregular_second_order(const DevSea &sea, long n, const double *x, const double *y,
-                           const double *z, const double *t, int which, double *out, Workspace &ws,
-                           void *stream_) {
-    (void)sea; (void)n; (void)x; (void)y; (void)z; (void)t; (void)which; (void)out; (void)ws; (void)stream_;
-    return E_UNSUPPORTED;
-}
-
 }  // namespace cfdwm

@@ -11,10 +11,13 @@
 // budget.
 //
 // Host code must not use the array's name as a device address (in host code
-// it names a host-side stand-in): the device address is looked up once per
-// device with cudaGetSymbolAddress, with that device current, on the first
-// call made on it.  That first call should therefore come before any stream
-// capture.
+// it names a host-side stand-in): the device address is looked up with
+// cudaGetSymbolAddress, once per device, with that device current.  Under
+// lazy module loading (the CUDA default) that lookup is also what loads this
+// file's module and commits the array's 32 MiB, so wave_Initialize does it
+// for the device it initialises on an irregular sea (noalloc_prepare), while
+// the caller may still allocate; calls only reuse the address.  Calls must
+// be made with that device current and on its memory.
 #include "cfdwm.h"
 #include "../../include/cfdwavemaker_gb300.h"
 
@@ -26,6 +29,7 @@
 namespace cfdwm {
 
 const DevSea *api_loaded_sea(int *wavetype);
+int api_model_device();
 void api_set_error(const char *msg);
 void *api_user_stream();
 
@@ -39,10 +43,12 @@ __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
 std::mutex g_setup_mtx;
 void *g_scratch_ptr[MAX_DEVICES] = {nullptr};
 
-// Device address of the scratch array on the current device (set-up on first use).
+// Device address of the scratch array on the current device (looked up once
+// per device; wave_Initialize does it for the model's device).
 int scratch_address(void **out) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) {
+        cudaGetLastError();
         api_set_error("no usable CUDA device for the scratch set-up");
         return E_CUDA;
     }
@@ -51,6 +57,7 @@ int scratch_address(void **out) {
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || p == nullptr) {
+            cudaGetLastError();
             api_set_error((std::string("cudaGetSymbolAddress failed: ") + cudaGetErrorString(e)).c_str());
             return E_CUDA;
         }
@@ -60,16 +67,26 @@ int scratch_address(void **out) {
     return OK;
 }
 
-bool device_accessible(const void *p) {
+// device memory of device `dev` (or managed memory)
+bool on_device(const void *p, int dev) {
     cudaPointerAttributes at;
     if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
         cudaGetLastError();
         return false;
     }
-    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+    if (at.type == cudaMemoryTypeManaged) return true;
+    return at.type == cudaMemoryTypeDevice && at.device == dev;
 }
 
 }  // namespace
+
+// Set-up at initialisation of an irregular sea on the current device.  A
+// failure here is not an initialisation error: the entry point reports it.
+int noalloc_prepare() {
+    void *p = nullptr;
+    return scratch_address(&p);
+}
+
 }  // namespace cfdwm
 
 using namespace cfdwm;
@@ -93,10 +110,27 @@ extern "C" int cfdwm_irregular_fields_noalloc(const double *x, const double *y, 
                       "call cfdwm_irregular_fields once first");
         return E_UNSUPPORTED;
     }
+    // the sea's tables live on the device current at wave_Initialize: the
+    // call and its arrays must be on that device too
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        api_set_error("no usable CUDA device");
+        return E_CUDA;
+    }
+    if (dev != api_model_device()) {
+        char msg[160];
+        std::snprintf(msg, sizeof msg,
+                      "cfdwm_irregular_fields_noalloc: current device %d, but the model was initialised on "
+                      "device %d", dev, api_model_device());
+        api_set_error(msg);
+        return E_BAD_ARGUMENT;
+    }
     const void *ptrs[5] = {x, y, z, t, out};
     for (const void *p : ptrs)
-        if (!p || !device_accessible(p)) {
-            api_set_error("cfdwm_irregular_fields_noalloc needs device-resident x, y, z, t and out");
+        if (!p || !on_device(p, dev)) {
+            api_set_error("cfdwm_irregular_fields_noalloc needs x, y, z, t and out in the memory of the "
+                          "device the model was initialised on");
             return E_BAD_ARGUMENT;
         }
     size_t need = irregular_eval_scratch_bytes(*sea, n);

@@ -364,7 +364,20 @@ __global__ void __launch_bounds__(128) k_qform_prep(QPrep a) {
 }
 
 // ---------------------------------------------------------------------------
-// Plain FP32 form (CUDA cores): thread per point, tiles staged in smem.
+// Plain FP32 form (CUDA cores), register-blocked.
+//
+// Block of 128 threads over 256 rows: thread t owns rows p and p + 128.  The
+// pair matrix is walked column tile by column tile (M outer, I = 0..M inner).
+// For the column tile M each thread keeps its two rows' 32 phasors (c, s) of
+// that tile in registers, packed as row pairs, so one coefficient read -- a
+// warp broadcast from shared memory -- feeds both rows through packed FP32x2
+// FMAs: per (pair, row pair) 8 FFMA2 against one 32-byte record read.  The
+// coefficient tiles (32 x 32 records of 8 floats, 32 KB) stream through two
+// shared-memory stages with cp.async, the next tile landing while the current
+// one is used.  The row phasor of component i is prefetched one i ahead.
+// Accumulation: the 32 terms of a tile row in FP32, then a Kahan pair per
+// (row, field), as before.  The lower triangle of the diagonal tiles holds
+// zeros, so every tile runs the full 32 x 32 loop.
 // ---------------------------------------------------------------------------
 struct QPlain {
     long rows;
@@ -375,52 +388,104 @@ struct QPlain {
     float *out;              // [rows][4]
 };
 
-constexpr int QPLAIN_SMEM = QT * QT * QNC * 4 + QT * 128 * 8;
+constexpr int QPL_ROWS = 256;                              // rows per block
+constexpr int QPL_TILE4 = QT * QT * QNC / 4;               // float4 per tile
+constexpr int QPLAIN_SMEM = 2 * QPL_TILE4 * 16;            // two stages, 64 KB
 
-__global__ void __launch_bounds__(128) k_qform_plain(QPlain a) {
+__device__ __forceinline__ void qpl_cp16(void *smem, const void *gmem) {
+    unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void qpl_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void qpl_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+__device__ __forceinline__ void qpl_kahan(float &S, float &C, float y) {
+    y -= C;
+    float t = S + y;
+    C = (t - S) - y;
+    S = t;
+}
+
+__global__ void __launch_bounds__(128, 2) k_qform_plain(QPlain a) {
     extern __shared__ float4 q_smem[];
-    float4 *s_tab = q_smem;                                         // QT*QT*QNC/4
-    float2 *s_ph = reinterpret_cast<float2 *>(q_smem + QT * QT * QNC / 4);   // QT*128
-    const long p = (long)blockIdx.x * 128 + threadIdx.x;
-    const bool valid = p < a.rows;
-    const long pc = valid ? p : 0;
-    float S[4] = {0, 0, 0, 0}, Cc[4] = {0, 0, 0, 0};
-    for (int I = 0; I < a.ntile; I++) {
-        for (int M = I; M < a.ntile; M++) {
-            __syncthreads();
-            const float4 *src = reinterpret_cast<const float4 *>(a.tab + qtile_index(I, M, a.ntile) * (long)QT * QT * QNC);
-            for (int e = threadIdx.x; e < QT * QT * QNC / 4; e += blockDim.x) s_tab[e] = src[e];
-            for (int mm = 0; mm < QT; mm++) s_ph[mm * 128 + threadIdx.x] = a.ph[(long)(M * QT + mm) * a.rows + pc];
-            __syncthreads();
-            if (!valid) continue;
-            for (int ii = 0; ii < QT; ii++) {
-                const int i = I * QT + ii;
-                const float2 pi = a.ph[(long)i * a.rows + p];
-                const float ri = a.rr[(long)i * a.rows + p];
-                float ec = 0, es = 0, uc = 0, us = 0, vc = 0, vs = 0, wc = 0, ws = 0;
-                const int m0 = (M == I) ? ii : 0;
-                for (int mm = m0; mm < QT; mm++) {
-                    const float4 c0 = s_tab[(ii * QT + mm) * 2];
-                    const float4 c1 = s_tab[(ii * QT + mm) * 2 + 1];
-                    const float2 pm = s_ph[mm * 128 + threadIdx.x];
-                    ec = fmaf(c0.x, pm.x, ec); es = fmaf(c0.y, pm.y, es);
-                    uc = fmaf(c0.z, pm.x, uc); us = fmaf(c0.w, pm.y, us);
-                    vc = fmaf(c1.x, pm.x, vc); vs = fmaf(c1.y, pm.y, vs);
-                    wc = fmaf(c1.z, pm.x, wc); ws = fmaf(c1.w, pm.y, ws);
-                }
-                float v[4] = {fmaf(pi.x, ec, pi.y * es), fmaf(pi.x, uc, pi.y * us),
-                              fmaf(pi.x, vc, pi.y * vs), fmaf(pi.y, wc, pi.x * ws)};
-                for (int f = 0; f < 4; f++) {
-                    float y = ri * v[f] - Cc[f];
-                    float tt = S[f] + y;
-                    Cc[f] = (tt - S[f]) - y;
-                    S[f] = tt;
-                }
+    const int tid = threadIdx.x;
+    const long p0 = (long)blockIdx.x * QPL_ROWS + tid, p1 = p0 + 128;
+    const long q0 = p0 < a.rows ? p0 : 0, q1 = p1 < a.rows ? p1 : 0;   // clamped reads
+    const int nt = a.ntile;
+    const long ntiles = (long)nt * (nt + 1) / 2;
+    const float4 *tab4 = reinterpret_cast<const float4 *>(a.tab);
+    float S0[4] = {0, 0, 0, 0}, C0[4] = {0, 0, 0, 0}, S1[4] = {0, 0, 0, 0}, C1[4] = {0, 0, 0, 0};
+    float2 pmc[QT], pms[QT];     // (row p, row p + 128) of c and s for the 32 components of tile M
+
+    // stage k of the walk: tile (I, M) with M outer
+    int lI = 0, lM = 0;          // next tile to load
+    auto issue = [&](long k) {
+        if (k < ntiles) {
+            const float4 *src = tab4 + qtile_index(lI, lM, nt) * (long)QPL_TILE4;
+            float4 *dst = q_smem + (k & 1) * QPL_TILE4;
+#pragma unroll 4
+            for (int e = tid; e < QPL_TILE4; e += 128) qpl_cp16(dst + e, src + e);
+            if (++lI > lM) { lI = 0; lM++; }
+        }
+        qpl_commit();
+    };
+    issue(0);
+    int I = 0, M = 0;
+    for (long k = 0; k < ntiles; k++) {
+        issue(k + 1);
+        if (I == 0) {
+#pragma unroll
+            for (int mm = 0; mm < QT; mm++) {
+                const long r = (long)(M * QT + mm) * a.rows;
+                const float2 x0 = a.ph[r + q0], x1 = a.ph[r + q1];
+                pmc[mm] = make_float2(x0.x, x1.x);
+                pms[mm] = make_float2(x0.y, x1.y);
             }
         }
+        qpl_wait1();
+        __syncthreads();
+        const float4 *st = q_smem + (k & 1) * QPL_TILE4;
+        long ri = (long)(I * QT) * a.rows;
+        float2 pi0 = a.ph[ri + q0], pi1 = a.ph[ri + q1];
+        float r0 = a.rr[ri + q0], r1 = a.rr[ri + q1];
+        for (int ii = 0; ii < QT; ii++) {
+            // prefetch the next row phasor (the last one re-reads a valid index)
+            const long rn = ri + (ii + 1 < QT ? a.rows : 0);
+            const float2 n0 = a.ph[rn + q0], n1 = a.ph[rn + q1];
+            const float nr0 = a.rr[rn + q0], nr1 = a.rr[rn + q1];
+            float2 ec = {0, 0}, es = {0, 0}, uc = {0, 0}, us = {0, 0}, vc = {0, 0}, vs = {0, 0}, wc = {0, 0},
+                   ws = {0, 0};
+            const float4 *rec = st + ii * QT * 2;
+#pragma unroll
+            for (int mm = 0; mm < QT; mm++) {
+                const float4 c0 = rec[2 * mm], c1 = rec[2 * mm + 1];
+                ec = __ffma2_rn(make_float2(c0.x, c0.x), pmc[mm], ec);
+                es = __ffma2_rn(make_float2(c0.y, c0.y), pms[mm], es);
+                uc = __ffma2_rn(make_float2(c0.z, c0.z), pmc[mm], uc);
+                us = __ffma2_rn(make_float2(c0.w, c0.w), pms[mm], us);
+                vc = __ffma2_rn(make_float2(c1.x, c1.x), pmc[mm], vc);
+                vs = __ffma2_rn(make_float2(c1.y, c1.y), pms[mm], vs);
+                wc = __ffma2_rn(make_float2(c1.z, c1.z), pmc[mm], wc);
+                ws = __ffma2_rn(make_float2(c1.w, c1.w), pms[mm], ws);
+            }
+            qpl_kahan(S0[0], C0[0], r0 * fmaf(pi0.x, ec.x, pi0.y * es.x));
+            qpl_kahan(S0[1], C0[1], r0 * fmaf(pi0.x, uc.x, pi0.y * us.x));
+            qpl_kahan(S0[2], C0[2], r0 * fmaf(pi0.x, vc.x, pi0.y * vs.x));
+            qpl_kahan(S0[3], C0[3], r0 * fmaf(pi0.y, wc.x, pi0.x * ws.x));
+            qpl_kahan(S1[0], C1[0], r1 * fmaf(pi1.x, ec.y, pi1.y * es.y));
+            qpl_kahan(S1[1], C1[1], r1 * fmaf(pi1.x, uc.y, pi1.y * us.y));
+            qpl_kahan(S1[2], C1[2], r1 * fmaf(pi1.x, vc.y, pi1.y * vs.y));
+            qpl_kahan(S1[3], C1[3], r1 * fmaf(pi1.y, wc.y, pi1.x * ws.y));
+            ri = rn;
+            pi0 = n0; pi1 = n1; r0 = nr0; r1 = nr1;
+        }
+        __syncthreads();     // the stage is refilled by the next issue
+        if (++I > M) { I = 0; M++; }
     }
-    if (valid)
-        for (int f = 0; f < 4; f++) a.out[p * 4 + f] = S[f];
+    if (p0 < a.rows)
+        for (int f = 0; f < 4; f++) a.out[p0 * 4 + f] = S0[f];
+    if (p1 < a.rows)
+        for (int f = 0; f < 4; f++) a.out[p1 * 4 + f] = S1[f];
 }
 
 // ---------------------------------------------------------------------------
@@ -1062,14 +1127,20 @@ int tcform_split(TcForm &f, const double *coef64, const int *bmap_host, int nblk
 template <int BN, bool TWO, bool PAIR>
 static int tc_max_units() {
     using CF = TcCfg<BN, TWO, PAIR>;
+    // computed on the device current at the first call and kept for the
+    // process (the library serves one device: the model's)
     static const int maxunits = [] {
         if (cudaFuncSetAttribute(k_qform_tc<BN, TWO, PAIR>, cudaFuncAttributeMaxDynamicSharedMemorySize, CF::SMEM) !=
-            cudaSuccess)
+            cudaSuccess) {
+            cudaGetLastError();     // a failure here only selects the other form
             return -1;
+        }
         int dev = 0, nsm = 0;
         if (cudaGetDevice(&dev) != cudaSuccess ||
-            cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+            cudaGetLastError();
             return -1;
+        }
         if (!PAIR) return nsm;
         cudaLaunchConfig_t c = {};
         cudaLaunchAttribute at[1];
@@ -1360,7 +1431,7 @@ int qform_eval(const DevSea &sea, long n, const double *x, const double *y, cons
         q.rows = mm; q.ntile = g_q.ntile_plain; q.tab = g_q.plain_tab; q.ph = ph; q.rr = rr;
         q.out = out + 4 * b;
         prof_begin(PK_QFORM, stream);
-        k_qform_plain<<<(unsigned)((mm + 127) / 128), 128, QPLAIN_SMEM, stream>>>(q);
+        k_qform_plain<<<(unsigned)((mm + QPL_ROWS - 1) / QPL_ROWS), 128, QPLAIN_SMEM, stream>>>(q);
         note_launch();
         prof_end(PK_QFORM, stream);
         CK(cudaGetLastError());

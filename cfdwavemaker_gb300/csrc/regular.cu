@@ -312,10 +312,16 @@ __global__ void __launch_bounds__(128) k_fenton_solve(RegIn in, double *sol, dou
         status = (int)red[0];
     }
     if (tid != 0) return;
+    // a Newton iterate that left the finite numbers (a wave beyond the
+    // highest one: the reference warns and serves NaN coefficients) is a
+    // failure here, status 4
+    if (status != 2)
+        for (int i = 1; i <= num; ++i)
+            if (!isfinite(z[i])) { status = 4; break; }
     for (int q = 0; q < SOL; q++) sol[q] = 0.0;
     sol[6] = status;
     sol[7] = N;
-    if (status == 2) return;
+    if (status == 2 || status == 4) return;
     // dimensional results and the output coefficients (FentonStream.cpp:213-239)
     double g = in.g, d = in.d;
     double k = f.finite ? (z[1] / d) : (z[2] / in.H);
@@ -485,7 +491,7 @@ int regular_build(const Config &cfg, DevRegular &r, void *stream_) {
     CK(cudaMalloc(&r.d_cf, sizeof cf));
     CK(cudaMemcpyAsync(r.d_cf, cf, sizeof cf, cudaMemcpyHostToDevice, stream));
     CK(cudaStreamSynchronize(stream));
-    if (r.status == 2) return E_SOLVER;
+    if (r.status == 2 || r.status == 4) return E_SOLVER;
     return OK;
 }
 

@@ -370,6 +370,9 @@ struct GridExtra {
     std::vector<double> kin_r, ramp_par;
     bool kin_valid = false;
     DepthForm df;              // tensor-core form of the column sums (method 1)
+    // live columns before row i (act_live is ascending in i ny + j):
+    // the live columns of rows [i0, i1) are act_live[row_live[i0] .. row_live[i1])
+    std::vector<long> row_live;
 };
 static std::vector<std::pair<const DevGrid *, GridExtra>> g_extra;
 static GridExtra *extra(const DevGrid &g) {
@@ -407,7 +410,10 @@ int grid_create(const Config &cfg, DevGrid &g, void *stream_) {
         CK(cudaMemsetAsync(g.Ut[f], 0, sizeof(float) * 4 * v, stream));
     }
     std::vector<int> ign(c), all, live;
+    GridExtra *xr = extra(g);
+    xr->row_live.assign(g.nx + 1, 0);
     for (int i = 0; i < g.nx; i++) {
+        xr->row_live[i] = (long)live.size();
         double xp = g.cfg.domain[0] + g.dx * i;
         for (int j = 0; j < g.ny; j++) {
             double yp = g.cfg.domain[2] + g.dy * j;
@@ -418,6 +424,7 @@ int grid_create(const Config &cfg, DevGrid &g, void *stream_) {
             if (!ig) live.push_back(i * g.ny + j);
         }
     }
+    xr->row_live[g.nx] = (long)live.size();
     CK(cudaMalloc(&g.IGNORE, sizeof(int) * c));
     CK(cudaMemcpyAsync(g.IGNORE, ign.data(), sizeof(int) * c, cudaMemcpyHostToDevice, stream));
     GridExtra *x = extra(g);
@@ -687,6 +694,53 @@ int grid_update(DevGrid &g, const DevSea &sea, Workspace &ws, void *stream_) {
 }
 
 bool grid_check_time(const DevGrid &g, double t) { return t > g.t0 + g.dt; }
+
+// ---------------------------------------------------------------------------
+// Column shard.  The reference's MPI build splits the grid's rows of columns
+// (index i) over the ranks by a work-balanced contiguous partition weighted
+// by the live columns of each row (lsgrid_spline.cpp:652-664,
+// mpi_utils.h:46-64); each rank fills its rows of the new slot and the slot's
+// ETA, UX, UY, UZ are all-gathered (lsgrid_spline.cpp:907-910) before every
+// rank recomputes the gradients.  A rank's rows [i0, i1) of a slot are
+// contiguous in every field ([slot][i][j] and [slot][i][j][m]), so a block is
+// one copy per field.
+// ---------------------------------------------------------------------------
+void grid_row_weights(const DevGrid &g, std::vector<long> &w) {
+    GridExtra *x = extra(g);
+    w.resize(g.nx);
+    for (int i = 0; i < g.nx; i++) w[i] = x->row_live[i + 1] - x->row_live[i];
+}
+
+int grid_step_block(DevGrid &g, const DevSea &sea, Workspace &ws, int i0, int i1, void *stream_) {
+    if (i0 < 0 || i1 > g.nx || i0 > i1) return E_BAD_ARGUMENT;
+    cudaStream_t stream = (cudaStream_t)stream_;
+    g.tstep++;
+    g.t0 += g.dt;
+    const double t2 = g.t0 + 2 * g.dt;
+    const int slot = (g.tstep + 3) % 4;
+    GridExtra *x = extra(g);
+    const long a = x->row_live[i0], b = x->row_live[i1];
+    return fill_cols(g, sea, ws, x->act_live + a, b - a, t2, g.ETA, g.U, g.nf == 4 ? g.U[3] : nullptr, slot, stream);
+}
+
+// rows [i0, i1) of field f (0 ETA, 1 + q the velocity / pressure field q) of
+// the newest slot to or from buf (device or host memory); returns the count
+long grid_block_elems(const DevGrid &g, int f, int i0, int i1) {
+    return (long)(i1 - i0) * g.ny * (f == 0 ? 1 : g.nl);
+}
+
+int grid_block_copy(DevGrid &g, int f, int i0, int i1, float *buf, bool into_grid, void *stream_) {
+    if (i0 < 0 || i1 > g.nx || i0 > i1 || f < 0 || f > g.nf || !buf) return E_BAD_ARGUMENT;
+    cudaStream_t stream = (cudaStream_t)stream_;
+    const int slot = (g.tstep + 3) % 4;
+    const long c = (long)g.nx * g.ny;
+    float *base = f == 0 ? g.ETA + (long)slot * c + (long)i0 * g.ny
+                         : g.U[f - 1] + ((long)slot * c + (long)i0 * g.ny) * g.nl;
+    const size_t bytes = sizeof(float) * grid_block_elems(g, f, i0, i1);
+    if (bytes == 0) return OK;
+    CK(cudaMemcpyAsync(into_grid ? base : buf, into_grid ? buf : base, bytes, cudaMemcpyDefault, stream));
+    return OK;
+}
 
 int grid_query(const DevGrid &g, long n, const double *x, const double *y, const double *z,
                const double *t, double *out, void *stream_) {

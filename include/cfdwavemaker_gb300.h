@@ -159,6 +159,19 @@ CFDWM_EXPORT int cfdwm_sgrid_state(double *t0, int *tstep);
 /* Regular-wave solution: k, c, mean velocity, Bernoulli R, L, T, then B_j
  * (Fenton); returns the count written. */
 CFDWM_EXPORT int cfdwm_regular_solution(double *dst, int cap);
+/* Status word of the last regular-wave set-up by wave_Initialize (the Fenton
+ * Newton solve of FentonStream::set_stream_properties, FentonStream.cpp:141-239):
+ *   0  converged (and always for Stokes 5th);
+ *   3  not fully converged at the last continuation step: the reference's
+ *      warning (FentonStream.cpp:208-209) is printed and the iterate is
+ *      served, as the reference serves it;
+ *   2  singular Jacobian (the reference throws, FentonStream.cpp:200-201):
+ *      wave_Initialize returned -7;
+ *   4  the iterate left the finite numbers (a wave beyond the highest one;
+ *      the reference warns and serves NaN coefficients): wave_Initialize
+ *      returned -7;
+ *  -1  no regular-wave set-up has run. */
+CFDWM_EXPORT int cfdwm_regular_status(void);
 /* Parse waveinput.dat text without touching the GPU.  scalars[16] receives
  * wavetype, order, depth, mtheta, swl, gravity, rho, tofmax, x0, y0,
  * dw_cutoff, dw_bandwidth, wave_length, wave_period, wave_height, ndir;
@@ -183,15 +196,18 @@ CFDWM_EXPORT int cfdwm_qform_eval(const double *x, const double *y, const double
  * for host codes that cannot let the library allocate device memory while
  * they run (solvers that reserve all device memory for their own pool at
  * start-up, or run under a fixed device-memory budget): this call performs
- * no cudaMalloc/cudaFree or other allocation.  x, y, z, t and out ([5][n])
- * must be device memory of the current device.  The workspace is one fixed
- * 32 MiB device array per GPU, held from library load until process exit;
- * a batch needs about (12 * Npad + 64) bytes per point, Npad = component
+ * no cudaMalloc/cudaFree or other allocation.  Make the call with the device
+ * that wave_Initialize ran on current, with x, y, z, t and out ([5][n]) in
+ * that device's memory; anything else is rejected with -3.  The workspace is
+ * one fixed 32 MiB device array per GPU, held until process exit.  Under
+ * lazy module loading (the CUDA default) it is committed when
+ * wave_Initialize loads an irregular sea (wave types 1 and 5), which also
+ * looks up its device address, so later calls make no set-up of their own.
+ * A batch needs about (12 * Npad + 64) bytes per point, Npad = component
  * count rounded up to a multiple of 32, and larger batches are rejected with
- * -8 (message in cfdwm_last_error).  The first call on a device looks up the
- * array's device address, so make it before any stream capture.  All calls
- * share the array: calls that overlap on the GPU (several host threads or
- * streams at once) race.  The call returns after the results are written.
+ * -8 (message in cfdwm_last_error).  All calls share the array: calls that
+ * overlap on the GPU (several host threads or streams at once) race.  The
+ * call returns after the results are written.
  * Wave type 5 models need one cfdwm_irregular_fields call first (it builds
  * the point-API pair table); without it the call returns -2. */
 CFDWM_EXPORT int cfdwm_irregular_fields_noalloc(const double *x, const double *y, const double *z,
@@ -253,6 +269,48 @@ CFDWM_EXPORT int cfdwm_sgrid_write_vtu(const char *path, int last);
  * Returns 0, -3 (bad parameters) or -4. */
 CFDWM_EXPORT int cfdwm_spectrum_components(const double *params, int nfreq, int ndir, unsigned long long seed,
                                            double *comps);
+
+/* ---------------------------------------------------------------------- */
+/* Part 4d: column shard of the s-grid ring over several GPUs (new beside  */
+/* the reference's MPI build, which these calls replace)                   */
+/* ---------------------------------------------------------------------- */
+/* The reference's MPI build splits the grid's rows of columns (index i) over
+ * the ranks (lsGridSpline::compute_mpi_partition, lsgrid_spline.cpp:652-664,
+ * with cfdwm_mpi::partition_weighted, mpi_utils.h:46-64), lets each rank fill
+ * its rows of the new slot and all-gathers the slot's ETA, UX, UY, UZ
+ * (lsgrid_spline.cpp:907-910, mpi_utils.h:69-79) before every rank
+ * recomputes the gradients.  Here one process per GPU loads the same model;
+ * the calls below are the rank's side of one such step, and the all-gather
+ * between them is the caller's (cfdwavemaker_gb300.shard does it with
+ * torch.distributed: NCCL on GPUs).
+ *
+ * Work-balanced contiguous partition of n rows with weights w (>= 0) over
+ * nranks: bounds[0..nranks], rank r owns rows [bounds[r], bounds[r+1]).  The
+ * reference's rule (mpi_utils.h:46-64), host only (no GPU needed). */
+CFDWM_EXPORT int cfdwm_partition_columns(const long *weights, int n, int nranks, int *bounds);
+/* The same for the loaded grid: weights = live (not ignored) columns per row
+ * (lsgrid_spline.cpp:652-664). */
+CFDWM_EXPORT int cfdwm_sgrid_partition(int nranks, int *bounds);
+/* 1 when wave_force_update(t) would step the ring (lsGridSpline::CheckTime,
+ * lsgrid_spline.cpp:610-615), else 0. */
+CFDWM_EXPORT int cfdwm_sgrid_due(double t);
+/* One ring step of the rank that owns rows [i0, i1): advances the ring
+ * (lsgrid_spline.cpp:847-860) and fills only those rows of the new slot (in
+ * the s-grid method of the model). */
+CFDWM_EXPORT int cfdwm_sgrid_step_block(int i0, int i1);
+/* Elements of rows [i0, i1) of one field of a slot: field 0 ETA ((i1-i0) ny),
+ * 1..3 UX, UY, UZ and 4 the pressure when the ring holds it
+ * ((i1-i0) ny nl). */
+CFDWM_EXPORT long cfdwm_sgrid_block_count(int field, int i0, int i1);
+/* Copies rows [i0, i1) of a field of the newest slot to dst / from src (host
+ * or device memory, [rows][ny] or [rows][ny][nl] as the ring stores them);
+ * return when the copy is done. */
+CFDWM_EXPORT int cfdwm_sgrid_block_export(int field, int i0, int i1, float *dst);
+CFDWM_EXPORT int cfdwm_sgrid_block_import(int field, int i0, int i1, const float *src);
+/* After every rank's rows are in the newest slot: the finite-difference
+ * gradients and the query image (lsgrid_spline.cpp:912-922), and the .vtu
+ * file of a [lsgrid2vtk] section. */
+CFDWM_EXPORT int cfdwm_sgrid_step_finish(void);
 
 /* ===========================================================================
  * Part 5 -- learned s-grid update (new; no counterpart in the reference).

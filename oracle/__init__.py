@@ -75,6 +75,10 @@ def lib():
         L.orc_sgrid_array.restype = C.c_long
         L.orc_sgrid_array.argtypes = [C.c_void_p, C.c_int, _dp]
         L.orc_sgrid_state.argtypes = [C.c_void_p, _dp, C.POINTER(C.c_int)]
+        L.orc_sgrid_advance.argtypes = [C.c_void_p]
+        L.orc_sgrid_gradients.argtypes = [C.c_void_p]
+        L.orc_sgrid_set_slot.restype = C.c_int
+        L.orc_sgrid_set_slot.argtypes = [C.c_void_p, C.c_int, _dp]
         L.orc_stokes5_create.restype = C.c_void_p
         L.orc_stokes5_create.argtypes = [C.c_double] * 11
         L.orc_stokes5_free.argtypes = [C.c_void_p]
@@ -197,6 +201,17 @@ class Sgrid:
 
     def update_columns(self, t, c0, c1, nthreads=0):
         lib().orc_sgrid_update_columns(self.h, self.sea.h, float(t), int(c0), int(c1), nthreads)
+
+    def advance(self):
+        lib().orc_sgrid_advance(self.h)
+
+    def gradients(self):
+        lib().orc_sgrid_gradients(self.h)
+
+    def set_slot(self, which, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        if lib().orc_sgrid_set_slot(self.h, int(which), a.ctypes.data_as(_dp)) != 0:
+            raise ValueError(which)
 
     def query(self, x, y, z, t, nthreads=0):
         """[n][4] eta, u, v, w; with the pressure field [n][5] (and p)."""

@@ -109,6 +109,12 @@ void orc_sgrid_update_columns(orc_sgrid *g, const orc_sea *s, double t, long c0,
  * 13 Vdy, 14 Vds, 15 Wdt, 16 Wdx, 17 Wdy, 18 Wds, 19 IGNORE (as double);
  * with the pressure: 20 PP, 21 Pdt, 22 Pdx, 23 Pdy, 24 Pds. */
 long orc_sgrid_array(const orc_sgrid *g, int which, double *dst);
+/* update() split as a rank of the reference's MPI build runs it: advance the
+ * ring, fill columns (orc_sgrid_update_columns at t0 + 2 dt), replace the
+ * newest slot of ETA/UX/UY/UZ (which 0..3) by the gathered one, gradients. */
+void orc_sgrid_advance(orc_sgrid *g);
+void orc_sgrid_gradients(orc_sgrid *g);
+int orc_sgrid_set_slot(orc_sgrid *g, int which, const double *src);
 /* export_vtu (lsgrid_spline.cpp:1222-1403) of the base slot (last = 0) or the
  * slot after it (last = 1) into the file `path`; 0 or -1. */
 int orc_sgrid_export_vtu(const orc_sgrid *g, const char *path, int last, const char *label);

@@ -254,6 +254,27 @@ void orc_sgrid_update_columns(orc_sgrid *g, const orc_sea *s, double t, long c0,
 
 int orc_sgrid_check_time(const orc_sgrid *g, double t) { return t > g->t0 + g->dt; }
 
+/* The three parts of update() (lsgrid_spline.cpp:847-931) as the MPI build
+ * runs them on each rank: advance the ring, fill a column subset
+ * (orc_sgrid_update_columns at t0 + 2 dt), set the gathered slot, gradients. */
+void orc_sgrid_advance(orc_sgrid *g) {
+    g->tstep++;
+    g->t0 += g->dt;
+}
+
+void orc_sgrid_gradients(orc_sgrid *g) { all_gradients(g); }
+
+/* Replaces the newest slot of array which (0 ETA, 1 UX, 2 UY, 3 UZ) by src. */
+int orc_sgrid_set_slot(orc_sgrid *g, int which, const double *src) {
+    size_t c = (size_t)g->nx * g->ny, v = c * g->nl;
+    int tt = (g->tstep + 3) % 4;
+    double *arr[4] = {g->ETA, g->UX, g->UY, g->UZ};
+    if (which < 0 || which > 3) return -1;
+    size_t n = which == 0 ? c : v;
+    memcpy(arr[which] + (size_t)tt * n, src, n * sizeof(double));
+    return 0;
+}
+
 /* square_vals / cube_vals, lsgrid_spline.cpp:368-384 */
 static void square_vals(const orc_sgrid *g, double *C, const double *d, int xp, int yp, int tid) {
     int nx = g->nx, ny = g->ny;

@@ -352,6 +352,49 @@ def spectral_moments(cfg):
     return m0, m1, m2
 
 
+PI_TRUNC = 3.1415926535897      # the truncated PI of Irregular.h:14
+
+
+def _interpolate_extrap(xd, yd, x):
+    """Irregular::interpolate with extrapolation, Irregular.cpp:1311-1334."""
+    n = len(xd)
+    i = 0
+    if x >= xd[n - 2]:
+        i = n - 2
+    else:
+        while x > xd[i + 1]:
+            i += 1
+    xL, yL, xR, yR = xd[i], yd[i], xd[i + 1], yd[i + 1]
+    return yL + (yR - yL) / (xR - xL) * (x - xL)
+
+
+def _mean_periods(cfg):
+    m0, m1, m2 = spectral_moments(cfg)
+    return 2.0 * PI_TRUNC * (m0 / m1), 2.0 * PI_TRUNC * math.sqrt(m0 / m2)
+
+
+def mean_wave_period(cfg, opt):
+    """Irregular::mean_wave_period, Irregular.cpp:1420-1436 (T1 for opt 1, T2 for opt 2)."""
+    t1, t2 = _mean_periods(cfg)
+    return {1: t1, 2: t2}.get(opt, 0.0)
+
+
+def phase_speed(cfg, opt):
+    """Irregular::phase_speed, Irregular.cpp:1372-1393."""
+    if opt not in (1, 2):
+        return 0.0
+    w = 2 * PI_TRUNC / _mean_periods(cfg)[opt - 1]
+    return w / _interpolate_extrap(cfg["omega"], cfg["k"], w)
+
+
+def mean_wave_length(cfg, opt):
+    """Irregular::mean_wave_length, Irregular.cpp:1399-1417."""
+    if opt not in (1, 2):
+        return 0.0
+    w = 2 * PI_TRUNC / _mean_periods(cfg)[opt - 1]
+    return (2.0 * PI_TRUNC) / _interpolate_extrap(cfg["omega"], cfg["k"], w)
+
+
 def bandwidth_estimator(cfg):
     """Irregular::bandwidth_estimator, Irregular.cpp:1439-1452."""
     if cfg["ndir"] > 1:

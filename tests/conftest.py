@@ -6,6 +6,9 @@ import pytest
 
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = os.path.join(REPO, "tests", "golden")
+# the reference's source tree, where present (CPU tests that read it skip
+# without it; nothing that runs on a GPU reads it)
+REF_TREE = os.environ.get("CFDWM_REFERENCE_TREE", "/root/reference")
 if REPO not in sys.path:
     sys.path.insert(0, REPO)
 

@@ -91,6 +91,16 @@ def child(case_dir, spec_json, out_path):
         L.refp_irr(6, n, _p(pts["x"]), _p(pts["y"]), _p(zz), _p(pts["t"]), _p(o))
         res["irr_uvw2"] = o.reshape(n, 4)
         res["irr_uvw2_z"] = zz
+    if kind == "helpers":
+        # the irregular sea's spectral helpers (Irregular.cpp:1372-1437 through
+        # CFDwavemaker.cpp's wave_* exports) and the water depth
+        for name in ("wave_mean_period", "wave_phase_speed", "wave_mean_length"):
+            getattr(L, name).restype = C.c_double
+            getattr(L, name).argtypes = [C.c_int]
+        L.wave_water_depth.restype = C.c_double
+        res["helpers"] = np.array([L.wave_mean_period(1), L.wave_mean_period(2), L.wave_phase_speed(1),
+                                   L.wave_phase_speed(2), L.wave_mean_length(1), L.wave_mean_length(2),
+                                   L.wave_water_depth()])
     if kind == "regular" and spec.get("fenton"):
         o = np.zeros(6 + 2 * 64)
         q = L.refp_fenton(_p(o))
@@ -330,6 +340,41 @@ def main():
                                             ref_point=(0.5, 1.0, -2.0)), 40.0, 10.0, 2.0)):
         _run_case(name, txt, {"kind": "regular", "points": reg_points(L_, d, H),
                               "fenton": name.startswith("fenton")})
+
+    # (10) spectral helpers of the irregular sea (wave_mean_period,
+    #      wave_phase_speed, wave_mean_length for opt 1 and 2, wave_water_depth)
+    one = {"x": [0.0], "y": [0.0], "z": [0.0], "t": [0.0]}
+    _run_case("helpers_config1", ss.write_irregular(None, ss.config1_sea(), 50.0, extrap=2),
+              {"kind": "helpers", "points": one})
+    _run_case("helpers_t005", t005, {"kind": "helpers", "points": one})
+
+    # (11) Fenton set-ups that the Newton iteration does not solve, with the
+    #      reference's own outcome: a wave near the highest one (warning, the
+    #      unconverged iterate is served), one beyond it (warning, NaN
+    #      coefficients served) and a steep deep-water wave whose Jacobian
+    #      turns singular (FentonStream.cpp:200-201 throws; the process ends).
+    if not ONLY or "fenton_fail" in ONLY:
+        res = {}
+        for tag, (H, d, T) in (("nonconv", (19.0, 20.0, 12.0)), ("nan", (30.0, 20.0, 12.0)),
+                               ("singular", (15.0, 20.0, 3.0))):
+            txt = ss.write_regular(None, "stream", H, d, period=T, order=24)
+            with tempfile.TemporaryDirectory() as dd:
+                with open(os.path.join(dd, "waveinput.dat"), "w") as fh:
+                    fh.write(txt)
+                out = os.path.join(dd, "o.npz")
+                spec = {"kind": "regular", "points": one, "fenton": True}
+                r = subprocess.run([sys.executable, __file__, "--child", dd, json.dumps(spec), out],
+                                   capture_output=True, text=True)
+                msg = r.stdout + r.stderr
+                res[tag + "_waveinput"] = np.array(txt)
+                res[tag + "_exit_ok"] = np.array(r.returncode == 0)
+                res[tag + "_warned"] = np.array("did not fully converge" in msg)
+                res[tag + "_singular"] = np.array("singular Jacobian" in msg)
+                if r.returncode == 0:
+                    res[tag + "_solution"] = np.load(out)["fenton_solution"]
+        out = os.path.join(HERE, "fenton_failures.npz")
+        np.savez_compressed(out, **res)
+        print("wrote", out, os.path.getsize(out), "bytes")
 
 
 if __name__ == "__main__":

@@ -7,7 +7,7 @@ import re
 import numpy as np
 import pytest
 
-from conftest import REPO, golden_cfg, load_golden
+from conftest import REF_TREE, REPO, golden_cfg, load_golden
 
 import cfdwavemaker_gb300 as cw
 
@@ -103,14 +103,71 @@ def test_missing_waveinput_returns_minus_one(lib, tmp_path):
         os.chdir(cwd)
 
 
-def test_spectral_helpers_match_reference_formulas(lib):
-    """wave_mean_period and friends are host-side (Irregular.cpp:1372-1437);
-    check the parser-side spectral moments through the oracle's restatement."""
+@pytest.mark.parametrize("case", ["helpers_config1", "helpers_t005"])
+def test_spectral_helper_restatement_matches_reference(case):
+    """The oracle's restatement of wave_mean_period, wave_phase_speed and
+    wave_mean_length (Irregular.cpp:1336-1437) against the values the
+    reference returned for the same seas (tests/golden/helpers_*.npz).  The
+    library's own values are checked against the same fixtures on the GPU
+    (tests/test_gpu_failures.py), where a sea can be loaded."""
     from oracle import waveinput
-    g = load_golden("t005_focused")
+    g = load_golden(case)
     cfg = golden_cfg(g)
-    m0, m1, m2 = waveinput.spectral_moments(cfg)
-    assert m0 > 0 and m1 > 0 and m2 > 0
+    got = [waveinput.mean_wave_period(cfg, 1), waveinput.mean_wave_period(cfg, 2), waveinput.phase_speed(cfg, 1),
+           waveinput.phase_speed(cfg, 2), waveinput.mean_wave_length(cfg, 1), waveinput.mean_wave_length(cfg, 2),
+           cfg["depth"]]
+    np.testing.assert_allclose(got, g["helpers"], rtol=1e-14, atol=0)
+
+
+REF_HEADER = os.path.join(REF_TREE, "src", "CFDwavemaker.h")
+REF_EXAMPLE = os.path.join(REF_TREE, "examples", "python", "cfdwavemaker.py")
+
+
+@pytest.mark.skipif(not os.path.exists(REF_HEADER), reason="reference tree not present")
+def test_prototypes_match_reference_header(lib, tmp_path):
+    """One C++ translation unit includes the reference's CFDwavemaker.h and
+    this library's header: a reference function declared here with another
+    return or parameter type is a conflicting declaration of a C function
+    (a compile error).  The unit takes the address of every function of the
+    reference header and links against the library, so each one resolves."""
+    import subprocess
+    text = re.sub(r"//[^\n]*|/\*.*?\*/", "", open(REF_HEADER).read(), flags=re.S)
+    names = re.findall(r"\b(\w+)\s*\([^;{()]*\)\s*;", text)
+    names = sorted(set(n for n in names if n not in ("if", "defined")))
+    assert len(names) >= 29, names
+    src = tmp_path / "proto.cpp"
+    src.write_text('#include "CFDwavemaker.h"\n#include "cfdwavemaker_gb300.h"\n'
+                   "extern \"C\" void *const cfdwm_addrs[] = {\n" +
+                   "".join("    (void *)&%s,\n" % n for n in names) + "};\nint main() { return 0; }\n")
+    libdir = os.path.join(REPO, "cfdwavemaker_gb300")
+    cmd = ["g++", "-std=c++17", "-Wall", "-Werror", "-I" + os.path.dirname(REF_HEADER),
+           "-I" + os.path.join(REPO, "include"), str(src), "-L" + libdir, "-lcfdwavemaker_gb300",
+           "-Wl,-rpath," + libdir, "-o", str(tmp_path / "proto")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+
+
+@pytest.mark.skipif(not os.path.exists(REF_EXAMPLE), reason="reference tree not present")
+def test_reference_python_binding_loads_unchanged(lib, tmp_path):
+    """The reference's own ctypes wrapper (examples/python/cfdwavemaker.py,
+    unmodified, imported from the reference tree) binds every function it
+    declares against this library, and the calls that need no loaded model
+    answer as the reference's do before wave_Initialize."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("ref_cfdwavemaker_example", REF_EXAMPLE)
+    mod = importlib.util.module_from_spec(spec)
+    cwd = os.getcwd()
+    try:
+        spec.loader.exec_module(mod)
+        wm = mod.CFDwavemaker(os.path.join(REPO, "cfdwavemaker_gb300", "libcfdwavemaker_gb300.so"),
+                              workdir=str(tmp_path))
+    finally:
+        os.chdir(cwd)
+    wm.cleanup()
+    assert wm.is_initialized() is False
+    assert wm.lib.wave_Seabed.restype is not None
+    assert wm.lib.wave_VeloX(0.0, 0.0, -1.0, 0.0) == 0.0
+    assert wm.lib.wave_SurfElev(0.0, 0.0, 0.0) == 0.0
 
 
 def test_depth_basis_host(lib):

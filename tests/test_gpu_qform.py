@@ -4,9 +4,16 @@ and the uvw2 velocities at z = 0 (Irregular.cpp:975-1102).
 
 Tolerance: normwise relative error max|gpu - ref| / max|ref| per field,
 TOL = 1e-5 for the plain FP32 form and the fp16-split tensor-core form.
-The bf16-split form keeps 16 significant bits per operand (8 + 8), about
-2^-16 relative, so its bar is TOL_BF16 = 1e-4 and the measured error is
-printed.
+
+The bf16-split form keeps 8 + 8 = 16 significant bits per operand: each
+operand's split leaves a relative error up to 2^-17 and the dropped lo x lo
+product is up to 2^-16 of the product, so every one of the 2N-term dot
+products carries an error of about 2^-16 of its terms' scale.  Over random
+phases the outputs and these errors are both sums of many independent terms of
+the same coefficients, so the normwise error settles near 2^-16 = 1.5e-5 at
+any N: above the 1e-5 bar.  Its bar is therefore TOL_BF16 = 2^-15 = 3.05e-5
+(two units of the split's rounding), and the fp16 split is the form that meets
+1e-5.
 """
 import os
 
@@ -21,7 +28,7 @@ import oracle
 pytestmark = pytest.mark.gpu
 
 TOL = 1e-5
-TOL_BF16 = 1e-4
+TOL_BF16 = 2.0 ** -15
 
 
 def _sea(ncomp_freq, ndir, seed):
@@ -128,20 +135,39 @@ def test_tensor_core_several_chunks(wm, torch):
         assert err <= TOL, (f, err)
 
 
-def test_full_size_sea_fp16_split(wm, torch):
+def _rms(a, b):
+    d = np.asarray(a, np.float64) - np.asarray(b, np.float64)
+    return float(np.sqrt(np.mean(d * d)) / np.max(np.abs(b)))
+
+
+@pytest.mark.parametrize("fp16", [True, False])
+def test_full_size_sea(wm, torch, fp16):
     """The benchmark's sea at full size: 256 frequencies x 16 directions = 4096
-    components (8.4e6 pair-cache pairs), 131,072 rows in two chunks; a sample of
-    rows in both chunks against the FP64 oracle."""
+    components (8.4e6 pair-cache pairs), 131,072 rows in two chunks.
+
+    Two references: the GPU plain FP32 form on every row (it is itself pinned
+    to the oracle below), and the FP64 oracle on 256 rows spread evenly over
+    both chunks.  Per field the normwise max and RMS errors are printed; the
+    max is held to TOL (fp16 split) or TOL_BF16 (bf16 split)."""
     txt = _sea(256, 16, 2024)
     n = 131072
-    x, y, t, got = _run(wm, torch, txt, n, 1, True, seed=13)
-    rng = np.random.default_rng(4)
-    rows = np.concatenate([rng.choice(65536, 12, replace=False), 65536 + rng.choice(65536, 12, replace=False)])
+    x, y, t, plain = _run(wm, torch, txt, n, 0, fp16, seed=13)
+    _, _, _, got = _run(wm, torch, txt, n, 1, fp16, seed=13)
+    rows = np.unique(np.linspace(0, n - 1, 256).round().astype(np.int64))
+    assert (rows < 65536).sum() >= 100 and (rows >= 65536).sum() >= 100
     ref = _reference(txt, x[rows], y[rows], t[rows])
+    bar = TOL if fp16 else TOL_BF16
     for f in range(4):
-        err = norm_rel_err(got[rows, f], ref[:, f])
-        print("fp16x3 N=4096 field", f, "err", err)
-        assert err <= TOL, (f, err)
+        e_plain = norm_rel_err(plain[rows, f], ref[:, f])
+        e_fp64 = norm_rel_err(got[rows, f], ref[:, f])
+        e_all = norm_rel_err(got[:, f], plain[:, f])
+        print("%s N=4096 field %d: vs FP64 (256 rows) max %.3e rms %.3e; vs plain (all %d rows) max %.3e "
+              "rms %.3e; plain vs FP64 %.3e" % ("fp16x3" if fp16 else "bf16x3", f, e_fp64,
+                                                _rms(got[rows, f], ref[:, f]), n, e_all,
+                                                _rms(got[:, f], plain[:, f]), e_plain))
+        assert e_plain <= 1e-6, (f, e_plain)
+        assert e_fp64 <= bar, (f, e_fp64)
+        assert e_all <= bar, (f, e_all)
 
 
 def test_tensor_core_fp16_split_component_ramps(wm, torch):

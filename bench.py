@@ -389,6 +389,29 @@ def surrogate_line(args, r):
     return line
 
 
+def surrogate_summary(args, r):
+    """The learned update's numbers for the default line: rate and speed-up
+    over the plain FP32 update at the working tolerance and at 1e-3, the
+    fallbacks, and the max errors of unchecked predictions over a window."""
+    sl = surrogate_line(args, r)
+    t3 = r["tol_1e-3"]
+    plain = sl["plain_every_step"]["value"]
+    return {
+        "workload": sl["config"]["workload"],
+        "value": sl["value"], "unit": "grid nodes/s", "ms_per_step": r["ms"],
+        "speedup_vs_plain": sl["speedup_vs_plain"], "working_tol": args.surr_tol,
+        "steps": sl["surrogate_steps"],
+        "plain_every_step": sl["plain_every_step"],
+        "tensor_core_every_step": r["tc_every_step"],
+        "tol_1e-3": dict(t3, speedup_vs_plain=t3["nodes_per_s"] / plain),
+        "max_err_eta": r["accuracy"]["network"]["max_eta"], "max_err_u": r["accuracy"]["network"]["max_u"],
+        "max_err_first_order_only": {"eta": r["accuracy"]["first_order_only"]["max_eta"],
+                                     "u": r["accuracy"]["first_order_only"]["max_u"]},
+        "target": ">= 10x the plain FP32 update at max error <= 1e-3 (eta, u; normwise)",
+        "clocks": r["clocks"],
+    }
+
+
 QFORM_WORKLOAD = ("precision form: second-order eta and z=0/Taylor-layer u, v, w (pair-cache coefficients) of "
                   "a 4096-component short-crested JONSWAP sea (256 freq x 16 dir, Hs 6 m, Tp 12 s, gamma 2, "
                   "cos-2s s=10, depth 100 m) at %d random (x, y, t) points")
@@ -1061,6 +1084,8 @@ def main():
     ap.add_argument("--oracle-rows", type=int, default=256,
                     help="rows of the precision workload checked against the FP64 oracle (spread over every chunk)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-surrogate", action="store_true",
+                    help="precision workload: leave out the learned-update summary")
     ap.add_argument("--grid", type=int, default=256,
                     help="columns per side of the s-grid (256 is the named workload; smaller sizes "
                          "are for profiling captures only)")
@@ -1104,7 +1129,15 @@ def main():
         r = run_qform(args)
         if r["rank"] != 0:
             return
-        print(json.dumps(qform_line(args, r)))
+        line = qform_line(args, r)
+        if r["ws"] == 1 and not args.no_surrogate:
+            # the other half of the metric: the learned s-grid update against
+            # the plain FP32 update, at the target tolerance 1e-3 (a shorter
+            # loop than --workload surrogate; single GPU only)
+            sa = argparse.Namespace(**vars(args))
+            sa.surr_steps, sa.plain_steps = 200, 10
+            line["surrogate"] = surrogate_summary(sa, run_surrogate(sa))
+        print(json.dumps(line))
         return
     if args.workload == "regular":
         r = run_regular(args)

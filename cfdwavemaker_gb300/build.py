@@ -22,13 +22,14 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden",
          "-I" + os.path.join(os.path.dirname(HERE), "include")]
 SOURCES = ["parser.cpp", "irregular.cu", "sgrid.cu", "regular.cu", "api.cu", "noalloc.cu", "qform.cu",
-           "surrogate.cu", "depthform.cu", "vtu.cpp", "smit.cu", "spectrum.cu", "shard.cpp"]
+           "surrogate.cu", "depthform.cu", "vtu.cpp", "smit.cu", "spectrum.cu", "shard.cpp", "convtc.cu"]
 
 
 def _compile(src):
     obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
     path = os.path.join(CSRC, src)
     deps = [path, os.path.join(CSRC, "cfdwm.h"), os.path.join(CSRC, "sgrid_geom.cuh"), os.path.join(CSRC, "ffmath.cuh"),
+            os.path.join(CSRC, "tc05.cuh"),
             os.path.join(os.path.dirname(HERE), "include", "cfdwavemaker_gb300.h")]
     if os.path.exists(obj) and all(os.path.getmtime(obj) >= os.path.getmtime(d) for d in deps):
         return obj, ""

@@ -998,6 +998,7 @@ int cfdwm_surrogate_forward(const float *x, int B, int H, int W, float *y) {
     cudaStream_t s = stream_of();
     int rc = surrogate_forward(x, B, H, W, y, s);
     if (!rc) CKR(cudaStreamSynchronize(s));
+    if (!rc) rc = surrogate_check(s);
     return rc;
 }
 

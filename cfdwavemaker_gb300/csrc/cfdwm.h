@@ -297,6 +297,9 @@ int surrogate_features(const Config &cfg, const DevSea &sea, DevGrid &g, Workspa
 int surrogate_targets(const Config &cfg, DevGrid &g, int slot, const float *base, const float *eta1, float *tg,
                       void *stream);
 int surrogate_forward(const float *x, int B, int H, int W, float *y, void *stream);
+// E_CUDA when a bounded wait of the network's tensor-core kernels expired
+// since the last check (the stream is synchronised)
+int surrogate_check(void *stream);
 int surrogate_loss_grad(const float *x, const float *tg, int B, int H, int W, double *loss, float *grad,
                         void *stream);
 int surrogate_train_step(const float *xs, const float *ts, long nsamples, const int *idx_host, int B, int H, int W,

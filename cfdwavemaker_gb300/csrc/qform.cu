@@ -36,6 +36,7 @@
 //  * k_qform_plain: the same sums on FP32 CUDA cores (the plain form).
 #include "cfdwm.h"
 #include "ffmath.cuh"
+#include "tc05.cuh"
 
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -415,7 +416,7 @@ __global__ void __launch_bounds__(128, 2) k_qform_plain(QPlain a) {
     const long ntiles = (long)nt * (nt + 1) / 2;
     const float4 *tab4 = reinterpret_cast<const float4 *>(a.tab);
     float S0[4] = {0, 0, 0, 0}, C0[4] = {0, 0, 0, 0}, S1[4] = {0, 0, 0, 0}, C1[4] = {0, 0, 0, 0};
-    float2 pmc[QT], pms[QT];     // (row p, row p + 128) of c and s for the 32 components of tile M
+    float2 pm0[QT], pm1[QT];     // (c, s) of the 32 components of tile M, rows p and p + 128
 
     // stage k of the walk: tile (I, M) with M outer
     int lI = 0, lM = 0;          // next tile to load
@@ -437,47 +438,50 @@ __global__ void __launch_bounds__(128, 2) k_qform_plain(QPlain a) {
 #pragma unroll
             for (int mm = 0; mm < QT; mm++) {
                 const long r = (long)(M * QT + mm) * a.rows;
-                const float2 x0 = a.ph[r + q0], x1 = a.ph[r + q1];
-                pmc[mm] = make_float2(x0.x, x1.x);
-                pms[mm] = make_float2(x0.y, x1.y);
+                pm0[mm] = a.ph[r + q0];
+                pm1[mm] = a.ph[r + q1];
             }
         }
         qpl_wait1();
         __syncthreads();
         const float4 *st = q_smem + (k & 1) * QPL_TILE4;
-        long ri = (long)(I * QT) * a.rows;
-        float2 pi0 = a.ph[ri + q0], pi1 = a.ph[ri + q1];
-        float r0 = a.rr[ri + q0], r1 = a.rr[ri + q1];
+        // row phasors of component i, prefetched two components ahead (the
+        // ones past the tile re-read its last component)
+        const long rbase = (long)(I * QT) * a.rows;
+        float2 pa0 = a.ph[rbase + q0], pa1 = a.ph[rbase + q1];
+        float ra0 = a.rr[rbase + q0], ra1 = a.rr[rbase + q1];
+        float2 pb0 = a.ph[rbase + a.rows + q0], pb1 = a.ph[rbase + a.rows + q1];
+        float rb0 = a.rr[rbase + a.rows + q0], rb1 = a.rr[rbase + a.rows + q1];
         for (int ii = 0; ii < QT; ii++) {
-            // prefetch the next row phasor (the last one re-reads a valid index)
-            const long rn = ri + (ii + 1 < QT ? a.rows : 0);
+            const long rn = rbase + (long)(ii + 2 < QT ? ii + 2 : QT - 1) * a.rows;
             const float2 n0 = a.ph[rn + q0], n1 = a.ph[rn + q1];
             const float nr0 = a.rr[rn + q0], nr1 = a.rr[rn + q1];
-            float2 ec = {0, 0}, es = {0, 0}, uc = {0, 0}, us = {0, 0}, vc = {0, 0}, vs = {0, 0}, wc = {0, 0},
-                   ws = {0, 0};
+            // (A_cos, A_sin) of each field times (c_m, s_m): the record's
+            // float pairs and the phasor are the two lanes of each FFMA2
+            float2 e0 = {0, 0}, u0 = {0, 0}, v0 = {0, 0}, w0 = {0, 0};
+            float2 e1 = {0, 0}, u1 = {0, 0}, v1 = {0, 0}, w1 = {0, 0};
             const float4 *rec = st + ii * QT * 2;
 #pragma unroll
             for (int mm = 0; mm < QT; mm++) {
                 const float4 c0 = rec[2 * mm], c1 = rec[2 * mm + 1];
-                ec = __ffma2_rn(make_float2(c0.x, c0.x), pmc[mm], ec);
-                es = __ffma2_rn(make_float2(c0.y, c0.y), pms[mm], es);
-                uc = __ffma2_rn(make_float2(c0.z, c0.z), pmc[mm], uc);
-                us = __ffma2_rn(make_float2(c0.w, c0.w), pms[mm], us);
-                vc = __ffma2_rn(make_float2(c1.x, c1.x), pmc[mm], vc);
-                vs = __ffma2_rn(make_float2(c1.y, c1.y), pms[mm], vs);
-                wc = __ffma2_rn(make_float2(c1.z, c1.z), pmc[mm], wc);
-                ws = __ffma2_rn(make_float2(c1.w, c1.w), pms[mm], ws);
+                const float2 ce = make_float2(c0.x, c0.y), cu = make_float2(c0.z, c0.w);
+                const float2 cv = make_float2(c1.x, c1.y), cw = make_float2(c1.z, c1.w);
+                e0 = __ffma2_rn(ce, pm0[mm], e0); e1 = __ffma2_rn(ce, pm1[mm], e1);
+                u0 = __ffma2_rn(cu, pm0[mm], u0); u1 = __ffma2_rn(cu, pm1[mm], u1);
+                v0 = __ffma2_rn(cv, pm0[mm], v0); v1 = __ffma2_rn(cv, pm1[mm], v1);
+                w0 = __ffma2_rn(cw, pm0[mm], w0); w1 = __ffma2_rn(cw, pm1[mm], w1);
             }
-            qpl_kahan(S0[0], C0[0], r0 * fmaf(pi0.x, ec.x, pi0.y * es.x));
-            qpl_kahan(S0[1], C0[1], r0 * fmaf(pi0.x, uc.x, pi0.y * us.x));
-            qpl_kahan(S0[2], C0[2], r0 * fmaf(pi0.x, vc.x, pi0.y * vs.x));
-            qpl_kahan(S0[3], C0[3], r0 * fmaf(pi0.y, wc.x, pi0.x * ws.x));
-            qpl_kahan(S1[0], C1[0], r1 * fmaf(pi1.x, ec.y, pi1.y * es.y));
-            qpl_kahan(S1[1], C1[1], r1 * fmaf(pi1.x, uc.y, pi1.y * us.y));
-            qpl_kahan(S1[2], C1[2], r1 * fmaf(pi1.x, vc.y, pi1.y * vs.y));
-            qpl_kahan(S1[3], C1[3], r1 * fmaf(pi1.y, wc.y, pi1.x * ws.y));
-            ri = rn;
-            pi0 = n0; pi1 = n1; r0 = nr0; r1 = nr1;
+            // eta, u, v: c_i (A_c . c) + s_i (A_s . s); w: s_i (C . c) + c_i (D . s)
+            qpl_kahan(S0[0], C0[0], ra0 * fmaf(pa0.x, e0.x, pa0.y * e0.y));
+            qpl_kahan(S0[1], C0[1], ra0 * fmaf(pa0.x, u0.x, pa0.y * u0.y));
+            qpl_kahan(S0[2], C0[2], ra0 * fmaf(pa0.x, v0.x, pa0.y * v0.y));
+            qpl_kahan(S0[3], C0[3], ra0 * fmaf(pa0.y, w0.x, pa0.x * w0.y));
+            qpl_kahan(S1[0], C1[0], ra1 * fmaf(pa1.x, e1.x, pa1.y * e1.y));
+            qpl_kahan(S1[1], C1[1], ra1 * fmaf(pa1.x, u1.x, pa1.y * u1.y));
+            qpl_kahan(S1[2], C1[2], ra1 * fmaf(pa1.x, v1.x, pa1.y * v1.y));
+            qpl_kahan(S1[3], C1[3], ra1 * fmaf(pa1.y, w1.x, pa1.x * w1.y));
+            pa0 = pb0; pa1 = pb1; ra0 = rb0; ra1 = rb1;
+            pb0 = n0; pb1 = n1; rb0 = nr0; rb1 = nr1;
         }
         __syncthreads();     // the stage is refilled by the next issue
         if (++I > M) { I = 0; M++; }
@@ -511,52 +515,10 @@ template <int BN, bool TWO, bool PAIR> struct TcCfg {
     static constexpr int ACOLS = TWO ? 2 * BN : BN;     // TMEM columns of one tile
     static constexpr int NBUF = 512 / ACOLS;             // accumulator buffers
 };
-constexpr long long WAIT_LIMIT = 1000000000LL;   // clock cycles (about 0.5 s)
 
-__device__ __forceinline__ uint32_t su32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t *b, uint32_t n) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(b)), "r"(n));
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *b, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(b)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try(uint64_t *b, uint32_t parity) {
-    uint32_t ok;
-    asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
-                 : "=r"(ok) : "r"(su32(b)), "r"(parity) : "memory");
-    return ok != 0;
-}
-// bounded wait: false (and the error word set) after WAIT_LIMIT cycles
-__device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity, int *err, int code) {
-    long long t0 = clock64();
-    while (!mbar_try(b, parity)) {
-        if (clock64() - t0 > WAIT_LIMIT) {
-            atomicExch(err, code);
-            return false;
-        }
-    }
-    return true;
-}
 __device__ __forceinline__ void tma_2d(void *dst, const CUtensorMap *m, uint64_t *bar, int x, int y) {
     asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];"
                  ::"r"(su32(dst)), "l"(m), "r"(su32(bar)), "r"(x), "r"(y) : "memory");
-}
-// K-major operand in the 128-byte swizzle layout: 8-row groups 1024 B apart
-__device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
-    uint64_t d = (uint64_t)((saddr & 0x3FFFF) >> 4);
-    d |= (uint64_t)1 << 16;
-    d |= (uint64_t)(1024 >> 4) << 32;
-    d |= (uint64_t)1 << 46;
-    d |= (uint64_t)2 << 61;
-    return d;
-}
-__device__ __forceinline__ void umma(uint32_t dt, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
-    asm volatile("{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}"
-                 ::"r"(dt), "l"(a), "l"(b), "r"(idesc), "r"(acc));
-}
-__device__ __forceinline__ void umma_commit(uint64_t *bar) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(bar)) : "memory");
 }
 // CTA-pair forms (cta_group::2).  The load lands in this CTA's shared memory
 // and signals the mbarrier at cluster address `bar`, which may be the peer's.
@@ -613,27 +575,6 @@ __device__ __forceinline__ uint32_t ncluster_x() {
 __device__ __forceinline__ void cluster_sync_all() {
     asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-        : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7]),
-          "=f"(v[8]), "=f"(v[9]), "=f"(v[10]), "=f"(v[11]), "=f"(v[12]), "=f"(v[13]), "=f"(v[14]), "=f"(v[15]),
-          "=f"(v[16]), "=f"(v[17]), "=f"(v[18]), "=f"(v[19]), "=f"(v[20]), "=f"(v[21]), "=f"(v[22]), "=f"(v[23]),
-          "=f"(v[24]), "=f"(v[25]), "=f"(v[26]), "=f"(v[27]), "=f"(v[28]), "=f"(v[29]), "=f"(v[30]), "=f"(v[31])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-}
-
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-        : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7]),
-          "=f"(v[8]), "=f"(v[9]), "=f"(v[10]), "=f"(v[11]), "=f"(v[12]), "=f"(v[13]), "=f"(v[14]), "=f"(v[15])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-}
-
 struct QTC {
     long rows;               // rows of this chunk
     int npad;                // components (multiple of 256)

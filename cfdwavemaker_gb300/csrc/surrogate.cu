@@ -27,12 +27,11 @@
 // be checked against the plain method on a sample of columns; when the
 // sampled error exceeds the tolerance the plain method fills the slot.
 //
-// GB300 notes: the convolution FLOPs are small (about 10 GFLOP per 256 x 256
-// step) next to the plain pair sum (about 4e13 operations), so the
-// convolutions are direct FP32 CUDA-core kernels with shared-memory tiles:
-// input tile + halo and a 16-output-channel weight slice per block, weight
-// reads as warp broadcasts.  The features form their phases in float-float
-// arithmetic in the kernel (no FP64 phasor table of the halo grid).
+// GB300 notes: the convolutions (forward, data and weight gradients) run as
+// implicit GEMMs on the tcgen05 tensor cores (convtc.cu), with the FP32
+// activations split into BF16 hi + lo parts and FP32 accumulation in TMEM.
+// The features form their phases in float-float arithmetic in the kernel (no
+// FP64 phasor table of the halo grid).
 #include "cfdwm.h"
 #include "ffmath.cuh"
 #include "sgrid_geom.cuh"
@@ -60,6 +59,16 @@ namespace cfdwm {
 
 GridGeom grid_geom(const DevGrid &g);
 
+// convtc.cu: valid 3x3 convolutions on the tcgen05 tensor cores
+int conv_tc_forward(const float *x, long xbs, const int *idx, const __nv_bfloat16 *w, const float *bias, int B,
+                    int C, int O, int H, int W, float *y, float *pre, int act, void *stream);
+int conv_tc_data_grad(const float *dy, const __nv_bfloat16 *w, const float *pre, int B, int C, int O, int H, int W,
+                      float *dx, void *stream);
+long conv_tc_wgt_slabs(int B, int H, int W, int *kslab, int *per_img);
+int conv_tc_weight_grad(const float *x, long xbs, const int *idx, const float *dy, int B, int C, int O, int H, int W,
+                        float *part, void *stream);
+int conv_tc_error(void *stream);
+
 namespace {
 
 constexpr int SH = 4;        // halo columns per side: 4 valid 3x3 convolutions
@@ -67,10 +76,6 @@ constexpr int NQ = 8;        // first-order channels per level
 constexpr int HID = 32;      // hidden channels
 constexpr float LOG2E = 1.4426950408889634f;
 
-// conv tiling
-constexpr int TY = 8, TX = 32;     // output pixels per block (rows x cols)
-constexpr int OT = 16;             // output channels per block
-constexpr int CKC = 8;             // input channels per shared-memory chunk
 
 __device__ __forceinline__ float ex2f(float x) {
     float y;
@@ -237,211 +242,6 @@ __global__ void k_halo_coords(GridGeom g, int nxh, int nyh, double *xy) {
     int ih = (int)(p / nyh), jh = (int)(p % nyh);
     xy[p] = g.d0 + g.dx * (ih - SH);
     xy[n + p] = g.d2 + g.dy * (jh - SH);
-}
-
-// ---------------------------------------------------------------------------
-// Convolutions (valid 3x3, [B][C][H][W] planes)
-// ---------------------------------------------------------------------------
-struct ConvArgs {
-    const float *x;
-    long xbs;                    // batch stride of x (elements)
-    const int *idx;              // sample index of batch entry b (null: b)
-    const __nv_bfloat16 *w;      // [O][C][9]
-    const float *bias;           // [O]
-    int B, C, O, H, W;           // input dims; output (H-2) x (W-2)
-    float *y;                    // [B][O][H-2][W-2]
-    float *pre;                  // pre-activation copy (null: none)
-    int act;                     // 1: SiLU
-};
-
-__global__ void __launch_bounds__(256) k_conv_fwd(ConvArgs a) {
-    __shared__ float s_x[CKC][TY + 2][TX + 2];
-    __shared__ __align__(16) float s_w[CKC * 9][OT];
-    const int Ho = a.H - 2, Wo = a.W - 2;
-    const int tilesX = (Wo + TX - 1) / TX;
-    const int x0 = (blockIdx.x % tilesX) * TX, y0 = (blockIdx.x / tilesX) * TY;
-    const int o0 = blockIdx.y * OT, b = blockIdx.z;
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    const float *X = a.x + (long)(a.idx ? a.idx[b] : b) * a.xbs;
-    const long plane = (long)a.H * a.W;
-    float acc[OT];
-#pragma unroll
-    for (int o = 0; o < OT; o++) acc[o] = (o0 + o < a.O) ? a.bias[o0 + o] : 0.f;
-    for (int c0 = 0; c0 < a.C; c0 += CKC) {
-        __syncthreads();
-        for (int e = threadIdx.x; e < CKC * (TY + 2) * (TX + 2); e += 256) {
-            int c = e / ((TY + 2) * (TX + 2)), r = (e / (TX + 2)) % (TY + 2), q = e % (TX + 2);
-            int gy = y0 + r, gx = x0 + q;
-            s_x[c][r][q] = (c0 + c < a.C && gy < a.H && gx < a.W) ? X[(long)(c0 + c) * plane + (long)gy * a.W + gx]
-                                                                 : 0.f;
-        }
-        for (int e = threadIdx.x; e < CKC * 9 * OT; e += 256) {
-            int o = e % OT, ck = e / OT, c = ck / 9, k = ck % 9;
-            s_w[ck][o] = (o0 + o < a.O && c0 + c < a.C)
-                             ? __bfloat162float(a.w[((long)(o0 + o) * a.C + c0 + c) * 9 + k])
-                             : 0.f;
-        }
-        __syncthreads();
-#pragma unroll 2
-        for (int c = 0; c < CKC; c++) {
-#pragma unroll
-            for (int ky = 0; ky < 3; ky++)
-#pragma unroll
-                for (int kx = 0; kx < 3; kx++) {
-                    const float xv = s_x[c][ty + ky][tx + kx];
-                    const float4 *wr = reinterpret_cast<const float4 *>(&s_w[c * 9 + ky * 3 + kx][0]);
-#pragma unroll
-                    for (int o4 = 0; o4 < OT / 4; o4++) {
-                        const float4 w4 = wr[o4];
-                        acc[4 * o4 + 0] = fmaf(w4.x, xv, acc[4 * o4 + 0]);
-                        acc[4 * o4 + 1] = fmaf(w4.y, xv, acc[4 * o4 + 1]);
-                        acc[4 * o4 + 2] = fmaf(w4.z, xv, acc[4 * o4 + 2]);
-                        acc[4 * o4 + 3] = fmaf(w4.w, xv, acc[4 * o4 + 3]);
-                    }
-                }
-        }
-    }
-    const int oy = y0 + ty, ox = x0 + tx;
-    if (oy >= Ho || ox >= Wo) return;
-    const long oplane = (long)Ho * Wo;
-#pragma unroll
-    for (int o = 0; o < OT; o++) {
-        if (o0 + o >= a.O) break;
-        long off = ((long)b * a.O + o0 + o) * oplane + (long)oy * Wo + ox;
-        float v = acc[o];
-        if (a.pre) a.pre[off] = v;
-        a.y[off] = a.act ? silu(v) : v;
-    }
-}
-
-// dx[b][c][y][x] = sum_o sum_k w[o][c][k] dy[b][o][y-ky][x-kx], times
-// silu'(pre[b][c][y][x]) when pre is given (the input was a SiLU output).
-struct ConvBwdArgs {
-    const float *dy;             // [B][O][H-2][W-2]
-    const __nv_bfloat16 *w;      // [O][C][9]
-    const float *pre;            // [B][C][H][W] or null
-    int B, C, O, H, W;
-    float *dx;                   // [B][C][H][W]
-};
-
-__global__ void __launch_bounds__(256) k_conv_bwd_data(ConvBwdArgs a) {
-    __shared__ float s_d[CKC][TY + 2][TX + 2];
-    __shared__ __align__(16) float s_w[CKC * 9][OT];
-    const int Ho = a.H - 2, Wo = a.W - 2;
-    const int tilesX = (a.W + TX - 1) / TX;
-    const int x0 = (blockIdx.x % tilesX) * TX, y0 = (blockIdx.x / tilesX) * TY;
-    const int c0 = blockIdx.y * OT, b = blockIdx.z;
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    const long oplane = (long)Ho * Wo;
-    float acc[OT];
-#pragma unroll
-    for (int c = 0; c < OT; c++) acc[c] = 0.f;
-    for (int q0 = 0; q0 < a.O; q0 += CKC) {
-        __syncthreads();
-        for (int e = threadIdx.x; e < CKC * (TY + 2) * (TX + 2); e += 256) {
-            int o = e / ((TY + 2) * (TX + 2)), r = (e / (TX + 2)) % (TY + 2), q = e % (TX + 2);
-            int gy = y0 - 2 + r, gx = x0 - 2 + q;
-            s_d[o][r][q] = (q0 + o < a.O && gy >= 0 && gy < Ho && gx >= 0 && gx < Wo)
-                               ? a.dy[((long)b * a.O + q0 + o) * oplane + (long)gy * Wo + gx]
-                               : 0.f;
-        }
-        for (int e = threadIdx.x; e < CKC * 9 * OT; e += 256) {
-            int c = e % OT, ok = e / OT, o = ok / 9, k = ok % 9;
-            s_w[ok][c] = (c0 + c < a.C && q0 + o < a.O)
-                             ? __bfloat162float(a.w[((long)(q0 + o) * a.C + c0 + c) * 9 + k])
-                             : 0.f;
-        }
-        __syncthreads();
-#pragma unroll 2
-        for (int o = 0; o < CKC; o++) {
-#pragma unroll
-            for (int ky = 0; ky < 3; ky++)
-#pragma unroll
-                for (int kx = 0; kx < 3; kx++) {
-                    const float dv = s_d[o][ty + 2 - ky][tx + 2 - kx];
-                    const float4 *wr = reinterpret_cast<const float4 *>(&s_w[o * 9 + ky * 3 + kx][0]);
-#pragma unroll
-                    for (int c4 = 0; c4 < OT / 4; c4++) {
-                        const float4 w4 = wr[c4];
-                        acc[4 * c4 + 0] = fmaf(w4.x, dv, acc[4 * c4 + 0]);
-                        acc[4 * c4 + 1] = fmaf(w4.y, dv, acc[4 * c4 + 1]);
-                        acc[4 * c4 + 2] = fmaf(w4.z, dv, acc[4 * c4 + 2]);
-                        acc[4 * c4 + 3] = fmaf(w4.w, dv, acc[4 * c4 + 3]);
-                    }
-                }
-        }
-    }
-    const int iy = y0 + ty, ix = x0 + tx;
-    if (iy >= a.H || ix >= a.W) return;
-    const long plane = (long)a.H * a.W;
-#pragma unroll
-    for (int c = 0; c < OT; c++) {
-        if (c0 + c >= a.C) break;
-        long off = ((long)b * a.C + c0 + c) * plane + (long)iy * a.W + ix;
-        float v = acc[c];
-        if (a.pre) v *= silu_d(a.pre[off]);
-        a.dx[off] = v;
-    }
-}
-
-// Partial weight and bias gradients of one slab (batch entry x output tile):
-//   dW[o][c][k] = sum_pixels dy[b][o][y][x] x[b][c][y+ky][x+kx],  db[o] = sum dy.
-struct ConvWgtArgs {
-    const float *x;
-    long xbs;
-    const int *idx;
-    const float *dy;             // [B][O][H-2][W-2]
-    int B, C, O, H, W;
-    float *part;                 // [nslab][O*C*9 + O]
-};
-
-__global__ void __launch_bounds__(128) k_conv_bwd_wgt(ConvWgtArgs a) {
-    __shared__ float s_d[OT][TY * TX + 1];
-    __shared__ float s_x[CKC][TY + 2][TX + 2];
-    const int Ho = a.H - 2, Wo = a.W - 2;
-    const int tilesX = (Wo + TX - 1) / TX, tilesY = (Ho + TY - 1) / TY;
-    const int slab = blockIdx.x;
-    const int b = slab / (tilesX * tilesY), tile = slab % (tilesX * tilesY);
-    const int x0 = (tile % tilesX) * TX, y0 = (tile / tilesX) * TY;
-    const int o0 = blockIdx.y * OT, c0 = blockIdx.z * CKC;
-    const int ol = threadIdx.x / CKC, cl = threadIdx.x % CKC;
-    const float *X = a.x + (long)(a.idx ? a.idx[b] : b) * a.xbs;
-    const long plane = (long)a.H * a.W, oplane = (long)Ho * Wo;
-    for (int e = threadIdx.x; e < OT * TY * TX; e += 128) {
-        int o = e / (TY * TX), pp = e % (TY * TX), py = pp / TX, px = pp % TX;
-        int gy = y0 + py, gx = x0 + px;
-        s_d[o][pp] = (o0 + o < a.O && gy < Ho && gx < Wo)
-                         ? a.dy[((long)b * a.O + o0 + o) * oplane + (long)gy * Wo + gx]
-                         : 0.f;
-    }
-    for (int e = threadIdx.x; e < CKC * (TY + 2) * (TX + 2); e += 128) {
-        int c = e / ((TY + 2) * (TX + 2)), r = (e / (TX + 2)) % (TY + 2), q = e % (TX + 2);
-        int gy = y0 + r, gx = x0 + q;
-        s_x[c][r][q] = (c0 + c < a.C && gy < a.H && gx < a.W) ? X[(long)(c0 + c) * plane + (long)gy * a.W + gx]
-                                                             : 0.f;
-    }
-    __syncthreads();
-    float acc[9], accb = 0.f;
-#pragma unroll
-    for (int k = 0; k < 9; k++) acc[k] = 0.f;
-    for (int py = 0; py < TY; py++) {
-        for (int px = 0; px < TX; px++) {
-            const float d = s_d[ol][py * TX + px];
-            accb += d;
-#pragma unroll
-            for (int ky = 0; ky < 3; ky++)
-#pragma unroll
-                for (int kx = 0; kx < 3; kx++) acc[ky * 3 + kx] = fmaf(d, s_x[cl][py + ky][px + kx], acc[ky * 3 + kx]);
-        }
-    }
-    const int o = o0 + ol, c = c0 + cl;
-    if (o >= a.O) return;
-    const long per = (long)a.O * a.C * 9 + a.O;
-    float *P = a.part + (long)slab * per;
-    if (c < a.C)
-#pragma unroll
-        for (int k = 0; k < 9; k++) P[((long)o * a.C + c) * 9 + k] = acc[k];
-    if (blockIdx.z == 0 && cl == 0) P[(long)a.O * a.C * 9 + o] = accb;
 }
 
 // grad[e] = sum over slabs of part[slab][e], in slab order
@@ -741,54 +541,41 @@ int surrogate_set_params(const float *src, long n, void *stream_) {
 }
 
 // ---- layer launchers ------------------------------------------------------
+// The convolutions run as implicit GEMMs on the tcgen05 tensor cores
+// (convtc.cu); the error word of their bounded waits is read where a call
+// synchronises anyway.
 static int conv_fwd(const Surrogate &s, int l, const float *x, long xbs, const int *idx, int B, int H, int W,
                     float *y, float *pre, int act, cudaStream_t st) {
-    ConvArgs a;
-    a.x = x; a.xbs = xbs; a.idx = idx; a.w = s.wbf + s.off_w[l]; a.bias = s.w32 + s.off_b[l];
-    a.B = B; a.C = s.ch[l]; a.O = s.ch[l + 1]; a.H = H; a.W = W; a.y = y; a.pre = pre; a.act = act;
-    int Ho = H - 2, Wo = W - 2;
-    dim3 grid((unsigned)(((Wo + TX - 1) / TX) * ((Ho + TY - 1) / TY)), (unsigned)((a.O + OT - 1) / OT),
-              (unsigned)B);
-    k_conv_fwd<<<grid, 256, 0, st>>>(a);
-    note_launch();
-    CK(cudaGetLastError());
-    return OK;
+    return conv_tc_forward(x, xbs, idx, s.wbf + s.off_w[l], s.w32 + s.off_b[l], B, s.ch[l], s.ch[l + 1], H, W, y,
+                           pre, act, st);
 }
 
 static int conv_bwd_data(const Surrogate &s, int l, const float *dy, const float *pre, int B, int H, int W,
                          float *dx, cudaStream_t st) {
-    ConvBwdArgs a;
-    a.dy = dy; a.w = s.wbf + s.off_w[l]; a.pre = pre;
-    a.B = B; a.C = s.ch[l]; a.O = s.ch[l + 1]; a.H = H; a.W = W; a.dx = dx;
-    dim3 grid((unsigned)(((W + TX - 1) / TX) * ((H + TY - 1) / TY)), (unsigned)((a.C + OT - 1) / OT),
-              (unsigned)B);
-    k_conv_bwd_data<<<grid, 256, 0, st>>>(a);
-    note_launch();
-    CK(cudaGetLastError());
-    return OK;
+    return conv_tc_data_grad(dy, s.wbf + s.off_w[l], pre, B, s.ch[l], s.ch[l + 1], H, W, dx, st);
 }
 
-static long wgt_slabs(int B, int H, int W) {
-    int Ho = H - 2, Wo = W - 2;
-    return (long)B * ((Wo + TX - 1) / TX) * ((Ho + TY - 1) / TY);
-}
+static long wgt_slabs(int B, int H, int W) { return conv_tc_wgt_slabs(B, H, W, nullptr, nullptr); }
 
 static int conv_bwd_wgt(Surrogate &s, int l, const float *x, long xbs, const int *idx, const float *dy, int B,
                         int H, int W, float *part, cudaStream_t st) {
-    ConvWgtArgs a;
-    a.x = x; a.xbs = xbs; a.idx = idx; a.dy = dy;
-    a.B = B; a.C = s.ch[l]; a.O = s.ch[l + 1]; a.H = H; a.W = W; a.part = part;
-    long nslab = wgt_slabs(B, H, W);
-    dim3 grid((unsigned)nslab, (unsigned)((a.O + OT - 1) / OT), (unsigned)((a.C + CKC - 1) / CKC));
-    k_conv_bwd_wgt<<<grid, 128, 0, st>>>(a);
-    note_launch();
-    CK(cudaGetLastError());
-    long nw = (long)a.O * a.C * 9, per = nw + a.O;
+    const int C = s.ch[l], O = s.ch[l + 1];
+    int rc = conv_tc_weight_grad(x, xbs, idx, dy, B, C, O, H, W, part, st);
+    if (rc) return rc;
+    const long nslab = wgt_slabs(B, H, W);
+    long nw = (long)O * C * 9, per = nw + O;
     k_sum_slabs<<<(unsigned)((per + 255) / 256), 256, 0, st>>>(per, (int)nslab, part, s.grad + s.off_w[l],
                                                                 s.grad + s.off_b[l], nw);
     note_launch();
     CK(cudaGetLastError());
     return OK;
+}
+
+static int conv_check(cudaStream_t st) {
+    int e = conv_tc_error(st);
+    if (e == 0) return OK;
+    std::fprintf(stderr, "cfdwm: a bounded wait of the tensor-core convolutions expired (code %d)\n", e);
+    return E_CUDA;
 }
 
 static int reserve_tr(Surrogate &s, size_t bytes) {
@@ -859,6 +646,7 @@ static int loss_grad(Surrogate &s, const float *x, const float *tg, const int *i
         double L = 0.0;
         for (float v : lp) L += v;
         *loss = L;
+        return conv_check(st);
     }
     return OK;
 }
@@ -907,6 +695,8 @@ int surrogate_train_step(const float *xs, const float *ts, long nsamples, const 
     CK(cudaGetLastError());
     return OK;
 }
+
+int surrogate_check(void *stream) { return conv_check((cudaStream_t)stream); }
 
 int surrogate_forward(const float *x, int B, int H, int W, float *y, void *stream_) {
     cudaStream_t st = (cudaStream_t)stream_;
@@ -1109,6 +899,8 @@ static int compare(Surrogate &s, DevGrid &g, int slot, const int *col, long n, f
     unsigned h[4];
     CK(cudaMemcpyAsync(h, s.d_err, sizeof(h), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    int rc = conv_check(st);
+    if (rc) return rc;
     for (int q = 0; q < 4; q++) {
         float v;
         std::memcpy(&v, &h[q], 4);

@@ -14,6 +14,7 @@ the 256 x 256 / 1 km grid (the network is convolutional, so patches train the
 operator that then runs on the full grid).
 
     python -m cfdwavemaker_gb300.surrogate train --seas 400 --steps 6000 --out W.bin
+    python -m cfdwavemaker_gb300.surrogate analyse     (how local the predicted part is)
 """
 from __future__ import annotations
 
@@ -162,9 +163,123 @@ class Trainer:
         self._ok(self.lib.cfdwm_surrogate_save(path.encode()))
 
 
+def _cubic_mid(a, axis):
+    """Values half-way between the samples of a along an axis: the 4-point
+    cubic (-1, 9, 9, -1) / 16, edge samples repeated."""
+    n = a.shape[axis]
+    idx = np.arange(n)
+    t = lambda d: np.take(a, np.clip(idx + d, 0, n - 1), axis=axis)
+    return (-t(-1) + 9 * t(0) + 9 * t(1) - t(2)) / 16.0
+
+
+def analyse(nx=256, ny=256, nl=16, dt=0.1, steps=20, margin=6):
+    """How local the second-order part of a ring slot is, on the 1024-component
+    sea of the s-grid workload (plain-method slots, the network's normalised
+    targets).  Returns, per field group (eta; u, v, w over the levels):
+
+    * share: max of the second-order part / max of the whole field (the
+      learned update's error bar is relative to the whole field);
+    * spectrum: fraction of the part's energy at wavelengths under 10, 8 and
+      6 columns;
+    * interp: max error, relative to the part's max, of recovering the
+      columns between exact samples: every other column in both directions
+      (a quarter exact), every other row (half), a checkerboard (half);
+    * time: the same for the slot half-way through a window of `steps`
+      ring steps from the two ends (linear in time).
+    """
+    import torch
+    import cfdwavemaker_gb300 as cw
+    from . import seastate as ss
+    lib = cw.load()
+    wm = cw.CFDwavemaker()
+    comps = ss.config3_sea()
+    grid = {"bounds": (0.0, 1000.0, 0.0, 1000.0), "nx": nx, "ny": ny, "nl": nl, "t0": 0.0, "dt": dt,
+            "stretch": (0.7, 1.5)}
+    cwd = os.getcwd()
+    os.chdir(tempfile.mkdtemp())
+    try:
+        if wm.initialize_text(ss.write_irregular(None, comps, 100.0, extrap=2, lsgrid=grid)) != 0:
+            raise RuntimeError(cw.last_error())
+        if lib.cfdwm_surrogate_create(nl, 1) != 0:
+            raise RuntimeError(cw.last_error())
+        feat = torch.empty((8 * nl, nx + 2 * SH, ny + 2 * SH), device="cuda")
+        base = torch.empty(3 * nx * ny * nl, device="cuda")
+        eta1 = torch.empty(nx * ny, device="cuda")
+        tgt = torch.empty((1 + 3 * nl, nx, ny), device="cuda")
+        p = cw._ptr
+
+        def newest():
+            t0 = C.c_double(0.0)
+            ts = C.c_int(0)
+            lib.cfdwm_sgrid_state(C.byref(t0), C.byref(ts))
+            slot = (ts.value + 3) % 4
+            if lib.cfdwm_surrogate_features(t0.value + 2 * dt, p(feat), p(base), p(eta1)) != 0 or \
+                    lib.cfdwm_surrogate_targets(slot, p(base), p(eta1), p(tgt)) != 0:
+                raise RuntimeError(cw.last_error())
+            torch.cuda.synchronize()
+            return tgt.cpu().numpy().astype(np.float64), slot
+
+        snaps = []
+        for k in range(steps + 1):
+            if k:
+                if lib.cfdwm_surrogate_step(0, 0.0, 0, None, None) != 0:
+                    raise RuntimeError(cw.last_error())
+            if k in (0, steps // 2, steps):
+                snaps.append(newest())
+        X, slot = snaps[-1]
+        eta = wm.sgrid_array(0).reshape(4, nx, ny)[slot]
+        U = [wm.sgrid_array(f).reshape(4, nx, ny, nl)[slot] for f in (1, 2, 3)]
+        umax = max(np.abs(u).max() for u in U)
+    finally:
+        os.chdir(cwd)
+    A2 = comps["A"] ** 2
+    sig2, km, om = A2.sum() / 2, (A2 * comps["k"]).sum() / A2.sum(), (A2 * comps["omega"]).sum() / A2.sum()
+    groups = {"eta": [0], "u": list(range(1, 1 + nl)), "v": list(range(1 + nl, 1 + 2 * nl)),
+              "w": list(range(1 + 2 * nl, 1 + 3 * nl))}
+    kx = np.fft.fftfreq(nx)[:, None]
+    ky = np.fft.fftfreq(ny)[None, :]
+    kk = np.sqrt(kx ** 2 + ky ** 2)
+    I, J = np.meshgrid(np.arange(nx), np.arange(ny), indexing="ij")
+    inner = (slice(margin, nx - margin), slice(margin, ny - margin))
+    out = {}
+    for g, chans in groups.items():
+        scale = km * sig2 if g == "eta" else km * sig2 * om
+        full = np.abs(eta).max() if g == "eta" else umax
+        r = {"share": float(max(np.abs(X[c]).max() for c in chans) * scale / full)}
+        P = sum(np.abs(np.fft.fft2(X[c] - X[c].mean())) ** 2 for c in chans)
+        r["spectrum"] = {"under_%d_columns" % L: float(P[kk > 1.0 / L].sum() / P.sum()) for L in (10, 8, 6)}
+        e = {"quarter": 0.0, "rows": 0.0, "checkerboard": 0.0}
+        for c in chans:
+            Z = X[c]
+            m = np.abs(Z).max()
+            # every other column both ways: the odd rows/columns from the even ones
+            Ze = Z[::2, ::2]
+            Zx = _cubic_mid(Ze, 0)                       # between even rows
+            G = np.zeros_like(Z)
+            G[::2, ::2] = Ze
+            G[1::2, ::2] = Zx[: G[1::2, ::2].shape[0]]
+            G[:, 1::2] = _cubic_mid(G[:, ::2], 1)[:, : G[:, 1::2].shape[1]]
+            e["quarter"] = max(e["quarter"], float(np.abs(G - Z)[inner].max() / m))
+            R = Z.copy()
+            R[1::2, :] = _cubic_mid(Z[::2, :], 0)[: R[1::2, :].shape[0]]
+            e["rows"] = max(e["rows"], float(np.abs(R - Z)[inner].max() / m))
+            odd = (I + J) % 2 == 1
+            Q = Z.copy()
+            ax = (-np.roll(Z, 3, 0) + 9 * np.roll(Z, 1, 0) + 9 * np.roll(Z, -1, 0) - np.roll(Z, -3, 0)) / 16
+            ay = (-np.roll(Z, 3, 1) + 9 * np.roll(Z, 1, 1) + 9 * np.roll(Z, -1, 1) - np.roll(Z, -3, 1)) / 16
+            Q[odd] = (0.5 * (ax + ay))[odd]
+            e["checkerboard"] = max(e["checkerboard"], float(np.abs(Q - Z)[inner].max() / m))
+        r["interp"] = e
+        X0, Xm, X1 = snaps[0][0], snaps[1][0], snaps[2][0]
+        r["time"] = float(max(np.abs(0.5 * (X0[c] + X1[c]) - Xm[c]).max() for c in chans) /
+                          max(np.abs(Xm[c]).max() for c in chans))
+        out[g] = r
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("cmd", choices=["train"])
+    ap.add_argument("cmd", choices=["train", "analyse"])
     ap.add_argument("--seas", type=int, default=250)
     ap.add_argument("--per-sea", type=int, default=8)
     ap.add_argument("--val-seas", type=int, default=16)
@@ -174,6 +289,10 @@ def main():
     ap.add_argument("--seed", type=int, default=11)
     ap.add_argument("--out", default=WEIGHTS)
     args = ap.parse_args()
+    if args.cmd == "analyse":
+        import json
+        print(json.dumps(analyse(), indent=1))
+        return
     tr = Trainer(seed=args.seed)
     t0 = time.time()
     X, T = tr.generate(args.seas, args.seed, per_sea=args.per_sea)

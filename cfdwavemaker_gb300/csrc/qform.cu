@@ -1065,6 +1065,17 @@ int tcform_split(TcForm &f, const double *coef64, const int *bmap_host, int nblk
 // device at once (one CTA per SM), at most one per tile unit.
 // CTAs (or CTA pairs) of this form that fit on the device at once; set and
 // queried once per process (thread-safe static initialisation); <= 0: none.
+// Row blocks per tile group of the tile walk (the group sweeps every column
+// tile while its rows of X and Y stay in L2); CFDWM_TC_GROUP overrides it.
+static int tc_group_m() {
+    static const int g = [] {
+        const char *e = std::getenv("CFDWM_TC_GROUP");
+        int v = e ? std::atoi(e) : 8;
+        return v >= 2 && v <= 512 ? v : 8;
+    }();
+    return g;
+}
+
 template <int BN, bool TWO, bool PAIR>
 static int tc_max_units() {
     using CF = TcCfg<BN, TWO, PAIR>;
@@ -1232,7 +1243,7 @@ int tcform_eval(TcForm &f, const DevSea &sea, long n, const double *x, const dou
             make_map(&mWl, f.Wlo, (long)f.nblk * npad, npad, BN / CSZ, f.fp16))
             return E_CUDA;
         QTC q;
-        q.rows = mm; q.npad = npad; q.ntn = npad / BN; q.group_m = 8; q.nblk = f.nblk; q.nout = f.nout;
+        q.rows = mm; q.npad = npad; q.ntn = npad / BN; q.group_m = tc_group_m(); q.nblk = f.nblk; q.nout = f.nout;
         q.bmap = f.bmap; q.Y = Y; q.ldy = mpad; q.colscale = f.colscale;
         q.out = out + (long)f.nout * b; q.fp16 = f.fp16 ? 1 : 0; q.err = f.err;
         long nrb = (mm + TBM - 1) / TBM;

@@ -15,6 +15,7 @@ operator that then runs on the full grid).
 
     python -m cfdwavemaker_gb300.surrogate train --seas 400 --steps 6000 --out W.bin
     python -m cfdwavemaker_gb300.surrogate analyse     (how local the predicted part is)
+    python -m cfdwavemaker_gb300.surrogate time        (device time of the network)
 """
 from __future__ import annotations
 
@@ -277,9 +278,59 @@ def analyse(nx=256, ny=256, nl=16, dt=0.1, steps=20, margin=6):
     return out
 
 
+def time_network(nl=16, nx=256, ny=256, batch=8, patch=64, reps=20):
+    """Device time of the network (the committed weights): one forward over an
+    nx x ny grid with its halo, and one training step (forward, loss,
+    backward, Adam) on `batch` patches of patch x patch outputs.  Inputs are
+    random; times in ms (CUDA events / host clock after a synchronise)."""
+    import torch
+    import cfdwavemaker_gb300 as cw
+    lib = cw.load()
+    if lib.cfdwm_surrogate_create(nl, 1) != 0 or lib.cfdwm_surrogate_load(WEIGHTS.encode()) != 0:
+        raise RuntimeError(cw.last_error())
+    H, W = nx + 2 * SH, ny + 2 * SH
+    g = torch.Generator(device="cuda").manual_seed(7)
+    x = torch.randn((1, 8 * nl, H, W), device="cuda", generator=g)
+    y = torch.empty((1, 1 + 3 * nl, nx, ny), device="cuda")
+
+    def fwd():
+        if lib.cfdwm_surrogate_forward(cw._ptr(x), 1, H, W, cw._ptr(y)) != 0:
+            raise RuntimeError(cw.last_error())
+    for _ in range(3):
+        fwd()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        fwd()
+    e1.record()
+    torch.cuda.synchronize()
+    out = {"forward_ms": e0.elapsed_time(e1) / reps, "grid": [nx, ny]}
+    P = patch + 2 * SH
+    X = torch.randn((4 * batch, 8 * nl, P, P), device="cuda", generator=g)
+    T = torch.randn((4 * batch, 1 + 3 * nl, patch, patch), device="cuda", generator=g)
+    loss = C.c_double(0.0)
+    idx = (C.c_int * batch)(*range(batch))
+
+    def step():
+        if lib.cfdwm_surrogate_train_step(cw._ptr(X), cw._ptr(T), 4 * batch, idx, batch, P, P, C.c_float(1e-5),
+                                          C.byref(loss)) != 0:
+            raise RuntimeError(cw.last_error())
+    for _ in range(3):
+        step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        step()
+    torch.cuda.synchronize()
+    out["train_step_ms"] = (time.perf_counter() - t0) * 1e3 / reps
+    out["train_batch"] = [batch, patch, patch]
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("cmd", choices=["train", "analyse"])
+    ap.add_argument("cmd", choices=["train", "analyse", "time"])
     ap.add_argument("--seas", type=int, default=250)
     ap.add_argument("--per-sea", type=int, default=8)
     ap.add_argument("--val-seas", type=int, default=16)
@@ -289,9 +340,9 @@ def main():
     ap.add_argument("--seed", type=int, default=11)
     ap.add_argument("--out", default=WEIGHTS)
     args = ap.parse_args()
-    if args.cmd == "analyse":
+    if args.cmd in ("analyse", "time"):
         import json
-        print(json.dumps(analyse(), indent=1))
+        print(json.dumps(analyse() if args.cmd == "analyse" else time_network(), indent=1))
         return
     tr = Trainer(seed=args.seed)
     t0 = time.time()

@@ -412,6 +412,35 @@ def surrogate_summary(args, r):
     }
 
 
+def other_workloads(args):
+    """Short runs of the other workloads for the default line (single GPU, no
+    CPU baselines; each has its own --workload run with the full record): the
+    s-grid update + 1e6 queries in both column forms, the point API, and the
+    regular waves."""
+    out = {}
+    for key, wl, method in (("sgrid_tensor_core", "sgrid", 1), ("sgrid_plain", "sgrid", 0), ("point", "point", 1)):
+        a = argparse.Namespace(**vars(args))
+        a.workload, a.sgrid_method, a.grid, a.shard, a.vertical_theory = wl, method, 256, False, "sharma"
+        a.steps, a.warmup = (3, 2) if (wl, method) == ("sgrid", 0) else (5, 3)
+        r = run_ours(a)
+        unit = "grid nodes/s" if wl == "sgrid" else "points/s"
+        out[key] = {"value": r["units"] / (r["ms"] / 1e3), "unit": unit, "ms_per_step": r["ms"],
+                    "steps": a.steps, "e2e": r["units"] / r["e2e_s"], "gpu_launches": r["launches"],
+                    "clocks": r["clocks"], "kernels": r["prof"]}
+        if "pressure_ms" in r:
+            out[key]["with_pressure_ms_per_step"] = r["pressure_ms"]
+    a = argparse.Namespace(**vars(args))
+    a.workload, a.steps, a.warmup = "regular", 3, 2
+    r = run_regular(a)
+    out["regular"] = {"value": 2 * r["n"] / (r["ms"] / 1e3), "unit": "points/s", "ms_per_step": r["ms"],
+                      "e2e": 2 * r["n"] / (r["e2e_ms"] / 1e3), "cases": r["cases"], "clocks": r["clocks"]}
+    out["workloads"] = {"sgrid": "256x256x16 s-grid of the 1024-component sea, one ring update (dt 0.5 s) + 1e6 "
+                                 "random spline queries per step",
+                        "point": "eta, u, w, dp of the 128-component long-crested sea at 256 x 32 z x 8 t",
+                        "regular": REG_WORKLOAD}
+    return out
+
+
 QFORM_WORKLOAD = ("precision form: second-order eta and z=0/Taylor-layer u, v, w (pair-cache coefficients) of "
                   "a 4096-component short-crested JONSWAP sea (256 freq x 16 dir, Hs 6 m, Tp 12 s, gamma 2, "
                   "cos-2s s=10, depth 100 m) at %d random (x, y, t) points")
@@ -794,11 +823,24 @@ def run_ours(args):
         htq = torch.empty(nq, dtype=torch.float64).pin_memory()
         hout = np.empty((nq, 4))
         nodes = args.grid * args.grid * 16
+        ring = None
+        if args.shard:
+            # the column shard: each rank fills its rows of every new slot and
+            # the slots are all-gathered (NCCL); the whole grid is the job
+            from cfdwavemaker_gb300.shard import ShardedRing
+            ring = ShardedRing(wm)
+            res["shard"] = {"bounds": ring.bounds, "rows": [ring.i0, ring.i1]}
+
+        def update(t):
+            if ring is not None:
+                ring.force_update(t)
+            else:
+                lib.wave_force_update(t)
 
         def step_device():
             # one ring update + 1e6 queries at a time inside the new interval
             state["t"] += dt
-            lib.wave_force_update(state["t"] + 1e-9)
+            update(state["t"] + 1e-9)
             t0, _ = wm.sgrid_state()
             dtq.fill_(t0 + 0.5 * dt)
             rc = lib.wave_Kinematics_batch(cw._ptr(dq[0]), cw._ptr(dq[1]), cw._ptr(dq[2]), cw._ptr(dtq),
@@ -807,7 +849,7 @@ def run_ours(args):
 
         def step_host():
             state["t"] += dt
-            lib.wave_force_update(state["t"] + 1e-9)
+            update(state["t"] + 1e-9)
             t0, _ = wm.sgrid_state()
             htq.fill_(t0 + 0.5 * dt)
             rc = lib.wave_Kinematics_batch(cw._ptr(hq[0].numpy()), cw._ptr(hq[1].numpy()),
@@ -1083,9 +1125,14 @@ def main():
                     help="row subset on which the plain FP32 form of the precision workload is timed")
     ap.add_argument("--oracle-rows", type=int, default=256,
                     help="rows of the precision workload checked against the FP64 oracle (spread over every chunk)")
+    ap.add_argument("--shard", action="store_true",
+                    help="s-grid workload under torchrun: split the ring's rows of columns over the ranks "
+                         "(strong scaling, one all-gather per new slot) instead of running replicas")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true",
                     help="precision workload: leave out the learned-update summary")
+    ap.add_argument("--no-others", action="store_true",
+                    help="precision workload: leave out the short runs of the other workloads")
     ap.add_argument("--grid", type=int, default=256,
                     help="columns per side of the s-grid (256 is the named workload; smaller sizes "
                          "are for profiling captures only)")
@@ -1137,6 +1184,8 @@ def main():
             sa = argparse.Namespace(**vars(args))
             sa.surr_steps, sa.plain_steps = 200, 10
             line["surrogate"] = surrogate_summary(sa, run_surrogate(sa))
+        if r["ws"] == 1 and not args.no_others:
+            line["other_workloads"] = other_workloads(args)
         print(json.dumps(line))
         return
     if args.workload == "regular":
@@ -1161,12 +1210,15 @@ def main():
     if r["rank"] != 0:
         return
     n = r["ws"]
-    value = r["units"] * n / (r["ms"] / 1e3)
-    e2e = r["units"] * n / r["e2e_s"]
+    # replicas: every rank updates its own whole grid; shard: the ranks share one
+    shared = args.workload == "sgrid" and args.shard
+    value = r["units"] * (1 if shared else n) / (r["ms"] / 1e3)
+    e2e = r["units"] * (1 if shared else n) / r["e2e_s"]
     pk, src = peaks()
     line = {
         "metric": METRIC, "value": value, "unit": unit, "n_gpus": n, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": r["ms"], "higher_is_better": True, "scaling": "weak",
+        "warmup": args.warmup, "ms_per_step": r["ms"], "higher_is_better": True,
+        "scaling": "strong" if shared else "weak",
         "vs_baseline": None,
         "dtype": "fp16x3 split tcgen05, FP32 accumulate (FP64 phases)" if r.get("depth_rank") else
                  "f32 (FP64 phases)", "data": "synthetic",
@@ -1181,6 +1233,8 @@ def main():
         "kernels": r["prof"],
         "peaks_source": src,
     }
+    if "shard" in r:
+        line["shard"] = r["shard"]
     if "vtu_s" in r:
         line["vtu_export"] = {"s": r["vtu_s"], "MB": r["vtu_bytes"] / 1e6,
                               "MB_per_s": r["vtu_bytes"] / 1e6 / r["vtu_s"], "threads": os.cpu_count()}

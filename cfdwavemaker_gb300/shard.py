@@ -39,6 +39,14 @@ def partition(weights, nranks, lib=None):
     return [int(v) for v in b]
 
 
+def _world(group):
+    """(rank, size) of the process group; one process without a group is rank 0 of 1."""
+    import torch.distributed as dist
+    if dist.is_available() and dist.is_initialized():
+        return dist.get_rank(group), dist.get_world_size(group)
+    return 0, 1
+
+
 def allgather_rows(local, bounds, group=None):
     """All-gather of row blocks.  Rank r holds rows [bounds[r], bounds[r+1])
     of an array as ``local`` (a tensor [rows_r, ...]); every rank receives the
@@ -47,11 +55,12 @@ def allgather_rows(local, bounds, group=None):
     each block is padded to the largest block."""
     import torch
     import torch.distributed as dist
-    ws = dist.get_world_size(group)
-    rank = dist.get_rank(group)
+    rank, ws = _world(group)
     sizes = [bounds[r + 1] - bounds[r] for r in range(ws)]
     if local.shape[0] != sizes[rank]:
         raise ValueError("rank %d holds %d rows, its block has %d" % (rank, local.shape[0], sizes[rank]))
+    if ws == 1:
+        return local
     m = max(max(sizes), 1)
     rest = tuple(local.shape[1:])
     pad = torch.zeros((m,) + rest, dtype=local.dtype, device=local.device)
@@ -71,10 +80,8 @@ class ShardedRing:
 
     def __init__(self, wm, group=None, device=None):
         import torch
-        import torch.distributed as dist
         self.wm, self.lib, self.group = wm, wm.lib, group
-        self.rank = dist.get_rank(group)
-        self.size = dist.get_world_size(group)
+        self.rank, self.size = _world(group)
         b = np.zeros(self.size + 1, dtype=np.int32)
         rc = self.lib.cfdwm_sgrid_partition(self.size, b.ctypes.data_as(C.POINTER(C.c_int)))
         if rc != 0:
@@ -106,6 +113,9 @@ class ShardedRing:
                 if rc != 0:
                     raise RuntimeError("cfdwm_sgrid_block_export: %d" % rc)
             whole = allgather_rows(mine, self.bounds, self.group).contiguous()
+            if whole.is_cuda:
+                # the collective ran on torch's stream, the import runs on the library's
+                torch.cuda.current_stream().synchronize()
             for r in range(self.size):
                 a, b = self.bounds[r], self.bounds[r + 1]
                 if r == self.rank or a == b:

@@ -31,6 +31,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdio>
+#include <mutex>
 
 namespace cfdwm {
 
@@ -361,8 +362,10 @@ int launch_ct(const TcConv &a, dim3 grid, cudaStream_t st) {
 }
 
 int *g_ct_err = nullptr;      // error word of the bounded waits (device)
+std::mutex g_ct_mtx;          // serialises the lazy allocations of this file
 
 int ct_err_word(int **p) {
+    std::lock_guard<std::mutex> lk(g_ct_mtx);
     if (!g_ct_err) {
         CK(cudaMalloc(&g_ct_err, sizeof(int)));
         CK(cudaMemset(g_ct_err, 0, sizeof(int)));
@@ -372,13 +375,15 @@ int ct_err_word(int **p) {
 }
 
 // The B operand of a forward or data-gradient launch, packed by k_ct_pack into
-// one device buffer that the launches of a stream reuse in turn (the network's
-// calls are made on one stream).
+// one device buffer that the launches reuse in turn.  The network is a
+// process-wide singleton driven from one stream (surrogate.cu); the buffer
+// follows the same rule, and its (re)allocation is serialised.
 __nv_bfloat16 *g_ct_w = nullptr;
 long g_ct_w_cap = 0;
 
 int ct_pack(const __nv_bfloat16 *w, int C, int O, int op, int NP, long Kp, cudaStream_t st,
             const __nv_bfloat16 **out) {
+    std::lock_guard<std::mutex> lk(g_ct_mtx);
     const long n = (long)NP * Kp;
     if (n > g_ct_w_cap) {
         if (g_ct_w) cudaFree(g_ct_w);

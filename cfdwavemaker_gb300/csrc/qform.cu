@@ -380,13 +380,17 @@ __global__ void __launch_bounds__(128) k_qform_prep(QPrep a) {
 // (row, field), as before.  The lower triangle of the diagonal tiles holds
 // zeros, so every tile runs the full 32 x 32 loop.
 // ---------------------------------------------------------------------------
+constexpr int QPL_MAXSEG = 32;
+
 struct QPlain {
     long rows;
     int ntile;
     const float *tab;        // plain tiles
     const float2 *ph;        // [npad][rows] (c, s)
     const float *rr;         // [npad][rows]
-    float *out;              // [rows][4]
+    int nseg;                // segments of the tile walk (units per row block)
+    int mb[QPL_MAXSEG + 1];  // segment g walks the column tiles M in [mb[g], mb[g + 1])
+    float *part;             // [nseg][rows][4]: each segment's sums
 };
 
 constexpr int QPL_ROWS = 256;                              // rows per block
@@ -410,16 +414,22 @@ __device__ __forceinline__ void qpl_kahan(float &S, float &C, float y) {
 __global__ void __launch_bounds__(128, 2) k_qform_plain(QPlain a) {
     extern __shared__ float4 q_smem[];
     const int tid = threadIdx.x;
-    const long p0 = (long)blockIdx.x * QPL_ROWS + tid, p1 = p0 + 128;
+    // unit = (segment, row block), segments outermost: the units in flight
+    // together walk the same few column tiles, whose records stay in L2
+    const long nrb = (a.rows + QPL_ROWS - 1) / QPL_ROWS;
+    const int seg = (int)(blockIdx.x / nrb);
+    const long rb = blockIdx.x % nrb;
+    const long p0 = rb * QPL_ROWS + tid, p1 = p0 + 128;
     const long q0 = p0 < a.rows ? p0 : 0, q1 = p1 < a.rows ? p1 : 0;   // clamped reads
     const int nt = a.ntile;
-    const long ntiles = (long)nt * (nt + 1) / 2;
+    const int mlo = a.mb[seg], mhi = a.mb[seg + 1];
+    const long ntiles = ((long)mhi * (mhi + 1) - (long)mlo * (mlo + 1)) / 2;
     const float4 *tab4 = reinterpret_cast<const float4 *>(a.tab);
     float S0[4] = {0, 0, 0, 0}, C0[4] = {0, 0, 0, 0}, S1[4] = {0, 0, 0, 0}, C1[4] = {0, 0, 0, 0};
     float2 pm0[QT], pm1[QT];     // (c, s) of the 32 components of tile M, rows p and p + 128
 
-    // stage k of the walk: tile (I, M) with M outer
-    int lI = 0, lM = 0;          // next tile to load
+    // stage k of the walk: tile (I, M) with M outer, M in [mlo, mhi)
+    int lI = 0, lM = mlo;        // next tile to load
     auto issue = [&](long k) {
         if (k < ntiles) {
             const float4 *src = tab4 + qtile_index(lI, lM, nt) * (long)QPL_TILE4;
@@ -431,7 +441,7 @@ __global__ void __launch_bounds__(128, 2) k_qform_plain(QPlain a) {
         qpl_commit();
     };
     issue(0);
-    int I = 0, M = 0;
+    int I = 0, M = mlo;
     for (long k = 0; k < ntiles; k++) {
         issue(k + 1);
         if (I == 0) {
@@ -486,10 +496,21 @@ __global__ void __launch_bounds__(128, 2) k_qform_plain(QPlain a) {
         __syncthreads();     // the stage is refilled by the next issue
         if (++I > M) { I = 0; M++; }
     }
+    // the segment's compensated sums
+    float *P = a.part + (long)seg * a.rows * 4;
     if (p0 < a.rows)
-        for (int f = 0; f < 4; f++) a.out[p0 * 4 + f] = S0[f];
+        for (int f = 0; f < 4; f++) P[p0 * 4 + f] = S0[f] - C0[f];
     if (p1 < a.rows)
-        for (int f = 0; f < 4; f++) a.out[p1 * 4 + f] = S1[f];
+        for (int f = 0; f < 4; f++) P[p1 * 4 + f] = S1[f] - C1[f];
+}
+
+// out[row][f] = the segments' sums added in segment order (Kahan)
+__global__ void k_qform_plain_sum(long rows, int nseg, const float *part, float *out) {
+    const long e = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (e >= rows * 4) return;
+    float S = 0.f, C = 0.f;
+    for (int g = 0; g < nseg; g++) qpl_kahan(S, C, part[(long)g * rows * 4 + e]);
+    out[e] = S - C;
 }
 
 // ---------------------------------------------------------------------------
@@ -1363,27 +1384,64 @@ int qform_eval(const DevSea &sea, long n, const double *x, const double *y, cons
     if (method == 1) return tcform_eval(g_q.tc, sea, n, x, y, t, 1, out, stream, tc_error);
     CK(cudaMemsetAsync(out, 0, sizeof(float) * 4 * n, stream));
     const long chunk = 1L << 16;
-    static bool pattr = false;
-    if (!pattr) {
-        CK(cudaFuncSetAttribute(k_qform_plain, cudaFuncAttributeMaxDynamicSharedMemorySize, QPLAIN_SMEM));
-        pattr = true;
-    }
+    // one-time, thread-safe (static initialisation)
+    static const cudaError_t pattr =
+        cudaFuncSetAttribute(k_qform_plain, cudaFuncAttributeMaxDynamicSharedMemorySize, QPLAIN_SMEM);
+    CK(pattr);
+    // two blocks of the kernel fit an SM (registers, shared memory)
+    static const int slots = [] {
+        int dev = 0, nsm = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+            cudaGetLastError();
+            return 2 * 148;
+        }
+        return 2 * nsm;
+    }();
+    const int nt = g_q.ntile_plain;
     long m = std::min(n, chunk);
-    size_t bytes = (sizeof(float2) + sizeof(float)) * (size_t)npad * m + sizeof(double) * 5 * m + 4096;
-    int rc = reserve_scratch(bytes);
+    auto up = [](size_t v) { return (v + 255) / 256 * 256; };
+    const size_t b_ph = up(sizeof(float2) * npad * m), b_rr = up(sizeof(float) * npad * m),
+                 b_first = up(sizeof(double) * 5 * m);
+    int rc = reserve_scratch(b_ph + b_rr + b_first + sizeof(float) * 4 * (size_t)QPL_MAXSEG * m);
     if (rc) return rc;
     for (long b = 0; b < n; b += chunk) {
         long mm = std::min(chunk, n - b);
         float2 *ph = (float2 *)g_q.scratch;
-        float *rr = (float *)((char *)g_q.scratch + ((sizeof(float2) * npad * mm + 255) / 256) * 256);
-        double *first = (double *)((char *)rr + ((sizeof(float) * npad * mm + 255) / 256) * 256);
+        float *rr = (float *)((char *)g_q.scratch + b_ph);
+        double *first = (double *)((char *)rr + b_rr);
+        float *part = (float *)((char *)first + b_first);
         rc = launch_phasors_public(sea, mm, x + b, y + b, t + b, 1, 1, 1, npad, ph, rr, first, stream);
         if (rc) return rc;
+        // The tile walk of a row block is cut into nseg segments of about equal
+        // work (at column-tile boundaries), so that the units -- row blocks x
+        // segments -- fill whole waves of the SMs' two block slots: nseg is the
+        // count in [4, 32] (at most one per column tile) whose waves are fullest.
+        const long nrb = (mm + QPL_ROWS - 1) / QPL_ROWS;
+        int nseg = 1;
+        double best = 0.0;
+        for (int g = 4; g <= std::min(QPL_MAXSEG, nt); g++) {
+            const long units = nrb * g;
+            const double fill = (double)units / (double)(((units + slots - 1) / slots) * slots);
+            if (fill > best + 1e-9) { best = fill; nseg = g; }
+        }
         QPlain q;
-        q.rows = mm; q.ntile = g_q.ntile_plain; q.tab = g_q.plain_tab; q.ph = ph; q.rr = rr;
-        q.out = out + 4 * b;
+        q.rows = mm; q.ntile = nt; q.tab = g_q.plain_tab; q.ph = ph; q.rr = rr; q.part = part;
+        q.nseg = nseg;
+        const long total = (long)nt * (nt + 1) / 2;
+        q.mb[0] = 0;
+        int M = 0;
+        long acc = 0;
+        for (int g = 1; g < nseg; g++) {
+            const long target = total * g / nseg;
+            while (M < nt && acc + (M + 1) <= target) { acc += M + 1; M++; }
+            q.mb[g] = std::max(M, q.mb[g - 1]);
+        }
+        q.mb[nseg] = nt;
         prof_begin(PK_QFORM, stream);
-        k_qform_plain<<<(unsigned)((mm + QPL_ROWS - 1) / QPL_ROWS), 128, QPLAIN_SMEM, stream>>>(q);
+        k_qform_plain<<<(unsigned)(nrb * nseg), 128, QPLAIN_SMEM, stream>>>(q);
+        note_launch();
+        k_qform_plain_sum<<<(unsigned)((mm * 4 + 255) / 256), 256, 0, stream>>>(mm, nseg, part, out + 4 * b);
         note_launch();
         prof_end(PK_QFORM, stream);
         CK(cudaGetLastError());

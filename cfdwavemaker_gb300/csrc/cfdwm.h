@@ -343,6 +343,10 @@ struct TcForm {
     bool built = false;
     int npad = 0, nblk = 0, nout = 0;
     bool fp16 = true;
+    // fp16 split with the cross products in the hi accumulator (lo parts not
+    // scaled): one accumulator, so the GEMM keeps two accumulator buffers and
+    // a tile's epilogue runs under the next tile's MMAs
+    bool one_acc = false;
     void *Whi = nullptr, *Wlo = nullptr;
     float *colscale = nullptr;
     int *bmap = nullptr;        // per block: X half, Y half, output column
@@ -353,7 +357,7 @@ struct TcForm {
     void *ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
 };
 int tcform_split(TcForm &f, const double *coef64, const int *bmap_host, int nblk, int nout, int npad, bool fp16,
-                 void *stream);
+                 void *stream, bool one_acc = false);
 int tcform_eval(TcForm &f, const DevSea &sea, long n, const double *x, const double *y, const double *t, long st,
                 float *out, void *stream, int *tc_error);
 void tcform_free(TcForm &f);

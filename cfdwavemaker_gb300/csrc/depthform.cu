@@ -37,9 +37,17 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <vector>
 
 namespace cfdwm {
+
+// the cross products of the fp16 split in the hi accumulator (default) or in
+// a second one (CFDWM_DF_TWO_ACC=1, the precision form's arrangement)
+static bool df_one_acc() {
+    const char *e = std::getenv("CFDWM_DF_TWO_ACC");
+    return !(e && e[0] == '1');
+}
 
 #define CK(x)                                                  \
     do {                                                       \
@@ -640,7 +648,10 @@ int depthform_build(const Config &cfg, const DevSea &sea, DepthForm &df, int nf,
             setb(b + 7, 1, 1, o + 3);
         }
     }
-    rc = tcform_split(df.tc, coef, bmap.data(), nblk, df.nout, npad, true, stream);
+    // fp16 split with one accumulator: the K range of a tile is short here
+    // (256-1024 components), so the cross products keep their bits in the hi
+    // accumulator, and the two accumulator buffers hide each tile's epilogue
+    rc = tcform_split(df.tc, coef, bmap.data(), nblk, df.nout, npad, true, stream, df_one_acc());
     cudaFree(coef);
     cudaFree(d_fk);
     cudaFree(d_gk);

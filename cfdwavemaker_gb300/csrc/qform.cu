@@ -186,7 +186,8 @@ __global__ void k_qform_plain_from64(int npad, int nt, const double *coef, float
 // FP32 accumulation keeps few guard bits, and adding terms 2^-11 smaller to
 // the hi-hi sum lost them (1.5e-5 at N = 4096 against 7e-6 with two).
 template <typename T16>
-__global__ void k_qform_split(int npad, int fp16, const double *coef, T16 *Whi, T16 *Wlo, float *colscale) {
+__global__ void k_qform_split(int npad, int fp16, double lo_scale, const double *coef, T16 *Whi, T16 *Wlo,
+                              float *colscale) {
     const int b = blockIdx.y, m = blockIdx.x;
     const double *row = coef + ((long)b * npad + m) * npad;
     __shared__ double red[32];
@@ -214,7 +215,7 @@ __global__ void k_qform_split(int npad, int fp16, const double *coef, T16 *Whi, 
         T16 hi, lo;
         if (fp16) {
             __half h = __float2half_rn((float)v);
-            __half l = __float2half_rn((float)((v - (double)__half2float(h)) * 2048.0));
+            __half l = __float2half_rn((float)((v - (double)__half2float(h)) * lo_scale));
             hi = *reinterpret_cast<T16 *>(&h);
             lo = *reinterpret_cast<T16 *>(&l);
         } else {
@@ -282,6 +283,7 @@ struct QPrep {
     long st;                   // element stride of t
     int cstride, ncomp, npad;
     int trivial_ramp, fp16;
+    float lo_scale;          // fp16: factor of the lo parts (2^11 with a cross accumulator, else 1)
     void *Xhi, *Xlo;           // [rows][2 npad]
     float *Y;                  // [2 npad][ldy], column-major: rows adjacent
     long ldy;                  // >= rows rounded up to PREP_ROWS
@@ -340,8 +342,8 @@ __global__ void __launch_bounds__(128) k_qform_prep(QPrep a) {
             __half2 *L = reinterpret_cast<__half2 *>((__half *)a.Xlo + o);
             H[0] = hc;
             H[a.npad / 2] = hs;
-            L[0] = __floats2half2_rn((xc0 - fc.x) * 2048.0f, (xc1 - fc.y) * 2048.0f);
-            L[a.npad / 2] = __floats2half2_rn((xs0 - fs.x) * 2048.0f, (xs1 - fs.y) * 2048.0f);
+            L[0] = __floats2half2_rn((xc0 - fc.x) * a.lo_scale, (xc1 - fc.y) * a.lo_scale);
+            L[a.npad / 2] = __floats2half2_rn((xs0 - fs.x) * a.lo_scale, (xs1 - fs.y) * a.lo_scale);
         } else {
             const __nv_bfloat162 hc = __floats2bfloat162_rn(xc0, xc1), hs = __floats2bfloat162_rn(xs0, xs1);
             const float2 fc = __bfloat1622float2(hc), fs = __bfloat1622float2(hs);
@@ -1055,11 +1057,11 @@ void tcform_free(TcForm &f) {
 
 // coef64: [nblk][npad (output column m)][npad (K index i)] FP64, W transposed.
 int tcform_split(TcForm &f, const double *coef64, const int *bmap_host, int nblk, int nout, int npad, bool fp16,
-                 void *stream_) {
+                 void *stream_, bool one_acc) {
     cudaStream_t stream = (cudaStream_t)stream_;
     tcform_free(f);
     if (npad % TBN != 0 || nblk < 1) return E_BAD_ARGUMENT;
-    f.npad = npad; f.nblk = nblk; f.nout = nout; f.fp16 = fp16;
+    f.npad = npad; f.nblk = nblk; f.nout = nout; f.fp16 = fp16; f.one_acc = fp16 && one_acc;
     size_t wel = (size_t)nblk * npad * npad;
     CK(cudaMalloc(&f.Whi, 2 * wel));
     CK(cudaMalloc(&f.Wlo, 2 * wel));
@@ -1068,10 +1070,10 @@ int tcform_split(TcForm &f, const double *coef64, const int *bmap_host, int nblk
     CK(cudaMemcpyAsync(f.bmap, bmap_host, sizeof(int) * 3 * nblk, cudaMemcpyHostToDevice, stream));
     dim3 gt((unsigned)npad, (unsigned)nblk);
     if (fp16)
-        k_qform_split<__half><<<gt, 256, 0, stream>>>(npad, 1, coef64, (__half *)f.Whi, (__half *)f.Wlo,
-                                                      f.colscale);
+        k_qform_split<__half><<<gt, 256, 0, stream>>>(npad, 1, f.one_acc ? 1.0 : 2048.0, coef64, (__half *)f.Whi,
+                                                      (__half *)f.Wlo, f.colscale);
     else
-        k_qform_split<__nv_bfloat16><<<gt, 256, 0, stream>>>(npad, 0, coef64, (__nv_bfloat16 *)f.Whi,
+        k_qform_split<__nv_bfloat16><<<gt, 256, 0, stream>>>(npad, 0, 1.0, coef64, (__nv_bfloat16 *)f.Whi,
                                                              (__nv_bfloat16 *)f.Wlo, f.colscale);
     note_launch();
     CK(cudaGetLastError());
@@ -1225,7 +1227,10 @@ int tcform_eval(TcForm &f, const DevSea &sea, long n, const double *x, const dou
     }
     const int BN = 256;
     // CTA pairs where two-CTA clusters fit on the device, else single CTAs
-    const bool pair = tc_pair() && (f.fp16 ? tc_max_units<256, true, true>() : tc_max_units<256, false, true>()) > 0;
+    // two accumulators (hi, cross) for the fp16 split unless the form keeps
+    // the cross products in the hi accumulator
+    const bool two = f.fp16 && !f.one_acc;
+    const bool pair = tc_pair() && (two ? tc_max_units<256, true, true>() : tc_max_units<256, false, true>()) > 0;
     const int CSZ = pair ? 2 : 1;
     int j = 0;
     for (long b = 0; b < n; b += chunk, j++) {
@@ -1248,6 +1253,7 @@ int tcform_eval(TcForm &f, const DevSea &sea, long n, const double *x, const dou
         pp.rows = mm; pp.row = rowrec; pp.comp = comprec; pp.phase = sea.d_phase; pp.t = t + b * st; pp.st = st;
         pp.cstride = sea.npad_g; pp.ncomp = sea.n; pp.npad = npad;
         pp.trivial_ramp = sea.trivial_ramp ? 1 : 0; pp.fp16 = f.fp16 ? 1 : 0;
+        pp.lo_scale = two ? 2048.0f : 1.0f;
         pp.Xhi = Xh; pp.Xlo = Xl; pp.Y = Y; pp.ldy = mpad;
         // a full grid: with two blocks per SM beside the GEMM the preparation
         // ran latency-bound at a tenth of its speed and became the bottleneck
@@ -1270,7 +1276,7 @@ int tcform_eval(TcForm &f, const DevSea &sea, long n, const double *x, const dou
         long nrb = (mm + TBM - 1) / TBM;
         long nunits = (nrb + CSZ - 1) / CSZ * (long)f.nblk * q.ntn;
         prof_begin(PK_QFORM, stream);
-        if (!f.fp16)
+        if (!two)
             rc = pair ? launch_tc<256, false, true>(mXh, mXl, mWh, mWl, q, nunits, stream)
                       : launch_tc<256, false, false>(mXh, mXl, mWh, mWl, q, nunits, stream);
         else

@@ -202,7 +202,9 @@ CFDWM_EXPORT int cfdwm_qform_eval(const double *x, const double *y, const double
  * one fixed 32 MiB device array per GPU, held until process exit.  Under
  * lazy module loading (the CUDA default) it is committed when
  * wave_Initialize loads an irregular sea (wave types 1 and 5), which also
- * looks up its device address, so later calls make no set-up of their own.
+ * looks up its device address, so later calls make no set-up of their own
+ * (should that lookup have failed there, the first call retries it: make
+ * that call before any stream capture).
  * A batch needs about (12 * Npad + 64) bytes per point, Npad = component
  * count rounded up to a multiple of 32, and larger batches are rejected with
  * -8 (message in cfdwm_last_error).  All calls share the array: calls that

@@ -347,6 +347,9 @@ struct TcForm {
     // scaled): one accumulator, so the GEMM keeps two accumulator buffers and
     // a tile's epilogue runs under the next tile's MMAs
     bool one_acc = false;
+    // K blocks (of 64) per accumulation segment of a column tile, 0: the whole
+    // upper-triangle K range in one accumulation
+    int kseg = 0;
     void *Whi = nullptr, *Wlo = nullptr;
     float *colscale = nullptr;
     int *bmap = nullptr;        // per block: X half, Y half, output column

@@ -26,8 +26,10 @@
 //    issues TMA loads (128B swizzle) of its 128 rows of X and its half of
 //    the W tile into a stage ring, one thread of CTA 0 issues tcgen05.mma
 //    (M=256, N=256, K=16) for the three split products Xh Wh + Xh Wl + Xl Wh
-//    into FP32 TMEM accumulators (fp16: the cross products go to a second
-//    accumulator with the lo parts scaled by 2^11), warps 2-9 read TMEM with
+//    into FP32 TMEM accumulators (fp16: one accumulator over K segments of
+//    512 terms, two TMEM buffers so that a unit's epilogue runs under the
+//    next unit's MMAs; or a second accumulator for the cross products, with
+//    the lo parts scaled by 2^11, over the whole K range), warps 2-9 read TMEM with
 //    tcgen05.ld, multiply by the right-hand phasors (column-major, loaded
 //    before the accumulator is ready) and reduce the row, one atomic add per
 //    (row, tile).  Tiles are ordered in groups so that the X and W tiles in
@@ -598,6 +600,8 @@ __device__ __forceinline__ uint32_t ncluster_x() {
 __device__ __forceinline__ void cluster_sync_all() {
     asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
+constexpr int QTC_MAXCU = 256;
+
 struct QTC {
     long rows;               // rows of this chunk
     int npad;                // components (multiple of 256)
@@ -612,6 +616,11 @@ struct QTC {
     float *out;              // [rows][nout] accumulated with atomics
     int fp16;
     int *err;
+    // column units: column tile cu_tn[u] over the K blocks [cu_kb0[u], cu_kb1[u])
+    // (a long K range of the upper triangle cut into segments, each with its
+    // own accumulation and epilogue)
+    int ncu;
+    unsigned short cu_tn[QTC_MAXCU], cu_kb0[QTC_MAXCU], cu_kb1[QTC_MAXCU];
 };
 
 // bounded wait that also gives up as soon as another role has set the error word
@@ -644,7 +653,7 @@ __device__ __forceinline__ bool mbar_wait_ec(uint64_t *b, uint32_t parity, int *
 
 struct TileInfo {
     long rb;
-    int blk, tn, nkb;
+    int blk, tn, kb0, kb1;
 };
 
 // grouped tile order: a group of group_m row units sweeps all column tiles.
@@ -655,7 +664,7 @@ struct TileInfo {
 // tile sequence.
 template <int BN, int CS>
 __device__ __forceinline__ bool tile_of(const QTC &a, long nru, long t, int crank, TileInfo &ti) {
-    const int ncol = a.nblk * a.ntn;
+    const int ncol = a.nblk * a.ncu;
     const long gm = a.group_m / CS > 0 ? a.group_m / CS : 1;
     const long per_group = gm * ncol;
     long grp = t / per_group, in = t % per_group;
@@ -666,9 +675,11 @@ __device__ __forceinline__ bool tile_of(const QTC &a, long nru, long t, int cran
     int ct = (int)(in / gsz);
     if (ru >= nru || ct >= ncol) return false;
     ti.rb = ru * CS + crank;
-    ti.blk = ct / a.ntn;
-    ti.tn = ct % a.ntn;
-    ti.nkb = (ti.tn * BN + BN) / TBK;          // upper triangle: i < m0 + BN
+    ti.blk = ct / a.ncu;
+    const int cu = ct % a.ncu;
+    ti.tn = a.cu_tn[cu];
+    ti.kb0 = a.cu_kb0[cu];
+    ti.kb1 = a.cu_kb1[cu];                      // upper triangle: i < m0 + BN
     return true;
 }
 
@@ -698,7 +709,8 @@ template <int BN, bool TWO, bool PAIR>
 __global__ void __launch_bounds__(TC_THREADS, 1) k_qform_tc(const __grid_constant__ CUtensorMap mXh,
                                                      const __grid_constant__ CUtensorMap mXl,
                                                      const __grid_constant__ CUtensorMap mWh,
-                                                     const __grid_constant__ CUtensorMap mWl, QTC a) {
+                                                     const __grid_constant__ CUtensorMap mWl,
+                                                     const __grid_constant__ QTC a) {
     using CF = TcCfg<BN, TWO, PAIR>;
     constexpr int CS = PAIR ? 2 : 1;
     constexpr int TSTAGES = CF::STAGES, STAGE_BYTES = CF::STAGE_BYTES, B_TILE = CF::B_TILE;
@@ -719,7 +731,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_qform_tc(const __grid_constan
     const long ncl = PAIR ? (long)ncluster_x() : (long)gridDim.x;
     const long nrb = (a.rows + TBM - 1) / TBM;
     const long nru = (nrb + CS - 1) / CS;
-    const long ntiles = nru * (long)a.nblk * a.ntn;
+    const long ntiles = nru * (long)a.nblk * a.ncu;
     // (a pair does not return early: its CTAs address each other until the end)
     if (!PAIR && *(volatile int *)a.err != 0) return;
 
@@ -762,7 +774,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_qform_tc(const __grid_constan
                 if (!tile_of<BN, CS>(a, nru, t, crank, ti)) continue;
                 const int khalf = a.bmap[3 * ti.blk];
                 const int m0 = ti.tn * BN;
-                for (int kb = 0; kb < ti.nkb; kb++, g++) {
+                for (int kb = ti.kb0; kb < ti.kb1; kb++, g++) {
                     int s = (int)(g % TSTAGES);
                     uint32_t ph = (uint32_t)((g / TSTAGES) & 1);
                     if (!mbar_wait_e(&empty[s], ph ^ 1, a.err, 1)) { ok = false; break; }
@@ -814,7 +826,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_qform_tc(const __grid_constan
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 const uint32_t acc = tmem + (uint32_t)(buf * ACOLS);
                 const uint32_t acc2 = TWO ? acc + BN : acc;     // fp16: cross products
-                for (int kb = 0; kb < ti.nkb; kb++, g++) {
+                for (int kb = ti.kb0; kb < ti.kb1; kb++, g++) {
                     int s = (int)(g % TSTAGES);
                     uint32_t ph = (uint32_t)((g / TSTAGES) & 1);
                     if (!mbar_wait_e(&full[s], ph, a.err, 2)) { ok = false; break; }
@@ -824,7 +836,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_qform_tc(const __grid_constan
                     uint64_t dWh = sdesc(base + 2 * A_TILE), dWl = sdesc(base + 2 * A_TILE + B_TILE);
                     for (int k = 0; k < TBK / 16; k++) {
                         uint64_t o = (uint64_t)(k * 32) >> 4;     // 16 elements = 32 bytes per step
-                        uint32_t first = (kb == 0 && k == 0) ? 0u : 1u;
+                        uint32_t first = (kb == ti.kb0 && k == 0) ? 0u : 1u;
                         if (PAIR) {
                             umma_pair(acc, dXh + o, dWh + o, idesc, first);
                             umma_pair(acc2, dXh + o, dWl + o, idesc, TWO ? first : 1u);
@@ -1273,8 +1285,23 @@ int tcform_eval(TcForm &f, const DevSea &sea, long n, const double *x, const dou
         q.rows = mm; q.npad = npad; q.ntn = npad / BN; q.group_m = tc_group_m(); q.nblk = f.nblk; q.nout = f.nout;
         q.bmap = f.bmap; q.Y = Y; q.ldy = mpad; q.colscale = f.colscale;
         q.out = out + (long)f.nout * b; q.fp16 = f.fp16 ? 1 : 0; q.err = f.err;
+        // column units: each column tile's upper-triangle K range, cut into
+        // segments of at most f.kseg K blocks when the form asks for it
+        q.ncu = 0;
+        for (int tn = 0; tn < q.ntn; tn++) {
+            const int nkb = (tn * BN + BN) / TBK;
+            int nseg = f.kseg > 0 ? (nkb + f.kseg - 1) / f.kseg : 1;
+            if (q.ntn * nseg > QTC_MAXCU) nseg = 1;
+            for (int sg = 0; sg < nseg; sg++) {
+                if (q.ncu >= QTC_MAXCU) return E_TOO_LARGE;
+                q.cu_tn[q.ncu] = (unsigned short)tn;
+                q.cu_kb0[q.ncu] = (unsigned short)(nkb * sg / nseg);
+                q.cu_kb1[q.ncu] = (unsigned short)(nkb * (sg + 1) / nseg);
+                q.ncu++;
+            }
+        }
         long nrb = (mm + TBM - 1) / TBM;
-        long nunits = (nrb + CSZ - 1) / CSZ * (long)f.nblk * q.ntn;
+        long nunits = (nrb + CSZ - 1) / CSZ * (long)f.nblk * q.ncu;
         prof_begin(PK_QFORM, stream);
         if (!two)
             rc = pair ? launch_tc<256, false, true>(mXh, mXl, mWh, mWl, q, nunits, stream)
@@ -1353,7 +1380,21 @@ int qform_build(const Config &cfg, const DevSea &sea, bool fp16, void *stream_) 
         bmap[3 * b + 1] = field == 3 ? 1 - kh : kh;
         bmap[3 * b + 2] = field;
     }
-    int rc = tcform_split(g_q.tc, coef, bmap, 8, 4, npad, fp16, stream);
+    // fp16: the cross products in the hi accumulator over K segments of at
+    // most 8 blocks (512 terms), so that the FP32 accumulation keeps their
+    // bits, and two TMEM buffers that hide each unit's epilogue (4096
+    // components at 1e6 points: the same cycles per step with 8, 16, 32 or 64
+    // blocks, the largest error against FP64 3.3e-6, 4.3e-6, 6.4e-6, 1.3e-5;
+    // the second accumulator over the whole K range, 5.1e-6 and 7 % more
+    // cycles).  CFDWM_QFORM_TWO_ACC=1 restores that arrangement,
+    // CFDWM_QFORM_KSEG sets the segment length.
+    const char *e2 = std::getenv("CFDWM_QFORM_TWO_ACC");
+    const bool one_acc = fp16 && !(e2 && e2[0] == '1');
+    int rc = tcform_split(g_q.tc, coef, bmap, 8, 4, npad, fp16, stream, one_acc);
+    if (one_acc) {
+        const char *ek = std::getenv("CFDWM_QFORM_KSEG");
+        g_q.tc.kseg = ek ? std::atoi(ek) : 8;
+    }
     cudaFree(coef);
     cudaFree(d_in);
     if (rc) return rc;

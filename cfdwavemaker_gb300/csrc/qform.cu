@@ -616,10 +616,11 @@ struct QTC {
     float *out;              // [rows][nout] accumulated with atomics
     int fp16;
     int *err;
-    // column units: column tile cu_tn[u] over the K blocks [cu_kb0[u], cu_kb1[u])
-    // (a long K range of the upper triangle cut into segments, each with its
-    // own accumulation and epilogue)
-    int ncu;
+    // column units per block: with seg = 0 unit u is column tile u over its
+    // whole upper-triangle K range; with seg = 1 it is column tile cu_tn[u]
+    // over the K blocks [cu_kb0[u], cu_kb1[u]) (a long K range cut into
+    // segments, each with its own accumulation and epilogue)
+    int ncu, seg;
     unsigned short cu_tn[QTC_MAXCU], cu_kb0[QTC_MAXCU], cu_kb1[QTC_MAXCU];
 };
 
@@ -677,9 +678,15 @@ __device__ __forceinline__ bool tile_of(const QTC &a, long nru, long t, int cran
     ti.rb = ru * CS + crank;
     ti.blk = ct / a.ncu;
     const int cu = ct % a.ncu;
-    ti.tn = a.cu_tn[cu];
-    ti.kb0 = a.cu_kb0[cu];
-    ti.kb1 = a.cu_kb1[cu];                      // upper triangle: i < m0 + BN
+    if (a.seg) {
+        ti.tn = a.cu_tn[cu];
+        ti.kb0 = a.cu_kb0[cu];
+        ti.kb1 = a.cu_kb1[cu];
+    } else {
+        ti.tn = cu;
+        ti.kb0 = 0;
+        ti.kb1 = (cu * BN + BN) / TBK;          // upper triangle: i < m0 + BN
+    }
     return true;
 }
 
@@ -1287,17 +1294,23 @@ int tcform_eval(TcForm &f, const DevSea &sea, long n, const double *x, const dou
         q.out = out + (long)f.nout * b; q.fp16 = f.fp16 ? 1 : 0; q.err = f.err;
         // column units: each column tile's upper-triangle K range, cut into
         // segments of at most f.kseg K blocks when the form asks for it
-        q.ncu = 0;
-        for (int tn = 0; tn < q.ntn; tn++) {
-            const int nkb = (tn * BN + BN) / TBK;
-            int nseg = f.kseg > 0 ? (nkb + f.kseg - 1) / f.kseg : 1;
-            if (q.ntn * nseg > QTC_MAXCU) nseg = 1;
-            for (int sg = 0; sg < nseg; sg++) {
-                if (q.ncu >= QTC_MAXCU) return E_TOO_LARGE;
-                q.cu_tn[q.ncu] = (unsigned short)tn;
-                q.cu_kb0[q.ncu] = (unsigned short)(nkb * sg / nseg);
-                q.cu_kb1[q.ncu] = (unsigned short)(nkb * (sg + 1) / nseg);
-                q.ncu++;
+        // (a column tile keeps its whole range where its segments would not
+        // fit the table: at most QTC_MAXCU / ntn segments per tile)
+        q.ncu = q.ntn;
+        q.seg = 0;
+        if (f.kseg > 0 && q.ntn <= QTC_MAXCU) {
+            q.ncu = 0;
+            q.seg = 1;
+            for (int tn = 0; tn < q.ntn; tn++) {
+                const int nkb = (tn * BN + BN) / TBK;
+                int nseg = (nkb + f.kseg - 1) / f.kseg;
+                if (q.ntn * nseg > QTC_MAXCU) nseg = 1;
+                for (int sg = 0; sg < nseg; sg++) {
+                    q.cu_tn[q.ncu] = (unsigned short)tn;
+                    q.cu_kb0[q.ncu] = (unsigned short)(nkb * sg / nseg);
+                    q.cu_kb1[q.ncu] = (unsigned short)(nkb * (sg + 1) / nseg);
+                    q.ncu++;
+                }
             }
         }
         long nrb = (mm + TBM - 1) / TBM;

@@ -120,6 +120,27 @@ def test_tensor_core_fp16_split_wide(wm, torch):
         assert err <= TOL, (f, err)
 
 
+@pytest.mark.parametrize("env", [{"CFDWM_QFORM_KSEG": "1"}, {"CFDWM_QFORM_KSEG": "3"},
+                                 {"CFDWM_QFORM_TWO_ACC": "1"}])
+def test_tensor_core_fp16_accumulation_arrangements(wm, torch, env, monkeypatch):
+    """The fp16 split's other accumulation arrangements on 2048 components
+    (column tiles of 4 to 32 K blocks of 64): one accumulator over K segments
+    of 1 block and of at most 3 blocks (segments of 2 and 3 blocks in one
+    tile where its count does not divide by 3), and the second
+    accumulator for the cross products over the whole K range; each against
+    the plain FP32 form of the same sea and points (which is within a few 1e-7
+    of FP64)."""
+    for k, v in env.items():
+        monkeypatch.setenv(k, v)
+    txt = _sea(128, 16, 23)
+    _, _, _, got = _run(wm, torch, txt, 256, 1, True)
+    _, _, _, plain = _run(wm, torch, txt, 256, 0, True)
+    for f in range(4):
+        err = norm_rel_err(got[:, f], plain[:, f])
+        print(env, "field", f, "err", err)
+        assert err <= TOL, (f, err)
+
+
 def test_tensor_core_several_chunks(wm, torch):
     """More than one 65,536-row chunk: the operands of the next chunk are
     prepared on a second stream while the GEMM of the previous one runs."""

@@ -515,7 +515,6 @@ def run_qform(args):
         timed.launches = lib.cfdwm_kernel_launches() - l0
         return e0.elapsed_time(e1) / steps
 
-    chunk = min(R, 65536)
     plain_chunk = None
     for fp16 in (0, 1):
         name = "tc_fp16x3" if fp16 else "tc_bf16x3"
@@ -530,7 +529,8 @@ def run_qform(args):
             kt = C.c_double(0.0)
             nk = lib.cfdwm_profile_read(6, C.byref(kt))
             lib.cfdwm_profile_enable(0)
-            plain_chunk = out[:chunk].cpu().numpy().astype(np.float64)
+            # the rows the plain form wrote (the first `sub` rows)
+            plain_chunk = out[:sub].cpu().numpy().astype(np.float64)
             orow_t = torch.tensor(orows, device="cuda")
             od = [a[orow_t].contiguous() for a in d]
             oo = torch.zeros((orows.size, 4), device="cuda", dtype=torch.float32)
@@ -549,7 +549,7 @@ def run_qform(args):
         lib.cfdwm_profile_enable(0)
         o = out.cpu().numpy()
         ev64 = stats(o[orows], ref)
-        evp = stats(o[:chunk], plain_chunk)
+        evp = stats(o[:plain_chunk.shape[0]], plain_chunk)
         res["forms"][name] = {"ms": ms, "rows": R, "pts_per_s": R / (ms / 1e3),
                               "err_vs_fp64": ev64, "err_vs_plain_chunk": evp,
                               # the bar: the worse of the two references, per field
@@ -557,7 +557,7 @@ def run_qform(args):
                               "build_s": build_s, "gemm_launches": int(nk), "launches": int(timed.launches),
                               "gemm_ms_per_step": tot.value / max(1, args.steps), "clocks": clocks}
     res["accuracy_rows"] = {"fp64_oracle_rows": int(orows.size), "fields": names,
-                            "plain_chunk_rows": int(chunk),
+                            "plain_chunk_rows": int(plain_chunk.shape[0]),
                             "norm": "max and rms of |form - ref| over the rows / max |ref| over the same rows; "
                                     "rms_rel = rms(form - ref) / rms(ref)"}
     # end to end: host arrays in pinned memory, copies inside the timed region

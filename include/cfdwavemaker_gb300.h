@@ -183,7 +183,11 @@ CFDWM_EXPORT int cfdwm_parse_text(const char *text, double *scalars, double *com
  * at z0 = 0 -- eta2 and the Taylor-layer u2, v2, w2 of the pair cache
  * (Irregular.cpp:223-293, 975-1102) -- as quadratic forms over the phasor
  * vectors.  build: fp16 != 0 splits operands into fp16 hi/lo parts, else
- * bf16 hi/lo.  eval: device arrays x, y, t (n points), out [n][4] FP32;
+ * bf16 hi/lo.  The fp16 split sums its three products in one FP32
+ * accumulator over K segments of 8 blocks of 64 components (environment
+ * CFDWM_QFORM_KSEG at build: another segment length, 0 for whole column
+ * tiles; CFDWM_QFORM_TWO_ACC=1: a second accumulator for the cross products
+ * instead).  eval: device arrays x, y, t (n points), out [n][4] FP32;
  * method 0 plain FP32 CUDA cores, 1 tcgen05 tensor cores. */
 CFDWM_EXPORT int cfdwm_qform_build(int fp16);
 CFDWM_EXPORT int cfdwm_qform_eval(const double *x, const double *y, const double *t, long n, int method,

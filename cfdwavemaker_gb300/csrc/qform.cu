@@ -182,11 +182,13 @@ __global__ void k_qform_plain_from64(int npad, int nt, const double *coef, float
 }
 
 // B operand of the tensor-core form, split into hi and lo 16-bit parts.
-// For fp16 each column m is scaled by 2^e_m (column maximum near 2^14) and
-// the lo part by a further 2^11; colscale[b][m] holds 2^-e_m (1 for bf16).
-// The fp16 cross products go to their own accumulator: the tensor cores'
-// FP32 accumulation keeps few guard bits, and adding terms 2^-11 smaller to
-// the hi-hi sum lost them (1.5e-5 at N = 4096 against 7e-6 with two).
+// For fp16 each column m is scaled by 2^e_m (column maximum near 2^14);
+// colscale[b][m] holds 2^-e_m (1 for bf16).  The lo part is scaled by a
+// further lo_scale: 2^11 where the fp16 cross products go to their own
+// accumulator, 1 where they share the hi accumulator.  Sharing it over a long
+// K range loses their low bits (the tensor cores' FP32 accumulation keeps few
+// guard bits: 1.5e-5 at N = 4096 over whole column tiles); over K segments of
+// 512 terms it does not (3.3e-6, against 5.1e-6 with the second accumulator).
 template <typename T16>
 __global__ void k_qform_split(int npad, int fp16, double lo_scale, const double *coef, T16 *Whi, T16 *Wlo,
                               float *colscale) {
@@ -523,9 +525,10 @@ __global__ void k_qform_plain_sum(long rows, int nseg, const float *part, float 
 constexpr int TBM = 128, TBK = 64;
 // variants (TMEM holds 512 FP32 columns), all with N = 256 MMAs (measured:
 // M = 128, N = 128 MMAs kept the tensor pipe about 60% busy, N = 256 about 80%):
-//   bf16, one accumulator, two accumulator buffers, so that the epilogue of
-//   one tile hides behind the next tile's MMAs;
-//   fp16, hi and cross accumulators filling TMEM, one buffer;
+//   one accumulator, two accumulator buffers, so that the epilogue of one
+//   tile unit hides behind the next unit's MMAs (bf16, and fp16 with the
+//   cross products in the hi accumulator);
+//   fp16 with hi and cross accumulators filling TMEM, one buffer (TWO);
 // each on one SM (M = 128) or on a CTA pair (M = 256, cta_group::2: each CTA
 // holds its 128 rows of X and half of the W tile, so each SM stages and reads
 // half the W bytes; measured 3-10% faster than the one-SM form).
@@ -694,8 +697,8 @@ __device__ __forceinline__ bool tile_of(const QTC &a, long nru, long t, int cran
 // in flight), ...  Warp 0 streams the operand tiles through the stage ring
 // (continuously across tiles), one thread of warp 1 issues the MMAs into TMEM
 // accumulator buffer j % NBUF of its j-th tile, warps 2-9 drain it when its
-// MMAs complete: with two buffers (bf16) the epilogue of tile j overlaps the
-// MMAs of tile j + 1.
+// MMAs complete: with two buffers (one accumulator) the epilogue of tile j
+// overlaps the MMAs of tile j + 1.
 // Epilogue warp w reads TMEM lane quarter w % 4 (its 32 rows) and column half
 // (w - 2) / 4; it loads its rows' right-hand phasors Y, scaled by the column
 // scales, before it waits for the accumulator, so those loads (coalesced: Y is
@@ -884,7 +887,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_qform_tc(const __grid_constan
             const float *Yc = a.Y + ((long)yhalf * a.npad + c0) * a.ldy + (live ? row : 0);
             const float *cs = a.colscale + (long)ti.blk * a.npad + c0;
             if (TWO) {
-                // fp16, one accumulator buffer: read this warp's TMEM rows first
+                // hi and cross accumulators, one buffer: read this warp's TMEM rows first
                 // (hi + cross / 2^11, HC values a thread), release the buffer to
                 // the next tile's MMAs, then load Y (column-major: the warp's 32
                 // rows of a column are adjacent) and reduce meanwhile
@@ -934,7 +937,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_qform_tc(const __grid_constan
                 j++;
                 continue;
             }
-            // bf16, two accumulator buffers: Y times the column scales; the
+            // one accumulator, two buffers: Y times the column scales; the
             // first NSL chunks of 32 columns are loaded before the accumulator
             // is ready, the others one chunk ahead
             constexpr int NSL = NCH < 2 ? NCH : 2;

@@ -55,6 +55,9 @@ constexpr int GRIDP_NC = 2;
 constexpr int POINTV_NC = 12; // point table: Pu, Mu, Pv, Mv, Pw, Mw, Pp, Mp, kp, km, Xpp, Xzz
 constexpr float LOG2E_F = 1.4426950408889634f;
 constexpr long SPLIT_TARGET_BLOCKS = 4 * 152;   // blocks a column-pair launch aims for
+// batches of at most this many points take the few-point kernels (a block
+// per point, the components or pair rows over its threads)
+constexpr long FEW_POINTS = 256;
 constexpr double TWO_PI = 6.283185307179586476925286766559;
 constexpr double INV_TWO_PI = 0.15915494309189533576888376337251;
 
@@ -539,6 +542,60 @@ __global__ void __launch_bounds__(128) k_phasors(PhArgs a) {
     for (int q = 0; q < 5; q++) a.first[q * a.n + p] = (double)sm[q] - (double)cm[q];
 }
 
+// Few points (a scalar call, a short batch): one block per point, the
+// components spread over the threads, so that a point's N phasors are formed
+// in parallel instead of by one thread in turn.  The same records and
+// arithmetic per (point, component) as k_phasors; each thread's share of the
+// five first-order sums is Kahan-compensated in FP32 and the 128 shares are
+// added in FP64 (per point, not per component).
+__global__ void __launch_bounds__(128) k_phasors_few(PhArgs a) {
+    __shared__ double s_red[4][5];
+    const long p = blockIdx.x;
+    float2 off[2];
+    ff_split(-a.fx, off[0].x, off[0].y);
+    ff_split(-a.fy, off[1].x, off[1].y);
+    const double tp = a.t[p * a.st];
+    const float2 dx = ff_add(ff_from_double(a.x[p * a.sx]), off[0]);
+    const float2 dy = ff_add(ff_from_double(a.y[p * a.sy]), off[1]);
+    const float2 tt = ff_from_double(tp);
+    const double *P = a.phase;
+    const int cs = a.cstride;
+    const float rconst = a.trivial_ramp ? (float)d_freq_ramp(tp, P[4 * cs], P[5 * cs], P[6 * cs]) : 0.f;
+    float sm[5] = {0, 0, 0, 0, 0}, cm[5] = {0, 0, 0, 0, 0};
+    for (int i = threadIdx.x; i < a.npad; i += blockDim.x) {
+        const float *R = a.rec + (long)i * PH_REC;
+        float c = 0.f, sn = 0.f, r = 0.f;
+        if (i < a.ncomp) {
+            float2 ph = ff_add(ff_mul(R[0], R[1], dx.x, dx.y), ff_mul(R[2], R[3], dy.x, dy.y));
+            ph = ff_add(ph, ff_mul(R[4], R[5], tt.x, tt.y));
+            ph = ff_add(ph, make_float2(R[6], R[7]));
+            ff_sincos_poly(ff_reduce_2pi(ph), sn, c);
+            r = a.trivial_ramp ? rconst : (float)d_freq_ramp(tp, P[4 * cs + i], P[5 * cs + i], P[6 * cs + i]);
+            const float rc = r * c, rs = r * sn;
+            ph_kahan(sm[0], cm[0], rc * R[8]);
+            ph_kahan(sm[1], cm[1], rc * R[9]);
+            ph_kahan(sm[2], cm[2], rc * R[10]);
+            ph_kahan(sm[3], cm[3], rs * R[11]);
+            ph_kahan(sm[4], cm[4], rc * R[12]);
+        }
+        a.ph[(long)i * a.n + p] = make_float2(c, sn);
+        a.rr[(long)i * a.n + p] = r;
+    }
+    double v[5];
+#pragma unroll
+    for (int q = 0; q < 5; q++) {
+        v[q] = (double)sm[q] - (double)cm[q];
+        for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_down_sync(0xffffffffu, v[q], o);
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0)
+        for (int q = 0; q < 5; q++) s_red[warp][q] = v[q];
+    __syncthreads();
+    if (threadIdx.x < 5)
+        a.first[threadIdx.x * a.n + p] = ((s_red[0][threadIdx.x] + s_red[1][threadIdx.x]) + s_red[2][threadIdx.x]) +
+                                         s_red[3][threadIdx.x];
+}
+
 // ---------------------------------------------------------------------------
 // Pair-sum kernels
 // ---------------------------------------------------------------------------
@@ -859,6 +916,99 @@ __global__ void __launch_bounds__(128) k_pairs_points(PairArgs a) {
     out[3 * a.ncol + p] = sq;
 }
 
+// Few points, point mode: block (point p, slice y); thread t takes row
+// ii = t % TT of tile pair 8 g + t / TT for g = y, y + nslice, ... (TT = 16: 8
+// tile pairs a pass).  A row is summed over its mm as in k_pairs_points (the
+// depth factors of component m formed per term here, since no other point
+// shares them), diagonal tile pairs add the first-order term of component
+// I TT + ii, each thread's rows are Kahan-summed, and the block's 128 sums
+// are added in FP32 into slice y's partial sums ([nslice][4][n], summed in
+// order by k_sum_slices).
+template <int TT>
+__global__ void __launch_bounds__(128) k_pairs_points_few(PairArgs a, int ntp, int nslice) {
+    __shared__ float s_red[4][4];
+    const long p = blockIdx.x;
+    const float z = a.z0[p];
+    const float zk = z * LOG2E_F, zetak = -2.f * (z + a.depth) * LOG2E_F;
+    const int ii = threadIdx.x % TT;
+    constexpr int PER = 128 / TT;           // tile pairs a pass
+    float su = 0, cu = 0, sv = 0, cv = 0, sw = 0, cw = 0, sq = 0, cq = 0;
+    for (int g = blockIdx.y; g * PER < ntp; g += nslice) {
+        int tp = g * PER + threadIdx.x / TT;
+        if (tp >= ntp) continue;
+        int I = 0, M = 0;
+        if (a.pairs) {
+            while (tp >= a.ntile - I) { tp -= a.ntile - I; I++; }
+            M = I + tp;
+        } else {
+            I = M = tp;
+        }
+        const int i = I * TT + ii;
+        const float2 pi = a.ph[(long)i * a.ncol + p];
+        const float ri = a.rr[(long)i * a.ncol + p];
+        float Fi, Gi;
+        depth_fg(a.cf[CF_K * a.cstride + i], zk, zetak, Fi, Gi);
+        const float qi = a.cf[CF_Q * a.cstride + i];
+        const float2 pxz_i = make_float2(qi * Fi, qi * Gi);
+        if (a.pairs) {
+            const float *T = a.tab + tile_index(I, M, a.ntile) * (long)TT * TT * POINTV_NC;
+            float au = 0, av = 0, aw = 0, ap = 0, ax = 0, az = 0;
+            for (int mm = (M == I) ? ii : 0; mm < TT; mm++) {
+                const int m = M * TT + mm;
+                const float *e = T + (ii * TT + mm) * POINTV_NC;
+                const float4 c0 = *reinterpret_cast<const float4 *>(e);
+                const float4 c1 = *reinterpret_cast<const float4 *>(e + 4);
+                const float4 c2 = *reinterpret_cast<const float4 *>(e + 8);
+                const float2 pm = a.ph[(long)m * a.ncol + p];
+                float Fm_, Gm_;
+                depth_fg(a.cf[CF_K * a.cstride + m], zk, zetak, Fm_, Gm_);
+                const float qm = a.cf[CF_Q * a.cstride + m];
+                const float2 xm = make_float2(qm * Fm_, qm * Gm_);
+                const float cc = pi.x * pm.x, ss = pi.y * pm.y;
+                const float sc = pi.y * pm.x, cs = pi.x * pm.y;
+                const float cp = cc - ss, cmn = cc + ss, sp = sc + cs, smn = sc - cs;
+                float Fp, Gp, Fm, Gm;
+                depth_fg(c2.x, zk, zetak, Fp, Gp);
+                depth_fg(c2.y, zk, zetak, Fm, Gm);
+                au = fmaf(c0.x * cp, Fp, fmaf(c0.y * cmn, Fm, au));
+                av = fmaf(c0.z * cp, Fp, fmaf(c0.w * cmn, Fm, av));
+                aw = fmaf(c1.x * sp, Gp, fmaf(c1.y * smn, Gm, aw));
+                ap = fmaf(c1.z * cp, Fp, fmaf(c1.w * cmn, Fm, ap));
+                ax = fmaf(c2.z, xm.x, ax);
+                az = fmaf(c2.w, xm.y, az);
+            }
+            ap = fmaf(pxz_i.x, ax, fmaf(pxz_i.y, az, ap));
+            kahan(su, cu, ri * au);
+            kahan(sv, cv, ri * av);
+            kahan(sw, cw, ri * aw);
+            kahan(sq, cq, ri * ap);
+        }
+        if (a.first && M == I) {
+            // first-order u1, v1, w1, dp1 and the linear dp2 diagonal terms of component i
+            const float au_ = a.cf[CF_AU * a.cstride + i] * ri;
+            kahan(su, cu, au_ * pxz_i.x * a.cf[CF_CT * a.cstride + i] * pi.x);
+            kahan(sv, cv, au_ * pxz_i.x * a.cf[CF_ST * a.cstride + i] * pi.x);
+            kahan(sw, cw, au_ * pxz_i.y * pi.y);
+            float pp = a.cf[CF_AP * a.cstride + i] * pxz_i.x * pi.x;
+            if (a.pairs)
+                pp += a.cf[CF_X1 * a.cstride + i] * pxz_i.x + a.cf[CF_Z1 * a.cstride + i] * pxz_i.y;
+            kahan(sq, cq, ri * pp);
+        }
+    }
+    float v[4] = {su - cu, sv - cv, sw - cw, sq - cq};
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+    for (int f = 0; f < 4; f++) {
+        for (int o = 16; o > 0; o >>= 1) v[f] += __shfl_down_sync(0xffffffffu, v[f], o);
+        if (lane == 0) s_red[warp][f] = v[f];
+    }
+    __syncthreads();
+    if (threadIdx.x < 4) {
+        const int f = threadIdx.x;
+        a.out[((long)blockIdx.y * 4 + f) * a.ncol + p] = ((s_red[0][f] + s_red[1][f]) + s_red[2][f]) + s_red[3][f];
+    }
+}
+
 // Elevation mode: eta2 from the pair cache (Irregular.cpp:223-293).  The
 // record holds A = P+M and B = M-P so that a pair contributes
 // c_i (A c_m) + s_i (B s_m); a row is c_i sum(A c_m) + s_i sum(B s_m).
@@ -997,7 +1147,10 @@ static int launch_phasors(const DevSea &sea, long n, const double *x, const doub
     a.ph = ph; a.rr = rr; a.first = first; a.rec = sea.d_phrec;
     if (!sea.d_phrec || npad > ((sea.npad_g + 255) / 256) * 256) return E_BAD_ARGUMENT;
     prof_begin(PK_PHASORS, stream);
-    k_phasors<<<(unsigned)((n + 127) / 128), 128, 0, stream>>>(a);
+    if (n <= FEW_POINTS)
+        k_phasors_few<<<(unsigned)n, 128, 0, stream>>>(a);
+    else
+        k_phasors<<<(unsigned)((n + 127) / 128), 128, 0, stream>>>(a);
     note_launch();
     prof_end(PK_PHASORS, stream);
     CK(cudaGetLastError());
@@ -1252,6 +1405,23 @@ static int launch_point_pairs(const DevSea &sea, long n, const float2 *ph, const
     a.depth = (float)sea.depth; a.out = out; a.pairs = pairs; a.first = 1;
     // few points: the tile-pair loop split over blockIdx.y, slices summed in order
     const int ntp = pairs ? sea.ntile_p * (sea.ntile_p + 1) / 2 : sea.ntile_p;
+    if (n <= FEW_POINTS && split_buf) {
+        // a block per (point, slice), the rows of 8 tile pairs over its threads
+        constexpr int PER = 128 / POINT_TILE;
+        const int npass = (ntp + PER - 1) / PER;
+        int nslice = (int)std::min<long>(npass, std::max<long>(1, split_cap / (4L * n)));
+        nslice = std::min(nslice, 65535);
+        a.out = split_buf;
+        prof_begin(PK_POINT_PAIRS, stream);
+        k_pairs_points_few<POINT_TILE><<<dim3((unsigned)n, (unsigned)nslice), 128, 0, stream>>>(a, ntp, nslice);
+        note_launch();
+        prof_end(PK_POINT_PAIRS, stream);
+        CK(cudaGetLastError());
+        k_sum_slices<<<(unsigned)((4 * n + 255) / 256), 256, 0, stream>>>(4 * n, nslice, split_buf, out);
+        note_launch();
+        CK(cudaGetLastError());
+        return OK;
+    }
     int nslice = point_slices(n, ntp);
     a.tp_per = (ntp + nslice - 1) / nslice;
     nslice = (ntp + a.tp_per - 1) / a.tp_per;
@@ -1300,7 +1470,7 @@ int irregular_eval(const DevSea &sea, long n, const double *x, const double *y, 
         float *eta2 = nullptr;
         if (((mask & 1) || smit) && sea.order == 2) {
             eta2 = L.sec + 4 * m;
-            rc = launch_eta_pairs(sea, m, L.ph, L.rr, eta2, stream);
+            rc = launch_eta_pairs(sea, m, L.ph, L.rr, eta2, stream, L.split, L.split_cap);
             if (rc) return rc;
         }
         if (smit) {

@@ -30,6 +30,7 @@ namespace cfdwm {
 
 static std::atomic<long> g_launches{0};
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+static void note_launches(long k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
 long launch_count() { return g_launches.load(); }
 
 // Per-kernel event profiler (single-threaded use: benchmarks and tests).
@@ -72,6 +73,8 @@ struct Model {
 };
 Model g_model;
 std::mutex g_model_mtx;
+// changes whenever the model is freed or rebuilt (scalar-call graphs compare it)
+std::atomic<long> g_model_gen{0};
 // status word of the last regular-wave set-up (cfdwm_regular_status)
 int g_last_reg_status = -1;
 
@@ -90,6 +93,16 @@ struct SurrUse {
 };
 SurrUse g_surr_use;
 
+// A scalar call's pipeline captured as a CUDA graph (one per thread and
+// quantity): the point is read from and the result written to a small pinned
+// buffer in place, so a call is one graph launch and one synchronisation.
+struct ScalarGraph {
+    cudaGraphExec_t exec = nullptr;
+    long gen = -1;                 // model generation at capture
+    const void *ws[3] = {nullptr, nullptr, nullptr};   // workspace bases at capture
+    long launches = 0;             // kernels in the graph
+};
+
 // Per-thread execution context: stream, workspace and staging buffers.
 struct ThreadCtx {
     cudaStream_t own = nullptr;
@@ -102,7 +115,17 @@ struct ThreadCtx {
     long cap = 0;
     double kin[4] = {0, 0, 0, 0};
     std::string err;
+    Workspace api_ws;         // eval_api's scratch (clamped z, model outputs)
+    Workspace pt_out;         // the one-point pipeline's outputs [6]
+    double *h_pt = nullptr;   // pinned: x, y, z, t of a scalar call, then its result
+    ScalarGraph sg[6];
+    bool sg_off = false;      // capture failed once on this thread: launch by launch
     ~ThreadCtx() {
+        for (auto &g : sg)
+            if (g.exec) cudaGraphExecDestroy(g.exec);
+        if (h_pt) cudaFreeHost(h_pt);
+        workspace_free(pt_out);
+        workspace_free(api_ws);
         if (d_in) cudaFree(d_in);
         if (d_out) cudaFree(d_out);
         if (h_pin) cudaFreeHost(h_pin);
@@ -277,7 +300,7 @@ int eval_api(long n, const double *x, const double *y, const double *z, const do
     size_t need = sizeof(double) * (size_t)n * 10;
     Workspace &ws = t_ctx.ws;
     // irregular_eval uses the same thread workspace; keep a separate buffer
-    static thread_local Workspace api_ws;
+    Workspace &api_ws = t_ctx.api_ws;
     int rc = workspace_reserve(api_ws, need);
     if (rc) return rc;
     double *zc = (double *)api_ws.base, *f = zc + n, *fe = f + 5 * n;
@@ -442,6 +465,7 @@ int run_batch(const double *x, const double *y, const double *z, const double *t
 
 void free_model() {
     Model &M = g_model;
+    g_model_gen.fetch_add(1);
     qform_free();
     sea_free(M.sea);
     grid_free(M.grid);
@@ -521,11 +545,85 @@ int initialize_from_text(const std::string &text) {
             std::fprintf(stderr, "FentonStream: warning - Newton iteration did not fully converge.\n");
     }
     M.init = true;
+    g_model_gen.fetch_add(1);
+    return OK;
+}
+
+// The one-point pipeline of quantity q on the thread's pinned point buffer:
+// eval_api reads x, y, z, t from it and the row of q is copied back into its
+// fifth element.
+int scalar_pipeline(int q, cudaStream_t s) {
+    double *in = t_ctx.h_pt;
+    int rc = workspace_reserve(t_ctx.pt_out, sizeof(double) * 6);
+    if (rc) return rc;
+    double *out = (double *)t_ctx.pt_out.base;
+    rc = eval_api(1, in, in + 1, in + 2, in + 3, 1 << q, out, s);
+    if (rc) return rc;
+    k_copy_row<<<1, 256, 0, s>>>(1, out + q, in + 4);
+    note_launch();
+    CKR(cudaGetLastError());
+    return OK;
+}
+
+// Scalar calls of the wave types whose tables stay fixed after
+// wave_Initialize (irregular and regular waves; the s-grid ring changes with
+// every update) replay a graph of scalar_pipeline.  The graph is captured
+// after one plain run of the pipeline (which reserves the workspaces) and
+// captured again when the model was rebuilt or a workspace has moved.
+int scalar_graph(int q, double x, double y, double z, double t, double *v) {
+    ThreadCtx &c = t_ctx;
+    if (!c.h_pt) CKR(cudaMallocHost(&c.h_pt, sizeof(double) * 8));
+    cudaStream_t s = stream_of();
+    ScalarGraph &g = c.sg[q];
+    const long gen = g_model_gen.load();
+    double *in = c.h_pt;
+    in[0] = x; in[1] = y; in[2] = z; in[3] = t;
+    if (g.exec && g.gen == gen && g.ws[0] == c.ws.base && g.ws[1] == c.api_ws.base && g.ws[2] == c.pt_out.base) {
+        CKR(cudaGraphLaunch(g.exec, s));
+        CKR(cudaStreamSynchronize(s));
+        note_launches(g.launches);
+        *v = in[4];
+        return OK;
+    }
+    if (g.exec) {
+        cudaGraphExecDestroy(g.exec);
+        g.exec = nullptr;
+    }
+    // the plain run: its result is this call's, and it reserves the workspaces
+    int rc = scalar_pipeline(q, s);
+    if (rc) return rc;
+    CKR(cudaStreamSynchronize(s));
+    *v = in[4];
+    const long l0 = launch_count();
+    cudaGraph_t graph = nullptr;
+    bool ok = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) {
+        const int prc = scalar_pipeline(q, s);
+        ok = cudaStreamEndCapture(s, &graph) == cudaSuccess && prc == OK && graph;
+    }
+    const long captured = launch_count() - l0;
+    note_launches(-captured);               // captured, not launched
+    if (ok) ok = cudaGraphInstantiate(&g.exec, graph, 0) == cudaSuccess;
+    if (graph) cudaGraphDestroy(graph);
+    if (!ok) {
+        cudaGetLastError();
+        g.exec = nullptr;
+        c.sg_off = true;
+        return OK;
+    }
+    g.gen = gen;
+    g.ws[0] = c.ws.base; g.ws[1] = c.api_ws.base; g.ws[2] = c.pt_out.base;
+    g.launches = captured;
     return OK;
 }
 
 double scalar(int q, double x, double y, double z, double t) {
     if (!g_model.init) return 0.0;
+    const int wt = g_model.cfg.wavetype;
+    if ((wt == WT_IRREGULAR || wt == WT_REGULAR) && !t_ctx.user_set && !prof_on() && !t_ctx.sg_off) {
+        double v = 0.0;
+        return scalar_graph(q, x, y, z, t, &v) == OK ? v : 0.0;
+    }
     double *outs[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     double v = 0.0;
     outs[q] = &v;

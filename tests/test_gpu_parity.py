@@ -89,6 +89,27 @@ def test_scalar_entry_points(wm, case):
         assert lib.SurfaceElevation(0, 0, x, y, t) == vals[0]
 
 
+def test_scalar_calls_after_model_and_workspace_changes(wm):
+    """Scalar calls replay a per-thread capture of the one-point pipeline; it
+    must follow a re-initialised model and workspaces that a large batch has
+    regrown.  The reference's values at the golden points, each time."""
+    def check(g):
+        scale = {name: max(np.max(np.abs(g["api_" + name])), 1e-30) for name in API}
+        for i in range(0, g["pt_x"].size, max(1, g["pt_x"].size // 6)):
+            x, y, z, t = (float(g["pt_" + k][i]) for k in "xyzt")
+            got = {"SurfElev": wm.lib.wave_SurfElev(x, y, t), "VeloX": wm.lib.wave_VeloX(x, y, z, t),
+                   "VeloZ": wm.lib.wave_VeloZ(x, y, z, t), "DynPres": wm.lib.wave_DynPres(x, y, z, t)}
+            for name, v in got.items():
+                assert abs(v - g["api_" + name][i]) / scale[name] <= TOL, (name, i)
+    ga, gb, gc = load_golden("config1_point"), load_golden("ramps_swl"), load_golden("stokes5")
+    for g in (ga, gb, gc, ga):
+        init(wm, g)
+        check(g)
+        n = 300_000
+        wm.velocity_batch(np.linspace(0, 300, n), np.zeros(n), np.full(n, -5.0), np.full(n, 1.0))
+        check(g)
+
+
 def test_t005_target_wave(wm):
     """The reference's own golden elevation series (tests/t005_focused_wave/targetwave.dat)."""
     g = load_golden("t005_focused")

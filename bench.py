@@ -412,6 +412,45 @@ def surrogate_summary(args, r):
     }
 
 
+def scalar_calls(ncall=1000, nthreads=8):
+    """The reference's own calling pattern: one point per call (wave_VeloX,
+    wave_SurfElev) on the 128-component point sea, host wall time per call
+    (each call returns its value, so it includes the device round trip), on
+    one host thread and on `nthreads` threads calling at once."""
+    import torch
+    from concurrent.futures import ThreadPoolExecutor
+    import cfdwavemaker_gb300 as cw
+    lib = cw.load()
+    cwd = os.getcwd()
+    os.chdir(tempfile.mkdtemp())
+    wm = cw.CFDwavemaker()
+    assert wm.initialize_text(point_config()) == 0, cw.last_error()
+    rng = np.random.default_rng(5)
+    xs = rng.uniform(0, 500, ncall); zs = rng.uniform(-40, 0, ncall); ts = rng.uniform(0, 8, ncall)
+    res = {}
+    for name, call in (("wave_VeloX", lambda i: lib.wave_VeloX(xs[i], 0.0, zs[i], ts[i])),
+                       ("wave_SurfElev", lambda i: lib.wave_SurfElev(xs[i], 0.0, ts[i]))):
+        for i in range(20):
+            call(i)
+        t0 = time.perf_counter()
+        for i in range(ncall):
+            call(i)
+        res[name + "_us_per_call"] = (time.perf_counter() - t0) / ncall * 1e6
+
+    def work(k):
+        for i in range(k * 250, k * 250 + 250):
+            lib.wave_VeloX(xs[i % ncall], 0.0, zs[i % ncall], ts[i % ncall])
+    with ThreadPoolExecutor(nthreads) as ex:
+        list(ex.map(work, range(nthreads)))
+        t0 = time.perf_counter()
+        list(ex.map(work, range(2 * nthreads)))
+        res["wave_VeloX_calls_per_s_%d_threads" % nthreads] = 2 * nthreads * 250 / (time.perf_counter() - t0)
+    wm.cleanup()
+    os.chdir(cwd)
+    torch.cuda.synchronize()
+    return res
+
+
 def other_workloads(args):
     """Short runs of the other workloads for the default line (single GPU, no
     CPU baselines; each has its own --workload run with the full record): the
@@ -429,6 +468,7 @@ def other_workloads(args):
                     "clocks": r["clocks"], "kernels": r["prof"]}
         if "pressure_ms" in r:
             out[key]["with_pressure_ms_per_step"] = r["pressure_ms"]
+    out["scalar_calls"] = scalar_calls()
     a = argparse.Namespace(**vars(args))
     a.workload, a.steps, a.warmup = "regular", 3, 2
     r = run_regular(a)

@@ -118,7 +118,7 @@ struct ThreadCtx {
     Workspace api_ws;         // eval_api's scratch (clamped z, model outputs)
     Workspace pt_out;         // the one-point pipeline's outputs [6]
     double *h_pt = nullptr;   // pinned: x, y, z, t of a scalar call, then its result
-    ScalarGraph sg[6];
+    ScalarGraph sg[7];        // quantities 0-5 (wave_SurfElev ... wave_nhPres), 6: wave_Kinematics
     bool sg_off = false;      // capture failed once on this thread: launch by launch
     ~ThreadCtx() {
         for (auto &g : sg)
@@ -551,9 +551,11 @@ int initialize_from_text(const std::string &text) {
 
 // The one-point pipeline of quantity q on the thread's pinned point buffer:
 // eval_api reads x, y, z, t from it and the row of q is copied back into its
-// fifth element.
+// fifth element (q = 6: the eta, u, v, w record of wave_Kinematics into the
+// fifth to eighth).
 int scalar_pipeline(int q, cudaStream_t s) {
     double *in = t_ctx.h_pt;
+    if (q == 6) return eval_api(1, in, in + 1, in + 2, in + 3, 15, nullptr, s, in + 4);
     int rc = workspace_reserve(t_ctx.pt_out, sizeof(double) * 6);
     if (rc) return rc;
     double *out = (double *)t_ctx.pt_out.base;
@@ -571,6 +573,7 @@ int scalar_pipeline(int q, cudaStream_t s) {
 // after one plain run of the pipeline (which reserves the workspaces) and
 // captured again when the model was rebuilt or a workspace has moved.
 int scalar_graph(int q, double x, double y, double z, double t, double *v) {
+    const int nv = q == 6 ? 4 : 1;          // values of the result
     ThreadCtx &c = t_ctx;
     if (!c.h_pt) CKR(cudaMallocHost(&c.h_pt, sizeof(double) * 8));
     cudaStream_t s = stream_of();
@@ -582,7 +585,7 @@ int scalar_graph(int q, double x, double y, double z, double t, double *v) {
         CKR(cudaGraphLaunch(g.exec, s));
         CKR(cudaStreamSynchronize(s));
         note_launches(g.launches);
-        *v = in[4];
+        for (int k = 0; k < nv; k++) v[k] = in[4 + k];
         return OK;
     }
     if (g.exec) {
@@ -593,7 +596,7 @@ int scalar_graph(int q, double x, double y, double z, double t, double *v) {
     int rc = scalar_pipeline(q, s);
     if (rc) return rc;
     CKR(cudaStreamSynchronize(s));
-    *v = in[4];
+    for (int k = 0; k < nv; k++) v[k] = in[4 + k];
     const long l0 = launch_count();
     cudaGraph_t graph = nullptr;
     bool ok = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
@@ -700,6 +703,12 @@ double *wave_Kinematics(double x, double y, double z, double t) {
     k[0] = k[1] = k[2] = k[3] = 0.0;
     int wt = g_model.cfg.wavetype;
     if (!g_model.init || (wt != WT_IRR_SGRID && wt != WT_IRREGULAR)) return k;
+    if (wt == WT_IRREGULAR && !t_ctx.user_set && !prof_on() && !t_ctx.sg_off) {
+        double v[4];
+        if (scalar_graph(6, x, y, z, t, v) == OK)
+            for (int q = 0; q < 4; q++) k[q] = v[q];
+        return k;
+    }
     double *outs[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     run_batch(&x, &y, &z, &t, 1, outs, 15, 0.0, nullptr, k);
     return k;

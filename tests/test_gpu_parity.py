@@ -92,8 +92,9 @@ def test_scalar_entry_points(wm, case):
 def test_scalar_calls_after_model_and_workspace_changes(wm):
     """Scalar calls replay a per-thread capture of the one-point pipeline; it
     must follow a re-initialised model and workspaces that a large batch has
-    regrown.  The reference's values at the golden points, each time."""
-    def check(g):
+    regrown.  The reference's values at the golden points, each time, and for
+    irregular waves wave_Kinematics' (eta, u, v, w) record of the point."""
+    def check(g, irregular):
         scale = {name: max(np.max(np.abs(g["api_" + name])), 1e-30) for name in API}
         for i in range(0, g["pt_x"].size, max(1, g["pt_x"].size // 6)):
             x, y, z, t = (float(g["pt_" + k][i]) for k in "xyzt")
@@ -101,13 +102,18 @@ def test_scalar_calls_after_model_and_workspace_changes(wm):
                    "VeloZ": wm.lib.wave_VeloZ(x, y, z, t), "DynPres": wm.lib.wave_DynPres(x, y, z, t)}
             for name, v in got.items():
                 assert abs(v - g["api_" + name][i]) / scale[name] <= TOL, (name, i)
-    ga, gb, gc = load_golden("config1_point"), load_golden("ramps_swl"), load_golden("stokes5")
-    for g in (ga, gb, gc, ga):
+            if irregular:
+                k = wm.kinematics(x, y, z, t)
+                for q, name in enumerate(("SurfElev", "VeloX", "VeloY", "VeloZ")):
+                    assert abs(k[q] - g["api_" + name][i]) / scale[name] <= TOL, ("Kinematics", name, i)
+    for case, irregular in (("config1_point", True), ("ramps_swl", True), ("stokes5", False),
+                            ("config1_point", True)):
+        g = load_golden(case)
         init(wm, g)
-        check(g)
+        check(g, irregular)
         n = 300_000
         wm.velocity_batch(np.linspace(0, 300, n), np.zeros(n), np.full(n, -5.0), np.full(n, 1.0))
-        check(g)
+        check(g, irregular)
 
 
 def test_t005_target_wave(wm):

@@ -334,13 +334,13 @@ def test_device_pointer_batch(wm):
 
 
 def test_empty_and_ragged_batches(wm):
-    """Batches of every size agree with the scalar calls.  Up to 256 points
+    """Batches of every size agree with the scalar calls.  Up to 512 points
     the few-point kernels run (a block per point), above it the per-thread
     ones; the two sum in different orders, so they agree to FP32 rounding."""
     g = load_golden("config1_point")
     init(wm, g)
     assert wm.lib.wave_SurfElev_batch(None, None, None, 0, None) == 0
-    for n in (1, 2, 127, 129, 256, 257, 1000):
+    for n in (1, 2, 127, 129, 512, 513, 1000):
         x = np.linspace(0, 300, n)
         eta = wm.surface_elevation_batch(x, np.zeros(n), np.full(n, 2.0))
         ref = np.array([wm.lib.wave_SurfElev(float(a), 0.0, 2.0) for a in x[:3]])
@@ -350,17 +350,17 @@ def test_empty_and_ragged_batches(wm):
 @pytest.mark.parametrize("case", ["config1_point", "short_spread", "ramps_swl", "linear"])
 def test_few_point_kernels_match_batch_kernels(wm, case):
     """The same points through the few-point kernels (batches of 1, 7 and
-    256 points) and through the per-thread kernels (one batch of all 300):
+    512 points) and through the per-thread kernels (one batch of all 600):
     every field within 1e-6 normwise of each other, and both within TOL of
     the reference's golden values where the golden points are used."""
     g = load_golden(case)
     init(wm, g)
     rng = np.random.default_rng(3)
     n0 = g["pt_x"].size
-    idx = np.concatenate([np.arange(n0), rng.choice(n0, max(0, 300 - n0), replace=True)])[:300]
+    idx = np.concatenate([np.arange(n0), rng.choice(n0, max(0, 600 - n0), replace=True)])[:600]
     x, y, z, t = (np.ascontiguousarray(g["pt_" + k][idx]) for k in "xyzt")
     whole = api_all(wm, x, y, z, t)
-    for size, count in ((1, 40), (7, 300), (256, 300)):
+    for size, count in ((1, 40), (7, 140), (512, 600)):
         parts = [api_all(wm, x[b:b + size], y[b:b + size], z[b:b + size], t[b:b + size])
                  for b in range(0, count, size)]
         got = [np.concatenate([pt[q] for pt in parts]) for q in range(len(API))]
@@ -368,7 +368,7 @@ def test_few_point_kernels_match_batch_kernels(wm, case):
         for q, name in enumerate(API):
             err = norm_rel_err(got[q], whole[q][:m])
             assert err <= 1e-6, (case, size, name, err)
-    sel = np.arange(min(n0, 300))
+    sel = np.arange(min(n0, 600))
     for q, name in enumerate(API):
         assert norm_rel_err(whole[q][sel], g["api_" + name][sel]) <= TOL, (case, name)
 

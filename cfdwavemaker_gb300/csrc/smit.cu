@@ -190,6 +190,8 @@ struct SmitArgs {
 };
 
 constexpr int SMIT_PARTS = 7;  // u, v, w, dp, d phi2/ds, eta_x, d phi1/ds
+// batches of at most this many points take k_smit_points_few
+constexpr long SMIT_FEW_POINTS = 512;
 
 template <int TT>
 __global__ void __launch_bounds__(128) k_smit_points(SmitArgs a) {
@@ -326,6 +328,110 @@ __global__ void __launch_bounds__(128) k_smit_points(SmitArgs a) {
     a.out[4 * a.ldo + p] = up ? 0.0 : (double)sq - cq;
 }
 
+// Few points (a scalar call, a short batch): block (point p, slice y), thread
+// t takes row ii = t % TT of tile pair 8 g + t / TT for g = y, y + nslice, ...
+// (TT = 16).  A row is the inner loop of k_smit_points for one point, with the
+// m tile's depth factors, phasors and ramps read per term (no other point
+// shares them); diagonal tile pairs add the first-order terms of component
+// I TT + ii.  Each thread's rows are Kahan-summed, the block's 128 sums added
+// in FP32 into slice y's seven partial sums, and k_smit_finish adds the
+// slices in order and forms the chain term.
+template <int TT>
+__global__ void __launch_bounds__(128) k_smit_points_few(SmitArgs a, int ntp, int nslice) {
+    __shared__ float s_red[4][SMIT_PARTS];
+    const long p = blockIdx.x;
+    const float h = a.depth;
+    const float zs = a.zs[p], sp1 = a.sp1[p];
+    const float zk = zs * L2E, zetak = -2.f * (zs + h) * L2E;
+    const int ii = threadIdx.x % TT;
+    constexpr int PER = 128 / TT;
+    float su = 0, cu = 0, sv = 0, cv = 0, sw = 0, cw = 0, sq = 0, cq = 0, sd = 0, cd = 0;
+    float ex = 0, cex = 0, ps = 0, cps = 0;
+    for (int g = blockIdx.y; g * PER < ntp; g += nslice) {
+        int tp = g * PER + threadIdx.x / TT;
+        if (tp >= ntp) continue;
+        int I = 0;
+        while (tp >= a.ntile - I) { tp -= a.ntile - I; I++; }
+        const int M = I + tp;
+        const int i = I * TT + ii;
+        const float2 pi = a.ph[(long)i * a.n + p];
+        const float ri = a.rr[(long)i * a.n + p];
+        float F, G;
+        sfg(a.cf[CF_K * a.cstride + i], zk, zetak, F, G);
+        const float qi = a.cf[CF_Q * a.cstride + i];
+        const float2 pfi = make_float2(qi * F, qi * G);
+        const float ki = a.cf[CF_K * a.cstride + i];
+        const float ai = a.cf[CF_KW * a.cstride + i];
+        const float A1 = ai * pfi.y, B1 = ai * ki * h * pfi.x;
+        const float *T = a.tab + stile(I, M, a.ntile) * (long)TT * TT * SNC;
+        float au = 0, av = 0, aw = 0, ap = 0, ad = 0;
+        for (int mm = (M == I) ? ii : 0; mm < TT; mm++) {
+            const int m = M * TT + mm;
+            const float *rec = T + (ii * TT + mm) * SNC;
+            const float4 c0 = *reinterpret_cast<const float4 *>(rec);
+            const float4 c1 = *reinterpret_cast<const float4 *>(rec + 4);
+            const float4 c2 = *reinterpret_cast<const float4 *>(rec + 8);
+            const float4 c3 = *reinterpret_cast<const float4 *>(rec + 12);
+            const float2 pm = a.ph[(long)m * a.n + p];
+            const float rm = a.rr[(long)m * a.n + p];
+            const float km = a.cf[CF_K * a.cstride + m], am = a.cf[CF_KW * a.cstride + m];
+            float Fm_, Gm_;
+            sfg(km, zk, zetak, Fm_, Gm_);
+            const float qm = a.cf[CF_Q * a.cstride + m];
+            const float2 pfm = make_float2(qm * Fm_, qm * Gm_);
+            const float cc = pi.x * pm.x, ss = pi.y * pm.y, sc = pi.y * pm.x, cs = pi.x * pm.y;
+            const float cp = cc - ss, cmn = cc + ss, sp = sc + cs, smn = sc - cs;
+            float Fp, Gp, Fm, Gm;
+            sfg(c0.z, zk, zetak, Fp, Gp);
+            sfg(c0.w, zk, zetak, Fm, Gm);
+            const float A2 = am * pfm.y, B2 = am * km * h * pfm.x;
+            const float hpc = -c0.x * cp * Fp, hmc = -c0.y * cmn * Fm;
+            const float hps = c0.x * c0.z * Gp, hms = c0.y * c0.w * Gm;
+            float tu = c1.x * hpc + c1.y * hmc + sp1 * (c3.x * (A1 + A2) * cp + c3.y * (A1 - A2) * cmn);
+            float tv = c1.z * hpc + c1.w * hmc;
+            float tw = -(hps * sp + hms * smn);
+            const float chch = pfi.x * pfm.x, shsh = pfi.y * pfm.y;
+            float tq = c2.x * hpc + c2.y * hmc + c2.z * (chch - shsh) * cp + c2.w * (chch + shsh) * cmn;
+            float td = -h * (hps * sp + hms * smn) + c3.z * ((A1 + A2) + sp1 * (B1 + B2)) * sp +
+                       c3.w * ((A1 - A2) + sp1 * (B1 - B2)) * smn;
+            au = fmaf(rm, tu, au);
+            av = fmaf(rm, tv, av);
+            aw = fmaf(rm, tw, aw);
+            ap = fmaf(rm, tq, ap);
+            ad = fmaf(rm, td, ad);
+        }
+        skahan(su, cu, ri * au);
+        skahan(sv, cv, ri * av);
+        skahan(sw, cw, ri * aw);
+        skahan(sq, cq, ri * ap);
+        skahan(sd, cd, ri * ad);
+        if (M == I) {
+            // first order of component i with the stretched profiles and the
+            // first-order sums of the chain term (Irregular.cpp:1638-1645, 1750-1760)
+            const float agk = a.cf[CF_AU * a.cstride + i] * ri;
+            const float ct = a.cf[CF_CT * a.cstride + i];
+            skahan(su, cu, agk * pfi.x * ct * pi.x);
+            skahan(sv, cv, agk * pfi.x * a.cf[CF_ST * a.cstride + i] * pi.x);
+            skahan(sw, cw, agk * pfi.y * pi.y);
+            skahan(sq, cq, a.cf[CF_AP * a.cstride + i] * ri * pfi.x * pi.x);
+            skahan(ex, cex, -a.cf[CF_A * a.cstride + i] * ki * ct * pi.y * ri);
+            skahan(ps, cps, agk * h * pfi.y * pi.y);
+        }
+    }
+    float v[SMIT_PARTS] = {su - cu, sv - cv, sw - cw, sq - cq, sd - cd, ex - cex, ps - cps};
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+    for (int f = 0; f < SMIT_PARTS; f++) {
+        for (int o = 16; o > 0; o >>= 1) v[f] += __shfl_down_sync(0xffffffffu, v[f], o);
+        if (lane == 0) s_red[warp][f] = v[f];
+    }
+    __syncthreads();
+    if (threadIdx.x < SMIT_PARTS) {
+        const int f = threadIdx.x;
+        a.part[((long)blockIdx.y * SMIT_PARTS + f) * a.n + p] = ((s_red[0][f] + s_red[1][f]) + s_red[2][f]) + s_red[3][f];
+    }
+}
+
 // The slices of a split launch summed in order, then the chain term.
 __global__ void k_smit_finish(long n, int nslice, const float *part, const float *chain, const float *above,
                               long ldo, double *out) {
@@ -378,10 +484,27 @@ int smit_eval(const DevSea &sea, long n, const double *z, const void *ph, const 
     a.ph = static_cast<const float2 *>(ph); a.rr = rr; a.cf = sea.d_cf; a.phase = sea.d_phase;
     a.zs = zs; a.sp1 = sp1; a.chain = chain; a.above = above;
     a.depth = (float)sea.depth; a.ldo = ldo; a.out = out;
+    const int ntp = sea.ntile_s * (sea.ntile_s + 1) / 2;
+    if (n <= SMIT_FEW_POINTS && split_buf) {
+        // a block per (point, slice), the rows of 8 tile pairs over its threads
+        constexpr int PER = 128 / ST;
+        const int npass = (ntp + PER - 1) / PER;
+        int nslice = (int)std::min<long>(npass, std::max<long>(1, split_cap / ((long)SMIT_PARTS * n)));
+        nslice = std::min(nslice, 65535);
+        a.part = split_buf;
+        prof_begin(PK_POINT_PAIRS, stream);
+        k_smit_points_few<ST><<<dim3((unsigned)n, (unsigned)nslice), 128, 0, stream>>>(a, ntp, nslice);
+        note_launch();
+        prof_end(PK_POINT_PAIRS, stream);
+        CK(cudaGetLastError());
+        k_smit_finish<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(n, nslice, split_buf, chain, above, ldo, out);
+        note_launch();
+        CK(cudaGetLastError());
+        return OK;
+    }
     // few points: the tile-pair loop split over blockIdx.y (as many blocks as
     // fill the GPU), the slices summed in order by k_smit_finish
     const long nblk = (n + 127) / 128;
-    const int ntp = sea.ntile_s * (sea.ntile_s + 1) / 2;
     const long target = 4L * 152;
     int nslice = nblk >= target ? 1 : (int)std::min<long>(ntp, (target + nblk - 1) / nblk);
     a.tp_per = (ntp + nslice - 1) / nslice;

@@ -71,6 +71,29 @@ def test_smit_random_points_vs_oracle(wm, case):
     assert np.any(above) and np.all(got[1][above] == 0.0) and np.all(got[4][above] == 0.0)
 
 
+def test_smit_few_point_kernel_matches_batch_kernel(wm):
+    """600 points in one batch (per-thread kernel) and in batches of 1, 9
+    and 100 (few-point kernel, a block per point): within 1e-6 normwise of
+    each other, and the batched ones within TOL of the FP64 oracle."""
+    g = load_golden("smit_spread")
+    cfg = golden_cfg(g)
+    rng = np.random.default_rng(10)
+    n = 600
+    x = rng.uniform(-150, 300, n)
+    y = rng.uniform(-80, 80, n)
+    z = rng.uniform(-cfg["depth"], 2.0, n)
+    t = rng.uniform(0.0, 30.0, n)
+    whole, ref = _check(wm, str(g["waveinput"]), x, y, z, t, "smit_spread whole")
+    for size, count in ((1, 30), (9, 600), (100, 600)):
+        parts = [_api(wm, x[b:b + size], y[b:b + size], z[b:b + size], t[b:b + size])
+                 for b in range(0, count, size)]
+        for q, name in enumerate(API):
+            got = np.concatenate([pt[q] for pt in parts])
+            m = got.size
+            assert norm_rel_err(got, whole[q][:m]) <= 1e-6, (size, name, norm_rel_err(got, whole[q][:m]))
+            assert norm_rel_err(got, ref[:m, q]) <= TOL, (size, name)
+
+
 def test_smit_short_crested_120(wm):
     from cfdwavemaker_gb300 import seastate as ss
     comps = ss.irregular_components(4.0, 10.0, 2.5, 24, 0.35, 1.7, 60.0, 123, ndir=5, spreading_s=5.0)

@@ -907,15 +907,36 @@ int cfdwm_qform_eval(const double *x, const double *y, const double *t, long n, 
     Model &M = g_model;
     if (!M.init) return E_NOT_INITIALIZED;
     if (n <= 0) return n == 0 ? OK : E_BAD_ARGUMENT;
-    if (!is_device(x) || !is_device(y) || !is_device(t) || !is_device(out)) {
-        set_error("cfdwm_qform_eval takes device arrays");
-        return E_BAD_ARGUMENT;
-    }
+    if (!x || !y || !t || !out) return E_BAD_ARGUMENT;
     cudaStream_t s = stream_of();
     int err = 0;
-    int rc = qform_eval(M.sea, n, x, y, t, method, out, s, method == 1 ? &err : nullptr);
-    if (rc) return rc;
-    if (!t_ctx.user_set || method == 1) CKR(cudaStreamSynchronize(s));
+    if (is_device(x) && is_device(y) && is_device(t) && is_device(out)) {
+        int rc = qform_eval(M.sea, n, x, y, t, method, out, s, method == 1 ? &err : nullptr);
+        if (rc) return rc;
+        if (!t_ctx.user_set || method == 1) CKR(cudaStreamSynchronize(s));
+    } else {
+        // host arrays: staged through the thread's device buffers in chunks
+        // of 2^20 points (x, y, t in, out [m][4] back); any mix of host and
+        // device arrays is accepted
+        const long chunk = 1L << 20;
+        int rc = ensure_cap(std::min(n, chunk));
+        if (rc) return rc;
+        const long cap = t_ctx.cap;
+        double *din = t_ctx.d_in;
+        float *dout = reinterpret_cast<float *>(t_ctx.d_out);
+        const double *src[3] = {x, y, t};
+        for (long b = 0; b < n; b += chunk) {
+            const long m = std::min(chunk, n - b);
+            for (int q = 0; q < 3; q++)
+                CKR(cudaMemcpyAsync(din + q * cap, src[q] + b, sizeof(double) * m, cudaMemcpyDefault, s));
+            int e = 0;
+            rc = qform_eval(M.sea, m, din, din + cap, din + 2 * cap, method, dout, s, method == 1 ? &e : nullptr);
+            if (rc) return rc;
+            err = err ? err : e;
+            CKR(cudaMemcpyAsync(out + 4 * b, dout, sizeof(float) * 4 * m, cudaMemcpyDefault, s));
+        }
+        CKR(cudaStreamSynchronize(s));
+    }
     if (err) {
         set_error("tensor-core kernel: a bounded wait expired (code " + std::to_string(err) + ")");
         return E_CUDA;

@@ -141,6 +141,29 @@ def test_tensor_core_fp16_accumulation_arrangements(wm, torch, env, monkeypatch)
         assert err <= TOL, (f, err)
 
 
+@pytest.mark.parametrize("method", [0, 1])
+def test_host_arrays(wm, torch, method):
+    """Host arrays (pageable NumPy and pinned, and a mix with device arrays)
+    give the device-array results: staged through the library's device
+    buffers, 70,001 points (more than one 65,536-row chunk)."""
+    txt = _sea(12, 4, 31)
+    n = 70001
+    x, y, t, want = _run(wm, torch, txt, n, method, True, seed=12)
+    out = np.zeros((n, 4), dtype=np.float32)
+    rc = wm.lib.cfdwm_qform_eval(cw._ptr(x), cw._ptr(y), cw._ptr(t), n, method, cw._ptr(out))
+    assert rc == 0, cw.last_error()
+    scale = np.max(np.abs(want), axis=0)
+    assert np.all(np.max(np.abs(out - want), axis=0) <= 1e-6 * scale)
+    dx = torch.tensor(x, device="cuda:0", dtype=torch.float64)
+    py = torch.from_numpy(y).pin_memory()
+    pout = torch.zeros((n, 4), dtype=torch.float32).pin_memory()
+    torch.cuda.synchronize()
+    rc = wm.lib.cfdwm_qform_eval(cw._ptr(dx), cw._ptr(py), cw._ptr(t), n, method, cw._ptr(pout))
+    assert rc == 0, cw.last_error()
+    assert np.all(np.max(np.abs(pout.numpy() - want), axis=0) <= 1e-6 * scale)
+    assert wm.lib.cfdwm_qform_eval(None, cw._ptr(y), cw._ptr(t), n, method, cw._ptr(out)) != 0
+
+
 def test_tensor_core_several_chunks(wm, torch):
     """More than one 65,536-row chunk: the operands of the next chunk are
     prepared on a second stream while the GEMM of the previous one runs."""

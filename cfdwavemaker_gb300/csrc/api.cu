@@ -117,6 +117,7 @@ struct ThreadCtx {
     std::string err;
     Workspace api_ws;         // eval_api's scratch (clamped z, model outputs)
     Workspace pt_out;         // the one-point pipeline's outputs [6]
+    Workspace qf_stage;       // the precision form's staging of host arrays
     double *h_pt = nullptr;   // pinned: x, y, z, t of a scalar call, then its result
     ScalarGraph sg[7];        // quantities 0-5 (wave_SurfElev ... wave_nhPres), 6: wave_Kinematics
     bool sg_off = false;      // capture failed once on this thread: launch by launch
@@ -125,6 +126,7 @@ struct ThreadCtx {
             if (g.exec) cudaGraphExecDestroy(g.exec);
         if (h_pt) cudaFreeHost(h_pt);
         workspace_free(pt_out);
+        workspace_free(qf_stage);
         workspace_free(api_ws);
         if (d_in) cudaFree(d_in);
         if (d_out) cudaFree(d_out);
@@ -915,15 +917,15 @@ int cfdwm_qform_eval(const double *x, const double *y, const double *t, long n, 
         if (rc) return rc;
         if (!t_ctx.user_set || method == 1) CKR(cudaStreamSynchronize(s));
     } else {
-        // host arrays: staged through the thread's device buffers in chunks
-        // of 2^20 points (x, y, t in, out [m][4] back); any mix of host and
-        // device arrays is accepted
-        const long chunk = 1L << 20;
-        int rc = ensure_cap(std::min(n, chunk));
+        // host arrays: staged through a device buffer of the thread in
+        // chunks of 2^22 points (x, y, t in, out [m][4] back: 40 bytes a
+        // point); any mix of host and device arrays is accepted
+        const long chunk = 1L << 22;
+        const long cap = std::min(n, chunk);
+        int rc = workspace_reserve(t_ctx.qf_stage, (size_t)cap * (3 * sizeof(double) + 4 * sizeof(float)));
         if (rc) return rc;
-        const long cap = t_ctx.cap;
-        double *din = t_ctx.d_in;
-        float *dout = reinterpret_cast<float *>(t_ctx.d_out);
+        double *din = (double *)t_ctx.qf_stage.base;
+        float *dout = reinterpret_cast<float *>(din + 3 * cap);
         const double *src[3] = {x, y, t};
         for (long b = 0; b < n; b += chunk) {
             const long m = std::min(chunk, n - b);

@@ -188,8 +188,8 @@ CFDWM_EXPORT int cfdwm_parse_text(const char *text, double *scalars, double *com
  * CFDWM_QFORM_KSEG at build: another segment length, 0 for whole column
  * tiles; CFDWM_QFORM_TWO_ACC=1: a second accumulator for the cross products
  * instead).  eval: arrays x, y, t (n points), out [n][4] FP32, in device
- * or host memory (host arrays are staged through device buffers in chunks of
- * 2^20 points); method 0 plain FP32 CUDA cores, 1 tcgen05 tensor cores. */
+ * or host memory (host arrays are staged through a device buffer in chunks of
+ * 2^22 points, 40 bytes a point); method 0 plain FP32 CUDA cores, 1 tcgen05 tensor cores. */
 CFDWM_EXPORT int cfdwm_qform_build(int fp16);
 CFDWM_EXPORT int cfdwm_qform_eval(const double *x, const double *y, const double *t, long n, int method,
                                   float *out);

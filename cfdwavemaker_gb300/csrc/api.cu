@@ -599,15 +599,26 @@ int scalar_graph(int q, double x, double y, double z, double t, double *v) {
     if (rc) return rc;
     CKR(cudaStreamSynchronize(s));
     for (int k = 0; k < nv; k++) v[k] = in[4 + k];
-    const long l0 = launch_count();
     cudaGraph_t graph = nullptr;
     bool ok = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
     if (ok) {
         const int prc = scalar_pipeline(q, s);
         ok = cudaStreamEndCapture(s, &graph) == cudaSuccess && prc == OK && graph;
     }
-    const long captured = launch_count() - l0;
-    note_launches(-captured);               // captured, not launched
+    // the kernels of the graph: counted by the launch counter at capture,
+    // though not launched then, and at every replay
+    long captured = 0;
+    if (ok) {
+        size_t nn = 0;
+        ok = cudaGraphGetNodes(graph, nullptr, &nn) == cudaSuccess;
+        std::vector<cudaGraphNode_t> nodes(nn);
+        if (ok && nn) ok = cudaGraphGetNodes(graph, nodes.data(), &nn) == cudaSuccess;
+        for (size_t k = 0; ok && k < nn; k++) {
+            cudaGraphNodeType ty;
+            if (cudaGraphNodeGetType(nodes[k], &ty) == cudaSuccess && ty == cudaGraphNodeTypeKernel) captured++;
+        }
+        note_launches(-captured);
+    }
     if (ok) ok = cudaGraphInstantiate(&g.exec, graph, 0) == cudaSuccess;
     if (graph) cudaGraphDestroy(graph);
     if (!ok) {

@@ -231,13 +231,13 @@ def test_tensor_core_fp16_split_component_ramps(wm, torch):
 
 
 @pytest.mark.parametrize("fp16", [True, False])
-@pytest.mark.parametrize("n", [333, 1000, 70001])
+@pytest.mark.parametrize("n", [1, 333, 1000, 70001])
 def test_tensor_core_pair_and_single_forms_agree(wm, torch, fp16, n):
     """The GEMM on CTA pairs (cta_group::2, M = 256) and on single CTAs
     (M = 128) gives the same sums: every 128-row block runs the same K
     sequence, and only the order of the per-tile atomic adds into each output
     (not fixed even between two runs) differs, so the bar is a few FP32
-    roundings, 1e-6 normwise.  Row counts of 3, 8 and 547 row blocks (two
+    roundings, 1e-6 normwise.  Row counts of 1, 3, 8 and 547 row blocks (two
     chunks) leave a row block past the last row in the last pair."""
     txt = _sea(40, 8, 37)
     outs = {}

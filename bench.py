@@ -403,6 +403,8 @@ def surrogate_summary(args, r):
         "steps": sl["surrogate_steps"],
         "plain_every_step": sl["plain_every_step"],
         "tensor_core_every_step": r["tc_every_step"],
+        # the learned update with its plain steps on the tensor-core s-grid form
+        "tensor_core_plain_steps": r["surrogate_tc_plain"],
         "tol_1e-3": dict(t3, speedup_vs_plain=t3["nodes_per_s"] / plain),
         "max_err_eta": r["accuracy"]["network"]["max_eta"], "max_err_u": r["accuracy"]["network"]["max_u"],
         "max_err_first_order_only": {"eta": r["accuracy"]["first_order_only"]["max_eta"],

@@ -29,7 +29,7 @@ def _compile(src):
     obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
     path = os.path.join(CSRC, src)
     deps = [path, os.path.join(CSRC, "cfdwm.h"), os.path.join(CSRC, "sgrid_geom.cuh"), os.path.join(CSRC, "ffmath.cuh"),
-            os.path.join(CSRC, "tc05.cuh"),
+            os.path.join(CSRC, "tc05.cuh"), os.path.join(CSRC, "ramp.cuh"),
             os.path.join(os.path.dirname(HERE), "include", "cfdwavemaker_gb300.h")]
     if os.path.exists(obj) and all(os.path.getmtime(obj) >= os.path.getmtime(d) for d in deps):
         return obj, ""

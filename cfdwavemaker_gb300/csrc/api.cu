@@ -11,6 +11,7 @@
 // multiplied by Ramp::ramp(t, x, y), the non-hydrostatic pressure of the
 // irregular sea is ramp * (dp - rho g eta).
 #include "cfdwm.h"
+#include "ramp.cuh"
 #include "../../include/cfdwavemaker_gb300.h"
 
 #include <cuda_runtime.h>
@@ -199,27 +200,7 @@ __global__ void k_clamp_z(long n, const double *z, double depth, double *zc) {
     if (p < n) zc[p] = fmax(-depth, z[p]);
 }
 
-// Ramp::ramp (Utils.cpp:42-68) times the selected rows of f[nf][n].
-struct RampDev {
-    int init, flags;
-    double lim[12];
-};
-__device__ double d_ramp(const RampDev &r, double t, double x, double y) {
-    if (!r.init) return 1.0;
-    double v[6] = {t, t, x, x, y, y};
-    double m = 1.0;
-    for (int q = 0; q < 6; q++) {
-        double rq = 1.0;
-        if (r.flags & (1 << q)) {
-            double a = (v[q] - r.lim[2 * q]) / (r.lim[2 * q + 1] - r.lim[2 * q]);
-            rq = (q & 1) ? fmax(fmin(1. - a, 1.), 0.) : fmax(fmin(a, 1.), 0.);
-        }
-        m = (q == 0) ? rq : fmin(m, rq);
-    }
-    return m;
-}
-
-// Irregular wave types 1/5 and regular 21 finish here: out rows
+// Irregular wave types 1 and 5 finish here: out rows
 // 0 SurfElev, 1 VeloX, 2 VeloY, 3 VeloZ, 4 DynPres, 5 nhPres.  sgp: the
 // s-grid holds the dynamic pressure (row 4 of its query).
 // The API rows of the model outputs: out[6][n] (eta, u, v, w, dp, nhpres;
@@ -238,7 +219,8 @@ __global__ void k_finish(long n, int wavetype, int sgp, RampDev r, double rho, d
         // f = [5][n] eta, u, v, w, dp of Irregular::*
         for (int q = 0; q < 5; q++) v[q] = f[q * n + p];
         v[5] = f[4 * n + p] - rho * g * f[0 * n + p];
-    } else if (wavetype == WT_IRR_SGRID) {
+    } else {
+        // WT_IRR_SGRID (regular waves write their rows in their own kernel)
         // f = [4][n] query at the clamped z (sgp: [5][n] with the pressure),
         // fe = [4][n] query at z = 0.  Without a pressure field the
         // reference's 0.0 (CFDwavemaker.cpp:1808-1812, 1815-1891); with one,
@@ -249,11 +231,6 @@ __global__ void k_finish(long n, int wavetype, int sgp, RampDev r, double rho, d
         v[3] = f[3 * n + p];
         v[4] = sgp ? f[4 * n + p] : 0.0;
         v[5] = sgp ? f[4 * n + p] - rho * g * f[0 * n + p] : 0.0;
-    } else {
-        // f = [5][n] eta, u, v, w, p_nh of the regular theory
-        for (int q = 0; q < 4; q++) v[q] = f[q * n + p];
-        v[4] = 0.0;
-        v[5] = f[4 * n + p];
     }
     if (ramped)
         for (int q = 0; q < 6; q++) v[q] *= rr;
@@ -298,6 +275,10 @@ int eval_api(long n, const double *x, const double *y, const double *z, const do
     if (!M.init) return E_NOT_INITIALIZED;
     if (n <= 0) return OK;
     int wt = M.cfg.wavetype;
+    RampDev rd = ramp_dev(M.cfg.ramp);
+    // regular waves: one kernel clamps z, evaluates, applies the ramp and
+    // writes the rows and records
+    if (wt == WT_REGULAR) return regular_eval(M.reg, M.cfg, n, x, y, z, t, rd, out, kin, s);
     // scratch: clamped z [n], model outputs [5][n] and [4][n]
     size_t need = sizeof(double) * (size_t)n * 10;
     Workspace &ws = t_ctx.ws;
@@ -309,7 +290,6 @@ int eval_api(long n, const double *x, const double *y, const double *z, const do
     k_clamp_z<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, z, M.cfg.depth, zc);
     note_launch();
     CKR(cudaGetLastError());
-    RampDev rd = ramp_dev(M.cfg.ramp);
     if (wt == WT_IRREGULAR) {
         int mask = 0;
         if (want & (1 | 32)) mask |= 1;
@@ -327,9 +307,6 @@ int eval_api(long n, const double *x, const double *y, const double *z, const do
         rc = grid_query(M.grid, n, x, y, zc, t, f, s);
         if (rc) return rc;
         fe = f;
-    } else if (wt == WT_REGULAR) {
-        rc = regular_eval(M.reg, M.cfg, n, x, y, zc, t, f, s);
-        if (rc) return rc;
     } else {
         return E_UNSUPPORTED;
     }

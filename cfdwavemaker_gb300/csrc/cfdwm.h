@@ -329,8 +329,13 @@ struct DevRegular {
 int regular_build(const Config &cfg, DevRegular &r, void *stream);
 void regular_free(DevRegular &r);
 // out [5][n] FP64: eta, u, v, w, nhpres (no ramp); z is used as given.
+struct RampDev;
+// The API rows ([6][n]: wave_SurfElev .. wave_nhPres) and/or the
+// wave_Kinematics records ([n][4]) of regular waves in one pass: z clamped at
+// the seabed, the ramp applied.
 int regular_eval(const DevRegular &r, const Config &cfg, long n, const double *x,
-                 const double *y, const double *z, const double *t, double *out, void *stream);
+                 const double *y, const double *z, const double *t, const RampDev &ramp, double *rows,
+                 double *kin, void *stream);
 int regular_solution(const DevRegular &r, double *dst, int cap, void *stream);
 
 // ---------------------------------------------------------------------------

@@ -16,6 +16,7 @@
 // cosh(j k y)/cosh(j k d) from two exponentials raised to the j-th power.
 #include "cfdwm.h"
 #include "ffmath.cuh"
+#include "ramp.cuh"
 
 #include <cuda_runtime.h>
 #include <cmath>
@@ -352,7 +353,10 @@ __global__ void __launch_bounds__(128) k_fenton_solve(RegIn in, double *sol, dou
 struct EvalArgs {
     long n;
     const double *x, *y, *z, *t;
-    double *out;        // [5][n]
+    double *rows;       // [6][n] API rows (wave_SurfElev .. wave_nhPres), or null
+    double *kin;        // [n][4] wave_Kinematics records, or null
+    RampDev ramp;
+    float2 nd;          // -depth as a float pair (the z clamp)
     const float *cf;    // [4][MAXN]: U, W, E, Q harmonic coefficients in FP32
     int N, finite;
     float2 P[6];        // k cos th, k sin th, -k c, -x0, -y0, -t0 as float pairs
@@ -367,6 +371,14 @@ struct EvalArgs {
 // once on the host), the coordinates are split into float pairs by integer
 // operations, the phase is formed in float-float and reduced, the sums are
 // FP32, and the outputs are widened to double exactly by integer operations.
+// e^x through the SFU's base-2 exponential (relative error a few 1e-7; the
+// arguments here are at most 0 and at least -2kh - a few)
+__device__ __forceinline__ float reg_exp(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x * 1.4426950408889634f));
+    return y;
+}
+
 __global__ void __launch_bounds__(128) k_regular_eval(EvalArgs a) {
     __shared__ float cU[MAXN], cW[MAXN], cE[MAXN], cQ[MAXN];
     for (int j = threadIdx.x; j < MAXN; j += blockDim.x) {
@@ -385,7 +397,7 @@ __global__ void __launch_bounds__(128) k_regular_eval(EvalArgs a) {
     float2 kx = ff_add(ff_mul(a.P[0].x, a.P[0].y, dx.x, dx.y), ff_mul(a.P[1].x, a.P[1].y, dy.x, dy.y));
     kx = ff_add(kx, ff_mul(a.P[2].x, a.P[2].y, dt.x, dt.y));
     float s1, c1;
-    sincosf(ff_reduce_2pi(kx), &s1, &c1);
+    ff_sincos_poly(ff_reduce_2pi(kx), s1, c1);
     const int N = a.N;
     // elevation: sum_j E_j cos(j kx)
     float cj = c1, sj = s1, eta = 0.f;
@@ -395,17 +407,18 @@ __global__ void __launch_bounds__(128) k_regular_eval(EvalArgs a) {
         cj = cn; sj = sn;
     }
     const float etao = eta + a.F[6];
-    // velocity sums with depth ratios
-    const float2 zf = ff_from_double(a.z[p]);
+    // velocity sums with depth ratios, z clamped at the seabed (max(-d, z))
+    float2 zf = ff_from_double(a.z[p]);
+    if (zf.x < a.nd.x || (zf.x == a.nd.x && zf.y < a.nd.y)) zf = a.nd;
     float su = 0.f, sw = 0.f;
     if (a.finite) {
         const float kd = a.F[3];
         const float ky = a.F[0] * ((zf.x + a.F[4]) + zf.y);
-        const float e1 = expf(ky - kd), e2 = expf(-2.f * ky), e3 = expf(-2.f * kd);
-        float p1 = 1.f, p2 = 1.f, p3 = 1.f;
+        const float e1 = reg_exp(ky - kd), e2 = reg_exp(-2.f * ky);
+        float p1 = 1.f, p2 = 1.f;
         cj = c1; sj = s1;
         for (int j = 0; j < N; j++) {
-            p1 *= e1; p2 *= e2; p3 *= e3;
+            p1 *= e1; p2 *= e2;
             // cosh(j ky)/cosh(j kd) = e^{j(ky-kd)} (1 + e^{-2 j ky}) q_j, q_j = 1/(1+e^{-2 j kd})
             float ch = p1 * (1.f + p2) * cQ[j];
             float shh = p1 * (1.f - p2) * cQ[j];
@@ -416,7 +429,7 @@ __global__ void __launch_bounds__(128) k_regular_eval(EvalArgs a) {
         }
     } else {
         const float ky = a.F[0] * ((zf.x + a.F[5]) + zf.y);
-        const float e1 = expf(ky);
+        const float e1 = reg_exp(ky);
         float p1 = 1.f;
         cj = c1; sj = s1;
         for (int j = 0; j < N; j++) {
@@ -428,15 +441,23 @@ __global__ void __launch_bounds__(128) k_regular_eval(EvalArgs a) {
         }
     }
     const float U = a.F[7] + su;
-    a.out[0 * a.n + p] = d_from_float(etao);
-    a.out[1 * a.n + p] = d_from_float(a.F[1] * U);
-    a.out[2 * a.n + p] = d_from_float(a.F[2] * U);
-    a.out[3 * a.n + p] = d_from_float(sw);
     // p_nh = rho (R - g (eta + d - z0) - q'^2 / 2), q'^2 = (U_osc - ubar)^2 + w^2;
     // F[8] = R - g (d - z0), and the elevation includes z0
     const float up = su - a.F[9];
     const float q2 = fmaf(up, up, sw * sw);
-    a.out[4 * a.n + p] = d_from_float(a.F[11] * (fmaf(-a.F[10], etao, a.F[8]) - 0.5f * q2));
+    // the API rows: eta, u, v, w, the dynamic pressure (0.0 for regular
+    // waves, as in the reference) and p_nh, times the ramp where one is set
+    // (FP64 multiplies only then: the FP64 rate is a small fraction of FP32's)
+    double v[6] = {d_from_float(etao), d_from_float(a.F[1] * U), d_from_float(a.F[2] * U), d_from_float(sw), 0.0,
+                   d_from_float(a.F[11] * (fmaf(-a.F[10], etao, a.F[8]) - 0.5f * q2))};
+    if (a.ramp.init) {
+        const double rr = d_ramp(a.ramp, a.t[p], a.x[p], a.y[p]);
+        for (int q = 0; q < 6; q++) v[q] *= rr;
+    }
+    if (a.rows)
+        for (int q = 0; q < 6; q++) a.rows[q * a.n + p] = v[q];
+    if (a.kin)
+        for (int q = 0; q < 4; q++) a.kin[4 * p + q] = v[q];
 }
 
 // ----------------------------- host side ---------------------------------
@@ -503,12 +524,15 @@ void regular_free(DevRegular &r) {
 }
 
 int regular_eval(const DevRegular &r, const Config &cfg, long n, const double *x, const double *y,
-                 const double *z, const double *t, double *out, void *stream_) {
+                 const double *z, const double *t, const RampDev &ramp, double *rows, double *kin,
+                 void *stream_) {
     cudaStream_t stream = (cudaStream_t)stream_;
     if (n <= 0) return OK;
     if (!r.d_cf) return E_NOT_INITIALIZED;
     EvalArgs a;
-    a.n = n; a.x = x; a.y = y; a.z = z; a.t = t; a.out = out; a.cf = r.d_cf;
+    a.n = n; a.x = x; a.y = y; a.z = z; a.t = t; a.rows = rows; a.kin = kin; a.cf = r.d_cf;
+    a.ramp = ramp;
+    ff_split(-cfg.depth, a.nd.x, a.nd.y);
     a.N = r.N;
     a.finite = (cfg.depth > 0.0 && cfg.depth < 1e8) ? 1 : 0;
     const double k = r.head[0], c = r.head[1], cth = r.head[8], sth = r.head[9];

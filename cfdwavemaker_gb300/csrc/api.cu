@@ -102,7 +102,20 @@ struct ScalarGraph {
     long gen = -1;                 // model generation at capture
     const void *ws[3] = {nullptr, nullptr, nullptr};   // workspace bases at capture
     long launches = 0;             // kernels in the graph
+    // s-grid: the ring state the query's arguments hold (slots, time, fields, arrays)
+    int tstep = -1, nf = 0;
+    double t0 = 0.0;
+    const void *ring[2] = {nullptr, nullptr};
 };
+
+// whether graph g was captured for the current s-grid ring state (always true
+// for the other wave types)
+bool ring_matches(const ScalarGraph &g) {
+    const Model &M = g_model;
+    if (M.cfg.wavetype != WT_IRR_SGRID) return true;
+    return g.tstep == M.grid.tstep && g.t0 == M.grid.t0 && g.nf == M.grid.nf && g.ring[0] == M.grid.QIMG &&
+           g.ring[1] == M.grid.ETA;
+}
 
 // Per-thread execution context: stream, workspace and staging buffers.
 struct ThreadCtx {
@@ -546,11 +559,11 @@ int scalar_pipeline(int q, cudaStream_t s) {
     return OK;
 }
 
-// Scalar calls of the wave types whose tables stay fixed after
-// wave_Initialize (irregular and regular waves; the s-grid ring changes with
-// every update) replay a graph of scalar_pipeline.  The graph is captured
+// Scalar calls replay a graph of scalar_pipeline.  The graph is captured
 // after one plain run of the pipeline (which reserves the workspaces) and
-// captured again when the model was rebuilt or a workspace has moved.
+// captured again when the model was rebuilt, a workspace has moved, or (wave
+// type 5) the ring has moved on: its query takes the ring's slots and time as
+// arguments, so a graph serves the calls between two ring updates.
 int scalar_graph(int q, double x, double y, double z, double t, double *v) {
     const int nv = q == 6 ? 4 : 1;          // values of the result
     ThreadCtx &c = t_ctx;
@@ -560,7 +573,8 @@ int scalar_graph(int q, double x, double y, double z, double t, double *v) {
     const long gen = g_model_gen.load();
     double *in = c.h_pt;
     in[0] = x; in[1] = y; in[2] = z; in[3] = t;
-    if (g.exec && g.gen == gen && g.ws[0] == c.ws.base && g.ws[1] == c.api_ws.base && g.ws[2] == c.pt_out.base) {
+    if (g.exec && g.gen == gen && g.ws[0] == c.ws.base && g.ws[1] == c.api_ws.base && g.ws[2] == c.pt_out.base &&
+        ring_matches(g)) {
         CKR(cudaGraphLaunch(g.exec, s));
         CKR(cudaStreamSynchronize(s));
         note_launches(g.launches);
@@ -607,13 +621,14 @@ int scalar_graph(int q, double x, double y, double z, double t, double *v) {
     g.gen = gen;
     g.ws[0] = c.ws.base; g.ws[1] = c.api_ws.base; g.ws[2] = c.pt_out.base;
     g.launches = captured;
+    g.tstep = g_model.grid.tstep; g.t0 = g_model.grid.t0; g.nf = g_model.grid.nf;
+    g.ring[0] = g_model.grid.QIMG; g.ring[1] = g_model.grid.ETA;
     return OK;
 }
 
 double scalar(int q, double x, double y, double z, double t) {
     if (!g_model.init) return 0.0;
-    const int wt = g_model.cfg.wavetype;
-    if ((wt == WT_IRREGULAR || wt == WT_REGULAR) && !t_ctx.user_set && !prof_on() && !t_ctx.sg_off) {
+    if (!t_ctx.user_set && !prof_on() && !t_ctx.sg_off) {
         double v = 0.0;
         return scalar_graph(q, x, y, z, t, &v) == OK ? v : 0.0;
     }
@@ -693,7 +708,7 @@ double *wave_Kinematics(double x, double y, double z, double t) {
     k[0] = k[1] = k[2] = k[3] = 0.0;
     int wt = g_model.cfg.wavetype;
     if (!g_model.init || (wt != WT_IRR_SGRID && wt != WT_IRREGULAR)) return k;
-    if (wt == WT_IRREGULAR && !t_ctx.user_set && !prof_on() && !t_ctx.sg_off) {
+    if (!t_ctx.user_set && !prof_on() && !t_ctx.sg_off) {
         double v[4];
         if (scalar_graph(6, x, y, z, t, v) == OK)
             for (int q = 0; q < 4; q++) k[q] = v[q];

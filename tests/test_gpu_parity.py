@@ -232,6 +232,18 @@ def test_sgrid_vs_reference(wm, case, method):
             assert norm_rel_err(arr, g["s%d_api_%s" % (k, name)]) <= TOL, (k, name)
         e = wm.surface_elevation_batch(qx, qy, np.full_like(qx, qt))
         assert norm_rel_err(e, g["s%d_api_SurfElev" % k]) <= TOL
+        # scalar calls (captured per ring state: they must follow the updates)
+        for i in range(0, qx.size, max(1, qx.size // 5)):
+            x, y, z = float(qx[i]), float(qy[i]), float(qz[i])
+            for name, val in (("VeloX", wm.lib.wave_VeloX(x, y, z, qt)),
+                              ("VeloZ", wm.lib.wave_VeloZ(x, y, z, qt)),
+                              ("SurfElev", wm.lib.wave_SurfElev(x, y, qt))):
+                ref = g["s%d_api_%s" % (k, name)]
+                assert abs(val - ref[i]) <= TOL * np.max(np.abs(ref)), (k, name, i)
+            kin = wm.kinematics(x, y, z, qt)
+            for c in range(4):
+                ref = g["s%d_kin" % k][:, c]
+                assert abs(kin[c] - ref[i]) <= TOL * np.max(np.abs(ref)), (k, "Kinematics", c, i)
 
 
 def test_sgrid_tensor_core_method_vs_plain(wm):

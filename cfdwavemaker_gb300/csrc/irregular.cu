@@ -629,11 +629,10 @@ struct PairArgs {
 // Depth factors with the normaliser folded into the coefficients:
 //   F = exp(kz) (1 + exp(-2k(z+h))),  G = exp(kz) (1 - exp(-2k(z+h))).
 __device__ __forceinline__ void depth_fg(float k, float zk, float zetak, float &F, float &G) {
-    float e1 = ex2(k * zk);
-    float e2 = ex2(k * zetak);
-    float t = e1 * e2;
-    F = e1 + t;
-    G = e1 - t;
+    const float e1 = ex2(k * zk);
+    const float e2 = ex2(k * zetak);
+    F = fmaf(e1, e2, e1);       // e1 (1 + e2), one rounding
+    G = fmaf(-e1, e2, e1);      // e1 (1 - e2)
 }
 
 // Column mode: u, v, w (PR: and the phase terms of the pressure, with the
@@ -882,10 +881,12 @@ __global__ void __launch_bounds__(128) k_pairs_points(PairArgs a) {
                         float Fp, Gp, Fm, Gm;
                         depth_fg(c2.x, zk, zetak, Fp, Gp);
                         depth_fg(c2.y, zk, zetak, Fm, Gm);
-                        au = fmaf(c0.x * cp, Fp, fmaf(c0.y * cmn, Fm, au));
-                        av = fmaf(c0.z * cp, Fp, fmaf(c0.w * cmn, Fm, av));
-                        aw = fmaf(c1.x * sp, Gp, fmaf(c1.y * smn, Gm, aw));
-                        ap = fmaf(c1.z * cp, Fp, fmaf(c1.w * cmn, Fm, ap));
+                        // the phase-and-depth products once, then one FMA per coefficient
+                        const float A = cp * Fp, B = cmn * Fm, Cq = sp * Gp, D = smn * Gm;
+                        au = fmaf(c0.x, A, fmaf(c0.y, B, au));
+                        av = fmaf(c0.z, A, fmaf(c0.w, B, av));
+                        aw = fmaf(c1.x, Cq, fmaf(c1.y, D, aw));
+                        ap = fmaf(c1.z, A, fmaf(c1.w, B, ap));
                         ax = fmaf(c2.z, xm.x, ax);
                         az = fmaf(c2.w, xm.y, az);
                     }
@@ -977,10 +978,11 @@ __global__ void __launch_bounds__(128) k_pairs_points_few(PairArgs a, int ntp, i
                 float Fp, Gp, Fm, Gm;
                 depth_fg(c2.x, zk, zetak, Fp, Gp);
                 depth_fg(c2.y, zk, zetak, Fm, Gm);
-                au = fmaf(c0.x * cp, Fp, fmaf(c0.y * cmn, Fm, au));
-                av = fmaf(c0.z * cp, Fp, fmaf(c0.w * cmn, Fm, av));
-                aw = fmaf(c1.x * sp, Gp, fmaf(c1.y * smn, Gm, aw));
-                ap = fmaf(c1.z * cp, Fp, fmaf(c1.w * cmn, Fm, ap));
+                const float A = cp * Fp, B = cmn * Fm, Cq = sp * Gp, D = smn * Gm;
+                au = fmaf(c0.x, A, fmaf(c0.y, B, au));
+                av = fmaf(c0.z, A, fmaf(c0.w, B, av));
+                aw = fmaf(c1.x, Cq, fmaf(c1.y, D, aw));
+                ap = fmaf(c1.z, A, fmaf(c1.w, B, ap));
                 ax = fmaf(c2.z, xm.x, ax);
                 az = fmaf(c2.w, xm.y, az);
             }

@@ -56,9 +56,9 @@ __host__ __device__ inline long stile(int I, int M, int nt) { return (long)I * n
 
 // e^{kz} (1 +- e^{-2k(z+h)}): the profiles with the normaliser left out
 __device__ __forceinline__ void sfg(float k, float zk, float zetak, float &F, float &G) {
-    float e1 = sx2(k * zk), t = e1 * sx2(k * zetak);
-    F = e1 + t;
-    G = e1 - t;
+    const float e1 = sx2(k * zk), e2 = sx2(k * zetak);
+    F = fmaf(e1, e2, e1);       // e1 (1 + e2), one rounding
+    G = fmaf(-e1, e2, e1);      // e1 (1 - e2)
 }
 
 // Eq. 10 inverted for H with the Sharma-Dean alpha (Irregular.cpp:926-929, 954-957)

@@ -100,7 +100,7 @@ SurrUse g_surr_use;
 struct ScalarGraph {
     cudaGraphExec_t exec = nullptr;
     long gen = -1;                 // model generation at capture
-    const void *ws[3] = {nullptr, nullptr, nullptr};   // workspace bases at capture
+    const void *ws[2] = {nullptr, nullptr};   // workspace bases at capture
     long launches = 0;             // kernels in the graph
     // s-grid: the ring state the query's arguments hold (slots, time, fields, arrays)
     int tstep = -1, nf = 0;
@@ -130,16 +130,14 @@ struct ThreadCtx {
     double kin[4] = {0, 0, 0, 0};
     std::string err;
     Workspace api_ws;         // eval_api's scratch (clamped z, model outputs)
-    Workspace pt_out;         // the one-point pipeline's outputs [6]
     Workspace qf_stage;       // the precision form's staging of host arrays
-    double *h_pt = nullptr;   // pinned: x, y, z, t of a scalar call, then its result
+    double *h_pt = nullptr;   // pinned [16]: x, y, z, t of a scalar call, then its rows
     ScalarGraph sg[7];        // quantities 0-5 (wave_SurfElev ... wave_nhPres), 6: wave_Kinematics
     bool sg_off = false;      // capture failed once on this thread: launch by launch
     ~ThreadCtx() {
         for (auto &g : sg)
             if (g.exec) cudaGraphExecDestroy(g.exec);
         if (h_pt) cudaFreeHost(h_pt);
-        workspace_free(pt_out);
         workspace_free(qf_stage);
         workspace_free(api_ws);
         if (d_in) cudaFree(d_in);
@@ -310,6 +308,12 @@ int eval_api(long n, const double *x, const double *y, const double *z, const do
         if (want & 4) mask |= 4;
         if (want & 8) mask |= 8;
         if (want & (16 | 32)) mask |= 16;
+        // the combining pass writes the API rows itself (no finishing pass),
+        // except where the Smit theory's kernels write the velocity rows
+        if ((out || kin) && !(M.sea.smit && (mask & 30))) {
+            const ApiRows ar{rd, M.cfg.rho, M.cfg.gravity, x, y, t, out, kin};
+            return irregular_eval(M.sea, n, x, y, zc, t, mask, nullptr, ws, s, &ar);
+        }
         CKR(cudaMemsetAsync(f, 0, sizeof(double) * 5 * n, s));
         rc = irregular_eval(M.sea, n, x, y, zc, t, mask, f, ws, s);
         if (rc) return rc;
@@ -542,21 +546,13 @@ int initialize_from_text(const std::string &text) {
 }
 
 // The one-point pipeline of quantity q on the thread's pinned point buffer:
-// eval_api reads x, y, z, t from it and the row of q is copied back into its
-// fifth element (q = 6: the eta, u, v, w record of wave_Kinematics into the
-// fifth to eighth).
+// eval_api reads x, y, z, t from its first four elements and writes the six
+// API rows of the point (one value each) into the next six, where row q is
+// read back (q = 6: the eta, u, v, w record of wave_Kinematics there).
 int scalar_pipeline(int q, cudaStream_t s) {
     double *in = t_ctx.h_pt;
     if (q == 6) return eval_api(1, in, in + 1, in + 2, in + 3, 15, nullptr, s, in + 4);
-    int rc = workspace_reserve(t_ctx.pt_out, sizeof(double) * 6);
-    if (rc) return rc;
-    double *out = (double *)t_ctx.pt_out.base;
-    rc = eval_api(1, in, in + 1, in + 2, in + 3, 1 << q, out, s);
-    if (rc) return rc;
-    k_copy_row<<<1, 256, 0, s>>>(1, out + q, in + 4);
-    note_launch();
-    CKR(cudaGetLastError());
-    return OK;
+    return eval_api(1, in, in + 1, in + 2, in + 3, 1 << q, in + 4, s);
 }
 
 // Scalar calls replay a graph of scalar_pipeline.  The graph is captured
@@ -566,19 +562,19 @@ int scalar_pipeline(int q, cudaStream_t s) {
 // arguments, so a graph serves the calls between two ring updates.
 int scalar_graph(int q, double x, double y, double z, double t, double *v) {
     const int nv = q == 6 ? 4 : 1;          // values of the result
+    const int r0 = q == 6 ? 4 : 4 + q;      // where they are in the pinned buffer
     ThreadCtx &c = t_ctx;
-    if (!c.h_pt) CKR(cudaMallocHost(&c.h_pt, sizeof(double) * 8));
+    if (!c.h_pt) CKR(cudaMallocHost(&c.h_pt, sizeof(double) * 16));
     cudaStream_t s = stream_of();
     ScalarGraph &g = c.sg[q];
     const long gen = g_model_gen.load();
     double *in = c.h_pt;
     in[0] = x; in[1] = y; in[2] = z; in[3] = t;
-    if (g.exec && g.gen == gen && g.ws[0] == c.ws.base && g.ws[1] == c.api_ws.base && g.ws[2] == c.pt_out.base &&
-        ring_matches(g)) {
+    if (g.exec && g.gen == gen && g.ws[0] == c.ws.base && g.ws[1] == c.api_ws.base && ring_matches(g)) {
         CKR(cudaGraphLaunch(g.exec, s));
         CKR(cudaStreamSynchronize(s));
         note_launches(g.launches);
-        for (int k = 0; k < nv; k++) v[k] = in[4 + k];
+        for (int k = 0; k < nv; k++) v[k] = in[r0 + k];
         return OK;
     }
     if (g.exec) {
@@ -589,7 +585,7 @@ int scalar_graph(int q, double x, double y, double z, double t, double *v) {
     int rc = scalar_pipeline(q, s);
     if (rc) return rc;
     CKR(cudaStreamSynchronize(s));
-    for (int k = 0; k < nv; k++) v[k] = in[4 + k];
+    for (int k = 0; k < nv; k++) v[k] = in[r0 + k];
     cudaGraph_t graph = nullptr;
     bool ok = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
     if (ok) {
@@ -619,7 +615,7 @@ int scalar_graph(int q, double x, double y, double z, double t, double *v) {
         return OK;
     }
     g.gen = gen;
-    g.ws[0] = c.ws.base; g.ws[1] = c.api_ws.base; g.ws[2] = c.pt_out.base;
+    g.ws[0] = c.ws.base; g.ws[1] = c.api_ws.base;
     g.launches = captured;
     g.tstep = g_model.grid.tstep; g.t0 = g_model.grid.t0; g.nf = g_model.grid.nf;
     g.ring[0] = g_model.grid.QIMG; g.ring[1] = g_model.grid.ETA;

@@ -207,9 +207,12 @@ void workspace_free(Workspace &ws);
 // Evaluate irregular-sea kinematics at n points (device pointers, FP64 in).
 // mask bits: 1 eta, 2 u, 4 v, 8 w, 16 dp.  out is [5][n] FP64 (no ramp, no
 // clamp): the reference's Irregular::eta/u/v/w/dp.
+struct ApiRows;
+// api: when given (and the sea is not on the Smit theory), the combining pass
+// writes the API rows and records of api instead of out (which may be null).
 int irregular_eval(const DevSea &sea, long n, const double *x, const double *y,
                    const double *z, const double *t, int mask, double *out,
-                   Workspace &ws, void *stream);
+                   Workspace &ws, void *stream, const ApiRows *api = nullptr);
 
 // Workspace bytes irregular_eval needs for a batch of n points.
 size_t irregular_eval_scratch_bytes(const DevSea &sea, long n);

@@ -27,6 +27,7 @@
 //    a Kahan (sum, carry) pair per output.
 #include "cfdwm.h"
 #include "ffmath.cuh"
+#include "ramp.cuh"
 
 #include <cuda_runtime.h>
 #include <algorithm>
@@ -1130,17 +1131,34 @@ __global__ void k_prep_z(long n, const double *z, double swl, int order, float *
 
 // Irregular::eta/u/v/w/dp assembled from the pieces (Irregular.cpp:9-157).
 // out has row stride ldo (the full batch length).
+// With api.rows or api.kin set, the API rows and records are written here
+// (the finishing pass folded in) instead of out.
 __global__ void k_combine(long n, long ldo, int order, double swl, const double *z,
                           const double *first, const float *sec, const float *eta2, int mask,
-                          double *out) {
+                          double *out, ApiRows api) {
     long p = blockIdx.x * (long)blockDim.x + threadIdx.x;
     if (p >= n) return;
     double za = (order == 2) ? fmax(0.0, z[p] - swl) : 0.0;
-    if (mask & 1) out[0 * ldo + p] = swl + first[0 * n + p] + (eta2 ? (double)eta2[p] : 0.0);
-    if (mask & 2) out[1 * ldo + p] = (double)sec[0 * n + p] + first[1 * n + p] * za;
-    if (mask & 4) out[2 * ldo + p] = (double)sec[1 * n + p] + first[2 * n + p] * za;
-    if (mask & 8) out[3 * ldo + p] = (double)sec[2 * n + p] + first[3 * n + p] * za;
-    if (mask & 16) out[4 * ldo + p] = (double)sec[3 * n + p] + first[4 * n + p] * za;
+    double v[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    if (mask & 1) v[0] = swl + first[0 * n + p] + (eta2 ? (double)eta2[p] : 0.0);
+    if (mask & 2) v[1] = (double)sec[0 * n + p] + first[1 * n + p] * za;
+    if (mask & 4) v[2] = (double)sec[1 * n + p] + first[2 * n + p] * za;
+    if (mask & 8) v[3] = (double)sec[2 * n + p] + first[3 * n + p] * za;
+    if (mask & 16) v[4] = (double)sec[3 * n + p] + first[4 * n + p] * za;
+    if (!api.rows && !api.kin) {
+        for (int q = 0; q < 5; q++)
+            if (mask & (1 << q)) out[q * ldo + p] = v[q];
+        return;
+    }
+    v[5] = v[4] - api.rho * api.g * v[0];
+    if (api.ramp.init) {
+        const double rr = d_ramp(api.ramp, api.t[p], api.x[p], api.y[p]);
+        for (int q = 0; q < 6; q++) v[q] *= rr;
+    }
+    if (api.rows)
+        for (int q = 0; q < 6; q++) api.rows[q * ldo + p] = v[q];
+    if (api.kin)
+        for (int q = 0; q < 4; q++) api.kin[4 * p + q] = v[q];
 }
 
 }  // namespace
@@ -1461,7 +1479,7 @@ static int launch_point_pairs(const DevSea &sea, long n, const float2 *ph, const
 // POINT_TILE, the grid kernels tiles of GRID_TILE; the workspace is sized for
 // npad_g >= npad_p so both fit.
 int irregular_eval(const DevSea &sea, long n, const double *x, const double *y, const double *z,
-                   const double *t, int mask, double *out, Workspace &ws, void *stream_) {
+                   const double *t, int mask, double *out, Workspace &ws, void *stream_, const ApiRows *api) {
     cudaStream_t stream = (cudaStream_t)stream_;
     if (n <= 0) return OK;
     const long chunk = 1L << 18;
@@ -1496,9 +1514,16 @@ int irregular_eval(const DevSea &sea, long n, const double *x, const double *y, 
                                     L.split_cap);
             if (rc) return rc;
         }
+        ApiRows ar{};
+        if (api && !smit) {
+            ar = *api;
+            ar.x = api->x + b; ar.y = api->y + b; ar.t = api->t + b;
+            ar.rows = api->rows ? api->rows + b : nullptr;
+            ar.kin = api->kin ? api->kin + 4 * b : nullptr;
+        }
         k_combine<<<(unsigned)((m + 255) / 256), 256, 0, stream>>>(m, n, sea.order, sea.swl, z + b,
                                                                    L.first, L.sec, eta2, smit ? (mask & 1) : mask,
-                                                                   out + b);
+                                                                   out ? out + b : nullptr, ar);
         note_launch();
         CK(cudaGetLastError());
     }

@@ -1,6 +1,7 @@
 // Ramp::ramp (Utils.cpp:42-68): the minimum of up to six clamped linear
 // ramps in t, x and y, shared by the finishing pass of the API rows and the
-// regular-wave kernel, which writes its rows itself.
+// kernels that write the API rows themselves (regular waves; the irregular
+// sums' combining pass).
 #pragma once
 
 namespace cfdwm {
@@ -24,5 +25,16 @@ __device__ __forceinline__ double d_ramp(const RampDev &r, double t, double x, d
     }
     return m;
 }
+
+// The API rows written by a kernel that ends the evaluation: rows [6][ldo]
+// (wave_SurfElev .. wave_nhPres) and/or wave_Kinematics records [n][4], the
+// ramp at (x, y, t) applied where one is set, p_nh = dp - rho g eta.
+struct ApiRows {
+    RampDev ramp;
+    double rho, g;
+    const double *x, *y, *t;
+    double *rows;
+    double *kin;
+};
 
 }  // namespace cfdwm

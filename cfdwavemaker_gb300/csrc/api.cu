@@ -290,9 +290,24 @@ int eval_api(long n, const double *x, const double *y, const double *z, const do
     // regular waves: one kernel clamps z, evaluates, applies the ramp and
     // writes the rows and records
     if (wt == WT_REGULAR) return regular_eval(M.reg, M.cfg, n, x, y, z, t, rd, out, kin, s);
+    Workspace &ws = t_ctx.ws;
+    int mask = 0;
+    if (wt == WT_IRREGULAR) {
+        if (want & (1 | 32)) mask |= 1;
+        if (want & 2) mask |= 2;
+        if (want & 4) mask |= 4;
+        if (want & 8) mask |= 8;
+        if (want & (16 | 32)) mask |= 16;
+        // irregular waves: the seabed clamp in the height pass and the API
+        // rows written by the combining pass (no clamp or finishing pass),
+        // except where the Smit theory's kernels write the velocity rows
+        if ((out || kin) && !(M.sea.smit && (mask & 30))) {
+            const ApiRows ar{rd, M.cfg.rho, M.cfg.gravity, x, y, t, out, kin};
+            return irregular_eval(M.sea, n, x, y, z, t, mask, nullptr, ws, s, &ar);
+        }
+    }
     // scratch: clamped z [n], model outputs [5][n] and [4][n]
     size_t need = sizeof(double) * (size_t)n * 10;
-    Workspace &ws = t_ctx.ws;
     // irregular_eval uses the same thread workspace; keep a separate buffer
     Workspace &api_ws = t_ctx.api_ws;
     int rc = workspace_reserve(api_ws, need);
@@ -302,18 +317,6 @@ int eval_api(long n, const double *x, const double *y, const double *z, const do
     note_launch();
     CKR(cudaGetLastError());
     if (wt == WT_IRREGULAR) {
-        int mask = 0;
-        if (want & (1 | 32)) mask |= 1;
-        if (want & 2) mask |= 2;
-        if (want & 4) mask |= 4;
-        if (want & 8) mask |= 8;
-        if (want & (16 | 32)) mask |= 16;
-        // the combining pass writes the API rows itself (no finishing pass),
-        // except where the Smit theory's kernels write the velocity rows
-        if ((out || kin) && !(M.sea.smit && (mask & 30))) {
-            const ApiRows ar{rd, M.cfg.rho, M.cfg.gravity, x, y, t, out, kin};
-            return irregular_eval(M.sea, n, x, y, zc, t, mask, nullptr, ws, s, &ar);
-        }
         CKR(cudaMemsetAsync(f, 0, sizeof(double) * 5 * n, s));
         rc = irregular_eval(M.sea, n, x, y, zc, t, mask, f, ws, s);
         if (rc) return rc;

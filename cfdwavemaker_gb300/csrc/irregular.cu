@@ -1122,10 +1122,12 @@ WsLayout layout(long n, int npad, void *base) {
 }
 
 // z0 = min(0, z - swl) (order 2/1) or z - swl (order 0), as float
-__global__ void k_prep_z(long n, const double *z, double swl, int order, float *z0) {
+// clamp: the seabed clamp of the wave_* calls (z below -depth evaluated at
+// -depth), or 0 for the unclamped sums of cfdwm_irregular_fields
+__global__ void k_prep_z(long n, const double *z, double swl, int order, int clamp, double depth, float *z0) {
     long p = blockIdx.x * (long)blockDim.x + threadIdx.x;
     if (p >= n) return;
-    double zz = z[p] - swl;
+    double zz = (clamp ? fmax(-depth, z[p]) : z[p]) - swl;
     z0[p] = (float)(order == 0 ? zz : fmin(0.0, zz));
 }
 
@@ -1505,7 +1507,8 @@ int irregular_eval(const DevSea &sea, long n, const double *x, const double *y, 
                            stream);
             if (rc) return rc;
         } else if (mask & 30) {
-            k_prep_z<<<(unsigned)((m + 255) / 256), 256, 0, stream>>>(m, z + b, sea.swl, sea.order, L.z0);
+            k_prep_z<<<(unsigned)((m + 255) / 256), 256, 0, stream>>>(m, z + b, sea.swl, sea.order, api ? 1 : 0,
+                                                                  sea.depth, L.z0);
             note_launch();
             CK(cudaGetLastError());
             // the point table is padded to POINT_TILE; the phasor rows beyond

@@ -89,6 +89,29 @@ def test_scalar_entry_points(wm, case):
         assert lib.SurfaceElevation(0, 0, x, y, t) == vals[0]
 
 
+def test_few_point_kernels_large_sea(wm):
+    """The few-point kernels on a 1280-component short-crested sea (80 pair
+    tiles a side: 3240 tile pairs, so the slices of a few-point launch loop
+    over several passes): batches of 1 and 300 points against one batch of
+    all 600 (the per-thread kernels), every field within 1e-6 normwise."""
+    from cfdwavemaker_gb300 import seastate as ss
+    comps = ss.irregular_components(5.0, 11.0, 2.5, 80, 0.3, 1.8, 60.0, 77, ndir=16, spreading_s=8.0)
+    txt = ss.write_irregular(None, comps, 60.0, extrap=2)
+    assert wm.initialize_text(txt) == 0, cw.last_error()
+    rng = np.random.default_rng(5)
+    n = 600
+    x = rng.uniform(-200, 200, n); y = rng.uniform(-200, 200, n)
+    z = rng.uniform(-60.0, 2.0, n); t = rng.uniform(0, 50, n)
+    whole = api_all(wm, x, y, z, t)
+    for size, count in ((1, 12), (300, 600)):
+        parts = [api_all(wm, x[b:b + size], y[b:b + size], z[b:b + size], t[b:b + size])
+                 for b in range(0, count, size)]
+        for q, name in enumerate(API):
+            got = np.concatenate([pt[q] for pt in parts])
+            err = norm_rel_err(got, whole[q][:got.size])
+            assert err <= 1e-6, (size, name, err)
+
+
 def test_scalar_calls_after_model_and_workspace_changes(wm):
     """Scalar calls replay a per-thread capture of the one-point pipeline; it
     must follow a re-initialised model and workspaces that a large batch has

@@ -816,7 +816,9 @@ __global__ void k_sum_slices(long n, int nslice, const float *part, float *out) 
 
 // Point mode: u, v, w, dp at one height per thread, point-API mask
 // (u2/v2/w2/dp2 of the reference, with rho folded into the p records).
-template <int TT>
+// VEL: the velocity sums, PR: the pressure sums (a call that asks for one of
+// them does not pay for the other; rows not computed are 0).
+template <int TT, bool VEL, bool PR>
 __global__ void __launch_bounds__(128) k_pairs_points(PairArgs a) {
     extern __shared__ float4 smem4[];
     float *s_tab = reinterpret_cast<float *>(smem4);                        // TT*TT*12
@@ -883,19 +885,28 @@ __global__ void __launch_bounds__(128) k_pairs_points(PairArgs a) {
                         depth_fg(c2.x, zk, zetak, Fp, Gp);
                         depth_fg(c2.y, zk, zetak, Fm, Gm);
                         // the phase-and-depth products once, then one FMA per coefficient
-                        const float A = cp * Fp, B = cmn * Fm, Cq = sp * Gp, D = smn * Gm;
-                        au = fmaf(c0.x, A, fmaf(c0.y, B, au));
-                        av = fmaf(c0.z, A, fmaf(c0.w, B, av));
-                        aw = fmaf(c1.x, Cq, fmaf(c1.y, D, aw));
-                        ap = fmaf(c1.z, A, fmaf(c1.w, B, ap));
-                        ax = fmaf(c2.z, xm.x, ax);
-                        az = fmaf(c2.w, xm.y, az);
+                        const float A = cp * Fp, B = cmn * Fm;
+                        if (VEL) {
+                            const float Cq = sp * Gp, D = smn * Gm;
+                            au = fmaf(c0.x, A, fmaf(c0.y, B, au));
+                            av = fmaf(c0.z, A, fmaf(c0.w, B, av));
+                            aw = fmaf(c1.x, Cq, fmaf(c1.y, D, aw));
+                        }
+                        if (PR) {
+                            ap = fmaf(c1.z, A, fmaf(c1.w, B, ap));
+                            ax = fmaf(c2.z, xm.x, ax);
+                            az = fmaf(c2.w, xm.y, az);
+                        }
                     }
-                    ap = fmaf(pxz_i.x, ax, fmaf(pxz_i.y, az, ap));
-                    kahan(su, cu, ri * au);
-                    kahan(sv, cv, ri * av);
-                    kahan(sw, cw, ri * aw);
-                    kahan(sq, cq, ri * ap);
+                    if (VEL) {
+                        kahan(su, cu, ri * au);
+                        kahan(sv, cv, ri * av);
+                        kahan(sw, cw, ri * aw);
+                    }
+                    if (PR) {
+                        ap = fmaf(pxz_i.x, ax, fmaf(pxz_i.y, az, ap));
+                        kahan(sq, cq, ri * ap);
+                    }
                 }
             }
             if (a.first && M == I) {
@@ -905,14 +916,18 @@ __global__ void __launch_bounds__(128) k_pairs_points(PairArgs a) {
                     const float2 pm = s_ph[mm * 128 + threadIdx.x];
                     const float2 xm = s_pz[mm * 128 + threadIdx.x];
                     const float rm = a.rr[(long)m * a.ncol + p];
-                    const float au_ = a.cf[CF_AU * a.cstride + m] * rm;
-                    kahan(su, cu, au_ * xm.x * a.cf[CF_CT * a.cstride + m] * pm.x);
-                    kahan(sv, cv, au_ * xm.x * a.cf[CF_ST * a.cstride + m] * pm.x);
-                    kahan(sw, cw, au_ * xm.y * pm.y);
-                    float pp = a.cf[CF_AP * a.cstride + m] * xm.x * pm.x;
-                    if (a.pairs)
-                        pp += a.cf[CF_X1 * a.cstride + m] * xm.x + a.cf[CF_Z1 * a.cstride + m] * xm.y;
-                    kahan(sq, cq, rm * pp);
+                    if (VEL) {
+                        const float au_ = a.cf[CF_AU * a.cstride + m] * rm;
+                        kahan(su, cu, au_ * xm.x * a.cf[CF_CT * a.cstride + m] * pm.x);
+                        kahan(sv, cv, au_ * xm.x * a.cf[CF_ST * a.cstride + m] * pm.x);
+                        kahan(sw, cw, au_ * xm.y * pm.y);
+                    }
+                    if (PR) {
+                        float pp = a.cf[CF_AP * a.cstride + m] * xm.x * pm.x;
+                        if (a.pairs)
+                            pp += a.cf[CF_X1 * a.cstride + m] * xm.x + a.cf[CF_Z1 * a.cstride + m] * xm.y;
+                        kahan(sq, cq, rm * pp);
+                    }
                 }
             }
         }
@@ -1426,8 +1441,8 @@ int launch_pressure_kin(const DevSea &sea, double t, int nz, double *kin, cudaSt
 }
 
 static int launch_point_pairs(const DevSea &sea, long n, const float2 *ph, const float *rr,
-                              const float *z0, float *out, int pairs, cudaStream_t stream, float *split_buf,
-                              long split_cap) {
+                              const float *z0, float *out, int pairs, int mask, cudaStream_t stream,
+                              float *split_buf, long split_cap) {
     PairArgs a{};
     a.ncol = n; a.nl = 1; a.nlg = 1; a.ntile = sea.ntile_p; a.tab = sea.d_tab_point;
     a.ph = ph; a.rr = rr; a.cf = sea.d_cf; a.cstride = sea.npad_g; a.z0 = z0;
@@ -1459,13 +1474,31 @@ static int launch_point_pairs(const DevSea &sea, long n, const float2 *ph, const
         a.tp_per = ntp;
     }
     if (nslice > 1) a.out = split_buf;
-    size_t smem = sizeof(float) * POINT_TILE * POINT_TILE * POINTV_NC + 2 * sizeof(float2) * POINT_TILE * 128;
+    const size_t smem = sizeof(float) * POINT_TILE * POINT_TILE * POINTV_NC + 2 * sizeof(float2) * POINT_TILE * 128;
     // set once per process (thread-safe static initialisation)
-    static const cudaError_t attr = cudaFuncSetAttribute(k_pairs_points<POINT_TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)smem);
+    static const cudaError_t attr = [&] {
+        cudaError_t e = cudaFuncSetAttribute(k_pairs_points<POINT_TILE, true, true>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_pairs_points<POINT_TILE, true, false>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_pairs_points<POINT_TILE, false, true>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        return e;
+    }();
     CK(attr);
+    // the velocity sums only where u, v or w is asked for, the pressure sums
+    // only where dp is
+    const bool vel = (mask & 14) != 0, pr = (mask & 16) != 0;
+    const dim3 grid((unsigned)((n + 127) / 128), (unsigned)nslice);
     prof_begin(PK_POINT_PAIRS, stream);
-    k_pairs_points<POINT_TILE><<<dim3((unsigned)((n + 127) / 128), (unsigned)nslice), 128, smem, stream>>>(a);
+    if (vel && pr)
+        k_pairs_points<POINT_TILE, true, true><<<grid, 128, smem, stream>>>(a);
+    else if (vel)
+        k_pairs_points<POINT_TILE, true, false><<<grid, 128, smem, stream>>>(a);
+    else
+        k_pairs_points<POINT_TILE, false, true><<<grid, 128, smem, stream>>>(a);
     note_launch();
     prof_end(PK_POINT_PAIRS, stream);
     CK(cudaGetLastError());
@@ -1513,8 +1546,8 @@ int irregular_eval(const DevSea &sea, long n, const double *x, const double *y, 
             CK(cudaGetLastError());
             // the point table is padded to POINT_TILE; the phasor rows beyond
             // npad_p are never read by the point kernel
-            rc = launch_point_pairs(sea, m, L.ph, L.rr, L.z0, L.sec, sea.order != 0 ? 1 : 0, stream, L.split,
-                                    L.split_cap);
+            rc = launch_point_pairs(sea, m, L.ph, L.rr, L.z0, L.sec, sea.order != 0 ? 1 : 0, mask, stream,
+                                    L.split, L.split_cap);
             if (rc) return rc;
         }
         ApiRows ar{};

@@ -1096,18 +1096,44 @@ struct WsLayout {
     size_t bytes;
 };
 
-// Slices of the tile-pair loop for a point launch of n points: enough blocks
-// to fill the GPU (SPLIT_TARGET_BLOCKS) when the points alone give fewer.
-static int point_slices(long n, int ntp) {
-    const long nblk = (n + 127) / 128;
-    if (nblk >= SPLIT_TARGET_BLOCKS || ntp <= 1) return 1;
-    return (int)std::min<long>(ntp, (SPLIT_TARGET_BLOCKS + nblk - 1) / nblk);
+// Slices of the tile-pair loop for a launch of nblk blocks (per slice) on a
+// GPU with `slots` resident blocks: the fewest slices (at most maxs, and at
+// most one per tile pair) whose blocks fill the waves they start to 85 %, or
+// else the best filling.  A launch of 512 point blocks on 760 slots fills
+// 67 % of its one wave; 4 slices fill 90 % of three.
+static int wave_slices(long nblk, int ntp, long slots, long maxs) {
+    const long top = std::max<long>(1, std::min<long>(ntp, maxs));
+    int best = 1;
+    double beste = -1.0;
+    for (long ns = 1; ns <= top; ns++) {
+        const double w = (double)(nblk * ns) / (double)slots;
+        const double eff = w / std::ceil(w);
+        if (eff > beste + 1e-9) {
+            beste = eff;
+            best = (int)ns;
+        }
+        if (eff >= 0.85) break;
+    }
+    return best;
 }
-// floats of the split region: up to 7 partial rows per slice and point.  A
-// split launch has fewer than SPLIT_TARGET_BLOCKS blocks of 128 points and
-// at most ceil(SPLIT_TARGET_BLOCKS / blocks) slices, so slices x points stay
-// below 128 (2 SPLIT_TARGET_BLOCKS); the region has that fixed size, whatever
-// the batch (a batch's last, short chunk may split while its first does not).
+
+// Resident blocks of a kernel on the current device (0 where the query fails).
+template <typename K>
+static long resident_slots(K kernel, int threads, size_t smem) {
+    int dev = 0, nsm = 0, per = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return (long)per * nsm;
+}
+// floats of the split region: room for 7 partial rows per slice and point at
+// slices x points = 256 SPLIT_TARGET_BLOCKS; the launches take no more
+// slices than the region holds for their batch.  It has that fixed size,
+// whatever the batch (a batch's last, short chunk may split while its first
+// does not).
 static long point_split_floats(long n) {
     (void)n;
     return 7L * 128 * 2 * SPLIT_TARGET_BLOCKS;
@@ -1213,26 +1239,23 @@ int launch_eta_pairs(const DevSea &sea, long n, const float2 *ph, const float *r
     a.ncol = n; a.nl = 1; a.nlg = 1; a.ntile = sea.ntile_g; a.tab = sea.d_tab_eta;
     a.ph = ph; a.rr = rr; a.cf = sea.d_cf; a.cstride = sea.npad_g; a.out = out;
     a.pairs = 1; a.first = 0;
-    // few columns: split the tile-pair loop over blockIdx.y (as the column kernel)
     const long nblk = (n + 127) / 128;
     const int ntp = sea.ntile_g * (sea.ntile_g + 1) / 2;
-    int nslice = 1;
-    a.tp_per = ntp;
-    if (split_buf && nblk < SPLIT_TARGET_BLOCKS) {
-        int want = (int)std::min<long>(ntp, (SPLIT_TARGET_BLOCKS + nblk - 1) / nblk);
-        int per = (ntp + want - 1) / want;
-        int ns = (ntp + per - 1) / per;
-        if ((long)ns * n <= split_cap && ns > 1) {
-            nslice = ns;
-            a.tp_per = per;
-            a.out = split_buf;
-        }
-    }
-    size_t smem = sizeof(float2) * (GRID_TILE * GRID_TILE + GRID_TILE * 128);
+    const size_t smem = sizeof(float2) * (GRID_TILE * GRID_TILE + GRID_TILE * 128);
     // set once per process (thread-safe static initialisation)
     static const cudaError_t attr = cudaFuncSetAttribute(k_pairs_eta<GRID_TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem);
     CK(attr);
+    static const long slots = [&] {
+        const long v = resident_slots(k_pairs_eta<GRID_TILE>, 128, smem);
+        return v > 0 ? v : SPLIT_TARGET_BLOCKS;
+    }();
+    // the tile-pair loop split over blockIdx.y where the columns alone do
+    // not fill whole waves of the resident blocks (slices summed in order)
+    int nslice = wave_slices(nblk, ntp, slots, split_buf ? split_cap / std::max<long>(1, n) : 1);
+    a.tp_per = (ntp + nslice - 1) / nslice;
+    nslice = (ntp + a.tp_per - 1) / a.tp_per;
+    if (nslice > 1) a.out = split_buf;
     prof_begin(PK_ETA_PAIRS, stream);
     k_pairs_eta<GRID_TILE><<<dim3((unsigned)nblk, (unsigned)nslice), 128, smem, stream>>>(a);
     note_launch();
@@ -1466,15 +1489,19 @@ static int launch_point_pairs(const DevSea &sea, long n, const float2 *ph, const
         CK(cudaGetLastError());
         return OK;
     }
-    int nslice = point_slices(n, ntp);
+    const size_t smem = sizeof(float) * POINT_TILE * POINT_TILE * POINTV_NC + 2 * sizeof(float2) * POINT_TILE * 128;
+    // the same shared memory in every variant: resident blocks once per process
+    static const long slots = [&] {
+        cudaFuncSetAttribute(k_pairs_points<POINT_TILE, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+        const long v = resident_slots(k_pairs_points<POINT_TILE, true, true>, 128, smem);
+        return v > 0 ? v : SPLIT_TARGET_BLOCKS;
+    }();
+    const long nblk = (n + 127) / 128;
+    int nslice = wave_slices(nblk, ntp, slots, split_buf ? split_cap / (4L * n) : 1);
     a.tp_per = (ntp + nslice - 1) / nslice;
     nslice = (ntp + a.tp_per - 1) / a.tp_per;
-    if (nslice > 1 && (!split_buf || 4L * n * nslice > split_cap)) {
-        nslice = 1;
-        a.tp_per = ntp;
-    }
     if (nslice > 1) a.out = split_buf;
-    const size_t smem = sizeof(float) * POINT_TILE * POINT_TILE * POINTV_NC + 2 * sizeof(float2) * POINT_TILE * 128;
     // set once per process (thread-safe static initialisation)
     static const cudaError_t attr = [&] {
         cudaError_t e = cudaFuncSetAttribute(k_pairs_points<POINT_TILE, true, true>,

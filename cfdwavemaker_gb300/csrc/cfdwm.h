@@ -186,9 +186,11 @@ int smit_build(const SmitIn &c, DevSea &sea, void *stream);
 // ramps, the first-order sums (first[0] = eta1) and eta2; scratch: 4 n floats;
 // split_buf (split_cap floats, or null): partial sums when the pair loop is
 // split over blocks for few points.
+// mask: bits 2, 4, 8 (u, v, w) ask for the velocity sums, 16 (dp) for the
+// pressure sum; rows not asked for are 0
 int smit_eval(const DevSea &sea, long n, const double *z, const void *ph, const float *rr, const double *first,
               const float *eta2, float *scratch, float *split_buf, long split_cap, long ldo, double *out,
-              void *stream);
+              int mask, void *stream);
 
 // Builds the device tables (component coefficients and the FP64 transfer
 // functions of the pair tables, computed on the device).  point_table: also

@@ -1564,7 +1564,7 @@ int irregular_eval(const DevSea &sea, long n, const double *x, const double *y, 
         }
         if (smit) {
             rc = smit_eval(sea, m, z + b, L.ph, L.rr, L.first, eta2, L.sec, L.split, L.split_cap, n, out + b,
-                           stream);
+                           mask, stream);
             if (rc) return rc;
         } else if (mask & 30) {
             k_prep_z<<<(unsigned)((m + 255) / 256), 256, 0, stream>>>(m, z + b, sea.swl, sea.order, api ? 1 : 0,

@@ -193,7 +193,10 @@ constexpr int SMIT_PARTS = 7;  // u, v, w, dp, d phi2/ds, eta_x, d phi1/ds
 // batches of at most this many points take k_smit_points_few
 constexpr long SMIT_FEW_POINTS = 512;
 
-template <int TT>
+// VEL: the velocity sums (u with its chain term, v, w), PR: the pressure sum;
+// a call that asks for one of them does not pay for the other (rows not
+// computed are 0).
+template <int TT, bool VEL, bool PR>
 __global__ void __launch_bounds__(128) k_smit_points(SmitArgs a) {
     extern __shared__ float4 smem4[];
     float *s_tab = reinterpret_cast<float *>(smem4);                  // TT*TT*SNC
@@ -271,27 +274,33 @@ __global__ void __launch_bounds__(128) k_smit_points(SmitArgs a) {
                     float Fp, Gp, Fm, Gm;
                     sfg(c0.z, zk, zetak, Fp, Gp);
                     sfg(c0.w, zk, zetak, Fm, Gm);
-                    const float A2 = s_a[mm] * pfm.y, B2 = s_a[mm] * s_k[mm] * h * pfm.x;
                     const float hpc = -c0.x * cp * Fp, hmc = -c0.y * cmn * Fm;   // bound wave, cos part
-                    const float hps = c0.x * c0.z * Gp, hms = c0.y * c0.w * Gm;  // bound wave, k Sh part
-                    float tu = c1.x * hpc + c1.y * hmc + sp1 * (c3.x * (A1 + A2) * cp + c3.y * (A1 - A2) * cmn);
-                    float tv = c1.z * hpc + c1.w * hmc;
-                    float tw = -(hps * sp + hms * smn);
-                    const float chch = pfi.x * pfm.x, shsh = pfi.y * pfm.y;
-                    float tp = c2.x * hpc + c2.y * hmc + c2.z * (chch - shsh) * cp + c2.w * (chch + shsh) * cmn;
-                    float td = -h * (hps * sp + hms * smn) + c3.z * ((A1 + A2) + sp1 * (B1 + B2)) * sp +
-                               c3.w * ((A1 - A2) + sp1 * (B1 - B2)) * smn;
-                    au = fmaf(rm, tu, au);
-                    av = fmaf(rm, tv, av);
-                    aw = fmaf(rm, tw, aw);
-                    ap = fmaf(rm, tp, ap);
-                    ad = fmaf(rm, td, ad);
+                    if (VEL) {
+                        const float A2 = s_a[mm] * pfm.y, B2 = s_a[mm] * s_k[mm] * h * pfm.x;
+                        const float hps = c0.x * c0.z * Gp, hms = c0.y * c0.w * Gm;  // bound wave, k Sh part
+                        float tu = c1.x * hpc + c1.y * hmc + sp1 * (c3.x * (A1 + A2) * cp + c3.y * (A1 - A2) * cmn);
+                        float tv = c1.z * hpc + c1.w * hmc;
+                        float tw = -(hps * sp + hms * smn);
+                        float td = -h * (hps * sp + hms * smn) + c3.z * ((A1 + A2) + sp1 * (B1 + B2)) * sp +
+                                   c3.w * ((A1 - A2) + sp1 * (B1 - B2)) * smn;
+                        au = fmaf(rm, tu, au);
+                        av = fmaf(rm, tv, av);
+                        aw = fmaf(rm, tw, aw);
+                        ad = fmaf(rm, td, ad);
+                    }
+                    if (PR) {
+                        const float chch = pfi.x * pfm.x, shsh = pfi.y * pfm.y;
+                        float tp = c2.x * hpc + c2.y * hmc + c2.z * (chch - shsh) * cp + c2.w * (chch + shsh) * cmn;
+                        ap = fmaf(rm, tp, ap);
+                    }
                 }
-                skahan(su, cu, ri * au);
-                skahan(sv, cv, ri * av);
-                skahan(sw, cw, ri * aw);
-                skahan(sq, cq, ri * ap);
-                skahan(sd, cd, ri * ad);
+                if (VEL) {
+                    skahan(su, cu, ri * au);
+                    skahan(sv, cv, ri * av);
+                    skahan(sw, cw, ri * aw);
+                    skahan(sd, cd, ri * ad);
+                }
+                if (PR) skahan(sq, cq, ri * ap);
             }
             if (M == I) {
                 // first order with the stretched profiles and the first-order
@@ -301,14 +310,16 @@ __global__ void __launch_bounds__(128) k_smit_points(SmitArgs a) {
                     const float2 pm = s_ph[mm * 128 + threadIdx.x];
                     const float2 pfm = s_pf[mm * 128 + threadIdx.x];
                     const float rm = s_r[mm * 128 + threadIdx.x];
-                    const float agk = a.cf[CF_AU * a.cstride + m] * rm;     // A g k / w
-                    const float ct = a.cf[CF_CT * a.cstride + m];
-                    skahan(su, cu, agk * pfm.x * ct * pm.x);
-                    skahan(sv, cv, agk * pfm.x * a.cf[CF_ST * a.cstride + m] * pm.x);
-                    skahan(sw, cw, agk * pfm.y * pm.y);
-                    skahan(sq, cq, a.cf[CF_AP * a.cstride + m] * rm * pfm.x * pm.x);
-                    skahan(ex, cex, -a.cf[CF_A * a.cstride + m] * s_k[mm] * ct * pm.y * rm);
-                    skahan(ps, cps, agk * h * pfm.y * pm.y);
+                    if (VEL) {
+                        const float agk = a.cf[CF_AU * a.cstride + m] * rm;     // A g k / w
+                        const float ct = a.cf[CF_CT * a.cstride + m];
+                        skahan(su, cu, agk * pfm.x * ct * pm.x);
+                        skahan(sv, cv, agk * pfm.x * a.cf[CF_ST * a.cstride + m] * pm.x);
+                        skahan(sw, cw, agk * pfm.y * pm.y);
+                        skahan(ex, cex, -a.cf[CF_A * a.cstride + m] * s_k[mm] * ct * pm.y * rm);
+                        skahan(ps, cps, agk * h * pfm.y * pm.y);
+                    }
+                    if (PR) skahan(sq, cq, a.cf[CF_AP * a.cstride + m] * rm * pfm.x * pm.x);
                 }
             }
         }
@@ -470,7 +481,7 @@ int smit_build(const SmitIn &c, DevSea &sea, void *stream_) {
 
 int smit_eval(const DevSea &sea, long n, const double *z, const void *ph, const float *rr, const double *first,
               const float *eta2, float *scratch, float *split_buf, long split_cap, long ldo, double *out,
-              void *stream_) {
+              int mask, void *stream_) {
     cudaStream_t stream = (cudaStream_t)stream_;
     if (!sea.d_tab_smit) return E_NOT_INITIALIZED;
     if (n <= 0) return OK;
@@ -516,10 +527,29 @@ int smit_eval(const DevSea &sea, long n, const double *z, const void *ph, const 
     a.part = nslice > 1 ? split_buf : nullptr;
     const size_t smem = sizeof(float) * ST * ST * SNC + 2 * sizeof(float2) * ST * 128 + sizeof(float) * ST * 128;
     // set once per process (thread-safe static initialisation)
-    static const cudaError_t attr = cudaFuncSetAttribute(k_smit_points<ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    static const cudaError_t attr = [&] {
+        cudaError_t e = cudaFuncSetAttribute(k_smit_points<ST, true, true>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_smit_points<ST, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_smit_points<ST, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem);
+        return e;
+    }();
     CK(attr);
+    // the velocity sums only where u, v or w is asked for, the pressure sum
+    // only where dp is
+    const bool vel = (mask & 14) != 0, pr = (mask & 16) != 0;
     prof_begin(PK_POINT_PAIRS, stream);
-    k_smit_points<ST><<<dim3((unsigned)nblk, (unsigned)nslice), 128, smem, stream>>>(a);
+    const dim3 grid((unsigned)nblk, (unsigned)nslice);
+    if (vel && pr)
+        k_smit_points<ST, true, true><<<grid, 128, smem, stream>>>(a);
+    else if (vel)
+        k_smit_points<ST, true, false><<<grid, 128, smem, stream>>>(a);
+    else
+        k_smit_points<ST, false, true><<<grid, 128, smem, stream>>>(a);
     note_launch();
     prof_end(PK_POINT_PAIRS, stream);
     CK(cudaGetLastError());

@@ -103,17 +103,6 @@ __device__ __forceinline__ void put8_split(uint8_t *hi, uint8_t *lo, int r, int 
         make_uint4(pack_bf16(l[0], l[1]), pack_bf16(l[2], l[3]), pack_bf16(l[4], l[5]), pack_bf16(l[6], l[7]));
 }
 
-// eight BF16 values (exact) into row r, chunk j
-__device__ __forceinline__ void put8(uint8_t *t, int r, int j, const __nv_bfloat16 *v) {
-    uint32_t q[4];
-#pragma unroll
-    for (int e = 0; e < 4; e++) {
-        __nv_bfloat162 h = __halves2bfloat162(v[2 * e], v[2 * e + 1]);
-        q[e] = *reinterpret_cast<uint32_t *>(&h);
-    }
-    *reinterpret_cast<uint4 *>(t + swz(r, j)) = make_uint4(q[0], q[1], q[2], q[3]);
-}
-
 constexpr int CT_THREADS = 256;           // two threads per A row, each half of its K stage
 
 template <int OP, int NP>

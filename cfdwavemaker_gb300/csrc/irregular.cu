@@ -66,8 +66,6 @@ constexpr long FEW_POINTS = 512;
 // an elevation batch of 1024 points 159 us against 193 us; 2048 points 210
 // against 205)
 constexpr long PH_FEW_POINTS = 1024;
-constexpr double TWO_PI = 6.283185307179586476925286766559;
-constexpr double INV_TWO_PI = 0.15915494309189533576888376337251;
 
 __device__ __forceinline__ float ex2(float x) {
     float y;

@@ -82,11 +82,6 @@ __device__ __forceinline__ float ex2f(float x) {
     asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
     return y;
 }
-__device__ __forceinline__ float silu(float a) { return a / (1.f + expf(-a)); }
-__device__ __forceinline__ float silu_d(float a) {
-    float s = 1.f / (1.f + expf(-a));
-    return s * (1.f + a * (1.f - s));
-}
 
 // ---------------------------------------------------------------------------
 // First-order channels
